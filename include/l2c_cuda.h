@@ -1,0 +1,100 @@
+/* l2c_cuda.h -- thin C ABI between the host C library (libleg2cheb.so) and the
+ * sm_103a CUDA implementation (libl2c_cuda.so).  Plain pointers and sizes only.
+ *
+ * Each entry point replaces a piece of the reference's src/C/leg2cheb.c:
+ *   l2c_gpu_plan_create   <- create_fmm / create_direct   (leg2cheb.c:820-1234, 758-818)
+ *   l2c_gpu_execute       <- execute / direct             (leg2cheb.c:1299-1500, 152-234)
+ *   l2c_gpu_near          <- directM / directL            (leg2cheb.c:236-376, 378-535)
+ *   l2c_gpu_plan_destroy  <- free_fmm / free_direct       (leg2cheb.c:688-756, 650-673)
+ *   l2c_lambda            <- Lambda                       (lambda.c:65-98)
+ *   l2c_lambda_int        <- LambdaI                      (lambda.c:101-191)
+ * Errors never abort: calls return 0 / NULL and l2c_gpu_last_error() explains.
+ */
+#ifndef L2C_CUDA_H
+#define L2C_CUDA_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct l2c_gpu_plan l2c_gpu_plan;
+
+/* Plan flags */
+#define L2C_PLAN_DIRECT_ONLY 1u /* O(N^2) direct sums whatever N (create_direct) */
+
+/* Execute flags */
+#define L2C_EXEC_ASYNC 1u       /* return without waiting (device pointers only)  */
+#define L2C_EXEC_NEAR_ONLY 2u   /* near-field band + final scaling only (directM/L) */
+
+/* Geometry of create_fmm (leg2cheb.c:860-871): L = ceil(log2(N/maxs)) - 2,
+ * s = ceil(N / 2^(L+2)), Nn = s 2^(L+2); L = 0 selects the direct method.
+ * Returns L. */
+size_t l2c_geometry(size_t N, size_t maxs, size_t *s, size_t *Nn);
+
+/* Build the device plan: Lambda tables, Chebyshev Vandermonde T, the far-field
+ * blocks A for each planned direction (directions: 0 L2C, 1 C2L, 2 both), all on
+ * the current CUDA device.  M = 18 (the modal form). */
+l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsigned flags);
+void l2c_gpu_plan_destroy(l2c_gpu_plan *plan);
+
+/* info[0..7] = N, L, s, Nn, number of blocks N_b, M, planned directions, maxs */
+int l2c_gpu_plan_info(const l2c_gpu_plan *plan, size_t *info);
+
+/* count transforms of length N: vector v reads in[v*dist + i*stride] and
+ * updates out[v*dist + i*stride], i < N, with the reference's contract
+ * (FMM: out = scale (out + far + near); direct: out overwritten).  in/out may be
+ * host or device pointers.  Returns the reference's flop count times count,
+ * 0 on failure. */
+size_t l2c_gpu_execute(l2c_gpu_plan *plan, const double *in, double *out, size_t direction,
+                       size_t count, size_t dist, size_t stride, unsigned flags);
+
+/* Wait for work queued with L2C_EXEC_ASYNC.  0 on success. */
+int l2c_gpu_synchronize(l2c_gpu_plan *plan);
+
+/* The plan's CUDA stream (a cudaStream_t), for callers timing device work. */
+void *l2c_gpu_plan_stream(l2c_gpu_plan *plan);
+
+/* Reference flop count of one transform in this direction (0 if unplanned). */
+size_t l2c_gpu_flops(const l2c_gpu_plan *plan, size_t direction);
+
+/* Kernel launches this plan has issued since it was created. */
+size_t l2c_gpu_launch_count(const l2c_gpu_plan *plan);
+
+/* Per-phase accounting.  Phases, in launch order: */
+#define L2C_PHASE_GATHER 0    /* strided / premultiplied input copy        */
+#define L2C_PHASE_NEAR 1      /* near-field band                           */
+#define L2C_PHASE_LEAF_UP 2   /* leaf values -> Chebyshev coefficients     */
+#define L2C_PHASE_TREE_UP 3   /* upward transfer, all levels               */
+#define L2C_PHASE_FAR 4       /* far-field blocks, all levels              */
+#define L2C_PHASE_TREE_DOWN 5 /* downward transfer, all levels             */
+#define L2C_PHASE_LEAF_DOWN 6 /* back to leaf values + scaling             */
+#define L2C_PHASE_DIRECT 7    /* O(N^2) direct method (L < 1)              */
+#define L2C_NPHASES 8
+/* Enable (1) or disable (0) CUDA-event timing of each phase on the plan's
+ * stream, and reset the counters.  0 on success. */
+int l2c_gpu_profile(l2c_gpu_plan *plan, int enable);
+/* Accumulated milliseconds and launches per phase since the last reset
+ * (arrays of L2C_NPHASES; either may be NULL).  Waits for recorded events.
+ * Returns L2C_NPHASES. */
+int l2c_gpu_profile_read(l2c_gpu_plan *plan, double *ms, size_t *launches);
+
+/* Copy plan tables to host memory, for checking plan construction.
+ * which: 0 = A[L2C], 1 = A[C2L], 2 = Lambda table a, 3 = an, 4 = dn, 5 = T.
+ * Returns the number of doubles copied (n_max caps it), 0 if absent. */
+size_t l2c_gpu_plan_copy(const l2c_gpu_plan *plan, int which, double *dst, size_t n_max);
+
+/* Lambda(z) and Lambda at integer z, host side, bit-identical to the device. */
+double l2c_lambda(double z);
+double l2c_lambda_int(size_t z);
+
+/* Last error message of the calling thread ("" if none). */
+const char *l2c_gpu_last_error(void);
+
+/* Library version string. */
+const char *l2c_gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

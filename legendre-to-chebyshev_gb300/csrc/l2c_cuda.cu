@@ -1,0 +1,958 @@
+// l2c_cuda.cu -- GB300 (sm_103a) implementation of the fast multipole
+// Legendre<->Chebyshev transform behind the C ABI of include/l2c_cuda.h.
+//
+// One plan = one transform length N.  Everything the transform reads is built
+// on the GPU at plan time and stays resident in HBM:
+//   a[N], an[N], dn[(N+1)/2]   Lambda tables              (leg2cheb.c:758-818)
+//   A[dir][3 N_b][18][18]      far-field blocks           (leg2cheb.c:924-995)
+//   T[2][s][18]                Chebyshev Vandermonde      (leg2cheb.c:621-648)
+// Execution of one batch of `count` vectors (leg2cheb.c:1299-1500):
+//   gather      x = parity-ready contiguous copy (C2L: v_j = j u_j)
+//   near band   y = out_in + near field                       (directM / directL)
+//   leaf up     w[L-1] = leaf blocks * T_parity, both parities (step 1)
+//   tree up     w[l] from w[l+1] through the binomial matrix  (step 2)
+//   far         c = A w, every level in one launch             (step 3)
+//   tree down   c[l+1] += B^T c[l]                             (step 4)
+//   leaf down   out = scale (y + c[L-1] * T_parity^T)          (step 5 + scaling)
+// FP64 is the scarce resource on this part (about 1 TFLOP/s against 74 TFLOP/s
+// FP32), so the kernels are written to spend as few FP64 instructions per
+// coefficient as the algorithm allows; index arithmetic is integer.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/l2c_cuda.h"
+#include "l2c_lambda.h"
+
+namespace {
+
+constexpr int M = 18;
+constexpr int MM = M * M;
+constexpr int NTRI = (MM + M) / 2;
+constexpr double TWO_OVER_PI = 0.63661977236758134308;  // 2/pi
+constexpr double SQRT_PI = 1.77245385090551602729816;
+constexpr double TWO_OVER_SQRT_PI = 1.12837916709551257390;
+
+thread_local char g_err[512] = "";
+
+void set_err(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+#define CK(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      set_err("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return 0;                                                                        \
+    }                                                                                  \
+  } while (0)
+
+__constant__ double c_lambda_int[256] = L2C_LAMBDA_INT_INIT;
+__constant__ double c_binom_lower[NTRI] = L2C_BINOM_LOWER_INIT;
+__constant__ double c_binom_upper[NTRI] = L2C_BINOM_UPPER_INIT;
+__constant__ double c_xj[M];       // cos((i + 1/2) pi / M), host libm values
+__constant__ double c_dct[M * M];  // cos(pi k (n + 1/2) / M), [k][n]
+
+// ---------------------------------------------------------------------------
+// Tree bookkeeping (leg2cheb.c:125-150), as closed forms.
+//   level l holds nb(l) = 2^(l+1) - 1 blocks and S(l) = 2 nb(l) slots;
+//   blocks before level l: off(l) = 2^(l+1) - l - 2; slots before it: 2 off(l).
+// Source slot j of level l is tree node j + 2; target slot t is node t.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline size_t blocks_before(size_t l) { return ((size_t)2 << l) - l - 2; }
+__host__ __device__ inline size_t slots_at(size_t l) { return ((size_t)4 << l) - 2; }
+
+// ---------------------------------------------------------------------------
+// Plan construction kernels
+// ---------------------------------------------------------------------------
+
+// a[i] = Lambda(i): table for i < 256; for i >= 256, Lambda(i) at multiples of 8
+// and a[j] = a[j-1] - (a[j-1]/2)/j in between (leg2cheb.c:767-779).
+__global__ void k_lambda_table(double *a, size_t N) {
+  const size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t i0 = g * 8;
+  if (i0 >= N) return;
+  const size_t stop = i0 + 8 < N ? i0 + 8 : N;
+  if (i0 < 256) {
+    for (size_t i = i0; i < stop; i++) a[i] = c_lambda_int[i];
+    return;
+  }
+  double v = l2c_lambda_eval((double)i0);
+  a[i0] = v;
+  for (size_t j = i0 + 1; j < stop; j++) {
+    v = __dsub_rn(v, __ddiv_rn(__dmul_rn(0.5, v), (double)j));
+    a[j] = v;
+  }
+}
+
+// an[i] = 1/(a[i] (2 i^2 + i)), an[0] = 2/sqrt(pi); dn[i] = a[i-1]/(2 i), dn[0] = 0
+// (leg2cheb.c:781-795).
+__global__ void k_c2l_tables(const double *__restrict__ a, double *an, double *dn, size_t N) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < N)
+    an[i] = (i == 0) ? TWO_OVER_SQRT_PI
+                     : __ddiv_rn(1.0, __dmul_rn(a[i], (double)(2 * i * i + i)));
+  if (i < (N + 1) / 2) dn[i] = (i == 0) ? 0.0 : __ddiv_rn(a[i - 1], (double)(2 * i));
+}
+
+// Shift-invariant factor Lambda((y-x)/2) of level l and offset q - p (block 0,
+// p = 0), filled persymmetrically as the reference does (leg2cheb.c:948-955):
+// computed where j < M - i, mirrored to (M-1-j, M-1-i).
+__global__ void k_assemble_f0(double *f0, size_t L, size_t s) {
+  const int l = blockIdx.x >> 1, q = blockIdx.x & 1;
+  const int i = threadIdx.x / M, j = threadIdx.x % M;
+  if (threadIdx.x >= MM || j >= M - i) return;
+  const size_t hl = (size_t)1 << (L - l - 1);
+  const size_t h = s * hl;
+  const double hd = (double)h;
+  const size_t x0 = h;                                // 2*(i0 + 0*h) + h with i0 = 0
+  const size_t y0 = 2 * (2 * s * hl + q * h) + h;     // 2*(j0 + q*h) + h
+  const double x = __dadd_rn((double)x0, __dmul_rn(c_xj[i], hd));
+  const double y = __dadd_rn((double)y0, __dmul_rn(c_xj[j], hd));
+  const double m0 = l2c_lambda_eval(__dmul_rn(__dsub_rn(y, x), 0.5));
+  double *F = f0 + (size_t)blockIdx.x * MM;
+  F[i * M + j] = m0;
+  F[(M - 1 - j) * M + (M - 1 - i)] = m0;
+}
+
+// One far-field block per CTA: blockIdx.x = 3 g + r, g = global block index,
+// r over (q,p) = (0,0), (1,0), (1,1).  Samples the kernel on the 18x18 Chebyshev
+// grid (leg2cheb.c:924-972) and converts it with a 2D DCT-II,
+// A = (4/M^2) C F C^T with row 0 and column 0 halved (dct.c:582-598).
+__global__ void __launch_bounds__(MM) k_assemble_A(const double *__restrict__ f0, double *A_l2c,
+                                                   double *A_c2l, size_t L, size_t s) {
+  __shared__ double sF1[MM];
+  __shared__ double sF[MM];
+  __shared__ double sT[MM];
+  const size_t g = blockIdx.x / 3;
+  const int r = blockIdx.x % 3;
+  const int q = r == 0 ? 0 : 1, p = r == 2 ? 1 : 0;
+  size_t l = 0;
+  while (l + 1 < L && blocks_before(l + 1) <= g) l++;
+  const size_t b = g - blocks_before(l);
+  const size_t hl = (size_t)1 << (L - l - 1);
+  const size_t h = s * hl;
+  const double hd = (double)h;
+  const size_t i0 = 2 * b * s * hl, j0 = i0 + 2 * s * hl;
+  const double x0 = (double)(2 * (i0 + p * h) + h);
+  const double y0 = (double)(2 * (j0 + q * h) + h);
+  const int t = threadIdx.x;
+  const int i = t / M, j = t % M;
+  // Lambda((x+y)/2), symmetric fill from (min, max) (leg2cheb.c:956-963)
+  {
+    const int lo = i < j ? i : j, hi = i < j ? j : i;
+    const double x = __dadd_rn(x0, __dmul_rn(c_xj[lo], hd));
+    const double y = __dadd_rn(y0, __dmul_rn(c_xj[hi], hd));
+    sF1[t] = l2c_lambda_eval(__dmul_rn(__dadd_rn(x, y), 0.5));
+  }
+  __syncthreads();
+  const double fpq = f0[((size_t)l * 2 + (q - p)) * MM + t];
+  const double x = __dadd_rn(x0, __dmul_rn(c_xj[i], hd));
+  const double y = __dadd_rn(y0, __dmul_rn(c_xj[j], hd));
+  for (int dir = 0; dir < 2; dir++) {
+    double *Ad = dir == 0 ? A_l2c : A_c2l;
+    if (Ad == nullptr) continue;
+    if (dir == 0) {
+      sF[t] = __dmul_rn(fpq, sF1[t]);
+    } else {
+      const double xy = __dadd_rn(x, y);
+      double den = __dmul_rn(sF1[t], xy);
+      den = __dmul_rn(den, __dadd_rn(xy, 1.0));
+      den = __dmul_rn(den, __dadd_rn(__dsub_rn(x, y), 1.0));
+      sF[t] = __dmul_rn(2.0, __ddiv_rn(fpq, den));
+    }
+    __syncthreads();
+    // rows: sT[i][k] = sum_n F[i][n] C[k][n]
+    {
+      const int k = j;
+      double acc = 0.0;
+#pragma unroll
+      for (int n = 0; n < M; n++) acc = fma(sF[i * M + n], c_dct[k * M + n], acc);
+      sT[i * M + k] = acc;
+    }
+    __syncthreads();
+    // columns: out[k1][k2] = sum_i C[k1][i] sT[i][k2]
+    {
+      const int k1 = i, k2 = j;
+      double acc = 0.0;
+#pragma unroll
+      for (int n = 0; n < M; n++) acc = fma(c_dct[k1 * M + n], sT[n * M + k2], acc);
+      acc *= (1.0 / 81.0);
+      if (k1 == 0) acc *= 0.5;
+      if (k2 == 0) acc *= 0.5;
+      Ad[(size_t)blockIdx.x * MM + t] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Execution kernels.  Batch layout: vector v of `count`; caller arrays use
+// (dist, stride); internal arrays are contiguous per vector (x, y: N each;
+// w, c: 2 parities x 2 N_b slots x M).
+// ---------------------------------------------------------------------------
+
+struct Geo {
+  long long N, s, h, nL, L, K, slots, leaf_base, count, dist, stride;
+};
+
+// x[v N + j] = in[v dist + j stride], premultiplied by j (j >= 2) for C2L
+// (leg2cheb.c:1325-1335).
+__global__ void k_gather(const double *__restrict__ in, double *__restrict__ x, Geo g, int c2l) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.count * g.N) return;
+  const long long v = idx / g.N, j = idx - v * g.N;
+  double u = in[v * g.dist + j * g.stride];
+  if (c2l && j >= 2) u = u * (double)j;
+  x[idx] = u;
+}
+
+// Near-field band, one output per thread.  For output j in block b = min(j/h, nL-1)
+// the band covers sources j + 2k < lim = min((b+2) h, N):
+//   L2C: sum_k (a[k] a[j+k]) x[j+2k]                               (leg2cheb.c:236-302)
+//   C2L: (sqrt(pi) x[j]) an[j] - sum_{k>=1} (dn[k] x[j+2k]) an[j+k] (leg2cheb.c:392-459)
+// y = out_in + band.
+__global__ void __launch_bounds__(256) k_near(const double *__restrict__ x, const double *out,
+                                              double *__restrict__ y,
+                                              const double *__restrict__ a,
+                                              const double *__restrict__ an,
+                                              const double *__restrict__ dn, Geo g, int c2l) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.count * g.N) return;
+  const long long v = idx / g.N, j = idx - v * g.N;
+  long long b = j / g.h;
+  if (b > g.nL - 1) b = g.nL - 1;
+  long long lim = (b + 2) * g.h;
+  if (lim > g.N) lim = g.N;
+  const double *xv = x + v * g.N;
+  double acc;
+  if (!c2l) {
+    acc = 0.0;
+    for (long long k = 0; j + 2 * k < lim; k++) acc = fma(a[k] * a[j + k], xv[j + 2 * k], acc);
+  } else {
+    acc = (SQRT_PI * xv[j]) * an[j];
+    for (long long k = 1; j + 2 * k < lim; k++) acc = fma(-(dn[k] * xv[j + 2 * k]), an[j + k], acc);
+  }
+  y[idx] = out[v * g.dist + j * g.stride] + acc;
+}
+
+// Step 1: leaf node t in [2, 2^(L+1)) of parity sg: w = sum_i x[t h + 2i + sg] T_sg[i][m].
+// One thread per (vector, node, parity, m).
+__global__ void __launch_bounds__(288) k_leaf_up(const double *__restrict__ x,
+                                                 const double *__restrict__ T,
+                                                 double *__restrict__ w, Geo g) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long per_vec = g.K * 2 * M;
+  if (idx >= g.count * per_vec) return;
+  const long long v = idx / per_vec;
+  long long rem = idx - v * per_vec;
+  const long long node = rem / (2 * M);
+  rem -= node * 2 * M;
+  const int sg = (int)(rem / M), m = (int)(rem % M);
+  const long long base = (node + 2) * g.h + sg;
+  const double *xv = x + v * g.N;
+  const double *Ts = T + (size_t)sg * g.s * M + m;
+  double acc = 0.0;
+  long long iend = (g.N - base + 1) / 2;  // number of i with base + 2i < N
+  if (iend > g.s) iend = g.s;
+  for (long long i = 0; i < iend; i++) acc = fma(xv[base + 2 * i], Ts[i * M], acc);
+  w[((v * 2 + sg) * g.slots + g.leaf_base + node) * M + m] = acc;
+}
+
+// Step 2, one level: parent slot j of level l from child slots 2j+2, 2j+3 of level
+// l+1 through the compact lower binomial matrix; z = x0 +- x1 by row/column
+// parity (leg2cheb.c:537-602).
+__global__ void k_tree_up(double *w, Geo g, long long parent_base, long long child_base,
+                          long long nparent) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long per_vec = 2 * nparent * M;
+  if (idx >= g.count * per_vec) return;
+  const long long vs = idx / (nparent * M);  // vector * 2 + parity
+  long long rem = idx - vs * nparent * M;
+  const long long jp = rem / M;
+  const int m = (int)(rem % M);
+  const double *x0 = w + (vs * g.slots + child_base + 2 * jp + 2) * M;
+  const double *x1 = x0 + M;
+  const double *Bm = c_binom_lower + m * (m + 1) / 2;
+  double acc = 0.0;
+  for (int i = 0; i <= m; i++) {
+    const double z = ((m + i) & 1) ? x0[i] - x1[i] : x0[i] + x1[i];
+    acc = fma(Bm[i], z, acc);
+  }
+  w[(vs * g.slots + parent_base + jp) * M + m] = acc;
+}
+
+// Step 3: far-field blocks of every level at once.  Global block gb owns slots
+// 2 gb, 2 gb + 1: c0 = A0 w0 + A1 w1, c1 = A2 w1 (leg2cheb.c:1419-1435).
+__global__ void __launch_bounds__(256) k_far(const double *__restrict__ A,
+                                             const double *__restrict__ w,
+                                             double *__restrict__ c, Geo g, long long nblocks) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long per_vs = nblocks * M;
+  if (idx >= g.count * 2 * per_vs) return;
+  const long long vs = idx / per_vs;
+  long long rem = idx - vs * per_vs;
+  const long long gb = rem / M;
+  const int m = (int)(rem % M);
+  const double *A0 = A + (3 * gb) * MM + m * M;
+  const double *A1 = A0 + MM, *A2 = A1 + MM;
+  const double *w0 = w + (vs * g.slots + 2 * gb) * M, *w1 = w0 + M;
+  double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < M; k++) {
+    t0 = fma(A0[k], w0[k], t0);
+    t1 = fma(A1[k], w1[k], t1);
+    t2 = fma(A2[k], w1[k], t2);
+  }
+  double *c0 = c + (vs * g.slots + 2 * gb) * M;
+  c0[m] = t0 + t1;
+  c0[M + m] = t2;
+}
+
+// Step 4, one level: parent target slot t of level l into children 2t, 2t+1 of
+// level l+1 through the compact upper (transposed) binomial matrix: se/so sum the
+// columns of equal/opposite parity, child0 += se + so, child1 += se - so
+// (leg2cheb.c:603-618).
+__global__ void k_tree_down(double *c, Geo g, long long parent_base, long long child_base,
+                            long long nparent) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.count * 2 * nparent * M) return;
+  const long long vs = idx / (nparent * M);
+  long long rem = idx - vs * nparent * M;
+  const long long tp = rem / M;
+  const int i = (int)(rem % M);
+  const double *xp = c + (vs * g.slots + parent_base + tp) * M;
+  const double *Bu = c_binom_upper + i * M - i * (i - 1) / 2 - i;  // Bu[j] = row i, column j
+  double se = 0.0, so = 0.0;
+  for (int j = i; j < M; j += 2) se = fma(Bu[j], xp[j], se);
+  for (int j = i + 1; j < M; j += 2) so = fma(Bu[j], xp[j], so);
+  double *ch = c + (vs * g.slots + child_base + 2 * tp) * M;
+  ch[i] += se + so;
+  ch[M + i] += se - so;
+}
+
+// Step 5 + scaling: out[j] = scale_j (y[j] + sum_m c[L-1][tau][m] T_sg[i][m]) with
+// tau = j / h, sg = j & 1, i = (j - tau h)/2; no far field for tau >= K.
+// L2C scale 2/pi (and 1/2 at j = 0, leg2cheb.c:360-374); C2L scale j + 1/2
+// (leg2cheb.c:519-532).
+__global__ void __launch_bounds__(256) k_leaf_down(const double *__restrict__ c,
+                                                   const double *__restrict__ T,
+                                                   const double *__restrict__ y, double *out,
+                                                   Geo g, int c2l) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.count * g.N) return;
+  const long long v = idx / g.N, j = idx - v * g.N;
+  const long long tau = j / g.h;
+  double far = 0.0;
+  if (tau < g.K) {
+    const int sg = (int)(j & 1);
+    const long long i = (j - tau * g.h) >> 1;
+    const double *cv = c + ((v * 2 + sg) * g.slots + g.leaf_base + tau) * M;
+    const double *Ti = T + ((size_t)sg * g.s + i) * M;
+#pragma unroll
+    for (int m = 0; m < M; m++) far = fma(cv[m], Ti[m], far);
+  }
+  double val = y[idx] + far;
+  if (!c2l) {
+    val = val * TWO_OVER_PI;
+    if (j == 0) val = val * 0.5;
+  } else {
+    val = val * ((double)j + 0.5);
+  }
+  out[v * g.dist + j * g.stride] = val;
+}
+
+// Direct O(N^2) transform for L < 1 (leg2cheb.c:152-234), with the reference's
+// contract: out[0..N) is zeroed contiguously before the line is written, the
+// L2C input is read contiguously, L2C accumulates into line elements past N.
+__global__ void __launch_bounds__(256) k_direct(const double *in, double *out,
+                                                const double *__restrict__ a,
+                                                const double *__restrict__ an,
+                                                const double *__restrict__ dn, Geo g, int c2l) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.count * g.N) return;
+  const long long v = idx / g.N, i = idx - v * g.N;
+  const double *u = in + v * g.dist;
+  double *b = out + v * g.dist;
+  double val;
+  if (!c2l) {
+    val = 0.0;
+    for (long long k = 0; i + 2 * k < g.N; k++)
+      val = fma((a[k] * TWO_OVER_PI) * a[k + i], u[i + 2 * k], val);
+    if (i == 0) val = val / 2;
+    if (i * g.stride >= g.N) val = b[i * g.stride] + val;
+  } else {
+    const double vi = (i == 0) ? u[0] : u[i * g.stride] * (double)i;
+    val = (SQRT_PI * vi) * an[i];
+    for (long long k = 1; i + 2 * k < g.N; k++) {
+      const long long n = i + 2 * k;
+      val = fma(-(dn[k] * an[k + i]), u[n * g.stride] * (double)n, val);
+    }
+    val = val * ((double)i + 0.5);
+  }
+  if (g.stride > 1 && (i % g.stride) != 0) b[i] = 0.0;  // contiguous zeroing of [0, N)
+  b[i * g.stride] = val;
+}
+
+inline unsigned blocks_for(long long n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Plan
+// ---------------------------------------------------------------------------
+struct l2c_gpu_plan;
+namespace {
+struct PhaseScope;
+}
+
+struct l2c_gpu_plan {
+  size_t N = 0, maxs = 0, L = 0, s = 0, Nn = 0, Nb = 0, h = 0, nL = 0, K = 0, slots = 0;
+  size_t dirs = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  double *a = nullptr, *an = nullptr, *dn = nullptr;
+  double *A[2] = {nullptr, nullptr};
+  double *T = nullptr;
+  // scratch, grown on demand
+  double *x = nullptr, *y = nullptr, *w = nullptr, *c = nullptr;
+  size_t cap_vec = 0;
+  double *st_in = nullptr, *st_out = nullptr;
+  size_t cap_st_in = 0, cap_st_out = 0;
+  size_t flops[2] = {0, 0};
+  std::mutex mu;
+  // launch accounting and optional per-phase CUDA-event timing
+  size_t launches = 0;
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;                 // recycled events
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  double phase_ms[L2C_NPHASES] = {0};
+  size_t phase_launches[L2C_NPHASES] = {0};
+};
+
+namespace {
+
+// Reference flop count (the value execute() returns), reproduced term by term,
+// including its unsigned wrap-around in directL's last block (leg2cheb.c:507-516).
+size_t ref_flops(const l2c_gpu_plan *p, size_t dir) {
+  const size_t N = p->N;
+  size_t f = 0;
+  if (p->L == 0) {
+    f = N;
+    for (size_t n = (dir == 0 ? 0 : 2); n < N; n += 2) f += 3 * (N - n);
+    return f + N;
+  }
+  const size_t L = p->L, s = p->s, MMs = (size_t)MM;
+  const size_t K = 2 * (((size_t)2 << (L - 1)) - 1);
+  size_t far = 4 * K * s * M;
+  for (size_t l = 1; l < L; l++) far += (((size_t)2 << l) - 2) * MMs;       // step 2
+  far += 3 * p->Nb * 2 * MMs;                                              // step 3
+  for (size_t l = 0; l + 1 < L; l++) far += (((size_t)2 << (l + 1)) - 2) * MMs;  // step 4
+  f = 2 * far;
+  const size_t h = 2 * s, nL = N / h, i0 = (nL - 1) * h;
+  size_t band = 0;
+  for (size_t n = (dir == 0 ? 0 : 2); n < 4 * s; n += 2) band += 3 * (n < h ? h : 2 * h - n);
+  f += (nL - 1) * band;
+  if (dir == 0) {
+    for (size_t n = 0; 2 * n + i0 < N; n++) f += 3 * (N - (2 * n + i0));
+    f += N;
+  } else {
+    f += 3 * N;
+    for (size_t n = 1; n < N - i0; n++) f += (N - (2 * n + i0)) * 3;
+    f += 2 * N;
+  }
+  return f;
+}
+
+bool grow(double **ptr, size_t *cap, size_t need) {
+  if (need <= *cap) return true;
+  if (*ptr) cudaFree(*ptr);
+  *ptr = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc(ptr, need * sizeof(double));
+  if (e != cudaSuccess) {
+    set_err("cudaMalloc(%zu bytes) failed: %s", need * sizeof(double), cudaGetErrorString(e));
+    *ptr = nullptr;
+    return false;
+  }
+  *cap = need;
+  return true;
+}
+
+cudaEvent_t take_event(l2c_gpu_plan *p) {
+  if (!p->ev_pool.empty()) {
+    cudaEvent_t e = p->ev_pool.back();
+    p->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+// Brackets the launches of one phase: counts them and, when profiling, records
+// CUDA events on the plan's stream around them.
+struct PhaseScope {
+  l2c_gpu_plan *p;
+  int phase;
+  cudaEvent_t e0 = nullptr;
+  PhaseScope(l2c_gpu_plan *pl, int ph, size_t nlaunch) : p(pl), phase(ph) {
+    p->launches += nlaunch;
+    p->phase_launches[ph] += nlaunch;
+    if (p->profiling) {
+      e0 = take_event(p);
+      if (e0) cudaEventRecord(e0, p->stream);
+    }
+  }
+  ~PhaseScope() {
+    if (!e0) return;
+    cudaEvent_t e1 = take_event(p);
+    if (!e1) return;
+    cudaEventRecord(e1, p->stream);
+    p->pending.push_back({phase, {e0, e1}});
+  }
+};
+
+void collect_profile(l2c_gpu_plan *p) {
+  for (auto &pe : p->pending) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(pe.second.second) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, pe.second.first, pe.second.second) == cudaSuccess)
+      p->phase_ms[pe.first] += ms;
+    p->ev_pool.push_back(pe.second.first);
+    p->ev_pool.push_back(pe.second.second);
+  }
+  p->pending.clear();
+}
+
+bool ensure_scratch(l2c_gpu_plan *p, size_t count) {
+  if (count <= p->cap_vec) return true;
+  size_t c0 = p->cap_vec;
+  size_t cx = c0 * p->N, cy = cx, cw = c0 * 2 * p->slots * M, cc = cw;
+  const size_t need = count;
+  if (!grow(&p->x, &cx, need * p->N) || !grow(&p->y, &cy, need * p->N)) return false;
+  if (p->L > 0) {
+    if (!grow(&p->w, &cw, need * 2 * p->slots * M) || !grow(&p->c, &cc, need * 2 * p->slots * M))
+      return false;
+  }
+  p->cap_vec = need;
+  return true;
+}
+
+bool is_device_ptr(const void *ptr) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+    else prev = -1;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// Device-pointer execution of one batch.
+size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, size_t count,
+                  size_t dist, size_t stride, bool near_only, bool input_ready) {
+  cudaStream_t st = p->stream;
+  const int c2l = dir == 1;
+  Geo g;
+  g.N = (long long)p->N;
+  g.s = (long long)p->s;
+  g.h = (long long)p->h;
+  g.nL = (long long)p->nL;
+  g.L = (long long)p->L;
+  g.K = (long long)p->K;
+  g.slots = (long long)p->slots;
+  g.leaf_base = p->L > 0 ? 2 * (long long)blocks_before(p->L - 1) : 0;
+  g.count = (long long)count;
+  g.dist = (long long)dist;
+  g.stride = (long long)stride;
+  const long long total = g.count * g.N;
+  if (total == 0) return 1;
+  if (!ensure_scratch(p, count)) return 0;
+
+  if (p->L == 0) {
+    PhaseScope ps(p, L2C_PHASE_DIRECT, 1);
+    k_direct<<<blocks_for(total, 256), 256, 0, st>>>(in, out, p->a, p->an, p->dn, g, c2l);
+    CK(cudaGetLastError());
+    return 1;
+  }
+  // contiguous (and for C2L premultiplied) copy of the input
+  const double *x = in;
+  if (!input_ready && (c2l || stride != 1 || (count > 1 && dist != p->N))) {
+    PhaseScope ps(p, L2C_PHASE_GATHER, 1);
+    k_gather<<<blocks_for(total, 256), 256, 0, st>>>(in, p->x, g, c2l);
+    CK(cudaGetLastError());
+    x = p->x;
+  }
+  {
+    PhaseScope ps(p, L2C_PHASE_NEAR, 1);
+    k_near<<<blocks_for(total, 256), 256, 0, st>>>(x, out, p->y, p->a, p->an, p->dn, g, c2l);
+    CK(cudaGetLastError());
+  }
+  if (near_only) {
+    Geo g0 = g;
+    g0.K = 0;
+    PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
+    k_leaf_down<<<blocks_for(total, 256), 256, 0, st>>>(p->c, p->T, p->y, out, g0, c2l);
+    CK(cudaGetLastError());
+    return 1;
+  }
+  const long long leaf_threads = g.count * g.K * 2 * M;
+  {
+    PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
+    k_leaf_up<<<blocks_for(leaf_threads, 288), 288, 0, st>>>(x, p->T, p->w, g);
+    CK(cudaGetLastError());
+  }
+  PhaseScope *ps_up = new PhaseScope(p, L2C_PHASE_TREE_UP, p->L - 1);
+  for (long long l = (long long)p->L - 2; l >= 0; l--) {
+    const long long np = (long long)slots_at((size_t)l);
+    const long long n = g.count * 2 * np * M;
+    k_tree_up<<<blocks_for(n, 256), 256, 0, st>>>(p->w, g, 2 * (long long)blocks_before(l),
+                                                   2 * (long long)blocks_before(l + 1), np);
+  }
+  delete ps_up;
+  CK(cudaGetLastError());
+  {
+    PhaseScope ps(p, L2C_PHASE_FAR, 1);
+    const long long n = g.count * 2 * (long long)p->Nb * M;
+    k_far<<<blocks_for(n, 256), 256, 0, st>>>(p->A[dir], p->w, p->c, g, (long long)p->Nb);
+    CK(cudaGetLastError());
+  }
+  {
+    PhaseScope ps(p, L2C_PHASE_TREE_DOWN, p->L - 1);
+    for (long long l = 0; l + 1 < (long long)p->L; l++) {
+      const long long np = (long long)slots_at((size_t)l);
+      const long long n = g.count * 2 * np * M;
+      k_tree_down<<<blocks_for(n, 256), 256, 0, st>>>(p->c, g, 2 * (long long)blocks_before(l),
+                                                       2 * (long long)blocks_before(l + 1), np);
+    }
+  }
+  CK(cudaGetLastError());
+  {
+    PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
+    k_leaf_down<<<blocks_for(total, 256), 256, 0, st>>>(p->c, p->T, p->y, out, g, c2l);
+    CK(cudaGetLastError());
+  }
+  return 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t l2c_geometry(size_t N, size_t maxs, size_t *s_out, size_t *Nn_out) {
+  const int L = (int)std::ceil(std::log2((double)N / (double)maxs)) - 2;
+  if (L < 1 || maxs == 0) {
+    if (s_out) *s_out = 0;
+    if (Nn_out) *Nn_out = N;
+    return 0;
+  }
+  const size_t s = (size_t)std::ceil((double)N / std::pow(2.0, L + 2));
+  if (s_out) *s_out = s;
+  if (Nn_out) *Nn_out = s * ((size_t)1 << (L + 2));
+  return (size_t)L;
+}
+
+l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsigned flags) {
+  g_err[0] = 0;
+  if (N == 0) {
+    set_err("N must be positive");
+    return nullptr;
+  }
+  if (directions > 2) {
+    set_err("direction must be 0 (L2C), 1 (C2L) or 2 (both)");
+    return nullptr;
+  }
+  l2c_gpu_plan *p = new (std::nothrow) l2c_gpu_plan();
+  if (!p) {
+    set_err("out of host memory");
+    return nullptr;
+  }
+  auto fail = [&]() -> l2c_gpu_plan * {
+    l2c_gpu_plan_destroy(p);
+    return nullptr;
+  };
+#define PCK(call)                                                                          \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) {                                                               \
+      set_err("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return fail();                                                                       \
+    }                                                                                      \
+  } while (0)
+  p->N = N;
+  p->maxs = maxs;
+  p->dirs = directions;
+  PCK(cudaGetDevice(&p->device));
+  PCK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  if (flags & L2C_PLAN_DIRECT_ONLY) {
+    p->L = 0;
+    p->Nn = N;
+  } else {
+    p->L = l2c_geometry(N, maxs, &p->s, &p->Nn);
+  }
+  cudaStream_t st = p->stream;
+  const bool need_c2l = directions == 1 || directions == 2;
+  PCK(cudaMalloc(&p->a, N * sizeof(double)));
+  k_lambda_table<<<blocks_for((long long)(N + 7) / 8, 128), 128, 0, st>>>(p->a, N);
+  PCK(cudaGetLastError());
+  if (need_c2l) {
+    PCK(cudaMalloc(&p->an, N * sizeof(double)));
+    PCK(cudaMalloc(&p->dn, ((N + 1) / 2 + 1) * sizeof(double)));
+    k_c2l_tables<<<blocks_for((long long)N, 256), 256, 0, st>>>(p->a, p->an, p->dn, N);
+    PCK(cudaGetLastError());
+  }
+  if (p->L > 0) {
+    const size_t L = p->L, s = p->s;
+    p->h = 2 * s;
+    p->nL = N / p->h;
+    p->Nb = ((size_t)2 << L) - (L + 2);
+    p->slots = 2 * p->Nb;
+    p->K = slots_at(L - 1);
+    // host-side constants: Chebyshev points and DCT cosines (libm, as the reference)
+    double xj[M], cs[MM];
+    for (int i = 0; i < M; i++) xj[i] = std::cos((i + 0.5) * M_PI / M);
+    for (int k = 0; k < M; k++)
+      for (int n = 0; n < M; n++) cs[k * M + n] = std::cos(M_PI * k * (n + 0.5) / M);
+    PCK(cudaMemcpyToSymbolAsync(c_xj, xj, sizeof(xj), 0, cudaMemcpyHostToDevice, st));
+    PCK(cudaMemcpyToSymbolAsync(c_dct, cs, sizeof(cs), 0, cudaMemcpyHostToDevice, st));
+    // Vandermonde T_j(-1 + i/s), i < 2s, rows split even | odd (leg2cheb.c:621-648)
+    std::vector<double> T(2 * s * M);
+    for (size_t i = 0; i < 2 * s; i++) {
+      double row[M];
+      const double xv = -1 + (double)i / (double)s;
+      const double x2 = 2 * xv;
+      row[0] = 1;
+      row[1] = xv;
+      for (int j = 2; j < M; j++) row[j] = row[j - 1] * x2 - row[j - 2];
+      const size_t r = (i % 2 == 0) ? i / 2 : s + i / 2;
+      std::memcpy(&T[r * M], row, sizeof(row));
+    }
+    PCK(cudaMalloc(&p->T, T.size() * sizeof(double)));
+    PCK(cudaMemcpyAsync(p->T, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    double *f0 = nullptr;
+    PCK(cudaMalloc(&f0, 2 * L * MM * sizeof(double)));
+    k_assemble_f0<<<(unsigned)(2 * L), MM, 0, st>>>(f0, L, s);
+    cudaError_t e = cudaGetLastError();
+    for (int d = 0; d < 2 && e == cudaSuccess; d++)
+      if (directions == (size_t)d || directions == 2)
+        e = cudaMalloc(&p->A[d], 3 * p->Nb * MM * sizeof(double));
+    if (e == cudaSuccess) {
+      // one CTA per (block, r); the grid is at most 3 (2^(L+1)) CTAs
+      k_assemble_A<<<(unsigned)(3 * p->Nb), MM, 0, st>>>(f0, p->A[0], p->A[1], L, s);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(f0);
+    PCK(e);
+  }
+  PCK(cudaStreamSynchronize(st));
+  for (size_t d = 0; d < 2; d++)
+    if (directions == d || directions == 2) p->flops[d] = ref_flops(p, d);
+  return p;
+#undef PCK
+}
+
+void l2c_gpu_plan_destroy(l2c_gpu_plan *p) {
+  if (!p) return;
+  DeviceGuard dg(p->device);
+  if (p->stream) cudaStreamSynchronize(p->stream);
+  collect_profile(p);
+  for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
+  double *bufs[] = {p->a, p->an, p->dn, p->A[0], p->A[1], p->T, p->x, p->y, p->w, p->c,
+                    p->st_in, p->st_out};
+  for (double *b : bufs)
+    if (b) cudaFree(b);
+  if (p->stream) cudaStreamDestroy(p->stream);
+  delete p;
+}
+
+int l2c_gpu_plan_info(const l2c_gpu_plan *p, size_t *info) {
+  if (!p || !info) return 0;
+  info[0] = p->N;
+  info[1] = p->L;
+  info[2] = p->s;
+  info[3] = p->Nn;
+  info[4] = p->Nb;
+  info[5] = M;
+  info[6] = p->dirs;
+  info[7] = p->maxs;
+  return 1;
+}
+
+size_t l2c_gpu_flops(const l2c_gpu_plan *p, size_t dir) { return (p && dir < 2) ? p->flops[dir] : 0; }
+
+void *l2c_gpu_plan_stream(l2c_gpu_plan *p) { return p ? (void *)p->stream : nullptr; }
+
+int l2c_gpu_synchronize(l2c_gpu_plan *p) {
+  if (!p) return 1;
+  DeviceGuard dg(p->device);
+  cudaError_t e = cudaStreamSynchronize(p->stream);
+  if (e != cudaSuccess) {
+    set_err("cudaStreamSynchronize failed: %s", cudaGetErrorString(e));
+    return 1;
+  }
+  return 0;
+}
+
+size_t l2c_gpu_execute(l2c_gpu_plan *p, const double *in, double *out, size_t dir, size_t count,
+                       size_t dist, size_t stride, unsigned flags) {
+  g_err[0] = 0;
+  if (!p || !in || !out) {
+    set_err("null plan or array");
+    return 0;
+  }
+  if (dir > 1) {
+    set_err("direction must be 0 (L2C) or 1 (C2L)");
+    return 0;
+  }
+  if (!(p->dirs == dir || p->dirs == 2)) {
+    set_err("direction %zu was not planned", dir);
+    return 0;
+  }
+  if (stride == 0) stride = 1;
+  if (count == 0) return 0;
+  if (count > 1 && dist == 0) {
+    set_err("dist must be positive for count > 1");
+    return 0;
+  }
+  const bool near_only = (flags & L2C_EXEC_NEAR_ONLY) != 0;
+  if (near_only && p->L == 0) {
+    set_err("near-field only execution needs an FMM plan (L >= 1)");
+    return 0;
+  }
+  std::lock_guard<std::mutex> lock(p->mu);
+  DeviceGuard dg(p->device);
+  const size_t N = p->N;
+  // span of caller memory the call touches (the direct path also zeroes [0, N))
+  size_t span = (count - 1) * dist + (N - 1) * stride + 1;
+  if (p->L == 0) span = std::max(span, (count - 1) * dist + N);
+  // directL semantics: contiguous, premultiplied input
+  const bool in_contig = near_only && dir == 1;
+  const size_t in_span = in_contig ? (count - 1) * dist + N : span;
+  const bool in_dev = is_device_ptr(in), out_dev = is_device_ptr(out);
+  if (!in_dev || !out_dev) {
+    // host memory: stage the touched span (the layout is kept, so the kernels
+    // see the same dist/stride)
+    if (!in_dev && !grow(&p->st_in, &p->cap_st_in, in_span)) return 0;
+    if (!out_dev && !grow(&p->st_out, &p->cap_st_out, span)) return 0;
+    if (!in_dev)
+      CK(cudaMemcpyAsync(p->st_in, in, in_span * sizeof(double), cudaMemcpyHostToDevice, p->stream));
+    if (!out_dev)
+      CK(cudaMemcpyAsync(p->st_out, out, span * sizeof(double), cudaMemcpyHostToDevice, p->stream));
+  }
+  const double *din = in_dev ? in : p->st_in;
+  double *dout = out_dev ? out : p->st_out;
+  if (!run_device(p, din, dout, dir, count, dist, stride, near_only, in_contig)) return 0;
+  if (!out_dev)
+    CK(cudaMemcpyAsync(out, dout, span * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+  if (!(flags & L2C_EXEC_ASYNC) || !in_dev || !out_dev) CK(cudaStreamSynchronize(p->stream));
+  size_t f = p->flops[dir];
+  if (near_only) f = 1;  // callers of directM/directL get their own count
+  return f * count;
+}
+
+size_t l2c_gpu_launch_count(const l2c_gpu_plan *p) { return p ? p->launches : 0; }
+
+int l2c_gpu_profile(l2c_gpu_plan *p, int enable) {
+  if (!p) return 1;
+  std::lock_guard<std::mutex> lock(p->mu);
+  DeviceGuard dg(p->device);
+  cudaStreamSynchronize(p->stream);
+  collect_profile(p);
+  for (int i = 0; i < L2C_NPHASES; i++) {
+    p->phase_ms[i] = 0.0;
+    p->phase_launches[i] = 0;
+  }
+  p->profiling = enable != 0;
+  return 0;
+}
+
+int l2c_gpu_profile_read(l2c_gpu_plan *p, double *ms, size_t *launches) {
+  if (!p) return 0;
+  std::lock_guard<std::mutex> lock(p->mu);
+  DeviceGuard dg(p->device);
+  collect_profile(p);
+  for (int i = 0; i < L2C_NPHASES; i++) {
+    if (ms) ms[i] = p->phase_ms[i];
+    if (launches) launches[i] = p->phase_launches[i];
+  }
+  return L2C_NPHASES;
+}
+
+size_t l2c_gpu_plan_copy(const l2c_gpu_plan *p, int which, double *dst, size_t n_max) {
+  if (!p || !dst) return 0;
+  const double *src = nullptr;
+  size_t n = 0;
+  switch (which) {
+    case 0:
+    case 1:
+      src = p->A[which];
+      n = 3 * p->Nb * MM;
+      break;
+    case 2:
+      src = p->a;
+      n = p->N;
+      break;
+    case 3:
+      src = p->an;
+      n = p->N;
+      break;
+    case 4:
+      src = p->dn;
+      n = (p->N + 1) / 2;
+      break;
+    case 5:
+      src = p->T;
+      n = 2 * p->s * M;
+      break;
+    default:
+      return 0;
+  }
+  if (!src) return 0;
+  n = std::min(n, n_max);
+  DeviceGuard dg(p->device);
+  if (cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    set_err("copy of plan data failed");
+    return 0;
+  }
+  return n;
+}
+
+double l2c_lambda(double z) { return l2c_lambda_eval(z); }
+
+double l2c_lambda_int(size_t z) {
+  static const double table[256] = L2C_LAMBDA_INT_INIT;
+  if (z > 255) return l2c_lambda_eval((double)z);
+  return table[z];
+}
+
+const char *l2c_gpu_last_error(void) { return g_err; }
+
+const char *l2c_gpu_version(void) { return "l2c-gb300 0.1 (sm_103a, fp64)"; }
+
+}  // extern "C"

@@ -1,0 +1,255 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference.
+
+Tolerance: 1e-14 relative max-norm, max|y - y_ref| / max|y_ref|, per direction
+(the FP64 bar of the transform's specification).  References:
+  * golden vectors from the unmodified reference (tests/golden),
+  * the oracle port (oracle/l2c_oracle.c) for cases the reference cannot run
+    (odd-N L2C) or that are too big for fixtures,
+  * the extended-precision direct sum (oracle/direct_ld.py)."""
+import numpy as np
+import pytest
+
+from oracle import direct_ld
+from tests.conftest import relerr
+from tests.golden.cases import CASES, make_input
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-14
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+
+    return torch
+
+
+@pytest.mark.parametrize("key", sorted(CASES))
+def test_golden_cases_host_pointers(lib, golden, key):
+    N, maxs, d, st, dist, seed = CASES[key]
+    u = make_input(N * st, dist, seed)
+    out = np.zeros(N * st)
+    if key.startswith("direct"):
+        p = lib.DirectPlan(N, 2)
+        flops = p(u, out, d, st)
+    else:
+        p = lib.Plan(N, maxs, direction=2)
+        flops = p.execute(u, out, d, st)
+    assert flops == int(golden[key + "/flops"])
+    assert relerr(out, golden[key + "/out"]) <= TOL
+
+
+@pytest.mark.parametrize("key", [k for k in sorted(CASES) if k.startswith("ones_")])
+def test_known_answers_N20(lib, key):
+    # src/bin/l2c.c:69-74
+    a = [1.7913439415860921e00, 2.3408718378050253e00, 1.8833606631960720e00,
+         1.6587642683880404e00, 1.4417173322290182e00]
+    b = [5.2631578947368418e-01, 7.5187969924812026e-02, 1.3268465280849182e-01,
+         1.7768205680441512e-01, 2.4367824933176932e-01]
+    d = 0 if "_d0_" in key else 1
+    p = lib.Plan(20, 64)
+    out = np.zeros(20)
+    p.execute(np.ones(20), out, d)
+    want = a if d == 0 else b
+    assert np.sqrt(np.sum((out[:5] - want) ** 2)) < 1e-7
+    assert np.max(np.abs(out[:5] - want)) < 4e-15
+
+
+@pytest.mark.parametrize("N,maxs", [(512, 64), (4096, 32), (16384, 64), (1 << 18, 64)])
+def test_plan_tables_match_oracle(lib, orc, N, maxs):
+    p = lib.Plan(N, maxs)
+    o = orc.Oracle(N, maxs, 2)
+    # Lambda table: identical arithmetic on both sides
+    assert np.array_equal(p.copy_table(2), o.lambda_table())
+    assert np.array_equal(p.copy_table(5), o.T())
+    for d in (0, 1):
+        A = p.copy_table(d).reshape(-1, 18, 18)
+        B = o.A(d).reshape(-1, 18, 18)
+        err = np.max(np.abs(A - B), axis=(1, 2)) / np.max(np.abs(B), axis=(1, 2))
+        assert err.max() < 1e-14
+
+
+@pytest.mark.parametrize("N", [257, 1023, 4097, 20001])
+def test_odd_N_l2c(lib, orc, N):
+    # the reference overruns its arrays here (leg2cheb.c:283-294); the oracle port
+    # and the extended-precision sum give the intended values
+    u = make_input(N, "uniform", N)
+    p = lib.Plan(N, 64)
+    out = np.zeros(N)
+    p.execute(u, out, 0)
+    assert relerr(out, orc.Oracle(N, 64, 2)(u, 0)[:N]) <= TOL
+    if N <= 5000:
+        assert direct_ld.rel_maxnorm(out, direct_ld.l2c_direct(u)) < 5e-15
+
+
+@pytest.mark.parametrize("N,maxs", [(1 << 20, 64), (1 << 20, 32), (1 << 21, 64), (1000003, 64)])
+@pytest.mark.parametrize("d", [0, 1])
+def test_large_single_vector_vs_oracle(lib, orc, N, maxs, d):
+    u = make_input(N, "sign", 17 + d)
+    if d == 0 and N % 2 == 1:
+        u = u.copy()
+    p = lib.Plan(N, maxs)
+    out = np.zeros(N)
+    flops = p.execute(u, out, d)
+    want = orc.Oracle(N, maxs, 2)(u, d)[:N]
+    assert relerr(out, want) <= TOL
+    assert flops == p.flops(d)
+
+
+@pytest.mark.parametrize("N", [1 << 20])
+def test_vs_extended_precision_sample(lib, N):
+    """Spot-check rows of a 2^20 transform against the extended-precision sum of
+    those rows (cost O(N) per row)."""
+    u = make_input(N, "sign", 99)
+    p = lib.Plan(N, 64)
+    out = np.zeros(N)
+    p.execute(u, out, 0)
+    a = direct_ld.lambda_table(N)
+    ul = u.astype(np.longdouble)
+    rows = [0, 1, 2, 777, N // 3, N // 2 + 1, N - 300, N - 2, N - 1]
+    for i in rows:
+        k = np.arange(0, (N - 1 - i) // 2 + 1)
+        val = np.sum(a[k] * a[k + i] * ul[i + 2 * k]) * 2 / direct_ld._PI
+        if i == 0:
+            val /= 2
+        assert abs(out[i] - float(val)) <= 2e-15 * np.max(np.abs(out))
+
+
+def test_device_pointers_match_host_path(lib, torch_cuda):
+    torch = torch_cuda
+    N = 1 << 16
+    u = make_input(N, "uniform", 5)
+    p = lib.Plan(N, 64)
+    for d in (0, 1):
+        host = np.zeros(N)
+        p.execute(u, host, d)
+        du = torch.from_numpy(u).cuda()
+        dout = torch.zeros(N, dtype=torch.float64, device="cuda")
+        p.execute(du, dout, d)
+        assert np.array_equal(dout.cpu().numpy(), host)
+
+
+def test_accumulates_into_output_like_reference(lib, orc):
+    # execute computes out = scale * (out_in + far + near) (leg2cheb.c:360-374, 519-532)
+    N = 4096
+    u = make_input(N, "uniform", 8)
+    pre = make_input(N, "gauss", 9)
+    p = lib.Plan(N, 64)
+    o = orc.Oracle(N, 64, 2)
+    for d in (0, 1):
+        out = pre.copy()
+        p.execute(u, out, d)
+        want = pre.copy()
+        o.execute(u, want, d)
+        assert relerr(out, want) <= TOL
+
+
+def test_batched_lines_of_3d_array(lib, orc):
+    # lines along the last axis of a 64x64x1024 array; a 8x8x1024 slab here
+    n0, n1, N = 8, 8, 1024
+    x = make_input(n0 * n1 * N, "gauss", 3).reshape(n0, n1, N) / (np.arange(N) + 1.0) ** 2
+    x = np.ascontiguousarray(x)
+    p = lib.Plan(N, 64)
+    o = orc.Oracle(N, 64, 2)
+    for d in (0, 1):
+        out = np.zeros_like(x)
+        flops = p.execute_batched(x, out, d, n0 * n1, N, 1)
+        assert flops == n0 * n1 * p.flops(d)
+        for i in (0, 17, 63):
+            line = x.reshape(-1, N)[i]
+            assert relerr(out.reshape(-1, N)[i], o(line, d)[:N]) <= TOL
+
+
+def test_batched_strided_axis0(lib, orc):
+    # lines along axis 0 of a (N, n1) array: dist = 1, stride = n1
+    N, n1 = 1000, 37
+    x = np.ascontiguousarray(make_input(N * n1, "uniform", 4).reshape(N, n1))
+    p = lib.Plan(N, 36)
+    o = orc.Oracle(N, 36, 2)
+    for d in (0, 1):
+        out = np.zeros_like(x)
+        p.execute_batched(x, out, d, n1, 1, n1)
+        for j in (0, 5, 36):
+            assert relerr(out[:, j], o(np.ascontiguousarray(x[:, j]), d)[:N]) <= TOL
+
+
+@pytest.mark.parametrize("axis", [0, 1, -1])
+def test_execute2d_matches_lines(lib, orc, axis):
+    # src/bin/l2c.c:297-351 (test_forward_2d) and 353-393 (round trip)
+    N0, N1 = 400, 402
+    x = np.ascontiguousarray(make_input(N0 * N1, "uniform", 12).reshape(N0, N1))
+    p2 = lib.Plan2D(N0, N1, axis, maxs=36)
+    out = np.zeros_like(x)
+    p2(x, out, 0)
+    o0, o1 = orc.Oracle(N0, 36, 2), orc.Oracle(N1, 36, 2)
+    if axis == 0:
+        want = np.stack([o0(np.ascontiguousarray(x[:, j]), 0)[:N0] for j in range(N1)], axis=1)
+    elif axis == 1:
+        want = np.stack([o1(x[i], 0)[:N1] for i in range(N0)])
+    else:
+        t = np.stack([o0(np.ascontiguousarray(x[:, j]), 0)[:N0] for j in range(N1)], axis=1)
+        want = np.stack([o1(np.ascontiguousarray(t[i]), 0)[:N1] for i in range(N0)])
+    assert relerr(out, want) <= 1e-13 if axis == -1 else relerr(out, want) <= TOL
+    if axis == -1:
+        back = np.zeros_like(x)
+        p2(out, back, 1)
+        assert np.sqrt(np.sum((back - x) ** 2)) < 1e-8  # src/bin/l2c.c:386-388
+
+
+def test_directM_directL_match_oracle_near_field(lib, orc):
+    # near field + final scaling only (leg2cheb.c:236-376, 378-535)
+    for N, st in ((2048, 1), (1000, 3)):
+        u = make_input(N * st, "uniform", 21)
+        p = lib.Plan(N, 64 if N == 2048 else 36)
+        o = orc.Oracle(N, 64 if N == 2048 else 36, 2)
+        out, want = np.zeros(N * st), np.zeros(N * st)
+        fm = p.directM(u, out, st)
+        assert fm == o.directM(u, want, st)
+        assert relerr(out, want) <= TOL
+        # directL takes the premultiplied contiguous input
+        v = u[: N * st : st] * np.arange(N)
+        v[:2] = u[: 2 * st : st]
+        v = np.ascontiguousarray(v)
+        out, want = np.zeros(N * st), np.zeros(N * st)
+        fl = p.directL(v, out, st)
+        assert fl == o.directL(v, want, st)
+        assert relerr(out, want) <= TOL
+
+
+def test_unplanned_direction_fails_cleanly(lib):
+    p = lib.Plan(4096, 64, direction=0)
+    out = np.zeros(4096)
+    with pytest.raises(lib.L2CError, match="not planned"):
+        p.execute(np.ones(4096), out, 1)
+    with pytest.raises(lib.L2CError):
+        p.execute(np.ones(4096), out, 3)
+
+
+def test_repeatable_bitwise(lib):
+    N = 1 << 18
+    u = make_input(N, "gauss", 1)
+    p = lib.Plan(N, 64)
+    r = []
+    for _ in range(3):
+        out = np.zeros(N)
+        p.execute(u, out, 0)
+        r.append(out)
+    assert np.array_equal(r[0], r[1]) and np.array_equal(r[1], r[2])
+
+
+@pytest.mark.parametrize("N", [1 << 22])
+def test_full_size_properties(lib, N):
+    """N = 2^22 (the mixed-precision single-vector size): linearity and the
+    L2C -> C2L round trip, size-independent properties of the exact transform."""
+    p = lib.Plan(N, 64)
+    u = make_input(N, "sign", 3)
+    v = make_input(N, "gauss", 4) / (np.arange(N) + 1.0)
+    fu, fv, fw = np.zeros(N), np.zeros(N), np.zeros(N)
+    p.execute(u, fu, 0)
+    p.execute(v, fv, 0)
+    p.execute(2.0 * u - 0.5 * v, fw, 0)
+    assert relerr(fw, 2.0 * fu - 0.5 * fv) < 1e-14
+    back = np.zeros(N)
+    p.execute(fu, back, 1)
+    assert relerr(back, u) < 1e-12
