@@ -17,6 +17,8 @@
 #ifndef LEG2CHEB_H
 #define LEG2CHEB_H
 
+#include <assert.h>
+#include <errno.h>
 #include <math.h>
 #include <stdbool.h>
 #include <stddef.h>
@@ -25,6 +27,10 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#if !defined(_WIN32)
+#include <sys/resource.h>
+#include <unistd.h>
+#endif
 
 /* The reference header pulls in FFTW and CBLAS, and its `l2c` driver relies on
  * that for its own FFTW/BLAS test modes.  The library itself needs neither. */
