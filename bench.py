@@ -68,7 +68,7 @@ def near_flops(N, s, direction):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -83,7 +83,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
@@ -219,12 +219,15 @@ def workload_config(N, maxs):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="single", choices=["single"])
     ap.add_argument("--N", type=int, default=1 << 20)
     ap.add_argument("--maxs", type=int, default=64)
+    ap.add_argument("--precompute", type=int, default=0,
+                    help="1: keep the near-field band weights in device memory (create_fmm's "
+                         "precompute argument)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
@@ -264,7 +267,7 @@ def main():
     abi = l2c.cuda_abi()
     N, maxs = args.N, args.maxs
     u = sign_decay_input(N, 1 + rank)
-    plan = l2c.Plan(N, maxs)
+    plan = l2c.Plan(N, maxs, precompute=args.precompute)
     stream = torch.cuda.ExternalStream(plan.stream, device=dev)
     du = torch.from_numpy(u).to(dev)
     douts = [torch.zeros(N, dtype=torch.float64, device=dev) for _ in range(2)]
@@ -364,7 +367,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded c_n = s_n/(n+1))",
-        "config": workload_config(N, maxs),
+        "config": dict(workload_config(N, maxs), precompute=args.precompute),
         "e2e": {"value": e2e_value, "unit": "coef/s", "h2d_bytes_per_step": 2 * 16 * N,
                 "d2h_bytes_per_step": 2 * 8 * N, "ms_per_step": e2e_step * 1e3},
         "gpu_launches": int(launches),

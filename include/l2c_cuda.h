@@ -21,7 +21,11 @@ extern "C" {
 typedef struct l2c_gpu_plan l2c_gpu_plan;
 
 /* Plan flags */
-#define L2C_PLAN_DIRECT_ONLY 1u /* O(N^2) direct sums whatever N (create_direct) */
+#define L2C_PLAN_DIRECT_ONLY 1u     /* O(N^2) direct sums whatever N (create_direct)  */
+#define L2C_PLAN_PRECOMPUTE_NEAR 2u /* keep the near-field band weights in device memory
+                                       (3s^2+s doubles per 2s coefficients and direction;
+                                       the reference's `precompute`, leg2cheb.c:1108-1193):
+                                       one FP64 FMA per band term instead of two ops */
 
 /* Execute flags */
 #define L2C_EXEC_ASYNC 1u       /* return without waiting (device pointers only)  */

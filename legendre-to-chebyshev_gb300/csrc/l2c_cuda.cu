@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -220,15 +221,35 @@ __global__ void k_gather(const double *__restrict__ in, double *__restrict__ x, 
 }
 
 // Near-field band, one output per thread.  For output j in block b = min(j/h, nL-1)
-// the band covers sources j + 2k < lim = min((b+2) h, N):
-//   L2C: sum_k (a[k] a[j+k]) x[j+2k]                               (leg2cheb.c:236-302)
-//   C2L: (sqrt(pi) x[j]) an[j] - sum_{k>=1} (dn[k] x[j+2k]) an[j+k] (leg2cheb.c:392-459)
-// y = out_in + band.
+// the band covers sources j + 2k < lim = min((b+2) h, N), with weight w(k, j):
+//   L2C: w = a[k] a[j+k]                                         (leg2cheb.c:236-302)
+//   C2L: w = sqrt(pi) an[j] (k = 0),  -(dn[k] an[j+k]) (k >= 1)  (leg2cheb.c:392-459)
+// and y = out_in + sum_k w(k, j) x[j+2k], accumulated by FMA from k = 0.
+// The weight is formed on the fly (one DMUL + one DFMA per term) or read from a
+// table built at plan time (one DFMA per term, same bits; see k_near_weights).
+__device__ __forceinline__ double near_weight(int c2l, long long k, long long j,
+                                              const double *__restrict__ a,
+                                              const double *__restrict__ an,
+                                              const double *__restrict__ dn) {
+  if (!c2l) return a[k] * a[j + k];
+  if (k == 0) return SQRT_PI * an[j];
+  return -(dn[k] * an[j + k]);
+}
+
+// Number of band terms of output position i of block b at source offset k
+// (the table layout of the precomputed weights, block-major, then k, then i).
+__device__ __forceinline__ long long band_count(long long k, long long b, const Geo &g) {
+  if (b < g.nL - 1) return k < g.s ? g.h : 2 * g.h - 2 * k;
+  const long long c = g.N - (g.nL - 1) * g.h - 2 * k;
+  return c > 0 ? c : 0;
+}
+
 __global__ void __launch_bounds__(256) k_near(const double *__restrict__ x, const double *out,
                                               double *__restrict__ y,
                                               const double *__restrict__ a,
                                               const double *__restrict__ an,
-                                              const double *__restrict__ dn, Geo g, int c2l) {
+                                              const double *__restrict__ dn,
+                                              const double *__restrict__ W, Geo g, int c2l) {
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= g.count * g.N) return;
   const long long v = idx / g.N, j = idx - v * g.N;
@@ -237,15 +258,48 @@ __global__ void __launch_bounds__(256) k_near(const double *__restrict__ x, cons
   long long lim = (b + 2) * g.h;
   if (lim > g.N) lim = g.N;
   const double *xv = x + v * g.N;
-  double acc;
-  if (!c2l) {
-    acc = 0.0;
-    for (long long k = 0; j + 2 * k < lim; k++) acc = fma(a[k] * a[j + k], xv[j + 2 * k], acc);
+  double acc = 0.0;
+  if (W == nullptr) {
+    for (long long k = 0; j + 2 * k < lim; k++)
+      acc = fma(near_weight(c2l, k, j, a, an, dn), xv[j + 2 * k], acc);
   } else {
-    acc = (SQRT_PI * xv[j]) * an[j];
-    for (long long k = 1; j + 2 * k < lim; k++) acc = fma(-(dn[k] * xv[j + 2 * k]), an[j + k], acc);
+    const long long i = j - b * g.h;
+    const double *Wb = W + b * (3 * g.s * g.s + g.s);
+    long long off = 0;
+    for (long long k = 0; j + 2 * k < lim; k++) {
+      acc = fma(Wb[off + i], xv[j + 2 * k], acc);
+      off += band_count(k, b, g);
+    }
   }
   y[idx] = out[v * g.dist + j * g.stride] + acc;
+}
+
+// Plan time: the band weights of every output, in the layout k_near reads.
+__global__ void k_near_weights(double *__restrict__ W, const double *__restrict__ a,
+                               const double *__restrict__ an, const double *__restrict__ dn,
+                               Geo g, int c2l) {
+  const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (j >= g.N) return;
+  long long b = j / g.h;
+  if (b > g.nL - 1) b = g.nL - 1;
+  long long lim = (b + 2) * g.h;
+  if (lim > g.N) lim = g.N;
+  const long long i = j - b * g.h;
+  double *Wb = W + b * (3 * g.s * g.s + g.s);
+  long long off = 0;
+  for (long long k = 0; j + 2 * k < lim; k++) {
+    Wb[off + i] = near_weight(c2l, k, j, a, an, dn);
+    off += band_count(k, b, g);
+  }
+}
+
+// Size of the weight table: (nL - 1) full blocks of 3 s^2 + s entries and the
+// last (ragged) block.
+inline size_t near_table_size(size_t N, size_t s) {
+  const size_t h = 2 * s, nL = N / h, rest = N - (nL - 1) * h;
+  size_t n = (nL - 1) * (3 * s * s + s);
+  for (size_t k = 0; 2 * k < rest; k++) n += rest - 2 * k;
+  return n;
 }
 
 // Step 1: leaf node t in [2, 2^(L+1)) of parity sg: w = sum_i x[t h + 2i + sg] T_sg[i][m].
@@ -435,6 +489,23 @@ struct l2c_gpu_plan {
   size_t cap_st_in = 0, cap_st_out = 0;
   size_t flops[2] = {0, 0};
   std::mutex mu;
+  // second stream for the near-field band, which runs beside the far-field chain
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  double *Wnear[2] = {nullptr, nullptr};  // precomputed band weights (optional)
+  // captured launch sequences, keyed by the call's shape and pointers
+  struct GraphEntry {
+    size_t dir, count, dist, stride;
+    const void *in;
+    void *out;
+    unsigned mode;
+    cudaGraphExec_t exec;
+    size_t launches;
+    size_t last_use;
+  };
+  std::vector<GraphEntry> graphs;
+  size_t use_clock = 0;
+  bool use_graphs = true;
   // launch accounting and optional per-phase CUDA-event timing
   size_t launches = 0;
   bool profiling = false;
@@ -510,19 +581,21 @@ struct PhaseScope {
   l2c_gpu_plan *p;
   int phase;
   cudaEvent_t e0 = nullptr;
-  PhaseScope(l2c_gpu_plan *pl, int ph, size_t nlaunch) : p(pl), phase(ph) {
+  cudaStream_t st;
+  PhaseScope(l2c_gpu_plan *pl, int ph, size_t nlaunch, cudaStream_t s_ = nullptr)
+      : p(pl), phase(ph), st(s_ ? s_ : pl->stream) {
     p->launches += nlaunch;
     p->phase_launches[ph] += nlaunch;
     if (p->profiling) {
       e0 = take_event(p);
-      if (e0) cudaEventRecord(e0, p->stream);
+      if (e0) cudaEventRecord(e0, st);
     }
   }
   ~PhaseScope() {
     if (!e0) return;
     cudaEvent_t e1 = take_event(p);
     if (!e1) return;
-    cudaEventRecord(e1, p->stream);
+    cudaEventRecord(e1, st);
     p->pending.push_back({phase, {e0, e1}});
   }
 };
@@ -539,8 +612,18 @@ void collect_profile(l2c_gpu_plan *p) {
   p->pending.clear();
 }
 
+// Captured graphs hold scratch and staging addresses: drop them whenever any
+// of those buffers is reallocated.
+void drop_graphs(l2c_gpu_plan *p) {
+  for (auto &g : p->graphs) cudaGraphExecDestroy(g.exec);
+  p->graphs.clear();
+}
+
 bool ensure_scratch(l2c_gpu_plan *p, size_t count) {
   if (count <= p->cap_vec) return true;
+  cudaStreamSynchronize(p->stream);
+  cudaStreamSynchronize(p->stream2);
+  drop_graphs(p);
   size_t c0 = p->cap_vec;
   size_t cx = c0 * p->N, cy = cx, cw = c0 * 2 * p->slots * M, cc = cw;
   const size_t need = count;
@@ -573,11 +656,7 @@ struct DeviceGuard {
   }
 };
 
-// Device-pointer execution of one batch.
-size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, size_t count,
-                  size_t dist, size_t stride, bool near_only, bool input_ready) {
-  cudaStream_t st = p->stream;
-  const int c2l = dir == 1;
+Geo make_geo(const l2c_gpu_plan *p, size_t count, size_t dist, size_t stride) {
   Geo g;
   g.N = (long long)p->N;
   g.s = (long long)p->s;
@@ -590,10 +669,18 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   g.count = (long long)count;
   g.dist = (long long)dist;
   g.stride = (long long)stride;
-  const long long total = g.count * g.N;
-  if (total == 0) return 1;
-  if (!ensure_scratch(p, count)) return 0;
+  return g;
+}
 
+// The launch sequence of one batch on device pointers (scratch already sized).
+// Near field on stream2 beside the far-field chain on stream; joined before the
+// final leaf-down kernel.
+size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, size_t count,
+                  size_t dist, size_t stride, bool near_only, bool input_ready) {
+  cudaStream_t st = p->stream, st2 = p->stream2;
+  const int c2l = dir == 1;
+  Geo g = make_geo(p, count, dist, stride);
+  const long long total = g.count * g.N;
   if (p->L == 0) {
     PhaseScope ps(p, L2C_PHASE_DIRECT, 1);
     k_direct<<<blocks_for(total, 256), 256, 0, st>>>(in, out, p->a, p->an, p->dn, g, c2l);
@@ -608,12 +695,14 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaGetLastError());
     x = p->x;
   }
-  {
-    PhaseScope ps(p, L2C_PHASE_NEAR, 1);
-    k_near<<<blocks_for(total, 256), 256, 0, st>>>(x, out, p->y, p->a, p->an, p->dn, g, c2l);
-    CK(cudaGetLastError());
-  }
+  const double *W = p->Wnear[dir];
   if (near_only) {
+    {
+      PhaseScope ps(p, L2C_PHASE_NEAR, 1);
+      k_near<<<blocks_for(total, 256), 256, 0, st>>>(x, out, p->y, p->a, p->an, p->dn, W, g,
+                                                     c2l);
+      CK(cudaGetLastError());
+    }
     Geo g0 = g;
     g0.K = 0;
     PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
@@ -621,20 +710,29 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaGetLastError());
     return 1;
   }
+  CK(cudaEventRecord(p->ev_fork, st));
+  CK(cudaStreamWaitEvent(st2, p->ev_fork, 0));
+  {
+    PhaseScope ps(p, L2C_PHASE_NEAR, 1, st2);
+    k_near<<<blocks_for(total, 256), 256, 0, st2>>>(x, out, p->y, p->a, p->an, p->dn, W, g, c2l);
+    CK(cudaGetLastError());
+  }
+  CK(cudaEventRecord(p->ev_join, st2));
   const long long leaf_threads = g.count * g.K * 2 * M;
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
     k_leaf_up<<<blocks_for(leaf_threads, 288), 288, 0, st>>>(x, p->T, p->w, g);
     CK(cudaGetLastError());
   }
-  PhaseScope *ps_up = new PhaseScope(p, L2C_PHASE_TREE_UP, p->L - 1);
-  for (long long l = (long long)p->L - 2; l >= 0; l--) {
-    const long long np = (long long)slots_at((size_t)l);
-    const long long n = g.count * 2 * np * M;
-    k_tree_up<<<blocks_for(n, 256), 256, 0, st>>>(p->w, g, 2 * (long long)blocks_before(l),
-                                                   2 * (long long)blocks_before(l + 1), np);
+  {
+    PhaseScope ps(p, L2C_PHASE_TREE_UP, p->L - 1);
+    for (long long l = (long long)p->L - 2; l >= 0; l--) {
+      const long long np = (long long)slots_at((size_t)l);
+      const long long n = g.count * 2 * np * M;
+      k_tree_up<<<blocks_for(n, 256), 256, 0, st>>>(p->w, g, 2 * (long long)blocks_before(l),
+                                                     2 * (long long)blocks_before(l + 1), np);
+    }
   }
-  delete ps_up;
   CK(cudaGetLastError());
   {
     PhaseScope ps(p, L2C_PHASE_FAR, 1);
@@ -652,11 +750,68 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     }
   }
   CK(cudaGetLastError());
+  CK(cudaStreamWaitEvent(st, p->ev_join, 0));
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
     k_leaf_down<<<blocks_for(total, 256), 256, 0, st>>>(p->c, p->T, p->y, out, g, c2l);
     CK(cudaGetLastError());
   }
+  return 1;
+}
+
+// Device-pointer execution of one batch: replay a captured graph of the launch
+// sequence when one exists for this call shape, else capture one (or launch
+// directly while per-phase profiling is on).
+size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, size_t count,
+                  size_t dist, size_t stride, bool near_only, bool input_ready) {
+  if (count == 0 || p->N == 0) return 1;
+  if (!ensure_scratch(p, count)) return 0;
+  const unsigned mode = (near_only ? 1u : 0u) | (input_ready ? 2u : 0u);
+  if (p->profiling || !p->use_graphs) {
+    return launch_all(p, in, out, dir, count, dist, stride, near_only, input_ready);
+  }
+  p->use_clock++;
+  for (auto &e : p->graphs) {
+    if (e.dir == dir && e.count == count && e.dist == dist && e.stride == stride && e.in == in &&
+        e.out == out && e.mode == mode) {
+      e.last_use = p->use_clock;
+      CK(cudaGraphLaunch(e.exec, p->stream));
+      p->launches += e.launches;
+      return 1;
+    }
+  }
+  const size_t before = p->launches;
+  CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+  const size_t ok = launch_all(p, in, out, dir, count, dist, stride, near_only, input_ready);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(p->stream, &graph);
+  if (!ok || ec != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    if (!ok) return 0;
+    set_err("stream capture failed: %s", cudaGetErrorString(ec));
+    return 0;
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) {
+    set_err("cudaGraphInstantiate failed: %s", cudaGetErrorString(ei));
+    return 0;
+  }
+  l2c_gpu_plan::GraphEntry e{dir, count, dist, stride, in, out, mode, exec,
+                             p->launches - before, p->use_clock};
+  if (p->graphs.size() >= 8) {
+    auto oldest = std::min_element(p->graphs.begin(), p->graphs.end(),
+                                   [](const l2c_gpu_plan::GraphEntry &a,
+                                      const l2c_gpu_plan::GraphEntry &b) {
+                                     return a.last_use < b.last_use;
+                                   });
+    cudaGraphExecDestroy(oldest->exec);
+    p->graphs.erase(oldest);
+  }
+  p->graphs.push_back(e);
+  CK(cudaGraphLaunch(exec, p->stream));
   return 1;
 }
 
@@ -709,6 +864,10 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   p->dirs = directions;
   PCK(cudaGetDevice(&p->device));
   PCK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  PCK(cudaStreamCreateWithFlags(&p->stream2, cudaStreamNonBlocking));
+  PCK(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+  PCK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
+  if (const char *env = std::getenv("L2C_NO_GRAPHS")) p->use_graphs = env[0] == '0';
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
     p->Nn = N;
@@ -769,6 +928,17 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cudaFree(f0);
     PCK(e);
+    if (flags & L2C_PLAN_PRECOMPUTE_NEAR) {
+      const size_t nw = near_table_size(N, s);
+      Geo g = make_geo(p, 1, N, 1);
+      for (int d = 0; d < 2; d++) {
+        if (!(directions == (size_t)d || directions == 2)) continue;
+        PCK(cudaMalloc(&p->Wnear[d], nw * sizeof(double)));
+        k_near_weights<<<blocks_for((long long)N, 256), 256, 0, st>>>(p->Wnear[d], p->a, p->an,
+                                                                       p->dn, g, d);
+        PCK(cudaGetLastError());
+      }
+    }
   }
   PCK(cudaStreamSynchronize(st));
   for (size_t d = 0; d < 2; d++)
@@ -781,10 +951,15 @@ void l2c_gpu_plan_destroy(l2c_gpu_plan *p) {
   if (!p) return;
   DeviceGuard dg(p->device);
   if (p->stream) cudaStreamSynchronize(p->stream);
+  if (p->stream2) cudaStreamSynchronize(p->stream2);
   collect_profile(p);
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
+  drop_graphs(p);
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  if (p->ev_join) cudaEventDestroy(p->ev_join);
+  if (p->stream2) cudaStreamDestroy(p->stream2);
   double *bufs[] = {p->a, p->an, p->dn, p->A[0], p->A[1], p->T, p->x, p->y, p->w, p->c,
-                    p->st_in, p->st_out};
+                    p->st_in, p->st_out, p->Wnear[0], p->Wnear[1]};
   for (double *b : bufs)
     if (b) cudaFree(b);
   if (p->stream) cudaStreamDestroy(p->stream);
@@ -858,6 +1033,10 @@ size_t l2c_gpu_execute(l2c_gpu_plan *p, const double *in, double *out, size_t di
   if (!in_dev || !out_dev) {
     // host memory: stage the touched span (the layout is kept, so the kernels
     // see the same dist/stride)
+    if ((!in_dev && in_span > p->cap_st_in) || (!out_dev && span > p->cap_st_out)) {
+      CK(cudaStreamSynchronize(p->stream));
+      drop_graphs(p);
+    }
     if (!in_dev && !grow(&p->st_in, &p->cap_st_in, in_span)) return 0;
     if (!out_dev && !grow(&p->st_out, &p->cap_st_out, span)) return 0;
     if (!in_dev)

@@ -290,7 +290,8 @@ fmm_plan *create_fmm(const size_t N, const size_t maxs, const size_t M, const si
   p->N = N;
   size_t s = 0, Nn = N;
   const size_t L = l2c_geometry(N, maxs, &s, &Nn);
-  l2c_gpu_plan *gp = l2c_gpu_plan_create(N, maxs, direction, 0);
+  l2c_gpu_plan *gp =
+      l2c_gpu_plan_create(N, maxs, direction, precompute ? L2C_PLAN_PRECOMPUTE_NEAR : 0);
   if (!gp) {
     free(p->A);
     free(p);

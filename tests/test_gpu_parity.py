@@ -253,3 +253,49 @@ def test_full_size_properties(lib, N):
     back = np.zeros(N)
     p.execute(fu, back, 1)
     assert relerr(back, u) < 1e-12
+
+
+@pytest.mark.parametrize("N,maxs", [(4096, 64), (5001, 64), (1 << 20, 32), (300, 64)])
+def test_precomputed_band_weights_bitwise(lib, N, maxs):
+    # create_fmm's precompute = 1 keeps the band weights in device memory; the
+    # weights are the same products, so results are bit-identical
+    u = make_input(N, "uniform", N + 1)
+    p0 = lib.Plan(N, maxs)
+    p1 = lib.Plan(N, maxs, precompute=1)
+    for d in (0, 1):
+        o0, o1 = np.zeros(N), np.zeros(N)
+        p0.execute(u, o0, d)
+        p1.execute(u, o1, d)
+        assert np.array_equal(o0, o1)
+
+
+def test_graph_cache_across_shapes(lib, orc):
+    # captured launch sequences are cached per call shape; growing the scratch
+    # buffers must invalidate them
+    N = 1024
+    p = lib.Plan(N, 64)
+    o = orc.Oracle(N, 64, 2)
+    rng = np.random.default_rng(0)
+    for count in (1, 4, 1, 64, 4, 1, 256, 64):
+        x = rng.uniform(-1, 1, (count, N))
+        for d in (0, 1):
+            out = np.zeros_like(x)
+            p.execute_batched(x, out, d, count, N, 1)
+            for i in {0, count - 1}:
+                assert relerr(out[i], o(x[i], d)[:N]) <= TOL
+
+
+def test_async_device_execution(lib, orc, torch_cuda):
+    torch = torch_cuda
+    N, count = 16384, 8
+    x = make_input(N * count, "sign", 5).reshape(count, N)
+    p = lib.Plan(N, 64)
+    dx = torch.from_numpy(x).cuda()
+    outs = [torch.zeros_like(dx) for _ in range(3)]
+    for o_ in outs:
+        p.execute_async(dx, o_, 0, count, N, 1)
+    p.synchronize()
+    o = orc.Oracle(N, 64, 2)
+    want = o(x[3], 0)[:N]
+    for o_ in outs:
+        assert relerr(o_.cpu().numpy()[3], want) <= TOL
