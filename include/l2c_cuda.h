@@ -88,6 +88,26 @@ int l2c_gpu_profile_read(l2c_gpu_plan *plan, double *ms, size_t *launches);
  * Returns the number of doubles copied (n_max caps it), 0 if absent. */
 size_t l2c_gpu_plan_copy(const l2c_gpu_plan *plan, int which, double *dst, size_t n_max);
 
+/* One transform that allocates no device memory (no counterpart in the
+ * reference).  For callers that cannot allocate at transform time -- an
+ * application that reserves the device for its own memory pool, a solver that
+ * must not risk allocation latency or failure inside a time step.  Same
+ * kernels and results as l2c_gpu_execute (count = 1), but the working buffers
+ * live in a fixed array of L2C_NOALLOC_SCRATCH_DOUBLES doubles (4 MiB) that
+ * every GPU loading this library holds until the process exits; the plan's own
+ * tables are built beforehand by l2c_gpu_plan_create, as set-up.
+ *   - in and out must be device pointers; FMM plans only (L >= 1).
+ *   - a plan needing more than the fixed array (2N + 144 N_b doubles; e.g.
+ *     N up to about 1.2e5 at maxs = 64) is rejected with an error message.
+ *   - the first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress), so make that first call before any stream capture.
+ *   - calls on one device are serialised and return after the work has
+ *     finished, since all of them share the array.
+ * Returns the reference's flop count, 0 on failure (l2c_gpu_last_error()). */
+#define L2C_NOALLOC_SCRATCH_DOUBLES (1u << 19)
+size_t l2c_gpu_execute_noalloc(l2c_gpu_plan *plan, const double *in, double *out,
+                               size_t direction, size_t stride);
+
 /* Lambda(z) and Lambda at integer z, host side, bit-identical to the device. */
 double l2c_lambda(double z);
 double l2c_lambda_int(size_t z);

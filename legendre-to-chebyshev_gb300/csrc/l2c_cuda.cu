@@ -1135,3 +1135,130 @@ const char *l2c_gpu_last_error(void) { return g_err; }
 const char *l2c_gpu_version(void) { return "l2c-gb300 0.1 (sm_103a, fp64)"; }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Execution without any device allocation.
+//
+// Some callers cannot allocate device memory at the moment they transform:
+// applications that reserve the whole device up front for their own memory
+// pool, long-running solvers that must not pay allocation latency or risk an
+// allocation failure inside a time step, and hosts that hand a library only
+// pre-sized buffers.  l2c_gpu_execute_noalloc serves them.  It runs the same
+// kernels as l2c_gpu_execute on device pointers, but its working buffers
+// (gathered input, near-field partial sums, the two coefficient trees) live in
+// the fixed array below instead of the plan's grown-on-demand scratch.  It calls
+// no cudaMalloc, cudaFree or other allocating routine.
+//
+// The array is a file-scope __device__ object: every GPU on which this library
+// is loaded holds it (L2C_NOALLOC_SCRATCH_DOUBLES doubles, 4 MiB) until the
+// process exits.  Host code may not take its name as a device address; the
+// device address is looked up once per device with cudaGetSymbolAddress.
+// ---------------------------------------------------------------------------
+namespace {
+
+static __device__ __align__(256) double g_noalloc_scratch[L2C_NOALLOC_SCRATCH_DOUBLES];
+
+constexpr int kMaxDevices = 64;
+double *g_noalloc_ptr[kMaxDevices] = {nullptr};
+std::mutex g_noalloc_mu;
+std::mutex g_noalloc_call_mu[kMaxDevices];  // one call at a time per device
+
+// Doubles of scratch one transform needs: x and y (N each), w and c (2 parities
+// x 2 N_b slots x 18 each).
+size_t noalloc_need(const l2c_gpu_plan *p) { return 2 * p->N + 2 * (2 * p->slots * M); }
+
+// Device address of the fixed scratch array on the current device (looked up on
+// the first call per device).
+double *noalloc_scratch_address(int dev) {
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_err("device index %d out of range for the fixed scratch table", dev);
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || ptr == nullptr) {
+      set_err("cudaGetSymbolAddress of the fixed scratch array failed: %s",
+              cudaGetErrorString(e));
+      return nullptr;
+    }
+    g_noalloc_ptr[dev] = static_cast<double *>(ptr);
+  }
+  return g_noalloc_ptr[dev];
+}
+
+}  // namespace
+
+
+extern "C" size_t l2c_gpu_execute_noalloc(l2c_gpu_plan *p, const double *in, double *out,
+                                          size_t dir, size_t stride) {
+  g_err[0] = 0;
+  if (!p || !in || !out) {
+    set_err("null plan or array");
+    return 0;
+  }
+  if (dir > 1 || !(p->dirs == dir || p->dirs == 2)) {
+    set_err("direction %zu was not planned", dir);
+    return 0;
+  }
+  if (p->L == 0) {
+    set_err("l2c_gpu_execute_noalloc needs an FMM plan (L >= 1)");
+    return 0;
+  }
+  if (stride == 0) stride = 1;
+  const size_t need = noalloc_need(p);
+  if (need > (size_t)L2C_NOALLOC_SCRATCH_DOUBLES) {
+    set_err("plan needs %zu scratch doubles; the fixed array holds %zu (N = %zu is too large "
+            "for l2c_gpu_execute_noalloc; use l2c_gpu_execute)",
+            need, (size_t)L2C_NOALLOC_SCRATCH_DOUBLES, p->N);
+    return 0;
+  }
+  if (!is_device_ptr(in) || !is_device_ptr(out)) {
+    set_err("l2c_gpu_execute_noalloc takes device pointers only (staging host arrays would "
+            "need device buffers)");
+    return 0;
+  }
+  if (p->device < 0 || p->device >= kMaxDevices) {
+    set_err("device index %d out of range", p->device);
+    return 0;
+  }
+  // The fixed array is shared by every call in this process on this device: the
+  // per-device lock, held until the work below has finished on the GPU, keeps
+  // calls from overlapping (overlapping calls would race on the array).
+  std::lock_guard<std::mutex> call_lock(g_noalloc_call_mu[p->device]);
+  std::lock_guard<std::mutex> lock(p->mu);
+  DeviceGuard dg(p->device);
+  double *base = noalloc_scratch_address(p->device);
+  if (!base) return 0;
+  // every scratch element below is written before it is read within one call
+  // (gather fills x, the band fills y, the leaf and upward kernels fill all of
+  // w, the far-field kernel fills all of c), so nothing needs clearing
+  double *x = base, *y = base + p->N;
+  double *w = y + p->N, *c = w + 2 * p->slots * M;
+  cudaStream_t st = p->stream;
+  const int c2l = dir == 1;
+  Geo g = make_geo(p, 1, p->N, stride);
+  const long long total = g.N;
+  k_gather<<<blocks_for(total, 256), 256, 0, st>>>(in, x, g, c2l);
+  k_near<<<blocks_for(total, 256), 256, 0, st>>>(x, out, y, p->a, p->an, p->dn, p->Wnear[dir],
+                                                 g, c2l);
+  k_leaf_up<<<blocks_for(g.K * 2 * M, 288), 288, 0, st>>>(x, p->T, w, g);
+  for (long long l = (long long)p->L - 2; l >= 0; l--) {
+    const long long np = (long long)slots_at((size_t)l);
+    k_tree_up<<<blocks_for(2 * np * M, 256), 256, 0, st>>>(w, g, 2 * (long long)blocks_before(l),
+                                                            2 * (long long)blocks_before(l + 1),
+                                                            np);
+  }
+  k_far<<<blocks_for(2 * (long long)p->Nb * M, 256), 256, 0, st>>>(p->A[dir], w, c, g,
+                                                                   (long long)p->Nb);
+  for (long long l = 0; l + 1 < (long long)p->L; l++) {
+    const long long np = (long long)slots_at((size_t)l);
+    k_tree_down<<<blocks_for(2 * np * M, 256), 256, 0, st>>>(
+        c, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
+  }
+  k_leaf_down<<<blocks_for(total, 256), 256, 0, st>>>(c, p->T, y, out, g, c2l);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  return p->flops[dir];
+}
