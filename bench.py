@@ -48,6 +48,12 @@ def sign_decay_input(N, seed):
     return rng.choice([-1.0, 1.0], N) / (np.arange(N, dtype=np.float64) + 1.0)
 
 
+def gauss2_lines(count, N, seed):
+    """Lines of a 64x64x1024-style array: iid N(0,1) times (n+1)^-2 along the line."""
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal((count, N)) / (np.arange(N, dtype=np.float64) + 1.0) ** 2
+
+
 def near_flops(N, s, direction):
     """Reference flop count of the near-field band (directM / directL)."""
     h = 2 * s
@@ -140,80 +146,144 @@ def measured_fp64_peak(torch, dev):
     return best
 
 
-def cpu_run(N, maxs, u, seconds, threads):
-    """Oracle port: L2C + C2L of u repeatedly for about `seconds`; returns
-    (coefficients per second, outputs, reps)."""
+def ragged_lengths(count, seed, lo=64, hi=65536):
+    """N log-uniform in [lo, hi], seeded."""
+    rng = np.random.default_rng(seed)
+    return np.round(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(np.int64)
+
+
+def workload_config(N, maxs, workload="single", count=1, total=None):
+    if workload == "ragged":
+        return {"workload": f"ragged list: {count} vectors, N log-uniform in [64, 65536] (seeded), "
+                            f"{total} coefficients in total, iid U[-1,1]; L2C and C2L, "
+                            f"maxs={maxs}, plain FP64, one set of launches per direction",
+                "vectors": count, "total_coefficients": total, "maxs": maxs,
+                "precision": "fp64", "l2_flush": "256 MiB write between steps",
+                "transforms_per_step": 2 * count}
+    L = math.ceil(math.log2(N / maxs)) - 2
+    s = math.ceil(N / 2 ** (L + 2)) if L >= 1 else 0
+    if workload == "batch":
+        desc = (f"batched lines: {count} transforms of N={N} along the last axis of a "
+                f"64x64x{N} float64 array (dist={N}, stride=1), x = N(0,1)(n+1)^-2; "
+                f"L2C then C2L of the result, maxs={maxs} (s={s}, L={L}), plain FP64")
+    else:
+        desc = (f"single vector L2C + C2L, N={N}, maxs={maxs} (s={s}, L={L}), "
+                "c_n = s_n/(n+1), plain FP64")
+    return {"workload": desc, "N": N, "maxs": maxs, "s": s, "L": L, "vectors": count,
+            "precision": "fp64", "l2_flush": "256 MiB write between steps",
+            "transforms_per_step": 2 * count}
+
+
+class Workload:
+    """A step: a list of transforms (direction, input, output) on one plan."""
+
+    def __init__(self, name, N, maxs, seed):
+        self.name, self.N, self.maxs = name, N, maxs
+        if name == "single":
+            self.count = 1
+            self.u = sign_decay_input(N, seed)[None, :]
+            # L2C and C2L of the same vector
+            self.calls = [(0, "u", "o0"), (1, "u", "o1")]
+        elif name == "batch":
+            self.count = 4096
+            self.u = gauss2_lines(self.count, N, seed)
+            # L2C of every line, then C2L of the result
+            self.calls = [(0, "u", "o0"), (1, "o0", "o1")]
+        elif name == "ragged":
+            self.Ns = ragged_lengths(2000, seed)
+            self.count = len(self.Ns)
+            self.total = int(self.Ns.sum())
+            rng = np.random.default_rng(seed + 1)
+            self.u = rng.uniform(-1.0, 1.0, self.total)[None, :]
+            self.calls = [(0, "u", "o0"), (1, "u", "o1")]
+            self.coefs_per_step = 2 * self.total
+            return
+        else:
+            raise ValueError(name)
+        self.coefs_per_step = 2 * self.count * N
+
+    def config(self):
+        return workload_config(self.N, self.maxs, self.name, self.count,
+                               getattr(self, "total", None))
+
+    def cpu_oracle(self, oracle):
+        if self.name == "ragged":
+            return oracle.RaggedOracle(self.Ns, self.maxs, 2)
+        return oracle.Oracle(self.N, self.maxs, 2)
+
+    def cpu_call(self, o, src, dst, d):
+        if self.name == "ragged":
+            o.execute(src[0], dst[0], d)
+        elif self.count == 1:
+            o.execute(src[0], dst[0], d)
+        else:
+            o.execute_batch(src, dst, d, self.count, self.N)
+
+
+def cpu_run(wl, seconds, threads):
+    """Oracle port on all host cores: the workload's step repeated for about
+    `seconds`; returns (coefficients per second, outputs, reps)."""
     sys.path.insert(0, REPO)
     from oracle import oracle
 
     oracle.set_threads(threads)
-    o = oracle.Oracle(N, maxs, 2)
-    outs = [np.zeros(N), np.zeros(N)]
+    o = wl.cpu_oracle(oracle)
+    bufs = {"u": np.ascontiguousarray(wl.u), "o0": np.zeros_like(wl.u), "o1": np.zeros_like(wl.u)}
     times = []
     t_start = time.perf_counter()
     while True:
-        for d in (0, 1):
-            outs[d][:] = 0
+        bufs["o0"][:] = 0
+        bufs["o1"][:] = 0
         t0 = time.perf_counter()
-        o.execute(u, outs[0], 0)
-        o.execute(u, outs[1], 1)
+        for d, src, dst in wl.calls:
+            wl.cpu_call(o, bufs[src], bufs[dst], d)
         times.append(time.perf_counter() - t0)
         if time.perf_counter() - t_start > seconds and len(times) >= 2:
             break
-    return 2 * N / statistics.median(times), outs, len(times)
+    return wl.coefs_per_step / statistics.median(times), bufs, len(times)
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    N, maxs = args.N, args.maxs
-    u = sign_decay_input(N, 1)
+    wl = Workload(args.workload, args.N, args.maxs, 1)
     threads = os.cpu_count() or 1
     sys.path.insert(0, REPO)
     from oracle import oracle
 
     oracle.set_threads(threads)
-    o = oracle.Oracle(N, maxs, 2)
-    outs = [np.zeros(N), np.zeros(N)]
-    for _ in range(args.warmup):
-        o.execute(u, outs[0], 0)
-        o.execute(u, outs[1], 1)
-    times = []
-    for _ in range(args.steps):
-        outs[0][:] = 0
-        outs[1][:] = 0
+    o = wl.cpu_oracle(oracle)
+    bufs = {"u": np.ascontiguousarray(wl.u), "o0": np.zeros_like(wl.u), "o1": np.zeros_like(wl.u)}
+
+    def step():
+        bufs["o0"][:] = 0
+        bufs["o1"][:] = 0
         t0 = time.perf_counter()
-        o.execute(u, outs[0], 0)
-        o.execute(u, outs[1], 1)
-        times.append(time.perf_counter() - t0)
+        for d, src, dst in wl.calls:
+            wl.cpu_call(o, bufs[src], bufs[dst], d)
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        step()
+    times = [step() for _ in range(args.steps)]
     t = sum(times) / len(times)
-    value = 2 * N / t
+    value = wl.coefs_per_step / t
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "coef/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload_config(N, maxs),
+        "config": wl.config(),
         "cpu_baseline": {"value": value, "unit": "coef/s", "cores": threads, "kind": "port",
-                         "sample": f"full workload: L2C + C2L of one N={N} vector per step, "
+                         "sample": f"full workload per step ({wl.coefs_per_step} coefficients), "
                                    f"{args.steps} steps; oracle port of the reference algorithm "
-                                   "(its sources are not on this machine)"},
+                                   "with OpenMP (the reference sources are not on this machine)"},
         "e2e": {"value": value, "unit": "coef/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
-
-
-def workload_config(N, maxs):
-    sys.path.insert(0, PKG)
-    L = math.ceil(math.log2(N / maxs)) - 2
-    s = math.ceil(N / 2 ** (L + 2)) if L >= 1 else 0
-    return {"workload": f"single vector L2C + C2L, N={N}, maxs={maxs} (s={s}, L={L}), "
-                        "c_n = s_n/(n+1), plain FP64",
-            "N": N, "maxs": maxs, "s": s, "L": L, "precision": "fp64",
-            "l2_flush": "256 MiB write between steps", "vectors_per_step": 2}
 
 
 def main():
@@ -222,8 +292,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="single", choices=["single"])
-    ap.add_argument("--N", type=int, default=1 << 20)
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "ragged"])
+    ap.add_argument("--N", type=int, default=None)
     ap.add_argument("--maxs", type=int, default=64)
     ap.add_argument("--precompute", type=int, default=0,
                     help="1: keep the near-field band weights in device memory (create_fmm's "
@@ -232,6 +302,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.N is None:
+        args.N = 1 << 20 if args.workload == "single" else 1024
     if args.impl == "reference":
         return run_reference(args)
 
@@ -253,6 +325,15 @@ def main():
 
             dist.barrier()
 
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        import torch.distributed as dist
+
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
     sys.path.insert(0, PKG)
     import importlib.util
 
@@ -262,27 +343,37 @@ def main():
     if rank == 0:
         bmod.build()
     barrier()
+    import ctypes
+
     import l2c_gb300 as l2c
 
     abi = l2c.cuda_abi()
-    N, maxs = args.N, args.maxs
-    u = sign_decay_input(N, 1 + rank)
-    plan = l2c.Plan(N, maxs, precompute=args.precompute)
+    wl = Workload(args.workload, args.N, args.maxs, 1 + rank)
+    N, maxs, count = wl.N, wl.maxs, wl.count
+    ragged = wl.name == "ragged"
+    if ragged:
+        plan = l2c.RaggedPlan(wl.Ns, maxs)
+    else:
+        plan = l2c.Plan(N, maxs, precompute=args.precompute)
     stream = torch.cuda.ExternalStream(plan.stream, device=dev)
-    du = torch.from_numpy(u).to(dev)
-    douts = [torch.zeros(N, dtype=torch.float64, device=dev) for _ in range(2)]
+    dbuf = {"u": torch.from_numpy(np.ascontiguousarray(wl.u)).to(dev)}
+    dbuf["o0"] = torch.zeros_like(dbuf["u"])
+    dbuf["o1"] = torch.zeros_like(dbuf["u"])
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     peak = measured_fp64_peak(torch, dev)
 
     def step():
         with torch.cuda.stream(stream):
             flush.fill_(1)
-            douts[0].zero_()
-            douts[1].zero_()
+            dbuf["o0"].zero_()
+            dbuf["o1"].zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        plan.execute_async(du, douts[0], 0)
-        plan.execute_async(du, douts[1], 1)
+        for d, src, dst in wl.calls:
+            if ragged:
+                plan.execute_async(dbuf[src], dbuf[dst], d)
+            else:
+                plan.execute_async(dbuf[src], dbuf[dst], d, count, N, 1)
         e1.record(stream)
         return e0, e1
 
@@ -291,9 +382,12 @@ def main():
     plan.synchronize()
     torch.cuda.synchronize()
 
-    # ---- timed region (device resident) ----
-    abi.l2c_gpu_profile(plan._gpu, 1)
-    launches0 = abi.l2c_gpu_launch_count(plan._gpu)
+    # ---- timed region (device resident), per-phase CUDA events on ----
+    if not ragged:
+        abi.l2c_gpu_profile(plan._gpu, 1)
+        launches0 = abi.l2c_gpu_launch_count(plan._gpu)
+    else:
+        launches0 = plan.launch_count()
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
@@ -305,91 +399,106 @@ def main():
     barrier()
     t_wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
-    launches = abi.l2c_gpu_launch_count(plan._gpu) - launches0
-    ms = [a.elapsed_time(b) for a, b in evs]
-    ms_step = sum(ms) / len(ms)
-    import ctypes
+    ms_step = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+    phases = {}
+    if not ragged:
+        launches = abi.l2c_gpu_launch_count(plan._gpu) - launches0
+        pms = (ctypes.c_double * 8)()
+        pl = (ctypes.c_size_t * 8)()
+        abi.l2c_gpu_profile_read(plan._gpu, pms, pl)
+        abi.l2c_gpu_profile(plan._gpu, 0)
+        names = ["gather", "near", "leaf_up", "tree_up", "far", "tree_down", "leaf_down", "direct"]
+        phases = {names[i]: {"ms_per_step": pms[i] / args.steps,
+                             "launches_per_step": pl[i] / args.steps} for i in range(8) if pl[i]}
+    else:
+        launches = plan.launch_count() - launches0
+    ms_step = max_over_ranks(ms_step)
+    value = wl.coefs_per_step * world / (ms_step * 1e-3)
 
-    pms = (ctypes.c_double * 8)()
-    pl = (ctypes.c_size_t * 8)()
-    abi.l2c_gpu_profile_read(plan._gpu, pms, pl)
-    abi.l2c_gpu_profile(plan._gpu, 0)
-    names = ["gather", "near", "leaf_up", "tree_up", "far", "tree_down", "leaf_down", "direct"]
-    phases = {names[i]: {"ms_per_step": pms[i] / args.steps, "launches_per_step": pl[i] / args.steps}
-              for i in range(8) if pl[i]}
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms_step], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = 2 * N * world / (ms_step * 1e-3)
+    # ---- graph-replay timing without per-phase events (reported beside value) ----
+    evs = [step() for _ in range(args.steps)]
+    plan.synchronize()
+    ms_graph = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / len(evs))
 
     # ---- e2e through execute() with pinned host buffers ----
-    hin = torch.from_numpy(u).pin_memory()
-    houts = [torch.zeros(N, dtype=torch.float64).pin_memory() for _ in range(2)]
+    hbuf = {"u": torch.from_numpy(np.ascontiguousarray(wl.u)).pin_memory()}
+    hbuf["o0"] = torch.zeros(wl.u.shape, dtype=torch.float64).pin_memory()
+    hbuf["o1"] = torch.zeros(wl.u.shape, dtype=torch.float64).pin_memory()
     e2e_t = []
-    for it in range(args.warmup + args.steps):
-        for h in houts:
-            h.zero_()
+    for it in range(args.warmup + min(args.steps, 50)):
+        hbuf["o0"].zero_()
+        hbuf["o1"].zero_()
         t0 = time.perf_counter()
-        plan.execute(hin, houts[0], 0)
-        plan.execute(hin, houts[1], 1)
+        for d, src, dst in wl.calls:
+            if ragged:
+                plan(hbuf[src], hbuf[dst], d)
+            else:
+                plan.execute_batched(hbuf[src], hbuf[dst], d, count, N, 1)
         dt = time.perf_counter() - t0
         if it >= args.warmup:
             e2e_t.append(dt)
-    e2e_step = sum(e2e_t) / len(e2e_t)
-    if world > 1:
-        import torch.distributed as dist
+    e2e_step = max_over_ranks(sum(e2e_t) / len(e2e_t))
+    e2e_value = wl.coefs_per_step * world / e2e_step
+    nbytes = 8 * wl.u.size
 
-        t = torch.tensor([e2e_step], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step = float(t.item())
-    e2e_value = 2 * N * world / e2e_step
-
-    # ---- roofline of the dominant kernel ----
-    dom = max(phases, key=lambda k: phases[k]["ms_per_step"])
-    L, s, _ = l2c.geometry(N, maxs)
+    # ---- roofline of the band kernel (the dominant FP64 kernel) ----
+    L, s, _ = l2c.geometry(N, maxs) if not ragged else (None, None, None)
     roof = None
-    if dom == "near":
-        flops_per_launch = (near_flops(N, s, 0) + near_flops(N, s, 1)) / 2.0
+    if ragged:
+        total_flops = sum(plan.flops(d) for d, _, _ in wl.calls)
+        achieved = total_flops / (ms_step * 1e-3) / 1e12
+        roof = {"bound": "tensor", "pipe": "fp64", "kernel": "whole step (all ragged kernels)",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": None,
+                "peak_source": "FP64 DGEMM measured in this run (cuBLAS float64 matmul 4096^3)"}
+    if "near" in phases and L >= 1:
+        nf = sum(near_flops(N, s, d) for d, _, _ in wl.calls) * count / len(wl.calls)
+        launches_near = phases["near"]["launches_per_step"] / len(wl.calls)
         avg_ms = phases["near"]["ms_per_step"] / phases["near"]["launches_per_step"]
+        flops_per_launch = nf / launches_near
         achieved = flops_per_launch / (avg_ms * 1e-3) / 1e12
         roof = {"bound": "tensor", "pipe": "fp64", "kernel": "k_near (near-field band)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": None,
                 "peak_source": "FP64 DGEMM measured in this run (cuBLAS float64 matmul 4096^3)",
-                "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_ms}
-    total_flops = plan.flops(0) + plan.flops(1)
+                "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_ms,
+                "note": "reference flop count of directM/directL (3 per band term); a term "
+                        "costs 2 FP64 issue slots (DMUL+DFMA) unless precompute=1"}
+    if not ragged:
+        total_flops = sum(plan.flops(d) for d, _, _ in wl.calls) * count
 
     line = {
         "metric": METRIC, "value": value, "unit": "coef/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded c_n = s_n/(n+1))",
-        "config": dict(workload_config(N, maxs), precompute=args.precompute),
-        "e2e": {"value": e2e_value, "unit": "coef/s", "h2d_bytes_per_step": 2 * 16 * N,
-                "d2h_bytes_per_step": 2 * 8 * N, "ms_per_step": e2e_step * 1e3},
+        "data": "synthetic (seeded)",
+        "config": dict(wl.config(), precompute=args.precompute),
+        "e2e": {"value": e2e_value, "unit": "coef/s",
+                "h2d_bytes_per_step": len(wl.calls) * 2 * nbytes,
+                "d2h_bytes_per_step": len(wl.calls) * nbytes, "ms_per_step": e2e_step * 1e3},
         "gpu_launches": int(launches),
         "clocks": clk,
         "roofline": roof,
         "phases": phases,
-        "fp64_tflops_whole_step": total_flops / (ms_step * 1e-3) / 1e12,
+        "ms_per_step_graph_replay": ms_graph,
+        "fp64_ref_tflops_whole_step": total_flops / (ms_step * 1e-3) / 1e12,
         "wall_s_timed_region": t_wall,
-        "plan": {"L": L, "s": s, "Nb": plan.Nb},
+        "plan": {"L": L, "s": s, "Nb": plan.Nb} if not ragged else {"vectors": count},
     }
+    got = {k: dbuf[k].cpu().numpy() for k in ("o0", "o1")}
+    if wl.name == "batch":
+        line["roundtrip_rel_err"] = float(np.max(np.abs(got["o1"] - wl.u)) / np.max(np.abs(wl.u)))
 
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        cpu_value, outs, reps = cpu_run(N, maxs, u, args.cpu_seconds, threads)
+        cpu_value, outs, reps = cpu_run(wl, args.cpu_seconds, threads)
         line["cpu_baseline"] = {
             "value": cpu_value, "unit": "coef/s", "cores": threads, "kind": "port",
-            "sample": f"{reps} repetitions of the full step (L2C + C2L, N={N}), median; "
-                      "oracle port of the reference algorithm with OpenMP"}
-        got = [douts[0].cpu().numpy(), douts[1].cpu().numpy()]
+            "sample": f"{reps} repetitions of the full step ({wl.coefs_per_step} coefficients), "
+                      "median; oracle port of the reference algorithm with OpenMP"}
         line["max_rel_err_vs_oracle"] = {
-            "l2c": float(np.max(np.abs(got[0] - outs[0])) / np.max(np.abs(outs[0]))),
-            "c2l": float(np.max(np.abs(got[1] - outs[1])) / np.max(np.abs(outs[1])))}
+            name: float(np.max(np.abs(got[k] - outs[k])) / np.max(np.abs(outs[k])))
+            for name, k in (("l2c", "o0"), ("c2l", "o1"))}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -108,6 +108,25 @@ size_t l2c_gpu_plan_copy(const l2c_gpu_plan *plan, int which, double *dst, size_
 size_t l2c_gpu_execute_noalloc(l2c_gpu_plan *plan, const double *in, double *out,
                                size_t direction, size_t stride);
 
+/* Ragged batches: count vectors of lengths N[0..count) (packed back to back in
+ * the caller's arrays: vector v starts at N[0] + ... + N[v-1]), each transformed
+ * exactly as execute() with create_fmm(N[v], maxs, 18, directions, 0, 0, 0)
+ * would (vectors with L < 1 take the direct method), in one set of launches whose
+ * count does not depend on the number of vectors.  No counterpart in the
+ * reference (its callers loop execute over plans, src/bin/l2c.c harnesses). */
+typedef struct l2c_gpu_ragged l2c_gpu_ragged;
+l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *N, size_t maxs,
+                                      size_t directions, unsigned flags);
+void l2c_gpu_ragged_destroy(l2c_gpu_ragged *plan);
+/* host or device pointers; returns the summed reference flop count, 0 on failure */
+size_t l2c_gpu_ragged_execute(l2c_gpu_ragged *plan, const double *in, double *out,
+                              size_t direction, unsigned flags);
+int l2c_gpu_ragged_synchronize(l2c_gpu_ragged *plan);
+size_t l2c_gpu_ragged_total(const l2c_gpu_ragged *plan);            /* sum of N */
+size_t l2c_gpu_ragged_flops(const l2c_gpu_ragged *plan, size_t direction);
+void *l2c_gpu_ragged_stream(l2c_gpu_ragged *plan);
+size_t l2c_gpu_ragged_launch_count(const l2c_gpu_ragged *plan);
+
 /* Lambda(z) and Lambda at integer z, host side, bit-identical to the device. */
 double l2c_lambda(double z);
 double l2c_lambda_int(size_t z);

@@ -184,6 +184,23 @@ const char *l2c_last_error(void);
 size_t execute_batched(const double *input_array, double *output_array, fmm_plan *fmmplan,
                        size_t direction, size_t count, size_t dist, size_t stride);
 
+/* Ragged batch: count vectors of lengths N[0..count), packed back to back
+ * (vector v starts at N[0] + ... + N[v-1]); each is transformed exactly as
+ * execute() with create_fmm(N[v], maxs, M, direction, ...) would, all in one set
+ * of GPU launches.  Returns the summed flop count, 0 on failure. */
+typedef struct {
+  size_t count;
+  size_t total; /* sum of N */
+  size_t maxs;
+  size_t direction;
+  void *gpu;
+} fmm_plan_ragged;
+fmm_plan_ragged *create_fmm_ragged(size_t count, const size_t *N, size_t maxs, size_t M,
+                                   size_t direction, size_t lagrange, size_t precompute, size_t v);
+size_t execute_ragged(const double *input_array, double *output_array, fmm_plan_ragged *plan,
+                      size_t direction);
+void free_fmm_ragged(fmm_plan_ragged *plan);
+
 #ifdef __cplusplus
 }
 #endif

@@ -209,15 +209,23 @@ struct Geo {
   long long N, s, h, nL, L, K, slots, leaf_base, count, dist, stride;
 };
 
-// x[v N + j] = in[v dist + j stride], premultiplied by j (j >= 2) for C2L
-// (leg2cheb.c:1325-1335).
+// Each phase is written once as a per-item device function working on one
+// vector's arrays; the uniform-batch kernels below and the ragged-batch kernels
+// (one launch over vectors of different N) both call them.
+
+// x[j] = in[j stride], premultiplied by j (j >= 2) for C2L (leg2cheb.c:1325-1335).
+__device__ __forceinline__ void gather_item(const double *__restrict__ in, double *__restrict__ x,
+                                            long long stride, int c2l, long long j) {
+  double u = in[j * stride];
+  if (c2l && j >= 2) u = u * (double)j;
+  x[j] = u;
+}
+
 __global__ void k_gather(const double *__restrict__ in, double *__restrict__ x, Geo g, int c2l) {
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= g.count * g.N) return;
   const long long v = idx / g.N, j = idx - v * g.N;
-  double u = in[v * g.dist + j * g.stride];
-  if (c2l && j >= 2) u = u * (double)j;
-  x[idx] = u;
+  gather_item(in + v * g.dist, x + v * g.N, g.stride, c2l, j);
 }
 
 // Near-field band, one output per thread.  For output j in block b = min(j/h, nL-1)
@@ -244,34 +252,103 @@ __device__ __forceinline__ long long band_count(long long k, long long b, const 
   return c > 0 ? c : 0;
 }
 
-__global__ void __launch_bounds__(256) k_near(const double *__restrict__ x, const double *out,
-                                              double *__restrict__ y,
-                                              const double *__restrict__ a,
-                                              const double *__restrict__ an,
-                                              const double *__restrict__ dn,
-                                              const double *__restrict__ W, Geo g, int c2l) {
-  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (idx >= g.count * g.N) return;
-  const long long v = idx / g.N, j = idx - v * g.N;
+// Band sum of output j for VB vectors (x rows g.N apart), two accumulator sets
+// (even and odd k) to halve the dependent FP64 chain.  W: precomputed weights of
+// this plan (or nullptr: weights formed on the fly).
+template <int VB>
+__device__ __forceinline__ void near_sums(const double *__restrict__ xv, long long xstride,
+                                          const double *__restrict__ a,
+                                          const double *__restrict__ an,
+                                          const double *__restrict__ dn,
+                                          const double *__restrict__ W, const Geo &g, int c2l,
+                                          long long j, double *res) {
   long long b = j / g.h;
   if (b > g.nL - 1) b = g.nL - 1;
   long long lim = (b + 2) * g.h;
   if (lim > g.N) lim = g.N;
-  const double *xv = x + v * g.N;
-  double acc = 0.0;
+  const long long nk = (lim - j + 1) / 2;  // terms k = 0 .. nk-1
+  double acc0[VB], acc1[VB];
+#pragma unroll
+  for (int u = 0; u < VB; u++) acc0[u] = acc1[u] = 0.0;
   if (W == nullptr) {
-    for (long long k = 0; j + 2 * k < lim; k++)
-      acc = fma(near_weight(c2l, k, j, a, an, dn), xv[j + 2 * k], acc);
+    long long k = 0;
+    for (; k + 1 < nk; k += 2) {
+      const double w0 = near_weight(c2l, k, j, a, an, dn);
+      const double w1 = near_weight(c2l, k + 1, j, a, an, dn);
+#pragma unroll
+      for (int u = 0; u < VB; u++) {
+        acc0[u] = fma(w0, xv[u * xstride + 2 * k], acc0[u]);
+        acc1[u] = fma(w1, xv[u * xstride + 2 * k + 2], acc1[u]);
+      }
+    }
+    if (k < nk) {
+      const double w0 = near_weight(c2l, k, j, a, an, dn);
+#pragma unroll
+      for (int u = 0; u < VB; u++) acc0[u] = fma(w0, xv[u * xstride + 2 * k], acc0[u]);
+    }
   } else {
     const long long i = j - b * g.h;
     const double *Wb = W + b * (3 * g.s * g.s + g.s);
-    long long off = 0;
-    for (long long k = 0; j + 2 * k < lim; k++) {
-      acc = fma(Wb[off + i], xv[j + 2 * k], acc);
-      off += band_count(k, b, g);
+    long long off = 0, k = 0;
+    // four terms per iteration, all loads issued before the FMAs, to keep
+    // enough weight loads in flight to cover DRAM latency
+    for (; k + 3 < nk; k += 4) {
+      const long long o1 = off + band_count(k, b, g);
+      const long long o2 = o1 + band_count(k + 1, b, g);
+      const long long o3 = o2 + band_count(k + 2, b, g);
+      const double w0 = Wb[off + i], w1 = Wb[o1 + i], w2 = Wb[o2 + i], w3 = Wb[o3 + i];
+      double xa[VB][4];
+#pragma unroll
+      for (int u = 0; u < VB; u++)
+#pragma unroll
+        for (int r = 0; r < 4; r++) xa[u][r] = xv[u * xstride + 2 * (k + r)];
+#pragma unroll
+      for (int u = 0; u < VB; u++) {
+        acc0[u] = fma(w0, xa[u][0], acc0[u]);
+        acc1[u] = fma(w1, xa[u][1], acc1[u]);
+        acc0[u] = fma(w2, xa[u][2], acc0[u]);
+        acc1[u] = fma(w3, xa[u][3], acc1[u]);
+      }
+      off = o3 + band_count(k + 3, b, g);
+    }
+    for (; k + 1 < nk; k += 2) {
+      const long long off1 = off + band_count(k, b, g);
+      const double w0 = Wb[off + i], w1 = Wb[off1 + i];
+#pragma unroll
+      for (int u = 0; u < VB; u++) {
+        acc0[u] = fma(w0, xv[u * xstride + 2 * k], acc0[u]);
+        acc1[u] = fma(w1, xv[u * xstride + 2 * k + 2], acc1[u]);
+      }
+      off = off1 + band_count(k + 1, b, g);
+    }
+    if (k < nk) {
+      const double w0 = Wb[off + i];
+#pragma unroll
+      for (int u = 0; u < VB; u++) acc0[u] = fma(w0, xv[u * xstride + 2 * k], acc0[u]);
     }
   }
-  y[idx] = out[v * g.dist + j * g.stride] + acc;
+#pragma unroll
+  for (int u = 0; u < VB; u++) res[u] = acc0[u] + acc1[u];
+}
+
+// VB vectors per thread: the weight of each term is formed (or loaded) once and
+// used for VB vectors.  blockIdx.x enumerates (output tile, vector group) with
+// the tile index fastest.  y = out_in + band.
+template <int VB>
+__global__ void __launch_bounds__(256, VB == 1 ? 5 : VB == 2 ? 4 : 2)
+    k_near(const double *__restrict__ x, const double *out, double *__restrict__ y,
+           const double *__restrict__ a, const double *__restrict__ an,
+           const double *__restrict__ dn, const double *__restrict__ W, Geo g, int c2l) {
+  const long long ntile = (g.N + blockDim.x - 1) / blockDim.x;
+  const long long tile = blockIdx.x % ntile, vg = blockIdx.x / ntile;
+  const long long j = tile * blockDim.x + threadIdx.x;
+  if (j >= g.N) return;
+  const long long v0 = vg * VB;
+  double res[VB];
+  near_sums<VB>(x + v0 * g.N + j, g.N, a, an, dn, W, g, c2l, j, res);
+#pragma unroll
+  for (int u = 0; u < VB; u++)
+    y[(v0 + u) * g.N + j] = out[(v0 + u) * g.dist + j * g.stride] + res[u];
 }
 
 // Plan time: the band weights of every output, in the layout k_near reads.
@@ -303,6 +380,25 @@ inline size_t near_table_size(size_t N, size_t s) {
 }
 
 // Step 1: leaf node t in [2, 2^(L+1)) of parity sg: w = sum_i x[t h + 2i + sg] T_sg[i][m].
+// xv: this vector's x; wv: this vector's w (2 parities x slots x M).
+__device__ __forceinline__ void leaf_up_item(const double *__restrict__ xv,
+                                             const double *__restrict__ T,
+                                             double *__restrict__ wv, const Geo &g,
+                                             long long node, int sg, int m) {
+  const long long base = (node + 2) * g.h + sg;
+  const double *Ts = T + (size_t)sg * g.s * M + m;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  long long iend = (g.N - base + 1) / 2;  // number of i with base + 2i < N
+  if (iend > g.s) iend = g.s;
+  long long i = 0;
+  for (; i + 3 < iend; i += 4) {
+#pragma unroll
+    for (int r = 0; r < 4; r++) acc[r] = fma(xv[base + 2 * (i + r)], Ts[(i + r) * M], acc[r]);
+  }
+  for (; i < iend; i++) acc[0] = fma(xv[base + 2 * i], Ts[i * M], acc[0]);
+  wv[((long long)sg * g.slots + g.leaf_base + node) * M + m] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+}
+
 // One thread per (vector, node, parity, m).
 __global__ void __launch_bounds__(288) k_leaf_up(const double *__restrict__ x,
                                                  const double *__restrict__ T,
@@ -314,42 +410,86 @@ __global__ void __launch_bounds__(288) k_leaf_up(const double *__restrict__ x,
   long long rem = idx - v * per_vec;
   const long long node = rem / (2 * M);
   rem -= node * 2 * M;
-  const int sg = (int)(rem / M), m = (int)(rem % M);
-  const long long base = (node + 2) * g.h + sg;
-  const double *xv = x + v * g.N;
-  const double *Ts = T + (size_t)sg * g.s * M + m;
-  double acc = 0.0;
-  long long iend = (g.N - base + 1) / 2;  // number of i with base + 2i < N
-  if (iend > g.s) iend = g.s;
-  for (long long i = 0; i < iend; i++) acc = fma(xv[base + 2 * i], Ts[i * M], acc);
-  w[((v * 2 + sg) * g.slots + g.leaf_base + node) * M + m] = acc;
+  leaf_up_item(x + v * g.N, T, w + v * 2 * g.slots * M, g, node, (int)(rem / M), (int)(rem % M));
 }
 
 // Step 2, one level: parent slot j of level l from child slots 2j+2, 2j+3 of level
-// l+1 through the compact lower binomial matrix; z = x0 +- x1 by row/column
-// parity (leg2cheb.c:537-602).
-__global__ void k_tree_up(double *w, Geo g, long long parent_base, long long child_base,
-                          long long nparent) {
-  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long per_vec = 2 * nparent * M;
-  if (idx >= g.count * per_vec) return;
-  const long long vs = idx / (nparent * M);  // vector * 2 + parity
-  long long rem = idx - vs * nparent * M;
-  const long long jp = rem / M;
-  const int m = (int)(rem % M);
-  const double *x0 = w + (vs * g.slots + child_base + 2 * jp + 2) * M;
-  const double *x1 = x0 + M;
-  const double *Bm = c_binom_lower + m * (m + 1) / 2;
-  double acc = 0.0;
-  for (int i = 0; i <= m; i++) {
-    const double z = ((m + i) & 1) ? x0[i] - x1[i] : x0[i] + x1[i];
-    acc = fma(Bm[i], z, acc);
+// l+1 through the compact lower binomial matrix (leg2cheb.c:537-602):
+//   b[m] = sum_{i<=m} B[m][i] x0[i] + sum_{i<=m} (-1)^(m+i) B[m][i] x1[i],
+// the +/- parity combination of the reference written as two independent FMA
+// chains.  A CTA takes TREE_TILE parents: their 36 child coefficients are staged
+// in shared memory with coalesced loads (children of consecutive parents are
+// contiguous), then warp m computes row m for every parent of the tile, so loop
+// lengths are warp-uniform and no load sits inside the FMA loop.
+constexpr int TREE_TILE = 32;
+constexpr int TREE_PAD = 2 * M + 1;  // padded row of staged children (bank spread)
+
+// One tile: child[p] points at the 2M child coefficients of item p, par[p] at
+// its M parent coefficients (nullptr: no item).
+__device__ __forceinline__ void tree_up_tile(const double *const *child, double *const *par,
+                                             const double *sB, double *sx) {
+  for (int e = threadIdx.x; e < TREE_TILE * 2 * M; e += blockDim.x) {
+    const int p = e / (2 * M), q = e - p * 2 * M;
+    sx[p * TREE_PAD + q] = par[p] ? child[p][q] : 0.0;
   }
-  w[(vs * g.slots + parent_base + jp) * M + m] = acc;
+  __syncthreads();
+  const int m = threadIdx.x >> 5, p = threadIdx.x & 31;
+  if (m >= M || par[p] == nullptr) return;
+  const double *x0 = sx + p * TREE_PAD, *x1 = x0 + M;
+  const double *Bm = sB + m * (m + 1) / 2;
+  double s0 = 0.0, s1 = 0.0;
+  for (int i = 0; i <= m; i++) {
+    const double bmi = Bm[i];
+    s0 = fma(bmi, x0[i], s0);
+    s1 = fma(((m + i) & 1) ? -bmi : bmi, x1[i], s1);
+  }
+  par[p][m] = s0 + s1;
 }
 
-// Step 3: far-field blocks of every level at once.  Global block gb owns slots
-// 2 gb, 2 gb + 1: c0 = A0 w0 + A1 w1, c1 = A2 w1 (leg2cheb.c:1419-1435).
+// blockDim = 32 * M; items (vector * 2 + parity, parent slot) in TREE_TILE tiles.
+__global__ void __launch_bounds__(32 * M) k_tree_up(double *w, Geo g, long long parent_base,
+                                                    long long child_base, long long nparent) {
+  __shared__ double sB[NTRI];
+  __shared__ double sx[TREE_TILE * TREE_PAD];
+  __shared__ const double *child[TREE_TILE];
+  __shared__ double *par[TREE_TILE];
+  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_lower[t];
+  if (threadIdx.x < TREE_TILE) {
+    const long long item = (long long)blockIdx.x * TREE_TILE + threadIdx.x;
+    const long long nitem = g.count * 2 * nparent;
+    const long long vs = item / nparent, jp = item - vs * nparent;
+    child[threadIdx.x] = w + (vs * g.slots + child_base + 2 * jp + 2) * M;
+    par[threadIdx.x] = item < nitem ? w + (vs * g.slots + parent_base + jp) * M : nullptr;
+  }
+  __syncthreads();
+  tree_up_tile(child, par, sB, sx);
+}
+
+// Step 3: far-field blocks.  Ablk: the three 18x18 blocks of a block owning
+// slots 2 gb, 2 gb + 1 of the tree ws / cs of one (vector, parity):
+// c0 = A0 w0 + A1 w1, c1 = A2 w1 (leg2cheb.c:1419-1435).
+__device__ __forceinline__ void far_item(const double *__restrict__ Ablk,
+                                         const double *__restrict__ ws, double *__restrict__ cs,
+                                         long long gb, int m) {
+  const double *A0 = Ablk + m * M;
+  const double *A1 = A0 + MM, *A2 = A1 + MM;
+  const double *w0 = ws + 2 * gb * M, *w1 = w0 + M;
+  double t0 = 0.0, t1 = 0.0, t2 = 0.0, u0 = 0.0, u1 = 0.0, u2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < M; k += 2) {
+    t0 = fma(A0[k], w0[k], t0);
+    t1 = fma(A1[k], w1[k], t1);
+    t2 = fma(A2[k], w1[k], t2);
+    u0 = fma(A0[k + 1], w0[k + 1], u0);
+    u1 = fma(A1[k + 1], w1[k + 1], u1);
+    u2 = fma(A2[k + 1], w1[k + 1], u2);
+  }
+  double *c0 = cs + 2 * gb * M;
+  c0[m] = (t0 + u0) + (t1 + u1);
+  c0[M + m] = t2 + u2;
+}
+
+// Every level at once: block gb's A blocks start at 3 gb M^2.
 __global__ void __launch_bounds__(256) k_far(const double *__restrict__ A,
                                              const double *__restrict__ w,
                                              double *__restrict__ c, Geo g, long long nblocks) {
@@ -359,48 +499,88 @@ __global__ void __launch_bounds__(256) k_far(const double *__restrict__ A,
   const long long vs = idx / per_vs;
   long long rem = idx - vs * per_vs;
   const long long gb = rem / M;
-  const int m = (int)(rem % M);
-  const double *A0 = A + (3 * gb) * MM + m * M;
-  const double *A1 = A0 + MM, *A2 = A1 + MM;
-  const double *w0 = w + (vs * g.slots + 2 * gb) * M, *w1 = w0 + M;
-  double t0 = 0.0, t1 = 0.0, t2 = 0.0;
-#pragma unroll
-  for (int k = 0; k < M; k++) {
-    t0 = fma(A0[k], w0[k], t0);
-    t1 = fma(A1[k], w1[k], t1);
-    t2 = fma(A2[k], w1[k], t2);
-  }
-  double *c0 = c + (vs * g.slots + 2 * gb) * M;
-  c0[m] = t0 + t1;
-  c0[M + m] = t2;
+  far_item(A + 3 * gb * MM, w + vs * g.slots * M, c + vs * g.slots * M, gb, (int)(rem % M));
 }
 
 // Step 4, one level: parent target slot t of level l into children 2t, 2t+1 of
 // level l+1 through the compact upper (transposed) binomial matrix: se/so sum the
-// columns of equal/opposite parity, child0 += se + so, child1 += se - so
-// (leg2cheb.c:603-618).
-__global__ void k_tree_down(double *c, Geo g, long long parent_base, long long child_base,
-                            long long nparent) {
-  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (idx >= g.count * 2 * nparent * M) return;
-  const long long vs = idx / (nparent * M);
-  long long rem = idx - vs * nparent * M;
-  const long long tp = rem / M;
-  const int i = (int)(rem % M);
-  const double *xp = c + (vs * g.slots + parent_base + tp) * M;
-  const double *Bu = c_binom_upper + i * M - i * (i - 1) / 2 - i;  // Bu[j] = row i, column j
+// columns of equal/opposite parity to the row, child0 += se + so,
+// child1 += se - so (leg2cheb.c:603-618).  Tiled as k_tree_up: the M parent
+// coefficients of TREE_TILE parents staged in shared memory, warp i computes row i.
+__device__ __forceinline__ void tree_down_tile(const double *const *par, double *const *child,
+                                               const double *sB, double *sx) {
+  for (int e = threadIdx.x; e < TREE_TILE * M; e += blockDim.x) {
+    const int p = e / M, q = e - p * M;
+    sx[p * TREE_PAD + q] = child[p] ? par[p][q] : 0.0;
+  }
+  __syncthreads();
+  const int i = threadIdx.x >> 5, p = threadIdx.x & 31;
+  if (i >= M || child[p] == nullptr) return;
+  const double *xp = sx + p * TREE_PAD;
+  const double *Bu = sB + i * M - i * (i - 1) / 2 - i;  // Bu[j] = row i, column j
   double se = 0.0, so = 0.0;
-  for (int j = i; j < M; j += 2) se = fma(Bu[j], xp[j], se);
-  for (int j = i + 1; j < M; j += 2) so = fma(Bu[j], xp[j], so);
-  double *ch = c + (vs * g.slots + child_base + 2 * tp) * M;
+  int j = i;
+  for (; j + 1 < M; j += 2) {
+    se = fma(Bu[j], xp[j], se);
+    so = fma(Bu[j + 1], xp[j + 1], so);
+  }
+  if (j < M) se = fma(Bu[j], xp[j], se);
+  double *ch = child[p];
   ch[i] += se + so;
   ch[M + i] += se - so;
+}
+
+__global__ void __launch_bounds__(32 * M) k_tree_down(double *c, Geo g, long long parent_base,
+                                                      long long child_base, long long nparent) {
+  __shared__ double sB[NTRI];
+  __shared__ double sx[TREE_TILE * TREE_PAD];
+  __shared__ const double *par[TREE_TILE];
+  __shared__ double *child[TREE_TILE];
+  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_upper[t];
+  if (threadIdx.x < TREE_TILE) {
+    const long long item = (long long)blockIdx.x * TREE_TILE + threadIdx.x;
+    const long long nitem = g.count * 2 * nparent;
+    const long long vs = item / nparent, tp = item - vs * nparent;
+    par[threadIdx.x] = c + (vs * g.slots + parent_base + tp) * M;
+    child[threadIdx.x] = item < nitem ? c + (vs * g.slots + child_base + 2 * tp) * M : nullptr;
+  }
+  __syncthreads();
+  tree_down_tile(par, child, sB, sx);
 }
 
 // Step 5 + scaling: out[j] = scale_j (y[j] + sum_m c[L-1][tau][m] T_sg[i][m]) with
 // tau = j / h, sg = j & 1, i = (j - tau h)/2; no far field for tau >= K.
 // L2C scale 2/pi (and 1/2 at j = 0, leg2cheb.c:360-374); C2L scale j + 1/2
-// (leg2cheb.c:519-532).
+// (leg2cheb.c:519-532).  cv: this vector's c; yv: its y; outv: its output line.
+__device__ __forceinline__ void leaf_down_item(const double *__restrict__ cv,
+                                               const double *__restrict__ T,
+                                               const double *__restrict__ yv, double *outv,
+                                               const Geo &g, int c2l, long long j) {
+  const long long tau = j / g.h;
+  double far = 0.0;
+  if (tau < g.K) {
+    const int sg = (int)(j & 1);
+    const long long i = (j - tau * g.h) >> 1;
+    const double *cc = cv + ((long long)sg * g.slots + g.leaf_base + tau) * M;
+    const double *Ti = T + ((size_t)sg * g.s + i) * M;
+    double f1 = 0.0;
+#pragma unroll
+    for (int m = 0; m < M; m += 2) {
+      far = fma(cc[m], Ti[m], far);
+      f1 = fma(cc[m + 1], Ti[m + 1], f1);
+    }
+    far += f1;
+  }
+  double val = yv[j] + far;
+  if (!c2l) {
+    val = val * TWO_OVER_PI;
+    if (j == 0) val = val * 0.5;
+  } else {
+    val = val * ((double)j + 0.5);
+  }
+  outv[j * g.stride] = val;
+}
+
 __global__ void __launch_bounds__(256) k_leaf_down(const double *__restrict__ c,
                                                    const double *__restrict__ T,
                                                    const double *__restrict__ y, double *out,
@@ -408,38 +588,18 @@ __global__ void __launch_bounds__(256) k_leaf_down(const double *__restrict__ c,
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= g.count * g.N) return;
   const long long v = idx / g.N, j = idx - v * g.N;
-  const long long tau = j / g.h;
-  double far = 0.0;
-  if (tau < g.K) {
-    const int sg = (int)(j & 1);
-    const long long i = (j - tau * g.h) >> 1;
-    const double *cv = c + ((v * 2 + sg) * g.slots + g.leaf_base + tau) * M;
-    const double *Ti = T + ((size_t)sg * g.s + i) * M;
-#pragma unroll
-    for (int m = 0; m < M; m++) far = fma(cv[m], Ti[m], far);
-  }
-  double val = y[idx] + far;
-  if (!c2l) {
-    val = val * TWO_OVER_PI;
-    if (j == 0) val = val * 0.5;
-  } else {
-    val = val * ((double)j + 0.5);
-  }
-  out[v * g.dist + j * g.stride] = val;
+  leaf_down_item(c + v * 2 * g.slots * M, T, y + v * g.N, out + v * g.dist, g, c2l, j);
 }
 
 // Direct O(N^2) transform for L < 1 (leg2cheb.c:152-234), with the reference's
 // contract: out[0..N) is zeroed contiguously before the line is written, the
 // L2C input is read contiguously, L2C accumulates into line elements past N.
-__global__ void __launch_bounds__(256) k_direct(const double *in, double *out,
-                                                const double *__restrict__ a,
-                                                const double *__restrict__ an,
-                                                const double *__restrict__ dn, Geo g, int c2l) {
-  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (idx >= g.count * g.N) return;
-  const long long v = idx / g.N, i = idx - v * g.N;
-  const double *u = in + v * g.dist;
-  double *b = out + v * g.dist;
+// u, b: this vector's input and output line.
+__device__ __forceinline__ void direct_item(const double *u, double *b,
+                                            const double *__restrict__ a,
+                                            const double *__restrict__ an,
+                                            const double *__restrict__ dn, const Geo &g, int c2l,
+                                            long long i) {
   double val;
   if (!c2l) {
     val = 0.0;
@@ -458,6 +618,16 @@ __global__ void __launch_bounds__(256) k_direct(const double *in, double *out,
   }
   if (g.stride > 1 && (i % g.stride) != 0) b[i] = 0.0;  // contiguous zeroing of [0, N)
   b[i * g.stride] = val;
+}
+
+__global__ void __launch_bounds__(256) k_direct(const double *in, double *out,
+                                                const double *__restrict__ a,
+                                                const double *__restrict__ an,
+                                                const double *__restrict__ dn, Geo g, int c2l) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.count * g.N) return;
+  const long long v = idx / g.N, i = idx - v * g.N;
+  direct_item(in + v * g.dist, out + v * g.dist, a, an, dn, g, c2l, i);
 }
 
 inline unsigned blocks_for(long long n, int threads) {
@@ -506,6 +676,7 @@ struct l2c_gpu_plan {
   std::vector<GraphEntry> graphs;
   size_t use_clock = 0;
   bool use_graphs = true;
+  bool overlap = false;  // near field on stream2 beside the far-field chain
   // launch accounting and optional per-phase CUDA-event timing
   size_t launches = 0;
   bool profiling = false;
@@ -519,8 +690,13 @@ namespace {
 
 // Reference flop count (the value execute() returns), reproduced term by term,
 // including its unsigned wrap-around in directL's last block (leg2cheb.c:507-516).
-size_t ref_flops(const l2c_gpu_plan *p, size_t dir) {
-  const size_t N = p->N;
+size_t ref_flops_geo(size_t N, size_t L, size_t s, size_t Nb, size_t dir);
+size_t ref_flops(const l2c_gpu_plan *p, size_t dir) { return ref_flops_geo(p->N, p->L, p->s, p->Nb, dir); }
+
+size_t ref_flops_geo(size_t N, size_t L_, size_t s_, size_t Nb, size_t dir) {
+  struct {
+    size_t L, s, Nb;
+  } q{L_, s_, Nb}, *p = &q;
   size_t f = 0;
   if (p->L == 0) {
     f = N;
@@ -656,6 +832,47 @@ struct DeviceGuard {
   }
 };
 
+// Near field for all vectors of a batch: full groups of 8 (4, 2) vectors per
+// thread, then the remainder.
+cudaError_t launch_near(const double *x, const double *out, double *y, const double *a,
+                        const double *an, const double *dn, const double *W, Geo g, int c2l,
+                        cudaStream_t st) {
+  const long long ntile = (g.N + 255) / 256;
+  long long v = 0;
+  while (v < g.count) {
+    const long long left = g.count - v;
+    const int vb = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+    const long long groups = left / vb;
+    Geo gg = g;
+    gg.count = groups * vb;
+    const double *xs = x + v * g.N;
+    const double *os = out + v * g.dist;
+    double *ys = y + v * g.N;
+    const unsigned grid = (unsigned)(ntile * groups);
+    switch (vb) {
+      case 8: k_near<8><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
+      case 4: k_near<4><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
+      case 2: k_near<2><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
+      default: k_near<1><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    v += groups * vb;
+  }
+  return cudaSuccess;
+}
+
+size_t near_launch_count(size_t count) {
+  size_t n = 0, v = 0;
+  while (v < count) {
+    const size_t left = count - v;
+    const size_t vb = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+    v += (left / vb) * vb;
+    n++;
+  }
+  return n;
+}
+
 Geo make_geo(const l2c_gpu_plan *p, size_t count, size_t dist, size_t stride) {
   Geo g;
   g.N = (long long)p->N;
@@ -698,10 +915,8 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   const double *W = p->Wnear[dir];
   if (near_only) {
     {
-      PhaseScope ps(p, L2C_PHASE_NEAR, 1);
-      k_near<<<blocks_for(total, 256), 256, 0, st>>>(x, out, p->y, p->a, p->an, p->dn, W, g,
-                                                     c2l);
-      CK(cudaGetLastError());
+      PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count));
+      CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, st));
     }
     Geo g0 = g;
     g0.K = 0;
@@ -710,14 +925,16 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaGetLastError());
     return 1;
   }
-  CK(cudaEventRecord(p->ev_fork, st));
-  CK(cudaStreamWaitEvent(st2, p->ev_fork, 0));
-  {
-    PhaseScope ps(p, L2C_PHASE_NEAR, 1, st2);
-    k_near<<<blocks_for(total, 256), 256, 0, st2>>>(x, out, p->y, p->a, p->an, p->dn, W, g, c2l);
-    CK(cudaGetLastError());
+  cudaStream_t stn = p->overlap ? st2 : st;
+  if (p->overlap) {
+    CK(cudaEventRecord(p->ev_fork, st));
+    CK(cudaStreamWaitEvent(st2, p->ev_fork, 0));
   }
-  CK(cudaEventRecord(p->ev_join, st2));
+  {
+    PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count), stn);
+    CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn));
+  }
+  if (p->overlap) CK(cudaEventRecord(p->ev_join, st2));
   const long long leaf_threads = g.count * g.K * 2 * M;
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
@@ -728,9 +945,8 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     PhaseScope ps(p, L2C_PHASE_TREE_UP, p->L - 1);
     for (long long l = (long long)p->L - 2; l >= 0; l--) {
       const long long np = (long long)slots_at((size_t)l);
-      const long long n = g.count * 2 * np * M;
-      k_tree_up<<<blocks_for(n, 256), 256, 0, st>>>(p->w, g, 2 * (long long)blocks_before(l),
-                                                     2 * (long long)blocks_before(l + 1), np);
+      k_tree_up<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
+          p->w, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
     }
   }
   CK(cudaGetLastError());
@@ -744,13 +960,12 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     PhaseScope ps(p, L2C_PHASE_TREE_DOWN, p->L - 1);
     for (long long l = 0; l + 1 < (long long)p->L; l++) {
       const long long np = (long long)slots_at((size_t)l);
-      const long long n = g.count * 2 * np * M;
-      k_tree_down<<<blocks_for(n, 256), 256, 0, st>>>(p->c, g, 2 * (long long)blocks_before(l),
-                                                       2 * (long long)blocks_before(l + 1), np);
+      k_tree_down<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
+          p->c, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
     }
   }
   CK(cudaGetLastError());
-  CK(cudaStreamWaitEvent(st, p->ev_join, 0));
+  if (p->overlap) CK(cudaStreamWaitEvent(st, p->ev_join, 0));
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
     k_leaf_down<<<blocks_for(total, 256), 256, 0, st>>>(p->c, p->T, p->y, out, g, c2l);
@@ -868,6 +1083,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   PCK(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
   PCK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
   if (const char *env = std::getenv("L2C_NO_GRAPHS")) p->use_graphs = env[0] == '0';
+  if (const char *env = std::getenv("L2C_OVERLAP")) p->overlap = env[0] == '1';
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
     p->Nn = N;
@@ -1241,20 +1457,19 @@ extern "C" size_t l2c_gpu_execute_noalloc(l2c_gpu_plan *p, const double *in, dou
   Geo g = make_geo(p, 1, p->N, stride);
   const long long total = g.N;
   k_gather<<<blocks_for(total, 256), 256, 0, st>>>(in, x, g, c2l);
-  k_near<<<blocks_for(total, 256), 256, 0, st>>>(x, out, y, p->a, p->an, p->dn, p->Wnear[dir],
-                                                 g, c2l);
+  k_near<1><<<blocks_for(total, 256), 256, 0, st>>>(x, out, y, p->a, p->an, p->dn,
+                                                    p->Wnear[dir], g, c2l);
   k_leaf_up<<<blocks_for(g.K * 2 * M, 288), 288, 0, st>>>(x, p->T, w, g);
   for (long long l = (long long)p->L - 2; l >= 0; l--) {
     const long long np = (long long)slots_at((size_t)l);
-    k_tree_up<<<blocks_for(2 * np * M, 256), 256, 0, st>>>(w, g, 2 * (long long)blocks_before(l),
-                                                            2 * (long long)blocks_before(l + 1),
-                                                            np);
+    k_tree_up<<<blocks_for(2 * np, TREE_TILE), 32 * M, 0, st>>>(
+        w, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
   }
   k_far<<<blocks_for(2 * (long long)p->Nb * M, 256), 256, 0, st>>>(p->A[dir], w, c, g,
                                                                    (long long)p->Nb);
   for (long long l = 0; l + 1 < (long long)p->L; l++) {
     const long long np = (long long)slots_at((size_t)l);
-    k_tree_down<<<blocks_for(2 * np * M, 256), 256, 0, st>>>(
+    k_tree_down<<<blocks_for(2 * np, TREE_TILE), 32 * M, 0, st>>>(
         c, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
   }
   k_leaf_down<<<blocks_for(total, 256), 256, 0, st>>>(c, p->T, y, out, g, c2l);
@@ -1262,3 +1477,505 @@ extern "C" size_t l2c_gpu_execute_noalloc(l2c_gpu_plan *p, const double *in, dou
   CK(cudaStreamSynchronize(st));
   return p->flops[dir];
 }
+
+// ---------------------------------------------------------------------------
+// Ragged batches: many vectors of different length N in one set of launches.
+//
+// For a fixed leaf size s the far-field blocks depend only on (s, depth below
+// the top, block index): level l of an L-level plan is level l + (L' - L) of an
+// L'-level plan with the same s, with the same leading blocks.  So one "donor"
+// plan per distinct s, built with the largest level count among the vectors that
+// use that s, supplies A, T and the Lambda tables (identical prefixes) for all of
+// them.  Each phase is one launch over the concatenated work items of every
+// vector; a thread finds its vector by binary search in the phase's prefix sums
+// of item counts, so work is spread evenly over the SMs whatever the mix of N.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct RVec {
+  Geo g;               // the vector's own geometry (count 1, stride 1)
+  long long io;        // offset in the packed caller arrays and in x / y scratch
+  long long wc;        // offset in the w / c scratch
+  int donor;           // donor plan supplying tables
+  int lshift;          // donor level = own level + lshift
+  int direct;          // 1: O(N^2) direct method (L < 1)
+};
+
+struct RDonor {
+  const double *a, *an, *dn, *T, *A[2];
+};
+
+__device__ __forceinline__ int find_vec(const long long *__restrict__ pre, int nvec, long long idx) {
+  int lo = 0, hi = nvec;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (pre[mid] <= idx) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_r_gather(const double *__restrict__ in, double *__restrict__ x,
+                           const RVec *__restrict__ V, const long long *__restrict__ pre, int nvec,
+                           int c2l) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= pre[nvec]) return;
+  const int v = find_vec(pre, nvec, idx);
+  const RVec &r = V[v];
+  if (r.direct) return;
+  gather_item(in + r.io, x + r.io, 1, c2l, idx - pre[v]);
+}
+
+__global__ void __launch_bounds__(256) k_r_near(const double *__restrict__ x, const double *out,
+                                                double *__restrict__ y,
+                                                const RVec *__restrict__ V,
+                                                const RDonor *__restrict__ D,
+                                                const long long *__restrict__ pre, int nvec,
+                                                int c2l) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= pre[nvec]) return;
+  const int v = find_vec(pre, nvec, idx);
+  const RVec &r = V[v];
+  if (r.direct) return;
+  const long long j = idx - pre[v];
+  const RDonor &d = D[r.donor];
+  double res[1];
+  near_sums<1>(x + r.io + j, 0, d.a, d.an, d.dn, nullptr, r.g, c2l, j, res);
+  y[r.io + j] = out[r.io + j] + res[0];
+}
+
+__global__ void __launch_bounds__(288) k_r_leaf_up(const double *__restrict__ x,
+                                                   double *__restrict__ w,
+                                                   const RVec *__restrict__ V,
+                                                   const RDonor *__restrict__ D,
+                                                   const long long *__restrict__ pre, int nvec) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= pre[nvec]) return;
+  const int v = find_vec(pre, nvec, idx);
+  const RVec &r = V[v];
+  const long long rem0 = idx - pre[v];
+  const long long node = rem0 / (2 * M);
+  const long long rem = rem0 - node * 2 * M;
+  leaf_up_item(x + r.io, D[r.donor].T, w + r.wc, r.g, node, (int)(rem / M), (int)(rem % M));
+}
+
+// depth d below the leaf level: vector parent level l = L - 1 - d; items are
+// (vector, parity, parent slot), 2 S(l) per vector
+__global__ void __launch_bounds__(32 * M) k_r_tree_up(double *w, const RVec *__restrict__ V,
+                                                      const long long *__restrict__ pre, int nvec,
+                                                      int d) {
+  __shared__ double sB[NTRI];
+  __shared__ double sx[TREE_TILE * TREE_PAD];
+  __shared__ const double *child[TREE_TILE];
+  __shared__ double *par[TREE_TILE];
+  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_lower[t];
+  if (threadIdx.x < TREE_TILE) {
+    const long long idx = (long long)blockIdx.x * TREE_TILE + threadIdx.x;
+    par[threadIdx.x] = nullptr;
+    child[threadIdx.x] = w;
+    if (idx < pre[nvec]) {
+      const int v = find_vec(pre, nvec, idx);
+      const RVec &r = V[v];
+      const long long l = r.g.L - 1 - d;
+      const long long np = (long long)slots_at((size_t)l);
+      const long long q = idx - pre[v];
+      const long long sg = q / np, jp = q - sg * np;
+      double *ws = w + r.wc + sg * r.g.slots * M;
+      child[threadIdx.x] = ws + (2 * (long long)blocks_before((size_t)l + 1) + 2 * jp + 2) * M;
+      par[threadIdx.x] = ws + (2 * (long long)blocks_before((size_t)l) + jp) * M;
+    }
+  }
+  __syncthreads();
+  tree_up_tile(child, par, sB, sx);
+}
+
+__global__ void __launch_bounds__(256) k_r_far(const double *__restrict__ w,
+                                               double *__restrict__ c,
+                                               const RVec *__restrict__ V,
+                                               const RDonor *__restrict__ D,
+                                               const long long *__restrict__ pre, int nvec,
+                                               int dir) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= pre[nvec]) return;
+  const int v = find_vec(pre, nvec, idx);
+  const RVec &r = V[v];
+  const long long nb = r.g.slots / 2;
+  const long long rem = idx - pre[v];
+  const int sg = (int)(rem / (nb * M));
+  const long long q = rem - sg * nb * M;
+  const long long gb = q / M;
+  const int m = (int)(q - gb * M);
+  long long l = 0;
+  while (l + 1 < r.g.L && (long long)blocks_before((size_t)l + 1) <= gb) l++;
+  const long long gd = (long long)blocks_before((size_t)(l + r.lshift)) + gb -
+                       (long long)blocks_before((size_t)l);
+  const long long off = r.wc + sg * r.g.slots * M;
+  far_item(D[r.donor].A[dir] + 3 * gd * MM, w + off, c + off, gb, m);
+}
+
+// level l (from the top) into level l + 1; items (vector, parity, parent slot)
+__global__ void __launch_bounds__(32 * M) k_r_tree_down(double *c, const RVec *__restrict__ V,
+                                                        const long long *__restrict__ pre,
+                                                        int nvec, int l) {
+  __shared__ double sB[NTRI];
+  __shared__ double sx[TREE_TILE * TREE_PAD];
+  __shared__ const double *par[TREE_TILE];
+  __shared__ double *child[TREE_TILE];
+  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_upper[t];
+  if (threadIdx.x < TREE_TILE) {
+    const long long idx = (long long)blockIdx.x * TREE_TILE + threadIdx.x;
+    child[threadIdx.x] = nullptr;
+    par[threadIdx.x] = c;
+    if (idx < pre[nvec]) {
+      const int v = find_vec(pre, nvec, idx);
+      const RVec &r = V[v];
+      const long long np = (long long)slots_at((size_t)l);
+      const long long q = idx - pre[v];
+      const long long sg = q / np, tp = q - sg * np;
+      double *cs = c + r.wc + sg * r.g.slots * M;
+      par[threadIdx.x] = cs + (2 * (long long)blocks_before((size_t)l) + tp) * M;
+      child[threadIdx.x] = cs + (2 * (long long)blocks_before((size_t)l + 1) + 2 * tp) * M;
+    }
+  }
+  __syncthreads();
+  tree_down_tile(par, child, sB, sx);
+}
+
+__global__ void __launch_bounds__(256) k_r_leaf_down(const double *__restrict__ c,
+                                                     const double *__restrict__ y, double *out,
+                                                     const RVec *__restrict__ V,
+                                                     const RDonor *__restrict__ D,
+                                                     const long long *__restrict__ pre, int nvec,
+                                                     int c2l) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= pre[nvec]) return;
+  const int v = find_vec(pre, nvec, idx);
+  const RVec &r = V[v];
+  if (r.direct) return;
+  leaf_down_item(c + r.wc, D[r.donor].T, y + r.io, out + r.io, r.g, c2l, idx - pre[v]);
+}
+
+__global__ void __launch_bounds__(256) k_r_direct(const double *in, double *out,
+                                                  const RVec *__restrict__ V,
+                                                  const RDonor *__restrict__ D,
+                                                  const long long *__restrict__ pre, int nvec,
+                                                  int c2l) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= pre[nvec]) return;
+  const int v = find_vec(pre, nvec, idx);
+  const RVec &r = V[v];
+  if (!r.direct) return;
+  const RDonor &d = D[r.donor];
+  direct_item(in + r.io, out + r.io, d.a, d.an, d.dn, r.g, c2l, idx - pre[v]);
+}
+
+}  // namespace
+
+struct l2c_gpu_ragged {
+  size_t count = 0, total = 0, maxs = 0, dirs = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<l2c_gpu_plan *> donors;
+  RVec *V = nullptr;
+  RDonor *D = nullptr;
+  long long *pre_all = nullptr;  // every prefix array, back to back
+  long long *pre_coef = nullptr, *pre_leaf = nullptr, *pre_far = nullptr;
+  std::vector<long long *> pre_up, pre_down;  // index d (1..Lmax-1), l (0..Lmax-2)
+  long long tot_coef = 0, tot_leaf = 0, tot_far = 0;
+  std::vector<long long> tot_up, tot_down;
+  bool any_direct = false, any_fmm = false;
+  int Lmax = 0;
+  double *x = nullptr, *y = nullptr, *w = nullptr, *c = nullptr;
+  double *st_in = nullptr, *st_out = nullptr;
+  size_t cap_in = 0, cap_out = 0;
+  size_t flops[2] = {0, 0};
+  size_t launches = 0;
+  std::mutex mu;
+};
+
+namespace {
+
+size_t ragged_launch(l2c_gpu_ragged *r, const double *in, double *out, size_t dir) {
+  cudaStream_t st = r->stream;
+  const int c2l = dir == 1, n = (int)r->count;
+  if (r->any_fmm) {
+    const double *x = in;  // L2C reads the caller's packed input directly
+    if (c2l) {
+      k_r_gather<<<blocks_for(r->tot_coef, 256), 256, 0, st>>>(in, r->x, r->V, r->pre_coef, n, 1);
+      x = r->x;
+      r->launches++;
+    }
+    k_r_near<<<blocks_for(r->tot_coef, 256), 256, 0, st>>>(x, out, r->y, r->V, r->D, r->pre_coef,
+                                                           n, c2l);
+    k_r_leaf_up<<<blocks_for(r->tot_leaf, 288), 288, 0, st>>>(x, r->w, r->V, r->D, r->pre_leaf, n);
+    r->launches += 2;
+    for (int d = 1; d < r->Lmax; d++) {
+      if (r->tot_up[d] == 0) continue;
+      k_r_tree_up<<<blocks_for(r->tot_up[d], TREE_TILE), 32 * M, 0, st>>>(r->w, r->V,
+                                                                        r->pre_up[d], n, d);
+      r->launches++;
+    }
+    k_r_far<<<blocks_for(r->tot_far, 256), 256, 0, st>>>(r->w, r->c, r->V, r->D, r->pre_far, n,
+                                                         (int)dir);
+    r->launches++;
+    for (int l = 0; l + 1 < r->Lmax; l++) {
+      if (r->tot_down[l] == 0) continue;
+      k_r_tree_down<<<blocks_for(r->tot_down[l], TREE_TILE), 32 * M, 0, st>>>(r->c, r->V,
+                                                                            r->pre_down[l], n, l);
+      r->launches++;
+    }
+    k_r_leaf_down<<<blocks_for(r->tot_coef, 256), 256, 0, st>>>(r->c, r->y, out, r->V, r->D,
+                                                                r->pre_coef, n, c2l);
+    r->launches++;
+  }
+  if (r->any_direct) {
+    k_r_direct<<<blocks_for(r->tot_coef, 256), 256, 0, st>>>(in, out, r->V, r->D, r->pre_coef, n,
+                                                             c2l);
+    r->launches++;
+  }
+  CK(cudaGetLastError());
+  return 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+void l2c_gpu_ragged_destroy(l2c_gpu_ragged *r) {
+  if (!r) return;
+  DeviceGuard dg(r->device);
+  if (r->stream) cudaStreamSynchronize(r->stream);
+  for (auto *d : r->donors) l2c_gpu_plan_destroy(d);
+  void *bufs[] = {r->V, r->D, r->pre_all, r->x, r->y, r->w, r->c, r->st_in, r->st_out};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  if (r->stream) cudaStreamDestroy(r->stream);
+  delete r;
+}
+
+l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *Ns, size_t maxs,
+                                      size_t directions, unsigned flags) {
+  (void)flags;
+  g_err[0] = 0;
+  if (count == 0 || !Ns || directions > 2) {
+    set_err("ragged plan needs count > 0, lengths, and direction 0, 1 or 2");
+    return nullptr;
+  }
+  l2c_gpu_ragged *r = new (std::nothrow) l2c_gpu_ragged();
+  if (!r) return nullptr;
+  auto fail = [&]() -> l2c_gpu_ragged * {
+    l2c_gpu_ragged_destroy(r);
+    return nullptr;
+  };
+#define RCK(call)                                                                          \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) {                                                               \
+      set_err("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return fail();                                                                       \
+    }                                                                                      \
+  } while (0)
+  r->count = count;
+  r->maxs = maxs;
+  r->dirs = directions;
+  RCK(cudaGetDevice(&r->device));
+  RCK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+  // geometry of every vector; largest level count per leaf size s
+  std::vector<size_t> L(count), S(count);
+  std::vector<std::pair<size_t, size_t>> smax;  // (s, Lmax)
+  size_t max_direct_N = 0;
+  for (size_t v = 0; v < count; v++) {
+    if (Ns[v] == 0) {
+      set_err("vector %zu has length 0", v);
+      return fail();
+    }
+    size_t sv = 0, nn = 0;
+    L[v] = l2c_geometry(Ns[v], maxs, &sv, &nn);
+    S[v] = sv;
+    r->total += Ns[v];
+    if (L[v] == 0) {
+      max_direct_N = std::max(max_direct_N, Ns[v]);
+      continue;
+    }
+    bool found = false;
+    for (auto &e : smax)
+      if (e.first == sv) {
+        e.second = std::max(e.second, L[v]);
+        found = true;
+      }
+    if (!found) smax.push_back({sv, L[v]});
+  }
+  // donors: one per s (A, T and Lambda tables), one direct-only table plan
+  std::vector<RDonor> hD;
+  std::vector<int> donor_of_s(smax.size());
+  for (size_t k = 0; k < smax.size(); k++) {
+    const size_t sv = smax[k].first, Lm = smax[k].second;
+    l2c_gpu_plan *d = l2c_gpu_plan_create(sv << (Lm + 2), sv, directions, 0);
+    if (!d) return fail();
+    if (d->L != Lm || d->s != sv) {
+      set_err("internal: donor geometry mismatch");
+      l2c_gpu_plan_destroy(d);
+      return fail();
+    }
+    r->donors.push_back(d);
+    hD.push_back(RDonor{d->a, d->an, d->dn, d->T, {d->A[0], d->A[1]}});
+    r->Lmax = std::max(r->Lmax, (int)Lm);
+  }
+  int direct_donor = -1;
+  if (max_direct_N > 0) {
+    l2c_gpu_plan *d = l2c_gpu_plan_create(max_direct_N, 1, directions, L2C_PLAN_DIRECT_ONLY);
+    if (!d) return fail();
+    r->donors.push_back(d);
+    hD.push_back(RDonor{d->a, d->an, d->dn, nullptr, {nullptr, nullptr}});
+    direct_donor = (int)hD.size() - 1;
+  }
+  // descriptors and the prefix sums of each phase's work items
+  std::vector<RVec> hV(count);
+  const int Lmax = r->Lmax;
+  std::vector<long long> pc(count + 1), pl(count + 1), pf(count + 1);
+  std::vector<std::vector<long long>> pu(std::max(Lmax, 1), std::vector<long long>(count + 1)),
+      pd(std::max(Lmax, 1), std::vector<long long>(count + 1));
+  long long io = 0, wc = 0;
+  for (size_t v = 0; v < count; v++) {
+    RVec &e = hV[v];
+    Geo &g = e.g;
+    g.N = (long long)Ns[v];
+    g.count = 1;
+    g.dist = 0;
+    g.stride = 1;
+    g.L = (long long)L[v];
+    e.io = io;
+    e.wc = wc;
+    e.direct = L[v] == 0;
+    long long n_leaf = 0, n_far = 0;
+    if (!e.direct) {
+      g.s = (long long)S[v];
+      g.h = 2 * g.s;
+      g.nL = g.N / g.h;
+      g.K = (long long)slots_at(L[v] - 1);
+      g.slots = 2 * (long long)blocks_before(L[v]);
+      g.leaf_base = 2 * (long long)blocks_before(L[v] - 1);
+      size_t k = 0;
+      while (smax[k].first != S[v]) k++;
+      e.donor = (int)k;
+      e.lshift = (int)(smax[k].second - L[v]);
+      n_leaf = g.K * 2 * M;
+      n_far = g.slots * M;  // 2 parities x N_b blocks x M
+      wc += 2 * g.slots * M;
+      r->any_fmm = true;
+    } else {
+      g.s = g.h = g.nL = g.K = g.slots = g.leaf_base = 0;
+      e.donor = direct_donor;
+      e.lshift = 0;
+      r->any_direct = true;
+    }
+    pc[v + 1] = pc[v] + g.N;
+    pl[v + 1] = pl[v] + n_leaf;
+    pf[v + 1] = pf[v] + n_far;
+    for (int d = 1; d < Lmax; d++) {
+      const long long l = (long long)L[v] - 1 - d;
+      pu[d][v + 1] = pu[d][v] + ((!e.direct && l >= 0) ? 2 * (long long)slots_at((size_t)l) : 0);
+    }
+    for (int l = 0; l + 1 < Lmax; l++)
+      pd[l][v + 1] = pd[l][v] + ((!e.direct && (long long)L[v] >= l + 2)
+                                     ? 2 * (long long)slots_at((size_t)l) : 0);
+    io += g.N;
+    for (size_t d = 0; d < 2; d++)
+      if (directions == d || directions == 2)
+        r->flops[d] += ref_flops_geo(Ns[v], L[v], S[v], e.direct ? 0 : blocks_before(L[v]), d);
+  }
+  r->tot_coef = pc[count];
+  r->tot_leaf = pl[count];
+  r->tot_far = pf[count];
+  r->tot_up.assign(std::max(Lmax, 1), 0);
+  r->tot_down.assign(std::max(Lmax, 1), 0);
+  const size_t nlev = (size_t)std::max(Lmax, 1);
+  const size_t npre = (3 + 2 * nlev) * (count + 1);
+  RCK(cudaMalloc(&r->pre_all, npre * sizeof(long long)));
+  std::vector<long long> all;
+  all.reserve(npre);
+  auto push = [&](const std::vector<long long> &vv) { all.insert(all.end(), vv.begin(), vv.end()); };
+  push(pc);
+  push(pl);
+  push(pf);
+  for (size_t d = 0; d < nlev; d++) push(pu[d]);
+  for (size_t l = 0; l < nlev; l++) push(pd[l]);
+  RCK(cudaMemcpy(r->pre_all, all.data(), npre * sizeof(long long), cudaMemcpyHostToDevice));
+  r->pre_coef = r->pre_all;
+  r->pre_leaf = r->pre_all + (count + 1);
+  r->pre_far = r->pre_all + 2 * (count + 1);
+  r->pre_up.resize(nlev);
+  r->pre_down.resize(nlev);
+  for (size_t d = 0; d < nlev; d++) {
+    r->pre_up[d] = r->pre_all + (3 + d) * (count + 1);
+    r->tot_up[d] = pu[d][count];
+  }
+  for (size_t l = 0; l < nlev; l++) {
+    r->pre_down[l] = r->pre_all + (3 + nlev + l) * (count + 1);
+    r->tot_down[l] = pd[l][count];
+  }
+  RCK(cudaMalloc(&r->V, count * sizeof(RVec)));
+  RCK(cudaMemcpy(r->V, hV.data(), count * sizeof(RVec), cudaMemcpyHostToDevice));
+  RCK(cudaMalloc(&r->D, std::max<size_t>(hD.size(), 1) * sizeof(RDonor)));
+  if (!hD.empty())
+    RCK(cudaMemcpy(r->D, hD.data(), hD.size() * sizeof(RDonor), cudaMemcpyHostToDevice));
+  RCK(cudaMalloc(&r->x, std::max<size_t>(r->total, 1) * sizeof(double)));
+  RCK(cudaMalloc(&r->y, std::max<size_t>(r->total, 1) * sizeof(double)));
+  RCK(cudaMalloc(&r->w, std::max<long long>(wc, 1) * sizeof(double)));
+  RCK(cudaMalloc(&r->c, std::max<long long>(wc, 1) * sizeof(double)));
+  return r;
+#undef RCK
+}
+
+size_t l2c_gpu_ragged_total(const l2c_gpu_ragged *r) { return r ? r->total : 0; }
+
+size_t l2c_gpu_ragged_flops(const l2c_gpu_ragged *r, size_t dir) {
+  return (r && dir < 2) ? r->flops[dir] : 0;
+}
+
+void *l2c_gpu_ragged_stream(l2c_gpu_ragged *r) { return r ? (void *)r->stream : nullptr; }
+
+size_t l2c_gpu_ragged_launch_count(const l2c_gpu_ragged *r) { return r ? r->launches : 0; }
+
+size_t l2c_gpu_ragged_execute(l2c_gpu_ragged *r, const double *in, double *out, size_t dir,
+                              unsigned flags) {
+  g_err[0] = 0;
+  if (!r || !in || !out) {
+    set_err("null plan or array");
+    return 0;
+  }
+  if (dir > 1 || !(r->dirs == dir || r->dirs == 2)) {
+    set_err("direction %zu was not planned", dir);
+    return 0;
+  }
+  std::lock_guard<std::mutex> lock(r->mu);
+  DeviceGuard dg(r->device);
+  const bool in_dev = is_device_ptr(in), out_dev = is_device_ptr(out);
+  const size_t n = r->total;
+  if (!in_dev) {
+    if (!grow(&r->st_in, &r->cap_in, n)) return 0;
+    CK(cudaMemcpyAsync(r->st_in, in, n * sizeof(double), cudaMemcpyHostToDevice, r->stream));
+  }
+  if (!out_dev) {
+    if (!grow(&r->st_out, &r->cap_out, n)) return 0;
+    CK(cudaMemcpyAsync(r->st_out, out, n * sizeof(double), cudaMemcpyHostToDevice, r->stream));
+  }
+  double *dout = out_dev ? out : r->st_out;
+  if (!ragged_launch(r, in_dev ? in : r->st_in, dout, dir)) return 0;
+  if (!out_dev)
+    CK(cudaMemcpyAsync(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
+  if (!(flags & L2C_EXEC_ASYNC) || !in_dev || !out_dev) CK(cudaStreamSynchronize(r->stream));
+  return r->flops[dir];
+}
+
+int l2c_gpu_ragged_synchronize(l2c_gpu_ragged *r) {
+  if (!r) return 1;
+  DeviceGuard dg(r->device);
+  if (cudaStreamSynchronize(r->stream) != cudaSuccess) {
+    set_err("cudaStreamSynchronize failed");
+    return 1;
+  }
+  return 0;
+}
+
+}  // extern "C"

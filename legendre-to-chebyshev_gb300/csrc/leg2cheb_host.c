@@ -494,3 +494,51 @@ size_t execute2D(const double *input_array, double *output_array, fmm_plan_2d *p
   herr("axis must be 0, 1 or -1");
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Ragged batches (extension)                                                */
+/* ------------------------------------------------------------------------ */
+fmm_plan_ragged *create_fmm_ragged(size_t count, const size_t *N, size_t maxs, size_t M,
+                                   size_t direction, size_t lagrange, size_t precompute,
+                                   size_t v) {
+  (void)precompute;
+  host_err[0] = 0;
+  if (M != L2C_M || lagrange != 0) {
+    herr("only the modal form with M = 18 is implemented");
+    return NULL;
+  }
+  fmm_plan_ragged *p = (fmm_plan_ragged *)calloc(1, sizeof(fmm_plan_ragged));
+  if (!p) {
+    herr("out of host memory");
+    return NULL;
+  }
+  l2c_gpu_ragged *g = l2c_gpu_ragged_create(count, N, maxs, direction, 0);
+  if (!g) {
+    free(p);
+    return NULL;
+  }
+  p->count = count;
+  p->total = l2c_gpu_ragged_total(g);
+  p->maxs = maxs;
+  p->direction = direction;
+  p->gpu = g;
+  if (v > 1) printf("ragged plan: %zu vectors, %zu coefficients\n", count, p->total);
+  return p;
+}
+
+size_t execute_ragged(const double *input_array, double *output_array, fmm_plan_ragged *p,
+                      size_t direction) {
+  host_err[0] = 0;
+  if (!p || !p->gpu) {
+    herr("null plan");
+    return 0;
+  }
+  return l2c_gpu_ragged_execute((l2c_gpu_ragged *)p->gpu, input_array, output_array, direction,
+                                0);
+}
+
+void free_fmm_ragged(fmm_plan_ragged *p) {
+  if (!p) return;
+  if (p->gpu) l2c_gpu_ragged_destroy((l2c_gpu_ragged *)p->gpu);
+  free(p);
+}

@@ -94,6 +94,21 @@ def load():
     cuda.l2c_gpu_plan_copy.argtypes = [vp, ctypes.c_int, vp, sz]
     cuda.l2c_geometry.restype = sz
     cuda.l2c_geometry.argtypes = [sz, sz, ctypes.POINTER(sz), ctypes.POINTER(sz)]
+    lib.create_fmm_ragged.restype = vp
+    lib.create_fmm_ragged.argtypes = [sz, vp, sz, sz, sz, sz, sz, sz]
+    lib.execute_ragged.restype = sz
+    lib.execute_ragged.argtypes = [vp, vp, vp, sz]
+    lib.free_fmm_ragged.argtypes = [vp]
+    cuda.l2c_gpu_ragged_execute.restype = sz
+    cuda.l2c_gpu_ragged_execute.argtypes = [vp, vp, vp, sz, ctypes.c_uint]
+    cuda.l2c_gpu_ragged_synchronize.restype = ctypes.c_int
+    cuda.l2c_gpu_ragged_synchronize.argtypes = [vp]
+    cuda.l2c_gpu_ragged_stream.restype = vp
+    cuda.l2c_gpu_ragged_stream.argtypes = [vp]
+    cuda.l2c_gpu_ragged_flops.restype = sz
+    cuda.l2c_gpu_ragged_flops.argtypes = [vp, sz]
+    cuda.l2c_gpu_ragged_launch_count.restype = sz
+    cuda.l2c_gpu_ragged_launch_count.argtypes = [vp]
     cuda.l2c_gpu_last_error.restype = ctypes.c_char_p
     cuda.l2c_gpu_version.restype = ctypes.c_char_p
     _lib, _cuda = lib, cuda
@@ -240,6 +255,62 @@ class Leg2Cheb:
             output_array[...] = self._output_array
             return output_array
         return self._output_array
+
+
+class RaggedPlan:
+    """A ragged batch (create_fmm_ragged / execute_ragged / free_fmm_ragged):
+    vectors of lengths Ns packed back to back, all transformed in one set of
+    GPU launches."""
+
+    def __init__(self, Ns, maxs=64, direction=BOTH, verbose=0):
+        lib = load()
+        self.Ns = np.asarray(Ns, dtype=np.uint64)
+        self.offsets = np.concatenate([[0], np.cumsum(self.Ns)]).astype(np.int64)
+        self.total = int(self.offsets[-1])
+        arr = np.ascontiguousarray(self.Ns, dtype=np.uint64)
+        self._p = lib.create_fmm_ragged(len(arr), arr.ctypes.data, maxs, 18, direction, 0, 0,
+                                        verbose)
+        if not self._p:
+            raise L2CError("create_fmm_ragged failed: " + last_error())
+        self._gpu = ctypes.c_void_p(ctypes.cast(self._p, ctypes.POINTER(ctypes.c_void_p * 5))
+                                    .contents[4])
+
+    @property
+    def stream(self):
+        return _cuda.l2c_gpu_ragged_stream(self._gpu)
+
+    def flops(self, direction):
+        return int(_cuda.l2c_gpu_ragged_flops(self._gpu, direction))
+
+    def launch_count(self):
+        return int(_cuda.l2c_gpu_ragged_launch_count(self._gpu))
+
+    def __call__(self, inp, out, direction):
+        f = _lib.execute_ragged(_ptr(inp), _ptr(out), self._p, direction)
+        if f == 0:
+            raise L2CError("execute_ragged failed: " + last_error())
+        return int(f)
+
+    def execute_async(self, inp, out, direction):
+        f = _cuda.l2c_gpu_ragged_execute(self._gpu, _ptr(inp), _ptr(out), direction, 1)
+        if f == 0:
+            raise L2CError(_cuda.l2c_gpu_last_error().decode())
+        return int(f)
+
+    def synchronize(self):
+        if _cuda.l2c_gpu_ragged_synchronize(self._gpu) != 0:
+            raise L2CError(_cuda.l2c_gpu_last_error().decode())
+
+    def close(self):
+        if getattr(self, "_p", None):
+            _lib.free_fmm_ragged(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class DirectPlan:

@@ -616,3 +616,27 @@ size_t orc_execute(const double *in, double *out, orc_plan *p, size_t dir, size_
   free(v);
   return flops;
 }
+
+/* Many independent transforms with one plan, one vector per OpenMP thread (the
+ * per-call parallel loops of orc_execute then run single-threaded inside this
+ * region).  The CPU harness for batched workloads; plan data is read-only and
+ * every call allocates its own work arrays, so concurrent calls are safe. */
+size_t orc_execute_batch(const double *in, double *out, orc_plan *p, size_t direction,
+                         size_t count, size_t dist, size_t stride) {
+  size_t flops = 0;
+#pragma omp parallel for reduction(+ : flops) schedule(dynamic, 1)
+  for (size_t v = 0; v < count; v++)
+    flops += orc_execute(in + v * dist, out + v * dist, p, direction, stride);
+  return flops;
+}
+
+/* Ragged list: vector v of plans[v]->N coefficients at in + off[v], out + off[v],
+ * one vector per OpenMP thread (CPU harness for ragged workloads). */
+size_t orc_execute_ragged(const double *in, double *out, orc_plan **plans, const size_t *off,
+                          size_t count, size_t direction) {
+  size_t flops = 0;
+#pragma omp parallel for reduction(+ : flops) schedule(dynamic, 1)
+  for (size_t v = 0; v < count; v++)
+    flops += orc_execute(in + off[v], out + off[v], plans[v], direction, 1);
+  return flops;
+}

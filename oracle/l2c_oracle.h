@@ -37,6 +37,16 @@ void orc_free(orc_plan *p);
 size_t orc_execute(const double *in, double *out, orc_plan *p, size_t direction,
                    size_t stride);
 
+/* count transforms of one plan, vector v at in + v*dist, out + v*dist, one
+ * vector per OpenMP thread (CPU harness for batched workloads). */
+size_t orc_execute_batch(const double *in, double *out, orc_plan *p, size_t direction,
+                         size_t count, size_t dist, size_t stride);
+
+/* Ragged list: vector v of plans[v]'s length at in + off[v], out + off[v],
+ * one vector per OpenMP thread (CPU harness for ragged workloads). */
+size_t orc_execute_ragged(const double *in, double *out, orc_plan **plans, const size_t *off,
+                          size_t count, size_t direction);
+
 /* Near field only, with the final scaling: directM (leg2cheb.c:236-376, L2C,
  * strided input and output) and directL (leg2cheb.c:378-535, C2L, input is the
  * premultiplied contiguous copy v, output strided).  FMM plans only. */

@@ -34,6 +34,10 @@ def load():
     lib.orc_execute.restype = sz
     lib.orc_execute.argtypes = [vp, vp, vp, sz, sz]
     lib.orc_plan_info.argtypes = [vp, vp]
+    lib.orc_execute_batch.restype = sz
+    lib.orc_execute_batch.argtypes = [vp, vp, vp, sz, sz, sz, sz]
+    lib.orc_execute_ragged.restype = sz
+    lib.orc_execute_ragged.argtypes = [vp, vp, vp, vp, sz, sz]
     for name in ("orc_directM", "orc_directL"):
         getattr(lib, name).restype = sz
         getattr(lib, name).argtypes = [vp, vp, vp, sz]
@@ -71,6 +75,11 @@ class Oracle:
         self.execute(np.ascontiguousarray(u, dtype=np.float64), out, direction, stride)
         return out
 
+    def execute_batch(self, u, out, direction, count, dist, stride=1):
+        assert u.dtype == np.float64 and out.dtype == np.float64
+        return int(load().orc_execute_batch(u.ctypes.data, out.ctypes.data, self._p, direction,
+                                            count, dist, stride))
+
     def directM(self, u, out, stride=1):
         return int(load().orc_directM(u.ctypes.data, out.ctypes.data, self._p, stride))
 
@@ -103,3 +112,23 @@ class Oracle:
 
 def set_threads(n):
     load().orc_set_threads(int(n))
+
+
+class RaggedOracle:
+    """Per-vector oracle plans for a ragged list (plans shared between equal N)."""
+
+    def __init__(self, Ns, maxs=64, direction=2):
+        self.Ns = [int(n) for n in Ns]
+        cache = {}
+        self.plans = []
+        for n in self.Ns:
+            if n not in cache:
+                cache[n] = Oracle(n, maxs, direction)
+            self.plans.append(cache[n])
+        self._keep = cache
+        self.offsets = np.concatenate([[0], np.cumsum(self.Ns)]).astype(np.uint64)
+        self._pp = (ctypes.c_void_p * len(self.plans))(*[p._p for p in self.plans])
+
+    def execute(self, u, out, direction):
+        return int(load().orc_execute_ragged(u.ctypes.data, out.ctypes.data, self._pp,
+                                             self.offsets.ctypes.data, len(self.Ns), direction))

@@ -299,3 +299,59 @@ def test_async_device_execution(lib, orc, torch_cuda):
     want = o(x[3], 0)[:N]
     for o_ in outs:
         assert relerr(o_.cpu().numpy()[3], want) <= TOL
+
+
+def ragged_lengths(count, seed, lo=64, hi=65536):
+    """N log-uniform in [lo, hi] (the ragged-list workload's distribution)."""
+    rng = np.random.default_rng(seed)
+    return np.round(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(np.int64)
+
+
+@pytest.mark.parametrize("maxs", [64, 36])
+def test_ragged_batch_matches_per_vector(lib, orc, maxs):
+    Ns = list(ragged_lengths(40, 7, 20, 20000)) + [20, 255, 256, 257, 300, 1023, 5001]
+    p = lib.RaggedPlan(Ns, maxs)
+    u = make_input(p.total, "uniform", 3)
+    for d in (0, 1):
+        out = np.zeros(p.total)
+        flops = p(u, out, d)
+        want_flops = 0
+        for v, N in enumerate(Ns):
+            a, b = p.offsets[v], p.offsets[v + 1]
+            o = orc.Oracle(int(N), maxs, 2)
+            w = np.zeros(int(N))
+            want_flops += o.execute(np.ascontiguousarray(u[a:b]), w, d)
+            assert relerr(out[a:b], w) <= TOL, (v, N, d)
+        assert flops == want_flops
+
+
+def test_ragged_accumulates_like_execute(lib):
+    Ns = [100, 4096, 777, 65536, 3000]
+    p = lib.RaggedPlan(Ns, 64)
+    u = make_input(p.total, "sign", 1)
+    pre = make_input(p.total, "gauss", 2)
+    for d in (0, 1):
+        out = pre.copy()
+        p(u, out, d)
+        for v, N in enumerate(Ns):
+            a, b = p.offsets[v], p.offsets[v + 1]
+            single = lib.Plan(int(N), 64)
+            want = pre[a:b].copy()
+            single.execute(np.ascontiguousarray(u[a:b]), want, d)
+            assert relerr(out[a:b], want) <= TOL
+
+
+def test_ragged_device_pointers_and_launch_count(lib, torch_cuda):
+    torch = torch_cuda
+    Ns = ragged_lengths(500, 11)
+    p = lib.RaggedPlan(Ns, 64)
+    u = make_input(p.total, "uniform", 4)
+    host = np.zeros(p.total)
+    p(u, host, 1)
+    du = torch.from_numpy(u).cuda()
+    dout = torch.zeros_like(du)
+    before = p.launch_count()
+    p.execute_async(du, dout, 1)
+    p.synchronize()
+    assert p.launch_count() - before <= 24  # independent of the 500 vectors
+    assert np.array_equal(dout.cpu().numpy(), host)
