@@ -465,6 +465,207 @@ __global__ void __launch_bounds__(32 * M) k_tree_up(double *w, Geo g, long long 
   tree_up_tile(child, par, sB, sx);
 }
 
+// Two-stage sweeps for deep trees.  Every tree level costs a launch and a chain
+// of dependent FP64 operations (64 cycles each on this part) however little work
+// it holds, so the L-1 levels of a sweep are not launched one by one:
+//   subtree kernels: one CTA per (vector, parity, subtree root r at level l0)
+//     runs the d = L-1-l0 levels below l0 in shared memory;
+//   top kernels: one CTA per (vector, parity) runs the levels above lt <= l0
+//     in shared memory; levels between lt and l0 (only for very deep trees) use
+//     the tiled per-level kernels above.
+// Node index t at level l covers 2^k nodes [t 2^k, (t+1) 2^k) at level l+k.
+// Source slots of level l are nodes 2..2^(l+2)-1 (slot = node - 2), target
+// slots are nodes 0..2^(l+2)-3.
+constexpr int SUB_PAD = M + 1;  // padded node stride in shared memory
+
+__device__ __forceinline__ void row_up(const double *sB, const double *x0, const double *x1, int m,
+                                       double &out) {
+  const double *Bm = sB + m * (m + 1) / 2;
+  double s0 = 0.0, s1 = 0.0;
+  for (int i = 0; i <= m; i++) {
+    const double bmi = Bm[i];
+    s0 = fma(bmi, x0[i], s0);
+    s1 = fma(((m + i) & 1) ? -bmi : bmi, x1[i], s1);
+  }
+  out = s0 + s1;
+}
+
+__device__ __forceinline__ void row_down(const double *sB, const double *xp, int i, double &se,
+                                         double &so) {
+  const double *Bu = sB + i * M - i * (i - 1) / 2 - i;
+  se = 0.0;
+  so = 0.0;
+  int j = i;
+  for (; j + 1 < M; j += 2) {
+    se = fma(Bu[j], xp[j], se);
+    so = fma(Bu[j + 1], xp[j + 1], so);
+  }
+  if (j < M) se = fma(Bu[j], xp[j], se);
+}
+
+// Upward, levels L-1 .. l0 of one subtree.  blockIdx.x = vs * R + r, R = 2^(l0+2).
+// Dynamic shared memory: (2^(d+1) - 1) nodes of SUB_PAD doubles.
+__global__ void __launch_bounds__(32 * M) k_up_sub(double *w, Geo g, int l0, int d) {
+  extern __shared__ double sm[];
+  __shared__ double sB[NTRI];
+  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_lower[t];
+  const long long R = 4LL << l0;
+  const long long vs = blockIdx.x / R, r = blockIdx.x - vs * R;
+  double *ws = w + vs * g.slots * M;
+  // leaf level of the subtree
+  const int nl = 1 << d;
+  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
+    const int p = e / M, m = e - p * M;
+    const long long t = r * nl + p;
+    sm[p * SUB_PAD + m] = t >= 2 ? ws[(g.leaf_base + t - 2) * M + m] : 0.0;
+  }
+  __syncthreads();
+  const int m = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *child = sm;
+  for (int k = 1; k <= d; k++) {
+    const int np = nl >> k;
+    double *par = child + 2 * np * SUB_PAD;
+    const int l = g.L - 1 - k;
+    const long long base = 2 * (long long)blocks_before((size_t)l);
+    if (m < M) {
+      for (int p = lane; p < np; p += 32) {
+        const long long u = r * np + p;
+        if (u < 2) continue;
+        double out;
+        row_up(sB, child + 2 * p * SUB_PAD, child + (2 * p + 1) * SUB_PAD, m, out);
+        par[p * SUB_PAD + m] = out;
+        ws[(base + u - 2) * M + m] = out;
+      }
+    }
+    __syncthreads();
+    child = par;
+  }
+}
+
+// Upward, levels lt-1 .. 0 of one (vector, parity) from level lt in global
+// memory.  Dynamic shared memory: sum over l <= lt of 2^(l+2) nodes.
+__global__ void __launch_bounds__(32 * M) k_up_top(double *w, Geo g, int lt) {
+  extern __shared__ double sm[];
+  __shared__ double sB[NTRI];
+  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_lower[t];
+  const long long vs = blockIdx.x;
+  double *ws = w + vs * g.slots * M;
+  // node t of level l at sm + (off(l) + t) * SUB_PAD, off(l) = 2^(l+2) - 4
+  const long long nt = 4LL << lt;
+  for (long long e = threadIdx.x; e < (nt - 2) * M; e += blockDim.x) {
+    const long long j = e / M;
+    const int m = (int)(e - j * M);
+    sm[((nt - 4) + j + 2) * SUB_PAD + m] = ws[(2 * (long long)blocks_before((size_t)lt) + j) * M + m];
+  }
+  __syncthreads();
+  const int m = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int l = lt - 1; l >= 0; l--) {
+    const long long nn = 4LL << l;  // nodes of level l
+    double *par = sm + (nn - 4) * SUB_PAD, *child = sm + (2 * nn - 4) * SUB_PAD;
+    const long long base = 2 * (long long)blocks_before((size_t)l);
+    if (m < M) {
+      for (long long u = 2 + lane; u < nn; u += 32) {
+        double out;
+        row_up(sB, child + 2 * u * SUB_PAD, child + (2 * u + 1) * SUB_PAD, m, out);
+        par[u * SUB_PAD + m] = out;
+        ws[(base + u - 2) * M + m] = out;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Downward, levels 0 .. lt of one (vector, parity): c[l+1] += B^T c[l] for
+// l < lt, then levels 1..lt written back.  Dynamic shared memory as k_up_top.
+__global__ void __launch_bounds__(32 * M) k_down_top(double *c, Geo g, int lt) {
+  extern __shared__ double sm[];
+  __shared__ double sB[NTRI];
+  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_upper[t];
+  const long long vs = blockIdx.x;
+  double *cs = c + vs * g.slots * M;
+  // target node t of level l at sm + (off(l) + t) * SUB_PAD; slots t < 2^(l+2)-2
+  for (int l = 0; l <= lt; l++) {
+    const long long nn = (4LL << l) - 2;
+    const long long off = (4LL << l) - 4, base = 2 * (long long)blocks_before((size_t)l);
+    for (long long e = threadIdx.x; e < nn * M; e += blockDim.x) {
+      const long long t = e / M;
+      const int m = (int)(e - t * M);
+      sm[(off + t) * SUB_PAD + m] = cs[(base + t) * M + m];
+    }
+  }
+  __syncthreads();
+  const int i = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int l = 0; l < lt; l++) {
+    const long long nn = (4LL << l) - 2;
+    double *par = sm + ((4LL << l) - 4) * SUB_PAD, *child = sm + ((8LL << l) - 4) * SUB_PAD;
+    if (i < M) {
+      for (long long t = lane; t < nn; t += 32) {
+        double se, so;
+        row_down(sB, par + t * SUB_PAD, i, se, so);
+        child[(2 * t) * SUB_PAD + i] += se + so;
+        child[(2 * t + 1) * SUB_PAD + i] += se - so;
+      }
+    }
+    __syncthreads();
+  }
+  for (int l = 1; l <= lt; l++) {
+    const long long nn = (4LL << l) - 2;
+    const long long off = (4LL << l) - 4, base = 2 * (long long)blocks_before((size_t)l);
+    for (long long e = threadIdx.x; e < nn * M; e += blockDim.x) {
+      const long long t = e / M;
+      const int m = (int)(e - t * M);
+      cs[(base + t) * M + m] = sm[(off + t) * SUB_PAD + m];
+    }
+  }
+}
+
+// Downward, levels l0 .. L-1 of one subtree (target root r at level l0);
+// writes the final leaf level.  blockIdx.x = vs * R + r.
+__global__ void __launch_bounds__(32 * M) k_down_sub(double *c, Geo g, int l0, int d) {
+  extern __shared__ double sm[];
+  __shared__ double sB[NTRI];
+  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_upper[t];
+  const long long R = 4LL << l0;
+  const long long vs = blockIdx.x / R, r = blockIdx.x - vs * R;
+  double *cs = c + vs * g.slots * M;
+  // level l0 + k of the subtree: 2^k nodes at sm + (2^k - 1) * SUB_PAD
+  for (int k = 0; k <= d; k++) {
+    const int nk = 1 << k;
+    const int l = l0 + k;
+    const long long nslot = (4LL << l) - 2, base = 2 * (long long)blocks_before((size_t)l);
+    double *lev = sm + (nk - 1) * SUB_PAD;
+    for (int e = threadIdx.x; e < nk * M; e += blockDim.x) {
+      const int p = e / M, m = e - p * M;
+      const long long t = r * nk + p;
+      lev[p * SUB_PAD + m] = t < nslot ? cs[(base + t) * M + m] : 0.0;
+    }
+  }
+  __syncthreads();
+  const int i = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int k = 0; k < d; k++) {
+    const int nk = 1 << k;
+    const long long nslot = (4LL << (l0 + k)) - 2;
+    double *par = sm + (nk - 1) * SUB_PAD, *child = sm + (2 * nk - 1) * SUB_PAD;
+    if (i < M) {
+      for (int p = lane; p < nk; p += 32) {
+        if (r * nk + p >= nslot) continue;
+        double se, so;
+        row_down(sB, par + p * SUB_PAD, i, se, so);
+        child[(2 * p) * SUB_PAD + i] += se + so;
+        child[(2 * p + 1) * SUB_PAD + i] += se - so;
+      }
+    }
+    __syncthreads();
+  }
+  const int nl = 1 << d;
+  const double *leaf = sm + (nl - 1) * SUB_PAD;
+  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
+    const int p = e / M, m = e - p * M;
+    const long long t = r * nl + p;
+    if (t < g.K) cs[(g.leaf_base + t) * M + m] = leaf[p * SUB_PAD + m];
+  }
+}
+
 // Step 3: far-field blocks.  Ablk: the three 18x18 blocks of a block owning
 // slots 2 gb, 2 gb + 1 of the tree ws / cs of one (vector, parity):
 // c0 = A0 w0 + A1 w1, c1 = A2 w1 (leg2cheb.c:1419-1435).
@@ -832,6 +1033,78 @@ struct DeviceGuard {
   }
 };
 
+// How a sweep over L levels is split (see k_up_sub): subtree root level l0,
+// subtree depth d = L-1-l0, top-kernel start level lt.  Roots per (vector,
+// parity) are 2^(l0+2); l0 is chosen so the subtree kernel has about two CTAs
+// per SM, d is at most 7 (shared memory), lt at most 4 (one CTA runs the top).
+struct TreePlan {
+  int l0, d, lt;
+  bool staged;  // false: one tiled launch per level
+};
+
+TreePlan tree_plan(size_t L, size_t count) {
+  TreePlan t{0, 0, 0, false};
+  if (L < 4) return t;
+  int l0 = 0;
+  while (l0 + 1 < (int)L - 1 && (double)count * 2.0 * (double)(8LL << l0) <= 2.0 * 152) l0++;
+  if ((int)L - 1 - l0 > 7) l0 = (int)L - 8;
+  t.l0 = l0;
+  t.d = (int)L - 1 - l0;
+  t.lt = std::min(l0, 4);
+  t.staged = t.d >= 1;
+  return t;
+}
+
+size_t tree_launches(const TreePlan &t, size_t L) {
+  if (!t.staged) return L - 1;
+  return 1 + (size_t)(t.l0 - t.lt) + (t.lt > 0 ? 1 : 0);
+}
+
+size_t sub_smem(int d) { return ((size_t)(2 << d) - 1) * SUB_PAD * sizeof(double); }
+size_t top_smem(int lt) { return ((size_t)(8LL << lt) - 4) * SUB_PAD * sizeof(double); }
+
+cudaError_t sweep_up(double *w, const Geo &g, const TreePlan &t, cudaStream_t st) {
+  if (!t.staged) {
+    for (long long l = g.L - 2; l >= 0; l--) {
+      const long long np = (long long)slots_at((size_t)l);
+      k_tree_up<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
+          w, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
+    }
+    return cudaGetLastError();
+  }
+  const unsigned nsub = (unsigned)(g.count * 2 * (4LL << t.l0));
+  k_up_sub<<<nsub, 32 * M, sub_smem(t.d), st>>>(w, g, t.l0, t.d);
+  for (long long l = t.l0 - 1; l >= t.lt; l--) {
+    const long long np = (long long)slots_at((size_t)l);
+    k_tree_up<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
+        w, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
+  }
+  if (t.lt > 0)
+    k_up_top<<<(unsigned)(g.count * 2), 32 * M, top_smem(t.lt), st>>>(w, g, t.lt);
+  return cudaGetLastError();
+}
+
+cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t st) {
+  if (!t.staged) {
+    for (long long l = 0; l + 1 < g.L; l++) {
+      const long long np = (long long)slots_at((size_t)l);
+      k_tree_down<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
+          c, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
+    }
+    return cudaGetLastError();
+  }
+  if (t.lt > 0)
+    k_down_top<<<(unsigned)(g.count * 2), 32 * M, top_smem(t.lt), st>>>(c, g, t.lt);
+  for (long long l = t.lt; l < t.l0; l++) {
+    const long long np = (long long)slots_at((size_t)l);
+    k_tree_down<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
+        c, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
+  }
+  const unsigned nsub = (unsigned)(g.count * 2 * (4LL << t.l0));
+  k_down_sub<<<nsub, 32 * M, sub_smem(t.d), st>>>(c, g, t.l0, t.d);
+  return cudaGetLastError();
+}
+
 // Near field for all vectors of a batch: full groups of 8 (4, 2) vectors per
 // thread, then the remainder.
 cudaError_t launch_near(const double *x, const double *out, double *y, const double *a,
@@ -941,15 +1214,11 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     k_leaf_up<<<blocks_for(leaf_threads, 288), 288, 0, st>>>(x, p->T, p->w, g);
     CK(cudaGetLastError());
   }
+  const TreePlan tp = tree_plan(p->L, count);
   {
-    PhaseScope ps(p, L2C_PHASE_TREE_UP, p->L - 1);
-    for (long long l = (long long)p->L - 2; l >= 0; l--) {
-      const long long np = (long long)slots_at((size_t)l);
-      k_tree_up<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
-          p->w, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
-    }
+    PhaseScope ps(p, L2C_PHASE_TREE_UP, tree_launches(tp, p->L));
+    CK(sweep_up(p->w, g, tp, st));
   }
-  CK(cudaGetLastError());
   {
     PhaseScope ps(p, L2C_PHASE_FAR, 1);
     const long long n = g.count * 2 * (long long)p->Nb * M;
@@ -957,14 +1226,9 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaGetLastError());
   }
   {
-    PhaseScope ps(p, L2C_PHASE_TREE_DOWN, p->L - 1);
-    for (long long l = 0; l + 1 < (long long)p->L; l++) {
-      const long long np = (long long)slots_at((size_t)l);
-      k_tree_down<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
-          p->c, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
-    }
+    PhaseScope ps(p, L2C_PHASE_TREE_DOWN, tree_launches(tp, p->L));
+    CK(sweep_down(p->c, g, tp, st));
   }
-  CK(cudaGetLastError());
   if (p->overlap) CK(cudaStreamWaitEvent(st, p->ev_join, 0));
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
