@@ -189,6 +189,14 @@ class Workload:
             self.u = gauss2_lines(self.count, N, seed)
             # L2C of every line, then C2L of the result
             self.calls = [(0, "u", "o0"), (1, "o0", "o1")]
+        elif name in ("mixed_batch", "mixed_batch_ref"):
+            self.count = 256
+            self.u = np.random.default_rng(seed).standard_normal((self.count, N))
+            self.calls = [(0, "u", "o0"), (1, "u", "o1")]
+        elif name == "mixed_single":
+            self.count = 1
+            self.u = np.random.default_rng(seed).standard_normal((1, N))
+            self.calls = [(0, "u", "o0"), (1, "u", "o1")]
         elif name == "ragged":
             self.Ns = ragged_lengths(2000, seed)
             self.count = len(self.Ns)
@@ -207,6 +215,8 @@ class Workload:
                                getattr(self, "total", None))
 
     def cpu_oracle(self, oracle):
+        if self.name == "mixed_batch_ref":
+            return oracle.Oracle(self.N, self.maxs, 2)
         if self.name == "ragged":
             return oracle.RaggedOracle(self.Ns, self.maxs, 2)
         return oracle.Oracle(self.N, self.maxs, 2)
@@ -216,6 +226,8 @@ class Workload:
             o.execute(src[0], dst[0], d)
         elif self.count == 1:
             o.execute(src[0], dst[0], d)
+        elif self.name == "mixed_batch_ref":
+            o.execute_batch(src, dst, d, self.count, self.N)
         else:
             o.execute_batch(src, dst, d, self.count, self.N)
 
@@ -286,13 +298,122 @@ def run_reference(args):
     return 0
 
 
+def run_mixed(args):
+    """Mixed form against plain FP64 on the same inputs: single vector N = 2^22
+    (mixed_single) or 256 vectors of N = 16384 (mixed_batch), iid N(0,1), L2C and
+    C2L of the same input per step.  value = the mixed form's throughput."""
+    import ctypes
+
+    import torch
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    sys.path.insert(0, PKG)
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("l2c_pkg_build", os.path.join(PKG, "build.py"))
+    bmod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bmod)
+    bmod.build()
+    import l2c_gb300 as l2c
+
+    wl = Workload(args.workload, args.N, args.maxs, 1)
+    N, count = wl.N, wl.count
+    du = torch.from_numpy(np.ascontiguousarray(wl.u)).to(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    peak = measured_fp64_peak(torch, dev)
+
+    def time_plan(plan):
+        stream = torch.cuda.ExternalStream(plan.stream, device=dev)
+        outs = [torch.zeros_like(du), torch.zeros_like(du)]
+
+        def step():
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+                outs[0].zero_()
+                outs[1].zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.execute_async(du, outs[0], 0, count, N, 1)
+            plan.execute_async(du, outs[1], 1, count, N, 1)
+            e1.record(stream)
+            return e0, e1
+
+        for _ in range(args.warmup):
+            step()
+        plan.synchronize()
+        l0 = l2c.cuda_abi().l2c_gpu_launch_count(plan._gpu)
+        evs = [step() for _ in range(args.steps)]
+        plan.synchronize()
+        launches = l2c.cuda_abi().l2c_gpu_launch_count(plan._gpu) - l0
+        ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+        return ms, [o.cpu().numpy() for o in outs], launches
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    results = {}
+    for name, maxs, mixed in (("plain_maxs64", 64, False), ("plain_maxs32", 32, False),
+                              ("mixed", args.maxs_mixed, True)):
+        plan = l2c.Plan(N, maxs, mixed=mixed)
+        ms, outs, launches = time_plan(plan)
+        results[name] = {"maxs": maxs, "s": plan.s, "L": plan.L, "ms_per_step": ms,
+                         "value": 2 * count * N / (ms * 1e-3), "launches": launches,
+                         "flops": plan.flops(0) + plan.flops(1), "outs": outs}
+        plan.close()
+    clk = clocks.stop()
+    # accuracy against the oracle port (FP64) on the same inputs
+    sys.path.insert(0, REPO)
+    from oracle import oracle
+
+    oracle.set_threads(os.cpu_count() or 1)
+    errs = {}
+    for name, r in results.items():
+        o = oracle.Oracle(N, r["maxs"], 2)
+        e = []
+        for d in (0, 1):
+            want = np.zeros_like(wl.u)
+            if count == 1:
+                o.execute(np.ascontiguousarray(wl.u[0]), want[0], d)
+            else:
+                o.execute_batch(np.ascontiguousarray(wl.u), want, d, count, N)
+            e.append(float(np.max(np.abs(r["outs"][d] - want)) / np.max(np.abs(want))))
+        errs[name] = {"l2c": e[0], "c2l": e[1]}
+        del r["outs"]
+    mixed = results["mixed"]
+    best_plain = min((results[k]["ms_per_step"], k) for k in results if k.startswith("plain"))
+    fp64_flops_mixed = None
+    line = {
+        "metric": METRIC, "value": mixed["value"], "unit": "coef/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (mixed: split-bf16 tensor-core far field, fp64 band)",
+        "data": "synthetic (seeded iid N(0,1))",
+        "config": {"workload": f"mixed vs plain FP64, {'single vector' if count == 1 else str(count) + ' vectors'} "
+                               f"of N={N}, L2C and C2L of the same input per step",
+                   "N": N, "vectors": count, "maxs_mixed": args.maxs_mixed,
+                   "l2_flush": "256 MiB write between steps"},
+        "plans": results,
+        "max_rel_err_vs_oracle": errs,
+        "speedup_mixed_vs_plain_maxs64": results["plain_maxs64"]["ms_per_step"] / mixed["ms_per_step"],
+        "speedup_mixed_vs_best_plain": best_plain[0] / mixed["ms_per_step"],
+        "best_plain": best_plain[1],
+        "clocks": clk,
+        "fp64_peak_tflops_measured": peak,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="single", choices=["single", "batch", "ragged"])
+    ap.add_argument("--workload", default="single",
+                    choices=["single", "batch", "ragged", "mixed_single", "mixed_batch"])
+    ap.add_argument("--maxs-mixed", type=int, default=16,
+                    help="leaf size bound of the mixed-form plan (mixed_* workloads)")
     ap.add_argument("--N", type=int, default=None)
     ap.add_argument("--maxs", type=int, default=64)
     ap.add_argument("--precompute", type=int, default=0,
@@ -303,7 +424,13 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.N is None:
-        args.N = 1 << 20 if args.workload == "single" else 1024
+        args.N = {"single": 1 << 20, "batch": 1024, "ragged": 1024, "mixed_single": 1 << 22,
+                  "mixed_batch": 16384}[args.workload]
+    if args.workload.startswith("mixed"):
+        if args.impl == "reference":
+            args.workload = "single" if args.workload == "mixed_single" else "mixed_batch_ref"
+        else:
+            return run_mixed(args)
     if args.impl == "reference":
         return run_reference(args)
 

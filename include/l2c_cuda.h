@@ -27,6 +27,11 @@ typedef struct l2c_gpu_plan l2c_gpu_plan;
                                        the reference's `precompute`, leg2cheb.c:1108-1193):
                                        one FP64 FMA per band term instead of two ops */
 
+#define L2C_PLAN_MIXED 4u /* mixed form: leaf, transfer and far-field products as
+                                FP64-accurate split-BF16 tensor-core products (no
+                                FP64 instructions); near-field band, accumulation and
+                                scaling in FP64.  Leaf sizes s <= 64. */
+
 /* Execute flags */
 #define L2C_EXEC_ASYNC 1u       /* return without waiting (device pointers only)  */
 #define L2C_EXEC_NEAR_ONLY 2u   /* near-field band + final scaling only (directM/L) */

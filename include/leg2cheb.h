@@ -184,6 +184,16 @@ const char *l2c_last_error(void);
 size_t execute_batched(const double *input_array, double *output_array, fmm_plan *fmmplan,
                        size_t direction, size_t count, size_t dist, size_t stride);
 
+/* create_fmm with extra plan options (bit flags):
+ *   L2C_FMM_MIXED   the mixed form: leaf, transfer and far-field products as
+ *                   FP64-accurate split-BF16 tensor-core products; near-field band,
+ *                   accumulation and scaling in FP64 (maxs <= 64)
+ * Same semantics as create_fmm otherwise. */
+#define L2C_FMM_MIXED 1u
+fmm_plan *create_fmm_ex(const size_t N, const size_t maxs, const size_t M, const size_t direction,
+                        const size_t lagrange, const size_t precompute, const size_t v,
+                        unsigned flags);
+
 /* Ragged batch: count vectors of lengths N[0..count), packed back to back
  * (vector v starts at N[0] + ... + N[v-1]); each is transformed exactly as
  * execute() with create_fmm(N[v], maxs, M, direction, ...) would, all in one set

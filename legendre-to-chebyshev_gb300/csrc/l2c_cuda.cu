@@ -32,6 +32,7 @@
 
 #include "../../include/l2c_cuda.h"
 #include "l2c_lambda.h"
+#include "l2c_ozaki.cuh"
 
 namespace {
 
@@ -838,6 +839,287 @@ inline unsigned blocks_for(long long n, int threads) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// Mixed-precision far field (L2C_PLAN_MIXED): the leaf, transfer and far-field
+// products on BF16 tensor cores through l2c_ozaki.cuh, FP64-accurate with no
+// FP64 instructions; the near-field band, the final accumulation and scaling
+// stay in FP64.  Every kernel: one warp per 8 right-hand-side columns; the
+// constant left factor is pre-sliced at plan time.
+// ---------------------------------------------------------------------------
+constexpr int MXW = 4;  // warps per CTA
+
+// 8 columns of K values (loader ld(c, k)) -> fix56 form and column exponents.
+template <int KT, class Loader>
+__device__ __forceinline__ void mx_stage(unsigned long long *Qf, int qld, int *Qe, int K,
+                                         Loader ld) {
+  const int lane = threadIdx.x & 31;
+  const int c = lane >> 2, k0 = lane & 3;
+  int e = l2c_oz::EXP_ZERO;
+  for (int k = k0; k < K; k += 4) e = max(e, l2c_oz::exp_bound(ld(c, k)));
+  e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
+  e = max(e, __shfl_xor_sync(0xffffffffu, e, 2));
+  for (int k = k0; k < KT * 16; k += 4) Qf[c * qld + k] = k < K ? l2c_oz::fix56(ld(c, k), e) : 0ull;
+  if (k0 == 0) Qe[c] = e;
+  __syncwarp();
+}
+
+template <int KT>
+struct MxSmem {
+  static constexpr int QLD = KT * 16 + 1;
+  unsigned long long Qf[MXW][8 * QLD];
+  int Qe[MXW][8];
+};
+
+// Leaf up (step 1): columns (parity, vector, leaf node), K = s, rows m < 18.
+// P = T_parity^T (18 x s): Pt + sg * SLICES * 18 * kld.
+template <int KT>
+__global__ void __launch_bounds__(32 * MXW)
+    k_mx_leaf_up(const double *__restrict__ x, double *__restrict__ w,
+                 const __nv_bfloat16 *__restrict__ Pt, const int *__restrict__ Pte, int kld,
+                 Geo g) {
+  __shared__ MxSmem<KT> sm;
+  const int wid = threadIdx.x >> 5;
+  const long long ncol = g.count * g.K, ngrp = (ncol + 7) / 8;
+  const long long grp = (long long)blockIdx.x * MXW + wid;
+  if (grp >= 2 * ngrp) return;
+  const int sg = (int)(grp / ngrp);
+  const long long col0 = (grp - sg * ngrp) * 8;
+  auto ld = [&](int c, int k) -> double {
+    const long long col = col0 + c;
+    if (col >= ncol || k >= g.s) return 0.0;
+    const long long v = col / g.K, node = col - v * g.K;
+    const long long idx = (node + 2) * g.h + 2 * k + sg;
+    return idx < g.N ? x[v * g.N + idx] : 0.0;
+  };
+  mx_stage<KT>(sm.Qf[wid], MxSmem<KT>::QLD, sm.Qe[wid], (int)g.s, ld);
+  double out[2][4];
+  l2c_oz::warp_tile<2, KT>(Pt + (size_t)sg * l2c_oz::SLICES * 18 * kld, 18 * kld, kld, 18,
+                           (int)g.s, Pte + sg * 18, sm.Qf[wid], MxSmem<KT>::QLD, sm.Qe[wid], out);
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int m = mt * 16 + (lane >> 2) + 8 * (e >> 1);
+      const long long col = col0 + 2 * (lane & 3) + (e & 1);
+      if (m >= M || col >= ncol) continue;
+      const long long v = col / g.K, node = col - v * g.K;
+      w[((v * 2 + sg) * g.slots + g.leaf_base + node) * M + m] = out[mt][e];
+    }
+}
+
+// Leaf down (step 5) + final scaling: columns (parity, vector, leaf target node),
+// K = 18, rows i < s.  P = T_parity (s x 18): Pn + sg * SLICES * s * 18.
+template <int MT>
+__global__ void __launch_bounds__(32 * MXW)
+    k_mx_leaf_down(const double *__restrict__ c, const double *__restrict__ y, double *out,
+                   const __nv_bfloat16 *__restrict__ Pn, const int *__restrict__ Pne, Geo g,
+                   int c2l) {
+  __shared__ MxSmem<2> sm;
+  const int wid = threadIdx.x >> 5;
+  const long long ncol = g.count * g.K, ngrp = (ncol + 7) / 8;
+  const long long grp = (long long)blockIdx.x * MXW + wid;
+  if (grp >= 2 * ngrp) return;
+  const int sg = (int)(grp / ngrp);
+  const long long col0 = (grp - sg * ngrp) * 8;
+  auto ld = [&](int cc, int k) -> double {
+    const long long col = col0 + cc;
+    if (col >= ncol || k >= M) return 0.0;
+    const long long v = col / g.K, tau = col - v * g.K;
+    return c[((v * 2 + sg) * g.slots + g.leaf_base + tau) * M + k];
+  };
+  mx_stage<2>(sm.Qf[wid], MxSmem<2>::QLD, sm.Qe[wid], M, ld);
+  double far[MT][4];
+  l2c_oz::warp_tile<MT, 2>(Pn + (size_t)sg * l2c_oz::SLICES * g.s * M, (int)(g.s * M), M,
+                           (int)g.s, M, Pne + sg * g.s, sm.Qf[wid], MxSmem<2>::QLD, sm.Qe[wid],
+                           far);
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const long long i = mt * 16 + (lane >> 2) + 8 * (e >> 1);
+      const long long col = col0 + 2 * (lane & 3) + (e & 1);
+      if (i >= g.s || col >= ncol) continue;
+      const long long v = col / g.K, tau = col - v * g.K;
+      const long long j = tau * g.h + 2 * i + sg;
+      if (j >= g.N) continue;
+      double val = y[v * g.N + j] + far[mt][e];
+      if (!c2l) {
+        val = val * TWO_OVER_PI;
+        if (j == 0) val = val * 0.5;
+      } else {
+        val = val * ((double)j + 0.5);
+      }
+      out[v * g.dist + j * g.stride] = val;
+    }
+}
+
+// Outputs past the last leaf target node (no far field): scaling only.
+__global__ void k_mx_tail(const double *__restrict__ y, double *out, Geo g, int c2l) {
+  const long long j0 = g.K * g.h, nt = g.N - j0;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (nt <= 0 || idx >= g.count * nt) return;
+  const long long v = idx / nt, j = j0 + (idx - v * nt);
+  double val = y[v * g.N + j];
+  if (!c2l) {
+    val = val * TWO_OVER_PI;
+    if (j == 0) val = val * 0.5;
+  } else {
+    val = val * ((double)j + 0.5);
+  }
+  out[v * g.dist + j * g.stride] = val;
+}
+
+// Far field (step 3), one block gb per warp group: columns (vector, parity).
+// c0 = [A0 A1] [w0; w1] (K = 36), c1 = A2 w1 (K = 18).  Slices per block:
+// P01 at Pf + gb * SLICES * 18 * 54 (row stride 54: [A0 A1 | A2]).
+__global__ void __launch_bounds__(32 * MXW)
+    k_mx_far(const double *__restrict__ w, double *__restrict__ c,
+             const __nv_bfloat16 *__restrict__ Pf, const int *__restrict__ Pfe, Geo g,
+             long long nblocks) {
+  __shared__ MxSmem<3> sm;
+  const int wid = threadIdx.x >> 5;
+  const long long ncol = 2 * g.count, ngrp = (ncol + 7) / 8;
+  const long long item = (long long)blockIdx.x * MXW + wid;
+  if (item >= nblocks * ngrp) return;
+  const long long gb = item / ngrp, col0 = (item - gb * ngrp) * 8;
+  const __nv_bfloat16 *P = Pf + gb * (long long)l2c_oz::SLICES * M * 54;
+  const int *Pe = Pfe + gb * 2 * M;
+  const int lane = threadIdx.x & 31;
+  for (int part = 0; part < 2; part++) {
+    const int K = part == 0 ? 2 * M : M;
+    auto ld = [&](int cc, int k) -> double {
+      const long long col = col0 + cc;
+      if (col >= ncol || k >= K) return 0.0;
+      return w[(col * g.slots + 2 * gb + part) * M + k];
+    };
+    mx_stage<3>(sm.Qf[wid], MxSmem<3>::QLD, sm.Qe[wid], K, ld);
+    double out[2][4];
+    l2c_oz::warp_tile<2, 3>(P + (part == 0 ? 0 : 2 * M), M * 54, 54, M, K, Pe + part * M,
+                            sm.Qf[wid], MxSmem<3>::QLD, sm.Qe[wid], out);
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const int m = mt * 16 + (lane >> 2) + 8 * (e >> 1);
+        const long long col = col0 + 2 * (lane & 3) + (e & 1);
+        if (m >= M || col >= ncol) continue;
+        c[(col * g.slots + 2 * gb + part) * M + m] = out[mt][e];
+      }
+    __syncwarp();
+  }
+}
+
+// Transfer trees, one level.  Up: P = [B | B'] (18 x 36), columns
+// (vector*2+parity, parent slot), K = 36 child coefficients.  Down:
+// P = [B^T; B^T'] (36 x 18), K = 18 parent coefficients, rows r < 18 add to the
+// first child, r >= 18 to the second.
+__global__ void __launch_bounds__(32 * MXW)
+    k_mx_tree_up(double *w, const __nv_bfloat16 *__restrict__ Pu, const int *__restrict__ Pue,
+                 Geo g, long long parent_base, long long child_base, long long nparent) {
+  __shared__ MxSmem<3> sm;
+  const int wid = threadIdx.x >> 5;
+  const long long ncol = g.count * 2 * nparent;
+  const long long col0 = ((long long)blockIdx.x * MXW + wid) * 8;
+  if (col0 >= ncol) return;
+  auto ld = [&](int cc, int k) -> double {
+    const long long col = col0 + cc;
+    if (col >= ncol || k >= 2 * M) return 0.0;
+    const long long vs = col / nparent, jp = col - vs * nparent;
+    return w[(vs * g.slots + child_base + 2 * jp + 2) * M + k];
+  };
+  mx_stage<3>(sm.Qf[wid], MxSmem<3>::QLD, sm.Qe[wid], 2 * M, ld);
+  double out[2][4];
+  l2c_oz::warp_tile<2, 3>(Pu, M * 2 * M, 2 * M, M, 2 * M, Pue, sm.Qf[wid], MxSmem<3>::QLD,
+                          sm.Qe[wid], out);
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int m = mt * 16 + (lane >> 2) + 8 * (e >> 1);
+      const long long col = col0 + 2 * (lane & 3) + (e & 1);
+      if (m >= M || col >= ncol) continue;
+      const long long vs = col / nparent, jp = col - vs * nparent;
+      w[(vs * g.slots + parent_base + jp) * M + m] = out[mt][e];
+    }
+}
+
+__global__ void __launch_bounds__(32 * MXW)
+    k_mx_tree_down(double *c, const __nv_bfloat16 *__restrict__ Pd, const int *__restrict__ Pde,
+                   Geo g, long long parent_base, long long child_base, long long nparent) {
+  __shared__ MxSmem<2> sm;
+  const int wid = threadIdx.x >> 5;
+  const long long ncol = g.count * 2 * nparent;
+  const long long col0 = ((long long)blockIdx.x * MXW + wid) * 8;
+  if (col0 >= ncol) return;
+  auto ld = [&](int cc, int k) -> double {
+    const long long col = col0 + cc;
+    if (col >= ncol || k >= M) return 0.0;
+    const long long vs = col / nparent, tp = col - vs * nparent;
+    return c[(vs * g.slots + parent_base + tp) * M + k];
+  };
+  mx_stage<2>(sm.Qf[wid], MxSmem<2>::QLD, sm.Qe[wid], M, ld);
+  double out[3][4];
+  l2c_oz::warp_tile<3, 2>(Pd, 2 * M * M, M, 2 * M, M, Pde, sm.Qf[wid], MxSmem<2>::QLD,
+                          sm.Qe[wid], out);
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int mt = 0; mt < 3; mt++)
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int r = mt * 16 + (lane >> 2) + 8 * (e >> 1);
+      const long long col = col0 + 2 * (lane & 3) + (e & 1);
+      if (r >= 2 * M || col >= ncol) continue;
+      const long long vs = col / nparent, tp = col - vs * nparent;
+      c[(vs * g.slots + child_base + 2 * tp) * M + r] += out[mt][e];  // r >= 18: second child
+    }
+}
+
+// Plan time: slices of a dense row-major FP64 matrix (rows x K, leading
+// dimension ldp) into S[(p-1) * sstride + r * kld + k] with per-row exponents.
+__global__ void k_oz_slice_rows(const double *__restrict__ P, int rows, int K, int ldp,
+                                __nv_bfloat16 *S, int kld, long long sstride, int *E) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  int e = l2c_oz::EXP_ZERO;
+  for (int k = 0; k < K; k++) e = max(e, l2c_oz::exp_bound(P[(long long)r * ldp + k]));
+  E[r] = e;
+  for (int k = 0; k < kld; k++) {
+    const unsigned long long f = k < K ? l2c_oz::fix56(P[(long long)r * ldp + k], e) : 0ull;
+    for (int q = 1; q <= l2c_oz::SLICES; q++)
+      S[(q - 1) * sstride + (long long)r * kld + k] = __float2bfloat16_rn(l2c_oz::slice(f, q));
+  }
+}
+
+// Plan time: far-field block slices, one thread per (block, row): the row of
+// [A0 A1] (36 values) and of A2 (18 values), each with its own exponent.
+__global__ void k_oz_slice_far(const double *__restrict__ A, long long nblocks,
+                               __nv_bfloat16 *S, int *E) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= nblocks * M) return;
+  const long long gb = idx / M;
+  const int m = (int)(idx - gb * M);
+  const double *A0 = A + 3 * gb * MM + m * M;
+  __nv_bfloat16 *Sb = S + gb * (long long)l2c_oz::SLICES * M * 54;
+  for (int part = 0; part < 2; part++) {
+    const int K = part == 0 ? 2 * M : M;
+    auto val = [&](int k) -> double {
+      return part == 0 ? (k < M ? A0[k] : A0[MM + k - M]) : A0[2 * MM + k];
+    };
+    int e = l2c_oz::EXP_ZERO;
+    for (int k = 0; k < K; k++) e = max(e, l2c_oz::exp_bound(val(k)));
+    E[gb * 2 * M + part * M + m] = e;
+    for (int k = 0; k < K; k++) {
+      const unsigned long long f = l2c_oz::fix56(val(k), e);
+      for (int q = 1; q <= l2c_oz::SLICES; q++)
+        Sb[(q - 1) * M * 54 + m * 54 + (part == 0 ? 0 : 2 * M) + k] =
+            __float2bfloat16_rn(l2c_oz::slice(f, q));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Plan
 // ---------------------------------------------------------------------------
 struct l2c_gpu_plan;
@@ -864,6 +1146,13 @@ struct l2c_gpu_plan {
   cudaStream_t stream2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double *Wnear[2] = {nullptr, nullptr};  // precomputed band weights (optional)
+  // mixed precision (L2C_PLAN_MIXED): sliced constant factors
+  bool mixed = false;
+  __nv_bfloat16 *oz_Tt = nullptr, *oz_Tn = nullptr, *oz_Bu = nullptr, *oz_Bd = nullptr;
+  int *oz_Tte = nullptr, *oz_Tne = nullptr, *oz_Bue = nullptr, *oz_Bde = nullptr;
+  int oz_kld = 0;                                   // row stride of oz_Tt (s rounded up to even)
+  __nv_bfloat16 *oz_A[2] = {nullptr, nullptr};      // far blocks, built on first batched call
+  int *oz_Ae[2] = {nullptr, nullptr};
   // captured launch sequences, keyed by the call's shape and pointers
   struct GraphEntry {
     size_t dir, count, dist, stride;
@@ -1162,6 +1451,92 @@ Geo make_geo(const l2c_gpu_plan *p, size_t count, size_t dist, size_t stride) {
   return g;
 }
 
+// Far field of the mixed form: leaf, tree and far-field products on tensor
+// cores (the far-field blocks only when the batch gives each block at least 8
+// right-hand sides; single vectors keep the FP64 block products).
+bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir, const Geo &g,
+                      cudaStream_t st) {
+  const int c2l = dir == 1;
+  const int kt = (int)((g.s + 15) / 16);
+  {
+    PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
+    const long long ngrp = 2 * ((g.count * g.K + 7) / 8);
+    const unsigned grid = (unsigned)((ngrp + MXW - 1) / MXW);
+    switch (kt) {
+      case 1: k_mx_leaf_up<1><<<grid, 32 * MXW, 0, st>>>(x, p->w, p->oz_Tt, p->oz_Tte, p->oz_kld, g); break;
+      case 2: k_mx_leaf_up<2><<<grid, 32 * MXW, 0, st>>>(x, p->w, p->oz_Tt, p->oz_Tte, p->oz_kld, g); break;
+      case 3: k_mx_leaf_up<3><<<grid, 32 * MXW, 0, st>>>(x, p->w, p->oz_Tt, p->oz_Tte, p->oz_kld, g); break;
+      default: k_mx_leaf_up<4><<<grid, 32 * MXW, 0, st>>>(x, p->w, p->oz_Tt, p->oz_Tte, p->oz_kld, g); break;
+    }
+    if (cudaGetLastError() != cudaSuccess) return false;
+  }
+  {
+    PhaseScope ps(p, L2C_PHASE_TREE_UP, p->L - 1);
+    for (long long l = g.L - 2; l >= 0; l--) {
+      const long long np = (long long)slots_at((size_t)l);
+      const long long ngrp = (g.count * 2 * np + 7) / 8;
+      k_mx_tree_up<<<(unsigned)((ngrp + MXW - 1) / MXW), 32 * MXW, 0, st>>>(
+          p->w, p->oz_Bu, p->oz_Bue, g, 2 * (long long)blocks_before((size_t)l),
+          2 * (long long)blocks_before((size_t)l + 1), np);
+    }
+    if (cudaGetLastError() != cudaSuccess) return false;
+  }
+  {
+    PhaseScope ps(p, L2C_PHASE_FAR, 1);
+    if (g.count >= 4 && p->oz_A[dir] != nullptr) {
+      const long long items = (long long)p->Nb * ((2 * g.count + 7) / 8);
+      k_mx_far<<<(unsigned)((items + MXW - 1) / MXW), 32 * MXW, 0, st>>>(
+          p->w, p->c, p->oz_A[dir], p->oz_Ae[dir], g, (long long)p->Nb);
+    } else {
+      const long long n = g.count * 2 * (long long)p->Nb * M;
+      k_far<<<blocks_for(n, 256), 256, 0, st>>>(p->A[dir], p->w, p->c, g, (long long)p->Nb);
+    }
+    if (cudaGetLastError() != cudaSuccess) return false;
+  }
+  {
+    PhaseScope ps(p, L2C_PHASE_TREE_DOWN, p->L - 1);
+    for (long long l = 0; l + 1 < g.L; l++) {
+      const long long np = (long long)slots_at((size_t)l);
+      const long long ngrp = (g.count * 2 * np + 7) / 8;
+      k_mx_tree_down<<<(unsigned)((ngrp + MXW - 1) / MXW), 32 * MXW, 0, st>>>(
+          p->c, p->oz_Bd, p->oz_Bde, g, 2 * (long long)blocks_before((size_t)l),
+          2 * (long long)blocks_before((size_t)l + 1), np);
+    }
+    if (cudaGetLastError() != cudaSuccess) return false;
+  }
+  if (p->overlap && cudaStreamWaitEvent(st, p->ev_join, 0) != cudaSuccess) return false;
+  {
+    PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 2);
+    const long long ngrp = 2 * ((g.count * g.K + 7) / 8);
+    const unsigned grid = (unsigned)((ngrp + MXW - 1) / MXW);
+    switch (kt) {
+      case 1: k_mx_leaf_down<1><<<grid, 32 * MXW, 0, st>>>(p->c, p->y, out, p->oz_Tn, p->oz_Tne, g, c2l); break;
+      case 2: k_mx_leaf_down<2><<<grid, 32 * MXW, 0, st>>>(p->c, p->y, out, p->oz_Tn, p->oz_Tne, g, c2l); break;
+      case 3: k_mx_leaf_down<3><<<grid, 32 * MXW, 0, st>>>(p->c, p->y, out, p->oz_Tn, p->oz_Tne, g, c2l); break;
+      default: k_mx_leaf_down<4><<<grid, 32 * MXW, 0, st>>>(p->c, p->y, out, p->oz_Tn, p->oz_Tne, g, c2l); break;
+    }
+    const long long tail = g.count * (g.N - g.K * g.h);
+    if (tail > 0) k_mx_tail<<<blocks_for(tail, 256), 256, 0, st>>>(p->y, out, g, c2l);
+    if (cudaGetLastError() != cudaSuccess) return false;
+  }
+  return true;
+}
+
+// Far-field block slices of the mixed form, built on the first batched call.
+bool ensure_mixed_far(l2c_gpu_plan *p, size_t dir) {
+  if (p->oz_A[dir]) return true;
+  const size_t nb = p->Nb;
+  if (cudaMalloc(&p->oz_A[dir], nb * l2c_oz::SLICES * M * 54 * sizeof(__nv_bfloat16)) !=
+          cudaSuccess ||
+      cudaMalloc(&p->oz_Ae[dir], nb * 2 * M * sizeof(int)) != cudaSuccess) {
+    set_err("cudaMalloc of the mixed-form far-field slices failed");
+    return false;
+  }
+  k_oz_slice_far<<<blocks_for((long long)(nb * M), 128), 128, 0, p->stream>>>(
+      p->A[dir], (long long)nb, p->oz_A[dir], p->oz_Ae[dir]);
+  return cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(p->stream) == cudaSuccess;
+}
+
 // The launch sequence of one batch on device pointers (scratch already sized).
 // Near field on stream2 beside the far-field chain on stream; joined before the
 // final leaf-down kernel.
@@ -1208,6 +1583,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn));
   }
   if (p->overlap) CK(cudaEventRecord(p->ev_join, st2));
+  if (p->mixed) return launch_mixed_far(p, x, out, dir, g, st) ? 1 : 0;
   const long long leaf_threads = g.count * g.K * 2 * M;
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
@@ -1245,6 +1621,7 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
                   size_t dist, size_t stride, bool near_only, bool input_ready) {
   if (count == 0 || p->N == 0) return 1;
   if (!ensure_scratch(p, count)) return 0;
+  if (p->mixed && p->L > 0 && count >= 4 && !ensure_mixed_far(p, dir)) return 0;
   const unsigned mode = (near_only ? 1u : 0u) | (input_ready ? 2u : 0u);
   if (p->profiling || !p->use_graphs) {
     return launch_all(p, in, out, dir, count, dist, stride, near_only, input_ready);
@@ -1408,6 +1785,73 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cudaFree(f0);
     PCK(e);
+    if (flags & L2C_PLAN_MIXED) {
+      if (s > 64) {
+        set_err("the mixed form supports leaf sizes s <= 64 (got s = %zu)", s);
+        return fail();
+      }
+      p->mixed = true;
+      const int kld = (int)((s + 1) & ~(size_t)1);
+      p->oz_kld = kld;
+      // dense constant factors on the host: T_parity^T (18 x kld), T_parity (s x 18),
+      // [B | B'] (18 x 36) and [B^T; B^T'] (36 x 18)
+      std::vector<double> Tt(2 * M * kld, 0.0), Tn(2 * s * M), Bu(M * 2 * M, 0.0),
+          Bd(2 * M * M, 0.0);
+      for (int sg = 0; sg < 2; sg++)
+        for (size_t i = 0; i < s; i++)
+          for (int m = 0; m < M; m++) {
+            const double v = T[(sg * s + i) * M + m];
+            Tt[(sg * M + m) * kld + i] = v;
+            Tn[(sg * s + i) * M + m] = v;
+          }
+      const double lower[NTRI] = L2C_BINOM_LOWER_INIT, upper[NTRI] = L2C_BINOM_UPPER_INIT;
+      for (int m = 0; m < M; m++)
+        for (int i = 0; i <= m; i++) {
+          const double b = lower[m * (m + 1) / 2 + i];
+          Bu[m * 2 * M + i] = b;
+          Bu[m * 2 * M + M + i] = ((m + i) & 1) ? -b : b;
+        }
+      for (int i = 0, k = 0; i < M; i++)
+        for (int j = i; j < M; j++, k++) {
+          Bd[i * M + j] = upper[k];
+          Bd[(M + i) * M + j] = ((j - i) & 1) ? -upper[k] : upper[k];
+        }
+      double *dtmp = nullptr;
+      const size_t ntmp = Tt.size() + Tn.size() + Bu.size() + Bd.size();
+      PCK(cudaMalloc(&dtmp, ntmp * sizeof(double)));
+      double *dTt = dtmp, *dTn = dTt + Tt.size(), *dBu = dTn + Tn.size(), *dBd = dBu + Bu.size();
+      cudaError_t e2 = cudaMemcpy(dTt, Tt.data(), Tt.size() * 8, cudaMemcpyHostToDevice);
+      if (e2 == cudaSuccess) e2 = cudaMemcpy(dTn, Tn.data(), Tn.size() * 8, cudaMemcpyHostToDevice);
+      if (e2 == cudaSuccess) e2 = cudaMemcpy(dBu, Bu.data(), Bu.size() * 8, cudaMemcpyHostToDevice);
+      if (e2 == cudaSuccess) e2 = cudaMemcpy(dBd, Bd.data(), Bd.size() * 8, cudaMemcpyHostToDevice);
+      const size_t S8 = l2c_oz::SLICES;
+      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Tt, S8 * Tt.size() * sizeof(__nv_bfloat16));
+      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Tn, S8 * Tn.size() * sizeof(__nv_bfloat16));
+      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Bu, S8 * Bu.size() * sizeof(__nv_bfloat16));
+      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Bd, S8 * Bd.size() * sizeof(__nv_bfloat16));
+      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Tte, 2 * M * sizeof(int));
+      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Tne, 2 * s * sizeof(int));
+      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Bue, M * sizeof(int));
+      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Bde, 2 * M * sizeof(int));
+      if (e2 == cudaSuccess) {
+        for (int sg = 0; sg < 2; sg++) {
+          k_oz_slice_rows<<<1, 64, 0, st>>>(dTt + sg * M * kld, M, (int)s, kld,
+                                            p->oz_Tt + sg * S8 * M * kld, kld, (long long)M * kld,
+                                            p->oz_Tte + sg * M);
+          k_oz_slice_rows<<<(unsigned)((s + 63) / 64), 64, 0, st>>>(
+              dTn + sg * s * M, (int)s, M, M, p->oz_Tn + sg * S8 * s * M, M, (long long)s * M,
+              p->oz_Tne + sg * s);
+        }
+        k_oz_slice_rows<<<1, 64, 0, st>>>(dBu, M, 2 * M, 2 * M, p->oz_Bu, 2 * M,
+                                          (long long)M * 2 * M, p->oz_Bue);
+        k_oz_slice_rows<<<1, 64, 0, st>>>(dBd, 2 * M, M, M, p->oz_Bd, M, (long long)2 * M * M,
+                                          p->oz_Bde);
+        e2 = cudaGetLastError();
+      }
+      if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(st);
+      cudaFree(dtmp);
+      PCK(e2);
+    }
     if (flags & L2C_PLAN_PRECOMPUTE_NEAR) {
       const size_t nw = near_table_size(N, s);
       Geo g = make_geo(p, 1, N, 1);
@@ -1441,6 +1885,10 @@ void l2c_gpu_plan_destroy(l2c_gpu_plan *p) {
   double *bufs[] = {p->a, p->an, p->dn, p->A[0], p->A[1], p->T, p->x, p->y, p->w, p->c,
                     p->st_in, p->st_out, p->Wnear[0], p->Wnear[1]};
   for (double *b : bufs)
+    if (b) cudaFree(b);
+  void *obufs[] = {p->oz_Tt, p->oz_Tn, p->oz_Bu, p->oz_Bd, p->oz_Tte, p->oz_Tne, p->oz_Bue,
+                   p->oz_Bde, p->oz_A[0], p->oz_A[1], p->oz_Ae[0], p->oz_Ae[1]};
+  for (void *b : obufs)
     if (b) cudaFree(b);
   if (p->stream) cudaStreamDestroy(p->stream);
   delete p;

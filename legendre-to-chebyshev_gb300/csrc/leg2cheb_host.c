@@ -265,6 +265,12 @@ static void vandermonde_host(double *T, size_t s) {
 
 fmm_plan *create_fmm(const size_t N, const size_t maxs, const size_t M, const size_t direction,
                      const size_t lagrange, const size_t precompute, const size_t v) {
+  return create_fmm_ex(N, maxs, M, direction, lagrange, precompute, v, 0);
+}
+
+fmm_plan *create_fmm_ex(const size_t N, const size_t maxs, const size_t M, const size_t direction,
+                        const size_t lagrange, const size_t precompute, const size_t v,
+                        unsigned flags) {
   host_err[0] = 0;
   if (M != L2C_M) {
     herr("only M = 18 is implemented (got M = %zu)", M);
@@ -290,8 +296,9 @@ fmm_plan *create_fmm(const size_t N, const size_t maxs, const size_t M, const si
   p->N = N;
   size_t s = 0, Nn = N;
   const size_t L = l2c_geometry(N, maxs, &s, &Nn);
-  l2c_gpu_plan *gp =
-      l2c_gpu_plan_create(N, maxs, direction, precompute ? L2C_PLAN_PRECOMPUTE_NEAR : 0);
+  unsigned gflags = precompute ? L2C_PLAN_PRECOMPUTE_NEAR : 0;
+  if (flags & L2C_FMM_MIXED) gflags |= L2C_PLAN_MIXED;
+  l2c_gpu_plan *gp = l2c_gpu_plan_create(N, maxs, direction, gflags);
   if (!gp) {
     free(p->A);
     free(p);

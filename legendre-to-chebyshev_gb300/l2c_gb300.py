@@ -49,6 +49,8 @@ def load():
     sz, dp, vp = ctypes.c_size_t, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p
     lib.create_fmm.restype = vp
     lib.create_fmm.argtypes = [sz] * 7
+    lib.create_fmm_ex.restype = vp
+    lib.create_fmm_ex.argtypes = [sz] * 7 + [ctypes.c_uint]
     lib.free_fmm.argtypes = [vp]
     lib.execute.restype = sz
     lib.execute.argtypes = [vp, vp, vp, sz, sz]
@@ -146,10 +148,13 @@ def geometry(N, maxs):
 class Plan:
     """An fmm_plan (create_fmm / free_fmm)."""
 
-    def __init__(self, N, maxs=36, M=18, direction=BOTH, lagrange=0, precompute=0, verbose=0):
+    def __init__(self, N, maxs=36, M=18, direction=BOTH, lagrange=0, precompute=0, verbose=0,
+                 mixed=False):
         lib = load()
         self.N, self.maxs, self.direction = int(N), int(maxs), int(direction)
-        self._p = lib.create_fmm(N, maxs, M, direction, lagrange, precompute, verbose)
+        self.mixed = bool(mixed)
+        self._p = lib.create_fmm_ex(N, maxs, M, direction, lagrange, precompute, verbose,
+                                    1 if mixed else 0)
         if not self._p:
             raise L2CError("create_fmm failed: " + last_error())
         gp = ctypes.cast(self._p, ctypes.POINTER(ctypes.c_void_p * 20)).contents[19]

@@ -8,6 +8,21 @@
  * cannot be built. */
 #include "l2c_oracle.h"
 
+#ifdef ORC_CBLAS
+/* The reference calls CBLAS dgemm for steps 1 and 5 (leg2cheb.c:1381, 1467);
+ * with ORC_CBLAS the port does the same through the OpenBLAS that scipy bundles
+ * (its CBLAS symbols carry a "scipy_" prefix), single-threaded inside OpenMP row
+ * blocks (OpenBLAS's own thread pool and OpenMP's oversubscribe the cores).  Step 3's 18x18 products stay in
+ * the port's OpenMP loop: the reference's dgemv calls inside an OpenMP loop
+ * (leg2cheb.c:1419-1435) serialise in OpenBLAS's thread server, an 8x slowdown
+ * on 8 threads, which would not be a fair baseline. */
+enum { OrcRowMajor = 101 };
+enum { OrcNoTrans = 111, OrcTrans = 112 };
+void scipy_cblas_dgemm(int, int, int, int, int, int, double, const double *, int, const double *,
+                       int, double, double *, int);
+void scipy_openblas_set_num_threads(int);
+#endif
+
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -33,6 +48,18 @@ void orc_set_threads(int n) {
   if (n > 0) omp_set_num_threads(n);
 #else
   (void)n;
+#endif
+#ifdef ORC_CBLAS
+  (void)n;
+  scipy_openblas_set_num_threads(1); /* threads come from OpenMP row blocks */
+#endif
+}
+
+int orc_uses_blas(void) {
+#ifdef ORC_CBLAS
+  return 1;
+#else
+  return 0;
 #endif
 }
 
@@ -535,6 +562,20 @@ size_t orc_execute(const double *in, double *out, orc_plan *p, size_t dir, size_
     /* step 1: leaf coefficients, wk[L-1] (K x M) = ia[2s:] (K x s) T_odd (s x M) */
     const double *To = &p->T[odd * s * M];
     double *wl = &wk[lvl[L - 1]];
+#ifdef ORC_CBLAS
+#pragma omp parallel
+    {
+      size_t r0 = 0, r1 = K;
+#ifdef _OPENMP
+      const size_t nt = (size_t)omp_get_num_threads(), id = (size_t)omp_get_thread_num();
+      r0 = K * id / nt;
+      r1 = K * (id + 1) / nt;
+#endif
+      if (r1 > r0)
+        scipy_cblas_dgemm(OrcRowMajor, OrcNoTrans, OrcNoTrans, (int)(r1 - r0), (int)M, (int)s,
+                          1.0, &ia[2 * s + r0 * s], (int)s, To, (int)M, 0.0, wl + r0 * M, (int)M);
+    }
+#else
 #pragma omp parallel for schedule(static)
     for (size_t r = 0; r < K; r++)
       for (size_t m = 0; m < M; m++) {
@@ -542,6 +583,7 @@ size_t orc_execute(const double *in, double *out, orc_plan *p, size_t dir, size_
         for (size_t i = 0; i < s; i++) acc += ia[2 * s + r * s + i] * To[i * M + m];
         wl[r * M + m] = acc;
       }
+#endif
     flops += 2 * K * s * M;
 
     /* step 2: upward transfer, leg2cheb.c:1385-1399 */
@@ -592,6 +634,20 @@ size_t orc_execute(const double *in, double *out, orc_plan *p, size_t dir, size_
 
     /* step 5: back to leaf values and scatter, leg2cheb.c:1467-1483 */
     const double *cl = &ck[lvl[L - 1]];
+#ifdef ORC_CBLAS
+#pragma omp parallel
+    {
+      size_t r0 = 0, r1 = K;
+#ifdef _OPENMP
+      const size_t nt = (size_t)omp_get_num_threads(), id = (size_t)omp_get_thread_num();
+      r0 = K * id / nt;
+      r1 = K * (id + 1) / nt;
+#endif
+      if (r1 > r0)
+        scipy_cblas_dgemm(OrcRowMajor, OrcNoTrans, OrcTrans, (int)(r1 - r0), (int)s, (int)M, 1.0,
+                          cl + r0 * M, (int)M, To, (int)M, 0.0, oa + r0 * s, (int)s);
+    }
+#else
 #pragma omp parallel for schedule(static)
     for (size_t r = 0; r < K; r++)
       for (size_t i = 0; i < s; i++) {
@@ -599,6 +655,7 @@ size_t orc_execute(const double *in, double *out, orc_plan *p, size_t dir, size_
         for (size_t m = 0; m < M; m++) acc += cl[r * M + m] * To[i * M + m];
         oa[r * s + i] = acc;
       }
+#endif
     flops += 2 * K * s * M;
     for (size_t k = 0; k < cnt; k++) out[(2 * k + odd) * stride] += oa[k];
   }

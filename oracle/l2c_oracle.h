@@ -63,6 +63,8 @@ const double *orc_plan_B(const orc_plan *p);                   /* 171       */
 const double *orc_plan_BT(const orc_plan *p);                  /* 171       */
 
 void orc_set_threads(int n);
+/* 1 when built against OpenBLAS (steps 1 and 5 through CBLAS dgemm, as the reference). */
+int orc_uses_blas(void);
 
 #ifdef __cplusplus
 }

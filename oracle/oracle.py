@@ -52,6 +52,7 @@ def load():
     lib.orc_LambdaI.restype = ctypes.c_double
     lib.orc_LambdaI.argtypes = [sz]
     lib.orc_set_threads.argtypes = [ctypes.c_int]
+    lib.orc_uses_blas.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -112,6 +113,10 @@ class Oracle:
 
 def set_threads(n):
     load().orc_set_threads(int(n))
+
+
+def uses_blas():
+    return bool(load().orc_uses_blas())
 
 
 class RaggedOracle:

@@ -1,0 +1,70 @@
+"""The mixed form (L2C_PLAN_MIXED): leaf, transfer and far-field products as
+split-BF16 tensor-core products with exact integer recombination.  Same
+accuracy bar as the FP64 path: 1e-14 relative max-norm against the oracle,
+per direction, on single vectors and on batches (where the far-field blocks
+also run on the tensor cores)."""
+import numpy as np
+import pytest
+
+from oracle import direct_ld
+from tests.conftest import relerr
+from tests.golden.cases import make_input
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-14
+
+
+@pytest.mark.parametrize("N,maxs", [(512, 64), (4096, 16), (4096, 32), (5000, 50), (65536, 16),
+                                    (1 << 20, 32), (1 << 20, 64), (300, 18)])
+@pytest.mark.parametrize("dist", ["uniform", "sign"])
+def test_mixed_single_vector(lib, orc, N, maxs, dist):
+    u = make_input(N, dist, N + maxs)
+    p = lib.Plan(N, maxs, mixed=True)
+    o = orc.Oracle(N, maxs, 2)
+    for d in (0, 1):
+        out = np.zeros(N)
+        p.execute(u, out, d)
+        assert relerr(out, o(u, d)[:N]) <= TOL, (N, maxs, d)
+
+
+@pytest.mark.parametrize("N,maxs,count", [(1024, 64, 16), (1024, 16, 64), (16384, 16, 8),
+                                          (2000, 50, 5)])
+def test_mixed_batch(lib, orc, N, maxs, count):
+    x = make_input(N * count, "gauss", 3).reshape(count, N) / (np.arange(N) + 1.0)
+    x = np.ascontiguousarray(x)
+    p = lib.Plan(N, maxs, mixed=True)
+    o = orc.Oracle(N, maxs, 2)
+    for d in (0, 1):
+        out = np.zeros_like(x)
+        p.execute_batched(x, out, d, count, N, 1)
+        for i in (0, count // 2, count - 1):
+            assert relerr(out[i], o(x[i], d)[:N]) <= TOL, (i, d)
+
+
+def test_mixed_vs_extended_precision(lib):
+    N = 8192
+    u = make_input(N, "uniform", 77)
+    p = lib.Plan(N, 16, mixed=True)
+    for d, f in ((0, direct_ld.l2c_direct), (1, direct_ld.c2l_direct)):
+        out = np.zeros(N)
+        p.execute(u, out, d)
+        assert direct_ld.rel_maxnorm(out, f(u)) < 5e-15
+
+
+def test_mixed_wide_dynamic_range(lib, orc):
+    # per-column scaling must cope with inputs spanning many orders of magnitude
+    N = 16384
+    rng = np.random.default_rng(5)
+    u = rng.standard_normal(N) * 10.0 ** rng.uniform(-12, 12, N)
+    p = lib.Plan(N, 32, mixed=True)
+    o = orc.Oracle(N, 32, 2)
+    for d in (0, 1):
+        out = np.zeros(N)
+        p.execute(u, out, d)
+        assert relerr(out, o(u, d)[:N]) <= TOL
+
+
+def test_mixed_rejects_large_leaves(lib):
+    with pytest.raises(lib.L2CError, match="s <= 64"):
+        lib.Plan(1 << 16, 200, mixed=True)  # s = 128
