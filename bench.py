@@ -347,7 +347,20 @@ def run_mixed(args):
         plan.synchronize()
         launches = l2c.cuda_abi().l2c_gpu_launch_count(plan._gpu) - l0
         ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
-        return ms, [o.cpu().numpy() for o in outs], launches
+        # per-phase CUDA events in a separate pass (graph replay off while profiling)
+        abi = l2c.cuda_abi()
+        abi.l2c_gpu_profile(plan._gpu, 1)
+        nprof = max(1, min(args.steps, 20))
+        for _ in range(nprof):
+            step()
+        plan.synchronize()
+        pms = (ctypes.c_double * 8)()
+        pl = (ctypes.c_size_t * 8)()
+        abi.l2c_gpu_profile_read(plan._gpu, pms, pl)
+        abi.l2c_gpu_profile(plan._gpu, 0)
+        names = ["gather", "near", "leaf_up", "tree_up", "far", "tree_down", "leaf_down", "direct"]
+        phases = {names[i]: round(pms[i] / nprof, 4) for i in range(8) if pl[i]}
+        return ms, [o.cpu().numpy() for o in outs], launches, phases
 
     clocks = ClockSampler(0)
     clocks.start()
@@ -355,9 +368,10 @@ def run_mixed(args):
     for name, maxs, mixed in (("plain_maxs64", 64, False), ("plain_maxs32", 32, False),
                               ("mixed", args.maxs_mixed, True)):
         plan = l2c.Plan(N, maxs, mixed=mixed)
-        ms, outs, launches = time_plan(plan)
+        ms, outs, launches, phases = time_plan(plan)
         results[name] = {"maxs": maxs, "s": plan.s, "L": plan.L, "ms_per_step": ms,
                          "value": 2 * count * N / (ms * 1e-3), "launches": launches,
+                         "phases_ms_per_step": phases,
                          "flops": plan.flops(0) + plan.flops(1), "outs": outs}
         plan.close()
     clk = clocks.stop()

@@ -840,110 +840,477 @@ inline unsigned blocks_for(long long n, int threads) {
 
 // ---------------------------------------------------------------------------
 // Mixed-precision far field (L2C_PLAN_MIXED): the leaf, transfer and far-field
-// products on BF16 tensor cores through l2c_ozaki.cuh, FP64-accurate with no
-// FP64 instructions; the near-field band, the final accumulation and scaling
-// stay in FP64.  Every kernel: one warp per 8 right-hand-side columns; the
-// constant left factor is pre-sliced at plan time.
+// products on FP16 tensor cores through l2c_ozaki.cuh, FP64-accurate with no
+// FP64 instruction in the products; the near-field band, the final
+// accumulation and scaling stay in FP64.  Every kernel: one warp per tile of
+// 16 right-hand-side columns against a constant factor pre-sliced at plan time
+// into per-lane fragments (l2c_oz::frag_index) that the CTA copies to shared
+// memory once; each warp streams its tiles through a two-deep cp.async
+// pipeline (the next tile's copies are in flight while one is computed).
 // ---------------------------------------------------------------------------
-constexpr int MXW = 4;  // warps per CTA
+constexpr int MXW = 4;              // warps per CTA
+constexpr int OZ_NT = 3;            // 18 outputs = 3 n-tiles of 8
+constexpr int OZ_ROWS = 8 * OZ_NT;  // padded output rows
+constexpr int OZ_TLD = 42;          // staged row of 36 (K = 2M) values, padded
+constexpr int OZ_CLD = 26;          // staged row of 18 (K = M) values, padded
+__host__ __device__ constexpr int oz_words(int NT, int KC) { return l2c_oz::SLICES * NT * KC * 32; }
 
-// 8 columns of K values (loader ld(c, k)) -> fix56 form and column exponents.
-template <int KT, class Loader>
-__device__ __forceinline__ void mx_stage(unsigned long long *Qf, int qld, int *Qe, int K,
-                                         Loader ld) {
-  const int lane = threadIdx.x & 31;
-  const int c = lane >> 2, k0 = lane & 3;
+// Plan time: the fragment words and row exponent of one row n of a matrix with
+// K columns (row(k) gives P[n][k]; rows past the matrix are zero).
+template <class Row>
+__host__ __device__ void oz_pack_row(Row row, bool live, int n, int K, int NT, int KC,
+                                     unsigned *frag, int *E) {
   int e = l2c_oz::EXP_ZERO;
-  for (int k = k0; k < K; k += 4) e = max(e, l2c_oz::exp_bound(ld(c, k)));
-  e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
-  e = max(e, __shfl_xor_sync(0xffffffffu, e, 2));
-  for (int k = k0; k < KT * 16; k += 4) Qf[c * qld + k] = k < K ? l2c_oz::fix56(ld(c, k), e) : 0ull;
-  if (k0 == 0) Qe[c] = e;
-  __syncwarp();
-}
-
-template <int KT>
-struct MxSmem {
-  static constexpr int QLD = KT * 16 + 1;
-  unsigned long long Qf[MXW][8 * QLD];
-  int Qe[MXW][8];
-};
-
-// Leaf up (step 1): columns (parity, vector, leaf node), K = s, rows m < 18.
-// P = T_parity^T (18 x s): Pt + sg * SLICES * 18 * kld.
-template <int KT>
-__global__ void __launch_bounds__(32 * MXW)
-    k_mx_leaf_up(const double *__restrict__ x, double *__restrict__ w,
-                 const __nv_bfloat16 *__restrict__ Pt, const int *__restrict__ Pte, int kld,
-                 Geo g) {
-  __shared__ MxSmem<KT> sm;
-  const int wid = threadIdx.x >> 5;
-  const long long ncol = g.count * g.K, ngrp = (ncol + 7) / 8;
-  const long long grp = (long long)blockIdx.x * MXW + wid;
-  if (grp >= 2 * ngrp) return;
-  const int sg = (int)(grp / ngrp);
-  const long long col0 = (grp - sg * ngrp) * 8;
-  auto ld = [&](int c, int k) -> double {
-    const long long col = col0 + c;
-    if (col >= ncol || k >= g.s) return 0.0;
-    const long long v = col / g.K, node = col - v * g.K;
-    const long long idx = (node + 2) * g.h + 2 * k + sg;
-    return idx < g.N ? x[v * g.N + idx] : 0.0;
-  };
-  mx_stage<KT>(sm.Qf[wid], MxSmem<KT>::QLD, sm.Qe[wid], (int)g.s, ld);
-  double out[2][4];
-  l2c_oz::warp_tile<2, KT>(Pt + (size_t)sg * l2c_oz::SLICES * 18 * kld, 18 * kld, kld, 18,
-                           (int)g.s, Pte + sg * 18, sm.Qf[wid], MxSmem<KT>::QLD, sm.Qe[wid], out);
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-      const int m = mt * 16 + (lane >> 2) + 8 * (e >> 1);
-      const long long col = col0 + 2 * (lane & 3) + (e & 1);
-      if (m >= M || col >= ncol) continue;
-      const long long v = col / g.K, node = col - v * g.K;
-      w[((v * 2 + sg) * g.slots + g.leaf_base + node) * M + m] = out[mt][e];
+  if (live)
+    for (int k = 0; k < K; k++) {
+      const int ek = l2c_oz::exp_bound(row(k));
+      e = e > ek ? e : ek;
+    }
+  E[n] = e;
+  const int nt = n >> 3, g = n & 7;
+  for (int c = 0; c < KC; c++)
+    for (int t = 0; t < 4; t++) {
+      const int k0 = 8 * c + 2 * t;
+      const long long y0 = live && k0 < K ? l2c_oz::fixbal(row(k0), e) : l2c_oz::RBAL;
+      const long long y1 = live && k0 + 1 < K ? l2c_oz::fixbal(row(k0 + 1), e) : l2c_oz::RBAL;
+      for (int q = 1; q <= l2c_oz::SLICES; q++)
+        frag[l2c_oz::frag_index(q, nt, c, 4 * g + t, NT, KC)] =
+            l2c_oz::half_bits((int)l2c_oz::digit_f(y0, q)) |
+            (l2c_oz::half_bits((int)l2c_oz::digit_f(y1, q)) << 16);
     }
 }
 
-// Leaf down (step 5) + final scaling: columns (parity, vector, leaf target node),
-// K = 18, rows i < s.  P = T_parity (s x 18): Pn + sg * SLICES * s * 18.
-template <int MT>
+// Far-field block fragments: block gb, part 0 = [A0 A1] (18 x 36), part 1 = A2
+// (18 x 18); words at F + gb * OZ_FAR_WORDS, exponents at E + gb * 2 * OZ_ROWS.
+constexpr int OZ_FAR_W0 = oz_words(OZ_NT, 5), OZ_FAR_WORDS = OZ_FAR_W0 + oz_words(OZ_NT, 3);
+__global__ void k_oz_pack_far(const double *__restrict__ A, long long nblocks, unsigned *F,
+                              int *E) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= nblocks * 2 * OZ_ROWS) return;
+  const long long gb = idx / (2 * OZ_ROWS);
+  const int rr = (int)(idx - gb * 2 * OZ_ROWS), part = rr / OZ_ROWS, n = rr - part * OZ_ROWS;
+  const double *A0 = A + 3 * gb * MM + (n < M ? n : 0) * M;
+  unsigned *Fb = F + gb * OZ_FAR_WORDS + (part ? OZ_FAR_W0 : 0);
+  int *Eb = E + gb * 2 * OZ_ROWS + part * OZ_ROWS;
+  if (part == 0)
+    oz_pack_row([&](int k) { return k < M ? A0[k] : A0[MM + k - M]; }, n < M, n, 2 * M, OZ_NT, 5,
+                Fb, Eb);
+  else
+    oz_pack_row([&](int k) { return A0[2 * MM + k]; }, n < M, n, M, OZ_NT, 3, Fb, Eb);
+}
+
+// Copy nwords fragment words (and nexp exponents) into shared memory.
+__device__ __forceinline__ void oz_load_frag(unsigned *dst, const unsigned *__restrict__ src,
+                                             int nwords, int *edst, const int *__restrict__ esrc,
+                                             int nexp) {
+  const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+  uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+  for (int i = threadIdx.x; i < nwords / 4; i += blockDim.x) d4[i] = s4[i];
+  for (int i = threadIdx.x; i < nexp; i += blockDim.x) edst[i] = esrc[i];
+}
+
+// Per-warp two-deep pipeline over tiles first, first + step, ... < ntile:
+// issue(tile, buf) starts the copies of a tile into buffer buf, work(tile, buf)
+// computes it once they have landed.
+template <class Issue, class Work>
+__device__ __forceinline__ void oz_tile_loop(long long first, long long step, long long ntile,
+                                             Issue issue, Work work) {
+  if (first >= ntile) return;
+  issue(first, 0);
+  l2c_oz::cp_commit();
+  int buf = 0;
+  for (long long tile = first; tile < ntile; tile += step) {
+    if (tile + step < ntile) issue(tile + step, buf ^ 1);
+    l2c_oz::cp_commit();
+    l2c_oz::cp_wait1();
+    __syncwarp();
+    work(tile, buf);
+    __syncwarp();
+    buf ^= 1;
+  }
+}
+
+// Combined integers of a 16 x (NT*8) tile; K past KMAX is split into two exact
+// accumulations whose integers are added.
+template <int NT, int KC>
+__device__ __forceinline__ void oz_tile_T(const unsigned *Pf, const long long *Ys, int yld, int ks,
+                                          long long (&T)[NT][4]) {
+  float acc[l2c_oz::NDIAG][NT][4];
+  if constexpr (KC <= l2c_oz::KMAX / 8) {
+    l2c_oz::mma_tile<NT, KC>(Pf, Ys, yld, ks, acc);
+#pragma unroll
+    for (int nt = 0; nt < NT; nt++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) T[nt][e] = l2c_oz::combine(acc, nt, e);
+  } else {
+    l2c_oz::mma_tile<NT, KC, 0, KC / 2>(Pf, Ys, yld, ks, acc);
+#pragma unroll
+    for (int nt = 0; nt < NT; nt++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) T[nt][e] = l2c_oz::combine(acc, nt, e);
+    l2c_oz::mma_tile<NT, KC, KC / 2, KC>(Pf, Ys, yld, ks, acc);
+#pragma unroll
+    for (int nt = 0; nt < NT; nt++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) T[nt][e] += l2c_oz::combine(acc, nt, e);
+  }
+}
+
+// Leaf up (step 1): tile = 16 consecutive leaf nodes of one vector; both
+// parities from one staged stretch of x (node r's h inputs in row r, parity
+// sg at even/odd positions).  P_sg = T_sg^T (18 x s), KC = ceil(s / 8).
+template <int KC>
 __global__ void __launch_bounds__(32 * MXW)
-    k_mx_leaf_down(const double *__restrict__ c, const double *__restrict__ y, double *out,
-                   const __nv_bfloat16 *__restrict__ Pn, const int *__restrict__ Pne, Geo g,
-                   int c2l) {
-  __shared__ MxSmem<2> sm;
-  const int wid = threadIdx.x >> 5;
-  const long long ncol = g.count * g.K, ngrp = (ncol + 7) / 8;
-  const long long grp = (long long)blockIdx.x * MXW + wid;
-  if (grp >= 2 * ngrp) return;
-  const int sg = (int)(grp / ngrp);
-  const long long col0 = (grp - sg * ngrp) * 8;
-  auto ld = [&](int cc, int k) -> double {
-    const long long col = col0 + cc;
-    if (col >= ncol || k >= M) return 0.0;
-    const long long v = col / g.K, tau = col - v * g.K;
-    return c[((v * 2 + sg) * g.slots + g.leaf_base + tau) * M + k];
+    k_mz_leaf_up(const double *__restrict__ x, double *__restrict__ w,
+                 const unsigned *__restrict__ Pf, const int *__restrict__ Pe, Geo g) {
+  constexpr int XLD = 16 * KC + 1, NW = oz_words(OZ_NT, KC);
+  extern __shared__ __align__(16) unsigned char mz_smem[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
+  unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
+  int *sE = reinterpret_cast<int *>(sP + 2 * NW);
+  int *Es = sE + 2 * OZ_ROWS + wid * 32;
+  double *Xw = reinterpret_cast<double *>(sE + 2 * OZ_ROWS + 32 * MXW) + wid * 2 * 16 * XLD;
+  oz_load_frag(sP, Pf, 2 * NW, sE, Pe, 2 * OZ_ROWS);
+  __syncthreads();
+  const long long tpv = (g.K + 15) / 16, ntile = g.count * tpv;
+  auto issue = [&](long long tile, int buf) {
+    const long long v = tile / tpv, node0 = (tile - v * tpv) * 16;
+    const double *xv = x + v * g.N;
+    double *X = Xw + buf * 16 * XLD;
+    for (int r = 0; r < 16; r++) {
+      const long long base = (node0 + r + 2) * g.h;
+      const bool live = node0 + r < g.K;
+      for (int j = lane; j < g.h; j += 32) {
+        const bool ok = live && base + j < g.N;
+        l2c_oz::cp_async8(X + r * XLD + j, ok ? xv + base + j : xv, ok ? 8 : 0);
+      }
+    }
   };
-  mx_stage<2>(sm.Qf[wid], MxSmem<2>::QLD, sm.Qe[wid], M, ld);
-  double far[MT][4];
-  l2c_oz::warp_tile<MT, 2>(Pn + (size_t)sg * l2c_oz::SLICES * g.s * M, (int)(g.s * M), M,
-                           (int)g.s, M, Pne + sg * g.s, sm.Qf[wid], MxSmem<2>::QLD, sm.Qe[wid],
-                           far);
-  const int lane = threadIdx.x & 31;
+  auto work = [&](long long tile, int buf) {
+    const long long v = tile / tpv, node0 = (tile - v * tpv) * 16;
+    double *X = Xw + buf * 16 * XLD;
+    l2c_oz::stage_fix(X, XLD, 2, (int)g.s, 8 * KC, Es);
+    l2c_oz::stage_fix(X + 1, XLD, 2, (int)g.s, 8 * KC, Es + 16);
+    const long long *Ys = reinterpret_cast<const long long *>(X);
+#pragma unroll 1
+    for (int sg = 0; sg < 2; sg++) {
+      long long T[OZ_NT][4];
+      oz_tile_T<OZ_NT, KC>(sP + sg * NW, Ys + sg, XLD, 2, T);
 #pragma unroll
-  for (int mt = 0; mt < MT; mt++)
+      for (int nt = 0; nt < OZ_NT; nt++)
 #pragma unroll
-    for (int e = 0; e < 4; e++) {
-      const long long i = mt * 16 + (lane >> 2) + 8 * (e >> 1);
-      const long long col = col0 + 2 * (lane & 3) + (e & 1);
-      if (i >= g.s || col >= ncol) continue;
-      const long long v = col / g.K, tau = col - v * g.K;
-      const long long j = tau * g.h + 2 * i + sg;
-      if (j >= g.N) continue;
-      double val = y[v * g.N + j] + far[mt][e];
+        for (int hr = 0; hr < 2; hr++) {
+          const int r = gq + 8 * hr, n = 8 * nt + 2 * t4;
+          if (n >= M || node0 + r >= g.K) continue;
+          const int ec = Es[sg * 16 + r] - 52;
+          double2 o;
+          o.x = l2c_oz::to_double(T[nt][2 * hr], ec + sE[sg * OZ_ROWS + n]);
+          o.y = l2c_oz::to_double(T[nt][2 * hr + 1], ec + sE[sg * OZ_ROWS + n + 1]);
+          *reinterpret_cast<double2 *>(
+              w + ((v * 2 + sg) * g.slots + g.leaf_base + node0 + r) * M + n) = o;
+        }
+    }
+  };
+  oz_tile_loop((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue, work);
+}
+
+size_t mz_leaf_up_smem(int KC) {
+  return (size_t)(2 * oz_words(OZ_NT, KC) + 2 * OZ_ROWS + 32 * MXW) * 4 +
+         (size_t)MXW * 2 * 16 * (16 * KC + 1) * sizeof(double);
+}
+
+// Transfer trees, one level.  Columns col = (vector * 2 + parity) * np + j.
+// Up: parent slot j of level l from child slots 2j+2, 2j+3 of level l+1
+// (36 contiguous coefficients), P = [B | B'] (18 x 36).
+constexpr int OZ_TREE_UP_WORDS = oz_words(OZ_NT, 5);
+__global__ void __launch_bounds__(32 * MXW)
+    k_mz_tree_up(double *w, const unsigned *__restrict__ Pf, const int *__restrict__ Pe, Geo g,
+                 long long parent_base, long long child_base, long long np) {
+  extern __shared__ __align__(16) unsigned char mz_smem[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
+  unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
+  int *sE = reinterpret_cast<int *>(sP + OZ_TREE_UP_WORDS);
+  int *Es = sE + OZ_ROWS + wid * 16;
+  long long *sB = reinterpret_cast<long long *>(sE + OZ_ROWS + 16 * MXW) + wid * 2 * 16;
+  double *Xw = reinterpret_cast<double *>(sB - wid * 2 * 16 + 2 * 16 * MXW) + wid * 2 * 16 * OZ_TLD;
+  oz_load_frag(sP, Pf, OZ_TREE_UP_WORDS, sE, Pe, OZ_ROWS);
+  __syncthreads();
+  const long long ncol = g.count * 2 * np, ntile = (ncol + 15) / 16;
+  auto issue = [&](long long tile, int buf) {
+    long long *B = sB + buf * 16;
+    if (lane < 16) {
+      const long long col = tile * 16 + lane;
+      long long b = -1;
+      if (col < ncol) {
+        const long long vs = col / np, j = col - vs * np;
+        b = (vs * g.slots + child_base + 2 * j + 2) * M;
+      }
+      B[lane] = b;
+    }
+    __syncwarp();
+    double *X = Xw + buf * 16 * OZ_TLD;
+    for (int e = lane; e < 16 * M; e += 32) {  // 16 columns x 18 pairs
+      const int r = e / M, k2 = e - r * M;
+      const long long b = B[r];
+      l2c_oz::cp_async16(X + r * OZ_TLD + 2 * k2, b >= 0 ? w + b + 2 * k2 : w, b >= 0 ? 16 : 0);
+    }
+  };
+  auto work = [&](long long tile, int buf) {
+    double *X = Xw + buf * 16 * OZ_TLD;
+    l2c_oz::stage_fix(X, OZ_TLD, 1, 2 * M, 40, Es);
+    long long T[OZ_NT][4];
+    oz_tile_T<OZ_NT, 5>(sP, reinterpret_cast<const long long *>(X), OZ_TLD, 1, T);
+#pragma unroll
+    for (int hr = 0; hr < 2; hr++) {
+      const int r = gq + 8 * hr;
+      const long long col = tile * 16 + r;
+      if (col >= ncol) continue;
+      const long long vs = col / np, j = col - vs * np;
+      double *dst = w + (vs * g.slots + parent_base + j) * M;
+      const int ec = Es[r] - 52;
+#pragma unroll
+      for (int nt = 0; nt < OZ_NT; nt++) {
+        const int n = 8 * nt + 2 * t4;
+        if (n >= M) continue;
+        double2 o;
+        o.x = l2c_oz::to_double(T[nt][2 * hr], ec + sE[n]);
+        o.y = l2c_oz::to_double(T[nt][2 * hr + 1], ec + sE[n + 1]);
+        *reinterpret_cast<double2 *>(dst + n) = o;
+      }
+    }
+  };
+  oz_tile_loop((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue, work);
+}
+
+constexpr size_t OZ_TREE_UP_SMEM = (size_t)(OZ_TREE_UP_WORDS + OZ_ROWS + 16 * MXW) * 4 +
+                                   (size_t)MXW * 2 * 16 * 8 +
+                                   (size_t)MXW * 2 * 16 * OZ_TLD * sizeof(double);
+
+// Down: child slots 2t, 2t+1 of level l+1 += [B^T; B^T'] c(parent slot t of
+// level l).  The sum with the child's own far field is formed exactly in the
+// fixed-point frame of the product when the magnitudes allow it.
+__device__ __forceinline__ double oz_add(double existing, long long T, int e) {
+  long long X;
+  if (l2c_oz::to_fixed(existing, e, X)) return l2c_oz::to_double(T + X, e);
+  return existing + l2c_oz::to_double(T, e);
+}
+
+constexpr int OZ_TREE_DOWN_WORDS = 2 * oz_words(OZ_NT, 3);
+// Per warp and buffer: 16 parent columns (18 values, row OZ_CLD) and the 16
+// pairs of child columns they add to (36 contiguous values each).
+__global__ void __launch_bounds__(32 * MXW)
+    k_mz_tree_down(double *c, const unsigned *__restrict__ Pf, const int *__restrict__ Pe, Geo g,
+                   long long parent_base, long long child_base, long long np) {
+  extern __shared__ __align__(16) unsigned char mz_smem[];
+  constexpr int NW = oz_words(OZ_NT, 3);
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
+  unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
+  int *sE = reinterpret_cast<int *>(sP + OZ_TREE_DOWN_WORDS);
+  int *Es = sE + 2 * OZ_ROWS + wid * 16;
+  long long *sB0 = reinterpret_cast<long long *>(sE + 2 * OZ_ROWS + 16 * MXW);
+  long long *sB = sB0 + wid * 2 * 2 * 16;  // [buf][parent | child][16]
+  double *X0 = reinterpret_cast<double *>(sB0 + 2 * 2 * 16 * MXW);
+  double *Xw = X0 + wid * 2 * 16 * OZ_CLD;
+  double *Cw = X0 + MXW * 2 * 16 * OZ_CLD + wid * 2 * 16 * 2 * M;
+  oz_load_frag(sP, Pf, OZ_TREE_DOWN_WORDS, sE, Pe, 2 * OZ_ROWS);
+  __syncthreads();
+  const long long ncol = g.count * 2 * np, ntile = (ncol + 15) / 16;
+  auto issue = [&](long long tile, int buf) {
+    long long *B = sB + buf * 32;
+    if (lane < 16) {
+      const long long col = tile * 16 + lane;
+      long long b = -1, cb = -1;
+      if (col < ncol) {
+        const long long vs = col / np, t = col - vs * np;
+        b = (vs * g.slots + parent_base + t) * M;
+        cb = (vs * g.slots + child_base + 2 * t) * M;
+      }
+      B[lane] = b;
+      B[16 + lane] = cb;
+    }
+    __syncwarp();
+    double *X = Xw + buf * 16 * OZ_CLD, *C = Cw + buf * 16 * 2 * M;
+    for (int e = lane; e < 16 * (M / 2); e += 32) {  // 16 columns x 9 pairs
+      const int r = e / (M / 2), k2 = e - r * (M / 2);
+      const long long b = B[r];
+      l2c_oz::cp_async16(X + r * OZ_CLD + 2 * k2, b >= 0 ? c + b + 2 * k2 : c, b >= 0 ? 16 : 0);
+    }
+    for (int e = lane; e < 16 * M; e += 32) {  // 16 child pairs x 18 pairs
+      const int r = e / M, k2 = e - r * M;
+      const long long b = B[16 + r];
+      l2c_oz::cp_async16(C + r * 2 * M + 2 * k2, b >= 0 ? c + b + 2 * k2 : c, b >= 0 ? 16 : 0);
+    }
+  };
+  auto work = [&](long long tile, int buf) {
+    double *X = Xw + buf * 16 * OZ_CLD;
+    const double *C = Cw + buf * 16 * 2 * M;
+    const long long *B = sB + buf * 32;
+    l2c_oz::stage_fix(X, OZ_CLD, 1, M, 24, Es);
+#pragma unroll 1
+    for (int ch = 0; ch < 2; ch++) {
+      long long T[OZ_NT][4];
+      oz_tile_T<OZ_NT, 3>(sP + ch * NW, reinterpret_cast<const long long *>(X), OZ_CLD, 1, T);
+#pragma unroll
+      for (int hr = 0; hr < 2; hr++) {
+        const int r = gq + 8 * hr;
+        const long long cb = B[16 + r];
+        if (cb < 0) continue;
+        double *dst = c + cb + ch * M;
+        const double *old = C + r * 2 * M + ch * M;
+        const int ec = Es[r] - 52;
+#pragma unroll
+        for (int nt = 0; nt < OZ_NT; nt++) {
+          const int n = 8 * nt + 2 * t4;
+          if (n >= M) continue;
+          double2 o;
+          o.x = oz_add(old[n], T[nt][2 * hr], ec + sE[ch * OZ_ROWS + n]);
+          o.y = oz_add(old[n + 1], T[nt][2 * hr + 1], ec + sE[ch * OZ_ROWS + n + 1]);
+          *reinterpret_cast<double2 *>(dst + n) = o;
+        }
+      }
+    }
+  };
+  oz_tile_loop((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue, work);
+}
+
+constexpr size_t OZ_TREE_DOWN_SMEM = (size_t)(OZ_TREE_DOWN_WORDS + 2 * OZ_ROWS + 16 * MXW) * 4 +
+                                     (size_t)MXW * 2 * 2 * 16 * 8 +
+                                     (size_t)MXW * 2 * 16 * (OZ_CLD + 2 * M) * sizeof(double);
+
+// Far field (step 3): CTA = (block gb, chunk of columns vs = vector * 2 +
+// parity).  c0 = [A0 A1] [w0; w1] (K = 36), c1 = A2 w1 (K = 18); both parts
+// use the exponent of the whole column [w0; w1].
+constexpr int OZ_FAR_COLS = 16 * MXW * 2;  // columns per CTA
+__global__ void __launch_bounds__(32 * MXW)
+    k_mz_far(const double *__restrict__ w, double *__restrict__ c,
+             const unsigned *__restrict__ Pf, const int *__restrict__ Pe, Geo g) {
+  extern __shared__ __align__(16) unsigned char mz_smem[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
+  unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
+  int *sE = reinterpret_cast<int *>(sP + OZ_FAR_WORDS);
+  int *Es = sE + 2 * OZ_ROWS + wid * 16;
+  double *Xw = reinterpret_cast<double *>(sE + 2 * OZ_ROWS + 16 * MXW) + wid * 2 * 16 * OZ_TLD;
+  const long long gb = blockIdx.x;
+  oz_load_frag(sP, Pf + gb * OZ_FAR_WORDS, OZ_FAR_WORDS, sE, Pe + gb * 2 * OZ_ROWS, 2 * OZ_ROWS);
+  __syncthreads();
+  const long long ncol = 2 * g.count, c0 = (long long)blockIdx.y * OZ_FAR_COLS;
+  const long long ntile = (min(ncol - c0, (long long)OZ_FAR_COLS) + 15) / 16;
+  auto issue = [&](long long tile, int buf) {
+    double *X = Xw + buf * 16 * OZ_TLD;
+    for (int e = lane; e < 16 * M; e += 32) {  // 16 columns x 18 pairs
+      const int r = e / M, k2 = e - r * M;
+      const long long col = c0 + tile * 16 + r;
+      const bool ok = col < ncol;
+      l2c_oz::cp_async16(X + r * OZ_TLD + 2 * k2, ok ? w + (col * g.slots + 2 * gb) * M + 2 * k2 : w,
+                         ok ? 16 : 0);
+    }
+  };
+  auto work = [&](long long tile, int buf) {
+    double *X = Xw + buf * 16 * OZ_TLD;
+    l2c_oz::stage_fix(X, OZ_TLD, 1, 2 * M, OZ_TLD, Es);
+    const long long *Ys = reinterpret_cast<const long long *>(X);
+#pragma unroll 1
+    for (int part = 0; part < 2; part++) {
+      long long T[OZ_NT][4];
+      if (part == 0)
+        oz_tile_T<OZ_NT, 5>(sP, Ys, OZ_TLD, 1, T);
+      else
+        oz_tile_T<OZ_NT, 3>(sP + OZ_FAR_W0, Ys + M, OZ_TLD, 1, T);
+#pragma unroll
+      for (int hr = 0; hr < 2; hr++) {
+        const int r = gq + 8 * hr;
+        const long long col = c0 + tile * 16 + r;
+        if (col >= ncol) continue;
+        double *dst = c + (col * g.slots + 2 * gb + part) * M;
+        const int ec = Es[r] - 52;
+#pragma unroll
+        for (int nt = 0; nt < OZ_NT; nt++) {
+          const int n = 8 * nt + 2 * t4;
+          if (n >= M) continue;
+          double2 o;
+          o.x = l2c_oz::to_double(T[nt][2 * hr], ec + sE[part * OZ_ROWS + n]);
+          o.y = l2c_oz::to_double(T[nt][2 * hr + 1], ec + sE[part * OZ_ROWS + n + 1]);
+          *reinterpret_cast<double2 *>(dst + n) = o;
+        }
+      }
+    }
+  };
+  oz_tile_loop(wid, MXW, ntile, issue, work);
+}
+
+constexpr size_t OZ_FAR_SMEM = (size_t)(OZ_FAR_WORDS + 2 * OZ_ROWS + 16 * MXW) * 4 +
+                               (size_t)MXW * 2 * 16 * OZ_TLD * sizeof(double);
+
+// Leaf down (step 5) + final scaling: tile = 16 consecutive leaf targets of one
+// vector, both parities; P_sg = T_sg (s x 18) in passes of 16 output rows
+// (two n-tiles, KC = 3).  The band sum y of the tile is copied to shared
+// memory with the tile's coefficients, the far field is added there, and the
+// sum is written, scaled, in output order.
+constexpr int OZ_LD_WORDS = oz_words(2, 3);
+__global__ void __launch_bounds__(32 * MXW)
+    k_mz_leaf_down(const double *__restrict__ c, const double *__restrict__ y, double *out,
+                   const unsigned *__restrict__ Pf, const int *__restrict__ Pe, Geo g, int c2l,
+                   int npass) {
+  extern __shared__ __align__(16) unsigned char mz_smem[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
+  const int nw = 2 * npass * OZ_LD_WORDS, ne = 2 * npass * 16;
+  unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
+  int *sE = reinterpret_cast<int *>(sP + nw);
+  int *Ec = sE + ne + wid * 32;
+  const long long per_warp = 2 * 2 * 16 * OZ_CLD + 2 * 16 * g.h;
+  double *Xw = reinterpret_cast<double *>(sE + ne + 32 * MXW) + wid * per_warp;
+  double *Ow = Xw + 2 * 2 * 16 * OZ_CLD;  // per buffer 16 rows of h outputs
+  oz_load_frag(sP, Pf, nw, sE, Pe, ne);
+  __syncthreads();
+  const long long tpv = (g.K + 15) / 16, ntile = g.count * tpv;
+  auto issue = [&](long long tile, int buf) {
+    const long long v = tile / tpv, tau0 = (tile - v * tpv) * 16;
+    const long long nrow = min(16LL, g.K - tau0);
+    double *X = Xw + buf * 2 * 16 * OZ_CLD;
+    for (int e = lane; e < 2 * 16 * (M / 2); e += 32) {  // 2 parities x 16 rows x 9 pairs
+      const int sr = e / (M / 2), k2 = e - sr * (M / 2), sg = sr >> 4, r = sr & 15;
+      const bool ok = r < nrow;
+      const double *src = c + ((v * 2 + sg) * g.slots + g.leaf_base + tau0 + r) * M + 2 * k2;
+      l2c_oz::cp_async16(X + sr * OZ_CLD + 2 * k2, ok ? src : c, ok ? 16 : 0);
+    }
+    const long long j0 = tau0 * g.h, jn = nrow * g.h;
+    const double *yv = y + v * g.N;
+    double *O = Ow + buf * 16 * g.h;
+    for (long long jj = lane; jj < jn; jj += 32) {
+      const bool ok = j0 + jj < g.N;
+      l2c_oz::cp_async8(O + jj, ok ? yv + j0 + jj : yv, ok ? 8 : 0);
+    }
+  };
+  auto work = [&](long long tile, int buf) {
+    const long long v = tile / tpv, tau0 = (tile - v * tpv) * 16;
+    double *O = Ow + buf * 16 * g.h;
+#pragma unroll 1
+    for (int sg = 0; sg < 2; sg++) {
+      double *X = Xw + (buf * 2 + sg) * 16 * OZ_CLD;
+      l2c_oz::stage_fix(X, OZ_CLD, 1, M, 24, Ec + 16 * sg);
+      const long long *Ys = reinterpret_cast<const long long *>(X);
+#pragma unroll 1
+      for (int ps = 0; ps < npass; ps++) {
+        long long T[2][4];
+        oz_tile_T<2, 3>(sP + (sg * npass + ps) * OZ_LD_WORDS, Ys, OZ_CLD, 1, T);
+        const int *Ep = sE + (sg * npass + ps) * 16;
+#pragma unroll
+        for (int nt = 0; nt < 2; nt++)
+#pragma unroll
+          for (int e = 0; e < 4; e++) {
+            const int r = gq + 8 * (e >> 1), il = 8 * nt + 2 * t4 + (e & 1), i = 16 * ps + il;
+            if (i >= g.s) continue;
+            O[r * g.h + 2 * i + sg] += l2c_oz::to_double(T[nt][e], Ec[16 * sg + r] - 52 + Ep[il]);
+          }
+      }
+    }
+    __syncwarp();
+    // y + far, scaled, in output order
+    const long long j0 = tau0 * g.h, jn = min(16LL, g.K - tau0) * g.h;
+    for (long long jj = lane; jj < jn; jj += 32) {
+      const long long j = j0 + jj;
+      if (j >= g.N) break;
+      double val = O[jj];
       if (!c2l) {
         val = val * TWO_OVER_PI;
         if (j == 0) val = val * 0.5;
@@ -952,6 +1319,13 @@ __global__ void __launch_bounds__(32 * MXW)
       }
       out[v * g.dist + j * g.stride] = val;
     }
+  };
+  oz_tile_loop((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue, work);
+}
+
+size_t mz_leaf_down_smem(long long s, int npass) {
+  return (size_t)(2 * npass * OZ_LD_WORDS + 2 * npass * 16 + 32 * MXW) * 4 +
+         (size_t)MXW * (2 * 2 * 16 * OZ_CLD + 2 * 16 * 2 * s) * sizeof(double);
 }
 
 // Outputs past the last leaf target node (no far field): scaling only.
@@ -969,156 +1343,6 @@ __global__ void k_mx_tail(const double *__restrict__ y, double *out, Geo g, int 
   }
   out[v * g.dist + j * g.stride] = val;
 }
-
-// Far field (step 3), one block gb per warp group: columns (vector, parity).
-// c0 = [A0 A1] [w0; w1] (K = 36), c1 = A2 w1 (K = 18).  Slices per block:
-// P01 at Pf + gb * SLICES * 18 * 54 (row stride 54: [A0 A1 | A2]).
-__global__ void __launch_bounds__(32 * MXW)
-    k_mx_far(const double *__restrict__ w, double *__restrict__ c,
-             const __nv_bfloat16 *__restrict__ Pf, const int *__restrict__ Pfe, Geo g,
-             long long nblocks) {
-  __shared__ MxSmem<3> sm;
-  const int wid = threadIdx.x >> 5;
-  const long long ncol = 2 * g.count, ngrp = (ncol + 7) / 8;
-  const long long item = (long long)blockIdx.x * MXW + wid;
-  if (item >= nblocks * ngrp) return;
-  const long long gb = item / ngrp, col0 = (item - gb * ngrp) * 8;
-  const __nv_bfloat16 *P = Pf + gb * (long long)l2c_oz::SLICES * M * 54;
-  const int *Pe = Pfe + gb * 2 * M;
-  const int lane = threadIdx.x & 31;
-  for (int part = 0; part < 2; part++) {
-    const int K = part == 0 ? 2 * M : M;
-    auto ld = [&](int cc, int k) -> double {
-      const long long col = col0 + cc;
-      if (col >= ncol || k >= K) return 0.0;
-      return w[(col * g.slots + 2 * gb + part) * M + k];
-    };
-    mx_stage<3>(sm.Qf[wid], MxSmem<3>::QLD, sm.Qe[wid], K, ld);
-    double out[2][4];
-    l2c_oz::warp_tile<2, 3>(P + (part == 0 ? 0 : 2 * M), M * 54, 54, M, K, Pe + part * M,
-                            sm.Qf[wid], MxSmem<3>::QLD, sm.Qe[wid], out);
-#pragma unroll
-    for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-      for (int e = 0; e < 4; e++) {
-        const int m = mt * 16 + (lane >> 2) + 8 * (e >> 1);
-        const long long col = col0 + 2 * (lane & 3) + (e & 1);
-        if (m >= M || col >= ncol) continue;
-        c[(col * g.slots + 2 * gb + part) * M + m] = out[mt][e];
-      }
-    __syncwarp();
-  }
-}
-
-// Transfer trees, one level.  Up: P = [B | B'] (18 x 36), columns
-// (vector*2+parity, parent slot), K = 36 child coefficients.  Down:
-// P = [B^T; B^T'] (36 x 18), K = 18 parent coefficients, rows r < 18 add to the
-// first child, r >= 18 to the second.
-__global__ void __launch_bounds__(32 * MXW)
-    k_mx_tree_up(double *w, const __nv_bfloat16 *__restrict__ Pu, const int *__restrict__ Pue,
-                 Geo g, long long parent_base, long long child_base, long long nparent) {
-  __shared__ MxSmem<3> sm;
-  const int wid = threadIdx.x >> 5;
-  const long long ncol = g.count * 2 * nparent;
-  const long long col0 = ((long long)blockIdx.x * MXW + wid) * 8;
-  if (col0 >= ncol) return;
-  auto ld = [&](int cc, int k) -> double {
-    const long long col = col0 + cc;
-    if (col >= ncol || k >= 2 * M) return 0.0;
-    const long long vs = col / nparent, jp = col - vs * nparent;
-    return w[(vs * g.slots + child_base + 2 * jp + 2) * M + k];
-  };
-  mx_stage<3>(sm.Qf[wid], MxSmem<3>::QLD, sm.Qe[wid], 2 * M, ld);
-  double out[2][4];
-  l2c_oz::warp_tile<2, 3>(Pu, M * 2 * M, 2 * M, M, 2 * M, Pue, sm.Qf[wid], MxSmem<3>::QLD,
-                          sm.Qe[wid], out);
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-      const int m = mt * 16 + (lane >> 2) + 8 * (e >> 1);
-      const long long col = col0 + 2 * (lane & 3) + (e & 1);
-      if (m >= M || col >= ncol) continue;
-      const long long vs = col / nparent, jp = col - vs * nparent;
-      w[(vs * g.slots + parent_base + jp) * M + m] = out[mt][e];
-    }
-}
-
-__global__ void __launch_bounds__(32 * MXW)
-    k_mx_tree_down(double *c, const __nv_bfloat16 *__restrict__ Pd, const int *__restrict__ Pde,
-                   Geo g, long long parent_base, long long child_base, long long nparent) {
-  __shared__ MxSmem<2> sm;
-  const int wid = threadIdx.x >> 5;
-  const long long ncol = g.count * 2 * nparent;
-  const long long col0 = ((long long)blockIdx.x * MXW + wid) * 8;
-  if (col0 >= ncol) return;
-  auto ld = [&](int cc, int k) -> double {
-    const long long col = col0 + cc;
-    if (col >= ncol || k >= M) return 0.0;
-    const long long vs = col / nparent, tp = col - vs * nparent;
-    return c[(vs * g.slots + parent_base + tp) * M + k];
-  };
-  mx_stage<2>(sm.Qf[wid], MxSmem<2>::QLD, sm.Qe[wid], M, ld);
-  double out[3][4];
-  l2c_oz::warp_tile<3, 2>(Pd, 2 * M * M, M, 2 * M, M, Pde, sm.Qf[wid], MxSmem<2>::QLD,
-                          sm.Qe[wid], out);
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int mt = 0; mt < 3; mt++)
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-      const int r = mt * 16 + (lane >> 2) + 8 * (e >> 1);
-      const long long col = col0 + 2 * (lane & 3) + (e & 1);
-      if (r >= 2 * M || col >= ncol) continue;
-      const long long vs = col / nparent, tp = col - vs * nparent;
-      c[(vs * g.slots + child_base + 2 * tp) * M + r] += out[mt][e];  // r >= 18: second child
-    }
-}
-
-// Plan time: slices of a dense row-major FP64 matrix (rows x K, leading
-// dimension ldp) into S[(p-1) * sstride + r * kld + k] with per-row exponents.
-__global__ void k_oz_slice_rows(const double *__restrict__ P, int rows, int K, int ldp,
-                                __nv_bfloat16 *S, int kld, long long sstride, int *E) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows) return;
-  int e = l2c_oz::EXP_ZERO;
-  for (int k = 0; k < K; k++) e = max(e, l2c_oz::exp_bound(P[(long long)r * ldp + k]));
-  E[r] = e;
-  for (int k = 0; k < kld; k++) {
-    const unsigned long long f = k < K ? l2c_oz::fix56(P[(long long)r * ldp + k], e) : 0ull;
-    for (int q = 1; q <= l2c_oz::SLICES; q++)
-      S[(q - 1) * sstride + (long long)r * kld + k] = __float2bfloat16_rn(l2c_oz::slice(f, q));
-  }
-}
-
-// Plan time: far-field block slices, one thread per (block, row): the row of
-// [A0 A1] (36 values) and of A2 (18 values), each with its own exponent.
-__global__ void k_oz_slice_far(const double *__restrict__ A, long long nblocks,
-                               __nv_bfloat16 *S, int *E) {
-  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (idx >= nblocks * M) return;
-  const long long gb = idx / M;
-  const int m = (int)(idx - gb * M);
-  const double *A0 = A + 3 * gb * MM + m * M;
-  __nv_bfloat16 *Sb = S + gb * (long long)l2c_oz::SLICES * M * 54;
-  for (int part = 0; part < 2; part++) {
-    const int K = part == 0 ? 2 * M : M;
-    auto val = [&](int k) -> double {
-      return part == 0 ? (k < M ? A0[k] : A0[MM + k - M]) : A0[2 * MM + k];
-    };
-    int e = l2c_oz::EXP_ZERO;
-    for (int k = 0; k < K; k++) e = max(e, l2c_oz::exp_bound(val(k)));
-    E[gb * 2 * M + part * M + m] = e;
-    for (int k = 0; k < K; k++) {
-      const unsigned long long f = l2c_oz::fix56(val(k), e);
-      for (int q = 1; q <= l2c_oz::SLICES; q++)
-        Sb[(q - 1) * M * 54 + m * 54 + (part == 0 ? 0 : 2 * M) + k] =
-            __float2bfloat16_rn(l2c_oz::slice(f, q));
-    }
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Plan
 // ---------------------------------------------------------------------------
@@ -1148,11 +1372,15 @@ struct l2c_gpu_plan {
   double *Wnear[2] = {nullptr, nullptr};  // precomputed band weights (optional)
   // mixed precision (L2C_PLAN_MIXED): sliced constant factors
   bool mixed = false;
-  __nv_bfloat16 *oz_Tt = nullptr, *oz_Tn = nullptr, *oz_Bu = nullptr, *oz_Bd = nullptr;
-  int *oz_Tte = nullptr, *oz_Tne = nullptr, *oz_Bue = nullptr, *oz_Bde = nullptr;
-  int oz_kld = 0;                                   // row stride of oz_Tt (s rounded up to even)
-  __nv_bfloat16 *oz_A[2] = {nullptr, nullptr};      // far blocks, built on first batched call
-  int *oz_Ae[2] = {nullptr, nullptr};
+  // fragment words (l2c_oz::frag_index layout) and row exponents of: T_parity^T
+  // (leaf up), [B | B'] (tree up), B^T and B^T' (tree down), T_parity in passes
+  // of 16 rows (leaf down), and the far-field blocks (built on the first batched
+  // call, per direction)
+  unsigned *oz_lu = nullptr, *oz_tu = nullptr, *oz_td = nullptr, *oz_ld = nullptr;
+  int *oz_lue = nullptr, *oz_tue = nullptr, *oz_tde = nullptr, *oz_lde = nullptr;
+  int oz_kc = 0, oz_npass = 0;  // leaf-up k8 chunks, leaf-down passes
+  unsigned *oz_far[2] = {nullptr, nullptr};
+  int *oz_fare[2] = {nullptr, nullptr};
   // captured launch sequences, keyed by the call's shape and pointers
   struct GraphEntry {
     size_t dir, count, dist, stride;
@@ -1454,19 +1682,27 @@ Geo make_geo(const l2c_gpu_plan *p, size_t count, size_t dist, size_t stride) {
 // Far field of the mixed form: leaf, tree and far-field products on tensor
 // cores (the far-field blocks only when the batch gives each block at least 8
 // right-hand sides; single vectors keep the FP64 block products).
+template <int KC>
+void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStream_t st) {
+  const long long tiles = g.count * ((g.K + 15) / 16);
+  const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
+  k_mz_leaf_up<KC><<<grid, 32 * MXW, mz_leaf_up_smem(KC), st>>>(x, p->w, p->oz_lu, p->oz_lue, g);
+}
+
 bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir, const Geo &g,
                       cudaStream_t st) {
   const int c2l = dir == 1;
-  const int kt = (int)((g.s + 15) / 16);
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
-    const long long ngrp = 2 * ((g.count * g.K + 7) / 8);
-    const unsigned grid = (unsigned)((ngrp + MXW - 1) / MXW);
-    switch (kt) {
-      case 1: k_mx_leaf_up<1><<<grid, 32 * MXW, 0, st>>>(x, p->w, p->oz_Tt, p->oz_Tte, p->oz_kld, g); break;
-      case 2: k_mx_leaf_up<2><<<grid, 32 * MXW, 0, st>>>(x, p->w, p->oz_Tt, p->oz_Tte, p->oz_kld, g); break;
-      case 3: k_mx_leaf_up<3><<<grid, 32 * MXW, 0, st>>>(x, p->w, p->oz_Tt, p->oz_Tte, p->oz_kld, g); break;
-      default: k_mx_leaf_up<4><<<grid, 32 * MXW, 0, st>>>(x, p->w, p->oz_Tt, p->oz_Tte, p->oz_kld, g); break;
+    switch (p->oz_kc) {
+      case 1: mz_leaf_up_launch<1>(p, x, g, st); break;
+      case 2: mz_leaf_up_launch<2>(p, x, g, st); break;
+      case 3: mz_leaf_up_launch<3>(p, x, g, st); break;
+      case 4: mz_leaf_up_launch<4>(p, x, g, st); break;
+      case 5: mz_leaf_up_launch<5>(p, x, g, st); break;
+      case 6: mz_leaf_up_launch<6>(p, x, g, st); break;
+      case 7: mz_leaf_up_launch<7>(p, x, g, st); break;
+      default: mz_leaf_up_launch<8>(p, x, g, st); break;
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -1474,19 +1710,19 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     PhaseScope ps(p, L2C_PHASE_TREE_UP, p->L - 1);
     for (long long l = g.L - 2; l >= 0; l--) {
       const long long np = (long long)slots_at((size_t)l);
-      const long long ngrp = (g.count * 2 * np + 7) / 8;
-      k_mx_tree_up<<<(unsigned)((ngrp + MXW - 1) / MXW), 32 * MXW, 0, st>>>(
-          p->w, p->oz_Bu, p->oz_Bue, g, 2 * (long long)blocks_before((size_t)l),
-          2 * (long long)blocks_before((size_t)l + 1), np);
+      const long long tiles = (g.count * 2 * np + 15) / 16;
+      const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
+      k_mz_tree_up<<<grid, 32 * MXW, OZ_TREE_UP_SMEM, st>>>(p->w, p->oz_tu, p->oz_tue, g,
+                                               2 * (long long)blocks_before((size_t)l),
+                                               2 * (long long)blocks_before((size_t)l + 1), np);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
   {
     PhaseScope ps(p, L2C_PHASE_FAR, 1);
-    if (g.count >= 4 && p->oz_A[dir] != nullptr) {
-      const long long items = (long long)p->Nb * ((2 * g.count + 7) / 8);
-      k_mx_far<<<(unsigned)((items + MXW - 1) / MXW), 32 * MXW, 0, st>>>(
-          p->w, p->c, p->oz_A[dir], p->oz_Ae[dir], g, (long long)p->Nb);
+    if (g.count >= 4 && p->oz_far[dir] != nullptr) {
+      const dim3 grid((unsigned)p->Nb, (unsigned)((2 * g.count + OZ_FAR_COLS - 1) / OZ_FAR_COLS));
+      k_mz_far<<<grid, 32 * MXW, OZ_FAR_SMEM, st>>>(p->w, p->c, p->oz_far[dir], p->oz_fare[dir], g);
     } else {
       const long long n = g.count * 2 * (long long)p->Nb * M;
       k_far<<<blocks_for(n, 256), 256, 0, st>>>(p->A[dir], p->w, p->c, g, (long long)p->Nb);
@@ -1497,43 +1733,39 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     PhaseScope ps(p, L2C_PHASE_TREE_DOWN, p->L - 1);
     for (long long l = 0; l + 1 < g.L; l++) {
       const long long np = (long long)slots_at((size_t)l);
-      const long long ngrp = (g.count * 2 * np + 7) / 8;
-      k_mx_tree_down<<<(unsigned)((ngrp + MXW - 1) / MXW), 32 * MXW, 0, st>>>(
-          p->c, p->oz_Bd, p->oz_Bde, g, 2 * (long long)blocks_before((size_t)l),
-          2 * (long long)blocks_before((size_t)l + 1), np);
+      const long long tiles = (g.count * 2 * np + 15) / 16;
+      const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
+      k_mz_tree_down<<<grid, 32 * MXW, OZ_TREE_DOWN_SMEM, st>>>(p->c, p->oz_td, p->oz_tde, g,
+                                                 2 * (long long)blocks_before((size_t)l),
+                                                 2 * (long long)blocks_before((size_t)l + 1), np);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
   if (p->overlap && cudaStreamWaitEvent(st, p->ev_join, 0) != cudaSuccess) return false;
   {
-    PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 2);
-    const long long ngrp = 2 * ((g.count * g.K + 7) / 8);
-    const unsigned grid = (unsigned)((ngrp + MXW - 1) / MXW);
-    switch (kt) {
-      case 1: k_mx_leaf_down<1><<<grid, 32 * MXW, 0, st>>>(p->c, p->y, out, p->oz_Tn, p->oz_Tne, g, c2l); break;
-      case 2: k_mx_leaf_down<2><<<grid, 32 * MXW, 0, st>>>(p->c, p->y, out, p->oz_Tn, p->oz_Tne, g, c2l); break;
-      case 3: k_mx_leaf_down<3><<<grid, 32 * MXW, 0, st>>>(p->c, p->y, out, p->oz_Tn, p->oz_Tne, g, c2l); break;
-      default: k_mx_leaf_down<4><<<grid, 32 * MXW, 0, st>>>(p->c, p->y, out, p->oz_Tn, p->oz_Tne, g, c2l); break;
-    }
     const long long tail = g.count * (g.N - g.K * g.h);
+    PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, tail > 0 ? 2 : 1);
+    const long long tiles = g.count * ((g.K + 15) / 16);
+    const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
+    k_mz_leaf_down<<<grid, 32 * MXW, mz_leaf_down_smem(g.s, p->oz_npass), st>>>(
+        p->c, p->y, out, p->oz_ld, p->oz_lde, g, c2l, p->oz_npass);
     if (tail > 0) k_mx_tail<<<blocks_for(tail, 256), 256, 0, st>>>(p->y, out, g, c2l);
     if (cudaGetLastError() != cudaSuccess) return false;
   }
   return true;
 }
 
-// Far-field block slices of the mixed form, built on the first batched call.
+// Far-field block fragments of the mixed form, built on the first batched call.
 bool ensure_mixed_far(l2c_gpu_plan *p, size_t dir) {
-  if (p->oz_A[dir]) return true;
+  if (p->oz_far[dir]) return true;
   const size_t nb = p->Nb;
-  if (cudaMalloc(&p->oz_A[dir], nb * l2c_oz::SLICES * M * 54 * sizeof(__nv_bfloat16)) !=
-          cudaSuccess ||
-      cudaMalloc(&p->oz_Ae[dir], nb * 2 * M * sizeof(int)) != cudaSuccess) {
-    set_err("cudaMalloc of the mixed-form far-field slices failed");
+  if (cudaMalloc(&p->oz_far[dir], nb * OZ_FAR_WORDS * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&p->oz_fare[dir], nb * 2 * OZ_ROWS * sizeof(int)) != cudaSuccess) {
+    set_err("cudaMalloc of the mixed-form far-field fragments failed");
     return false;
   }
-  k_oz_slice_far<<<blocks_for((long long)(nb * M), 128), 128, 0, p->stream>>>(
-      p->A[dir], (long long)nb, p->oz_A[dir], p->oz_Ae[dir]);
+  k_oz_pack_far<<<blocks_for((long long)(nb * 2 * OZ_ROWS), 128), 128, 0, p->stream>>>(
+      p->A[dir], (long long)nb, p->oz_far[dir], p->oz_fare[dir]);
   return cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(p->stream) == cudaSuccess;
 }
 
@@ -1791,20 +2023,17 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
         return fail();
       }
       p->mixed = true;
-      const int kld = (int)((s + 1) & ~(size_t)1);
-      p->oz_kld = kld;
-      // dense constant factors on the host: T_parity^T (18 x kld), T_parity (s x 18),
-      // [B | B'] (18 x 36) and [B^T; B^T'] (36 x 18)
-      std::vector<double> Tt(2 * M * kld, 0.0), Tn(2 * s * M), Bu(M * 2 * M, 0.0),
-          Bd(2 * M * M, 0.0);
-      for (int sg = 0; sg < 2; sg++)
-        for (size_t i = 0; i < s; i++)
-          for (int m = 0; m < M; m++) {
-            const double v = T[(sg * s + i) * M + m];
-            Tt[(sg * M + m) * kld + i] = v;
-            Tn[(sg * s + i) * M + m] = v;
-          }
+      const int KC = (int)((s + 7) / 8), npass = (int)((s + 15) / 16);
+      p->oz_kc = KC;
+      p->oz_npass = npass;
+      // constant factors, sliced on the host into fragment words
+      struct RowOf {  // P[n][k] = base[n * rs + k * cs]
+        const double *base;
+        long long rs, cs;
+        __host__ __device__ double operator()(int k) const { return base[k * cs]; }
+      };
       const double lower[NTRI] = L2C_BINOM_LOWER_INIT, upper[NTRI] = L2C_BINOM_UPPER_INIT;
+      std::vector<double> Bu(M * 2 * M, 0.0), Bd(2 * M * M, 0.0);
       for (int m = 0; m < M; m++)
         for (int i = 0; i <= m; i++) {
           const double b = lower[m * (m + 1) / 2 + i];
@@ -1816,41 +2045,58 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
           Bd[i * M + j] = upper[k];
           Bd[(M + i) * M + j] = ((j - i) & 1) ? -upper[k] : upper[k];
         }
-      double *dtmp = nullptr;
-      const size_t ntmp = Tt.size() + Tn.size() + Bu.size() + Bd.size();
-      PCK(cudaMalloc(&dtmp, ntmp * sizeof(double)));
-      double *dTt = dtmp, *dTn = dTt + Tt.size(), *dBu = dTn + Tn.size(), *dBd = dBu + Bu.size();
-      cudaError_t e2 = cudaMemcpy(dTt, Tt.data(), Tt.size() * 8, cudaMemcpyHostToDevice);
-      if (e2 == cudaSuccess) e2 = cudaMemcpy(dTn, Tn.data(), Tn.size() * 8, cudaMemcpyHostToDevice);
-      if (e2 == cudaSuccess) e2 = cudaMemcpy(dBu, Bu.data(), Bu.size() * 8, cudaMemcpyHostToDevice);
-      if (e2 == cudaSuccess) e2 = cudaMemcpy(dBd, Bd.data(), Bd.size() * 8, cudaMemcpyHostToDevice);
-      const size_t S8 = l2c_oz::SLICES;
-      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Tt, S8 * Tt.size() * sizeof(__nv_bfloat16));
-      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Tn, S8 * Tn.size() * sizeof(__nv_bfloat16));
-      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Bu, S8 * Bu.size() * sizeof(__nv_bfloat16));
-      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Bd, S8 * Bd.size() * sizeof(__nv_bfloat16));
-      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Tte, 2 * M * sizeof(int));
-      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Tne, 2 * s * sizeof(int));
-      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Bue, M * sizeof(int));
-      if (e2 == cudaSuccess) e2 = cudaMalloc(&p->oz_Bde, 2 * M * sizeof(int));
-      if (e2 == cudaSuccess) {
-        for (int sg = 0; sg < 2; sg++) {
-          k_oz_slice_rows<<<1, 64, 0, st>>>(dTt + sg * M * kld, M, (int)s, kld,
-                                            p->oz_Tt + sg * S8 * M * kld, kld, (long long)M * kld,
-                                            p->oz_Tte + sg * M);
-          k_oz_slice_rows<<<(unsigned)((s + 63) / 64), 64, 0, st>>>(
-              dTn + sg * s * M, (int)s, M, M, p->oz_Tn + sg * S8 * s * M, M, (long long)s * M,
-              p->oz_Tne + sg * s);
-        }
-        k_oz_slice_rows<<<1, 64, 0, st>>>(dBu, M, 2 * M, 2 * M, p->oz_Bu, 2 * M,
-                                          (long long)M * 2 * M, p->oz_Bue);
-        k_oz_slice_rows<<<1, 64, 0, st>>>(dBd, 2 * M, M, M, p->oz_Bd, M, (long long)2 * M * M,
-                                          p->oz_Bde);
-        e2 = cudaGetLastError();
+      const int wlu = oz_words(OZ_NT, KC), wtu = oz_words(OZ_NT, 5), wtd = oz_words(OZ_NT, 3);
+      std::vector<unsigned> lu(2 * wlu), tu(wtu), td(2 * wtd), ld(2 * npass * OZ_LD_WORDS);
+      std::vector<int> lue(2 * OZ_ROWS), tue(OZ_ROWS), tde(2 * OZ_ROWS), lde(2 * npass * 16);
+      for (int sg = 0; sg < 2; sg++) {
+        const double *Ts = T.data() + sg * s * M;  // T_sg(i, m) = Ts[i * M + m]
+        for (int n = 0; n < OZ_ROWS; n++)          // leaf up: P[m][i] = T_sg(i, m)
+          oz_pack_row(RowOf{Ts + (n < M ? n : 0), 0, M}, n < M, n, (int)s, OZ_NT, KC,
+                      lu.data() + sg * wlu, lue.data() + sg * OZ_ROWS);
+        for (int ps = 0; ps < npass; ps++)         // leaf down: P[i][m] = T_sg(i, m)
+          for (int n = 0; n < 16; n++) {
+            const size_t i = 16 * (size_t)ps + n;
+            oz_pack_row(RowOf{Ts + (i < s ? i : 0) * M, 0, 1}, i < s, n, M, 2, 3,
+                        ld.data() + (sg * npass + ps) * OZ_LD_WORDS,
+                        lde.data() + (sg * npass + ps) * 16);
+          }
       }
-      if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(st);
-      cudaFree(dtmp);
-      PCK(e2);
+      for (int n = 0; n < OZ_ROWS; n++) {
+        oz_pack_row(RowOf{Bu.data() + (n < M ? n : 0) * 2 * M, 0, 1}, n < M, n, 2 * M, OZ_NT, 5,
+                    tu.data(), tue.data());
+        for (int ch = 0; ch < 2; ch++)
+          oz_pack_row(RowOf{Bd.data() + (ch * M + (n < M ? n : 0)) * M, 0, 1}, n < M, n, M, OZ_NT,
+                      3, td.data() + ch * wtd, tde.data() + ch * OZ_ROWS);
+      }
+      auto upload = [&](auto **dst, const auto &v) -> cudaError_t {
+        const size_t bytes = v.size() * sizeof(v[0]);
+        cudaError_t e = cudaMalloc(dst, bytes);
+        if (e == cudaSuccess) e = cudaMemcpy(*dst, v.data(), bytes, cudaMemcpyHostToDevice);
+        return e;
+      };
+      PCK(upload(&p->oz_lu, lu));
+      PCK(upload(&p->oz_lue, lue));
+      PCK(upload(&p->oz_tu, tu));
+      PCK(upload(&p->oz_tue, tue));
+      PCK(upload(&p->oz_td, td));
+      PCK(upload(&p->oz_tde, tde));
+      PCK(upload(&p->oz_ld, ld));
+      PCK(upload(&p->oz_lde, lde));
+      // kernels whose shared memory can pass the 48 KB default
+      PCK(cudaFuncSetAttribute(k_mz_leaf_down, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)mz_leaf_down_smem(4 * 16, 4)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_up, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)OZ_TREE_UP_SMEM));
+      PCK(cudaFuncSetAttribute(k_mz_tree_down, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)OZ_TREE_DOWN_SMEM));
+      PCK(cudaFuncSetAttribute(k_mz_far, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)OZ_FAR_SMEM));
+#define L2C_MZ_ATTR(kc)                                                                      \
+  PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                           (int)mz_leaf_up_smem(kc)));
+      L2C_MZ_ATTR(1) L2C_MZ_ATTR(2) L2C_MZ_ATTR(3) L2C_MZ_ATTR(4)
+      L2C_MZ_ATTR(5) L2C_MZ_ATTR(6) L2C_MZ_ATTR(7) L2C_MZ_ATTR(8)
+#undef L2C_MZ_ATTR
     }
     if (flags & L2C_PLAN_PRECOMPUTE_NEAR) {
       const size_t nw = near_table_size(N, s);
@@ -1886,8 +2132,9 @@ void l2c_gpu_plan_destroy(l2c_gpu_plan *p) {
                     p->st_in, p->st_out, p->Wnear[0], p->Wnear[1]};
   for (double *b : bufs)
     if (b) cudaFree(b);
-  void *obufs[] = {p->oz_Tt, p->oz_Tn, p->oz_Bu, p->oz_Bd, p->oz_Tte, p->oz_Tne, p->oz_Bue,
-                   p->oz_Bde, p->oz_A[0], p->oz_A[1], p->oz_Ae[0], p->oz_Ae[1]};
+  void *obufs[] = {p->oz_lu,  p->oz_tu,     p->oz_td,     p->oz_ld,      p->oz_lue,
+                   p->oz_tue, p->oz_tde,    p->oz_lde,    p->oz_far[0],  p->oz_far[1],
+                   p->oz_fare[0], p->oz_fare[1]};
   for (void *b : obufs)
     if (b) cudaFree(b);
   if (p->stream) cudaStreamDestroy(p->stream);

@@ -1,34 +1,45 @@
-// l2c_ozaki.cuh -- FP64-accurate small matrix products on BF16 tensor cores.
+// l2c_ozaki.cuh -- FP64-accurate small matrix products on FP16 tensor cores.
 //
 // Error-free splitting (Ozaki, Ogita, Oishi & Rump, "Error-free transformations
 // of matrix multiplication by using fast routines of matrix multiplication and
-// its applications", Numer. Algorithms 59 (2012)), arranged so that no FP64
-// instruction is spent on the product:
+// its applications", Numer. Algorithms 59 (2012)), arranged so that the product
+// itself spends no FP64 instruction:
 //
-//  * every row of the constant left factor P and every column of the data
-//    factor Q shares a power-of-two scale 2^E with |x| < 2^E for all its entries;
-//  * |x| 2^(56-E) is truncated to a 56-bit integer and cut into eight 7-bit
-//    slices, x = sign * 2^E * sum_p s_p 2^(-7p), s_p in [0, 127] -- each slice is
-//    an exact BF16 value;
-//  * slice products with p + q <= OZ_DMAX are summed per diagonal d = p + q on
-//    the tensor cores (mma.sync m16n8k16, BF16 in, FP32 accumulate); all
-//    partial sums are integers below 2^24, so the accumulation is exact;
-//  * the diagonal sums are combined exactly in 64-bit integer arithmetic,
-//    T = sum_{d<=8} D_d 2^(7(8-d)) + floor(D_9 / 2^7), and T 2^(E_P + E_Q - 56) is
-//    rounded once to a double by bit construction.
-// Truncation of the operands and of the dropped diagonals bounds the error by
-// about K 2^-53 |P|_row |Q|_col, the same order as FP64 summation.
+//  * every row of the constant factor P and every column of the data factor Q
+//    shares a power-of-two scale 2^E with |x| < 2^E for all its entries;
+//  * X = trunc(x 2^(53-E)) (|X| < 2^53) is written with six base-2^9 digits,
+//    X = sum_p d_p 2^(9(6-p)): the five low digits are balanced, d_p in
+//    [-256, 255] (the 9-bit fields of Y = X + R, R = 256 sum_{k<5} 2^(9k), less
+//    256), the top digit is d_1 = floor(Y / 2^45) in [-256, 256].  Every digit
+//    is an exact FP16 value;
+//  * digit products with p + q <= DMAX = 7 are summed per diagonal d = p + q on
+//    the tensor cores (mma.sync m16n8k16 / m16n8k8, FP16 in, FP32 accumulate).
+//    A diagonal holds at most 6 digit pairs of magnitude <= 2^16, so for
+//    K <= 40 terms every partial sum is an integer below 2^24 and the FP32
+//    accumulation is exact;
+//  * the diagonal sums are combined exactly in 64-bit integers,
+//    T = sum_{d<=6} D_d 2^(9(6-d)) + floor(D_7 / 2^9), and the product is
+//    T 2^(E_P + E_Q - 52), rounded once to a double by bit construction.
+// The dropped diagonals (d >= 8) and the floor bound the error by a few units
+// of 2^-53 |P|_row |Q|_col per product, the order of FP64 summation.
+//
+// Warp tile: 16 data columns (the mma "rows", A operand, sliced in registers)
+// times NT x 8 outputs (the mma "columns", B operand: P transposed, pre-sliced
+// at plan time into per-lane fragments held in shared memory).
 #ifndef L2C_OZAKI_CUH
 #define L2C_OZAKI_CUH
 
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 namespace l2c_oz {
 
-constexpr int SLICES = 8;  // 7-bit slices
-constexpr int FRAC = 56;   // fixed-point fraction bits = 7 * SLICES
-constexpr int DMAX = 9;    // slice pairs p + q <= DMAX
+constexpr int SLICES = 6;  // base-2^9 digits
+constexpr int FRAC = 53;   // fixed-point fraction bits
+constexpr int DMAX = 7;    // digit pairs p + q <= DMAX
+constexpr int NDIAG = DMAX - 1;
+constexpr int KMAX = 40;   // terms per exact accumulation
 constexpr int EXP_ZERO = -4000;
+constexpr long long RBAL = 0x100804020100ll;  // 256 in each of the five low digits
 
 // Smallest E with |x| < 2^E (EXP_ZERO for zero and subnormals).
 __host__ __device__ inline int exp_bound(double x) {
@@ -38,35 +49,96 @@ __host__ __device__ inline int exp_bound(double x) {
   return ex == 0 ? EXP_ZERO : ex - 1022;
 }
 
-// Sign in bit 63, |x| 2^(56-E) truncated toward zero in bits 0..55 (|x| < 2^E).
-__host__ __device__ inline unsigned long long fix56(double x, int E) {
+// Y = trunc(x 2^(FRAC-E)) + RBAL (|x| < 2^E; RBAL for zero).
+__host__ __device__ inline long long fixbal(double x, int E) {
   unsigned long long b;
   memcpy(&b, &x, sizeof(b));
   const int ex = (int)((b >> 52) & 0x7FF);
-  if (ex == 0 || E == EXP_ZERO) return 0;
+  if (ex == 0 || E == EXP_ZERO) return RBAL;
   const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-  const int sh = 1075 + E - ex - FRAC;
-  unsigned long long q;
-  if (sh >= 64)
-    q = 0;
-  else if (sh <= 0)
-    q = m << (-sh);
-  else
-    q = m >> sh;
-  return q | (b & (1ull << 63));
+  const int sh = 1075 + E - ex - FRAC;  // >= 0 when |x| < 2^E
+  const long long q = sh >= 64 ? 0 : (long long)(m >> sh);
+  return (b >> 63) ? RBAL - q : RBAL + q;
 }
 
-// Signed slice p (1 = most significant) of a fix56 value.
-__host__ __device__ inline float slice(unsigned long long f, int p) {
-  const int v = (int)((f >> (FRAC - 7 * p)) & 127);
-  return (f >> 63) ? -(float)v : (float)v;
+// Digit p (1 = most significant) of Y as an exact float.
+__host__ __device__ inline float digit_f(long long Y, int p) {
+  if (p == 1) return (float)(Y >> 45);
+  return (float)(int)((Y >> (9 * (SLICES - p))) & 511) - 256.0f;
 }
 
+// FP16 bits of an integer of magnitude <= 2048 (exact).
+__host__ __device__ inline unsigned half_bits(int v) {
+  if (v == 0) return 0u;
+  const unsigned s = v < 0 ? 0x8000u : 0u;
+  unsigned a = (unsigned)(v < 0 ? -v : v);
+  int e = 0;
+  while ((a >> (e + 1)) != 0) e++;  // a in [2^e, 2^(e+1))
+  return s | ((unsigned)(e + 15) << 10) | ((a << (10 - e)) & 0x3FFu);
+}
+
+#ifdef __CUDACC__
+// Y split into two 27-bit words: hi holds digits 1..3 (signed), lo digits 4..6.
+struct Ysplit {
+  int hi;
+  unsigned lo;
+};
+__device__ __forceinline__ Ysplit ysplit(long long Y) {
+  return {(int)(Y >> 27), (unsigned)Y & 0x7FFFFFFu};
+}
+// Digit p of a split word as a float, by exponent-field arithmetic (exact).
+template <int P>
+__device__ __forceinline__ float dig(const Ysplit &y) {
+  if (P == 1) return __fsub_rn(__int_as_float(0x4B400000 + (y.hi >> 18)), 12582912.0f);
+  constexpr int sh = P <= 3 ? 9 * (3 - P) : 9 * (6 - P);
+  const unsigned w = P <= 3 ? (unsigned)y.hi : y.lo;
+  return __fsub_rn(__uint_as_float(((w >> sh) & 511u) | 0x4B000000u), 8388864.0f);
+}
 __device__ __forceinline__ unsigned pack2(float lo, float hi) {
-  __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+  __half2 h = __floats2half2_rn(lo, hi);
   return *reinterpret_cast<unsigned *>(&h);
 }
 
+__device__ __forceinline__ void mma16(float (&c)[4], const unsigned (&a)[4], unsigned b0,
+                                      unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ void mma8(float (&c)[4], unsigned a0, unsigned a1, unsigned b0) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(b0));
+}
+
+// Asynchronous global -> shared copies (bytes = 0 fills zeros).
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int bytes) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(bytes));
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem, int bytes) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(bytes));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+#endif
+
+// Fragment word of P^T for slice q (1-based), n-tile nt, k8-chunk c and lane
+// (g = lane >> 2, t = lane & 3): P[8 nt + g][8 c + 2t .. 2t+1] as an FP16 pair.
+// Chunks are interleaved in pairs (one 64-bit load per k16 step); an odd last
+// chunk stands alone.  One matrix holds SLICES * NT * KC * 32 words.
+__host__ __device__ inline int frag_index(int q, int nt, int c, int lane, int NT, int KC) {
+  const int base = ((q - 1) * NT + nt) * KC * 32;
+  if ((KC & 1) && c == KC - 1) return base + c * 32 + lane;
+  return base + (c & ~1) * 32 + 2 * lane + (c & 1);
+}
+
+#ifdef __CUDACC__
 // T 2^e rounded to nearest-even as a double (T a signed 64-bit integer).
 __device__ __forceinline__ double to_double(long long T, int e) {
   if (T == 0) return 0.0;
@@ -88,93 +160,122 @@ __device__ __forceinline__ double to_double(long long T, int e) {
   return __longlong_as_double((long long)bits);
 }
 
-__device__ __forceinline__ void mma_bf16(float c[4], unsigned a0, unsigned a1, unsigned a2,
-                                         unsigned a3, unsigned b0, unsigned b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+// x truncated to a multiple of 2^e as an integer, when |x| < 2^(e+60); returns
+// false (and leaves X alone) otherwise.
+__device__ __forceinline__ bool to_fixed(double x, int e, long long &X) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (ex == 0) {
+    X = 0;
+    return true;
+  }
+  if (ex - 1022 > e + 60) return false;
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int sh = e + 1075 - ex;  // x = m 2^(ex-1075) = (m >> sh) 2^e
+  unsigned long long q;
+  if (sh >= 64)
+    q = 0;
+  else if (sh <= 0)
+    q = m << (-sh);
+  else
+    q = m >> sh;
+  X = (b >> 63) ? -(long long)q : (long long)q;
+  return true;
 }
 
-// One warp: C = P Q for rows < MT*16 (rows >= mr are zero) and the warp's 8
-// columns, FP64-accurate.
-//   Ps  slices of P, element (p, r, k) at Ps[(p-1) * sstride + r * kld + k], k < kld
-//       (entries with k >= K are never read: they are treated as zero)
-//   Pe  per-row scale exponents of P
-//   Qf  the 8 columns in fix56 form, Qf[c * qld + k], k < KT*16 (zero padded)
-//   Qe  per-column scale exponents
-// out[mt][e]: row mt*16 + (lane >> 2) + 8 (e >> 1), column 2 (lane & 3) + (e & 1).
-template <int MT, int KT>
-__device__ __forceinline__ void warp_tile(const __nv_bfloat16 *__restrict__ Ps, int sstride,
-                                          int kld, int mr, int K, const int *__restrict__ Pe,
-                                          const unsigned long long *Qf, int qld, const int *Qe,
-                                          double out[MT][4]) {
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  // B fragments of every slice: b0 = (k = 2t, 2t+1; col g), b1 = (k + 8)
-  unsigned bf[SLICES][KT][2];
+// Combined integer T of output (nt, e) from the NDIAG diagonal accumulators
+// (each an exact integer below 2^24).
+template <int NT>
+__device__ __forceinline__ long long combine(const float (&acc)[NDIAG][NT][4], int nt, int e) {
+  long long T = 0;
 #pragma unroll
-  for (int ks = 0; ks < KT; ks++) {
-    const unsigned long long *c = Qf + g * qld + ks * 16 + 2 * t;
-    const unsigned long long f0 = c[0], f1 = c[1], f8 = c[8], f9 = c[9];
-#pragma unroll
-    for (int q = 0; q < SLICES; q++) {
-      bf[q][ks][0] = pack2(slice(f0, q + 1), slice(f1, q + 1));
-      bf[q][ks][1] = pack2(slice(f8, q + 1), slice(f9, q + 1));
-    }
-  }
-  long long T[MT][4];
-#pragma unroll
-  for (int mt = 0; mt < MT; mt++)
-#pragma unroll
-    for (int e = 0; e < 4; e++) T[mt][e] = 0;
-#pragma unroll
-  for (int d = 2; d <= DMAX; d++) {
-    float acc[MT][4];
-#pragma unroll
-    for (int mt = 0; mt < MT; mt++)
-#pragma unroll
-      for (int e = 0; e < 4; e++) acc[mt][e] = 0.f;
-#pragma unroll
-    for (int p = 1; p <= SLICES; p++) {
-      const int q = d - p;
-      if (q < 1 || q > SLICES) continue;
-#pragma unroll
-      for (int ks = 0; ks < KT; ks++) {
-        const int k0 = ks * 16 + 2 * t;
-#pragma unroll
-        for (int mt = 0; mt < MT; mt++) {
-          const int r0 = mt * 16 + g, r1 = r0 + 8;
-          const __nv_bfloat16 *base = Ps + (p - 1) * sstride;
-          unsigned a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-          if (r0 < mr) {
-            if (k0 < K) a0 = *reinterpret_cast<const unsigned *>(base + r0 * kld + k0);
-            if (k0 + 8 < K) a2 = *reinterpret_cast<const unsigned *>(base + r0 * kld + k0 + 8);
-          }
-          if (r1 < mr) {
-            if (k0 < K) a1 = *reinterpret_cast<const unsigned *>(base + r1 * kld + k0);
-            if (k0 + 8 < K) a3 = *reinterpret_cast<const unsigned *>(base + r1 * kld + k0 + 8);
-          }
-          mma_bf16(acc[mt], a0, a1, a2, a3, bf[q - 1][ks][0], bf[q - 1][ks][1]);
-        }
-      }
-    }
-#pragma unroll
-    for (int mt = 0; mt < MT; mt++)
-#pragma unroll
-      for (int e = 0; e < 4; e++) {
-        const long long v = (long long)__float2ll_rz(acc[mt][e]);
-        T[mt][e] = d < DMAX ? (T[mt][e] << 7) + v : T[mt][e] + (v >> 7);
-      }
-  }
-#pragma unroll
-  for (int mt = 0; mt < MT; mt++)
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-      const int r = mt * 16 + g + 8 * (e >> 1), c = 2 * t + (e & 1);
-      out[mt][e] = r < mr ? to_double(T[mt][e], Pe[r] + Qe[c] - FRAC) : 0.0;
-    }
+  for (int d = 0; d < NDIAG - 1; d++) T = T * 512 + __float2int_rn(acc[d][nt][e]);
+  return T + (__float2int_rn(acc[NDIAG - 1][nt][e]) >> 9);
 }
+
+// The warp's 16 x (NT*8) tile over k8-chunks [C0, C1): acc[d-2][nt][.] = sum
+// over k of the diagonal-d digit products, for the data columns (rows of the
+// tile) in Ys.  C1 - C0 <= 5 (K <= 40) keeps the accumulation exact.
+//   Ys : offset words Y of the 16 columns, column r at Ys[r * yld + k * ks],
+//        k < 8 C1 (entries past the true K are RBAL, i.e. zero);
+//   Pf : the fragment words of P^T (frag_index layout with KC chunks).
+// Output element (nt, e) of the lane is data column (lane >> 2) + 8 (e >> 1)
+// and output row 8 nt + 2 (lane & 3) + (e & 1).
+template <int NT, int KC, int C0 = 0, int C1 = KC>
+__device__ __forceinline__ void mma_tile(const unsigned *__restrict__ Pf, const long long *Ys,
+                                         int yld, int ks, float (&acc)[NDIAG][NT][4]) {
+  static_assert(C1 - C0 <= KMAX / 8, "accumulation would not be exact");
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int d = 0; d < NDIAG; d++)
+#pragma unroll
+    for (int nt = 0; nt < NT; nt++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) acc[d][nt][e] = 0.f;
+  const long long *r0 = Ys + g * yld + 2 * t * ks, *r1 = r0 + 8 * yld;
+#pragma unroll
+  for (int c = C0; c < C1; c += 2) {
+    if (c + 1 < C1) {
+      const Ysplit y0 = ysplit(r0[(8 * c) * ks]), y1 = ysplit(r0[(8 * c + 1) * ks]);
+      const Ysplit y2 = ysplit(r1[(8 * c) * ks]), y3 = ysplit(r1[(8 * c + 1) * ks]);
+      const Ysplit y4 = ysplit(r0[(8 * c + 8) * ks]), y5 = ysplit(r0[(8 * c + 9) * ks]);
+      const Ysplit y6 = ysplit(r1[(8 * c + 8) * ks]), y7 = ysplit(r1[(8 * c + 9) * ks]);
+      unsigned a[SLICES][4];
+#define L2C_OZ_SLICE(P)                                      \
+  a[P - 1][0] = pack2(dig<P>(y0), dig<P>(y1));               \
+  a[P - 1][1] = pack2(dig<P>(y2), dig<P>(y3));               \
+  a[P - 1][2] = pack2(dig<P>(y4), dig<P>(y5));               \
+  a[P - 1][3] = pack2(dig<P>(y6), dig<P>(y7));
+      L2C_OZ_SLICE(1) L2C_OZ_SLICE(2) L2C_OZ_SLICE(3)
+      L2C_OZ_SLICE(4) L2C_OZ_SLICE(5) L2C_OZ_SLICE(6)
+#undef L2C_OZ_SLICE
+#pragma unroll
+      for (int q = 1; q <= SLICES; q++)
+#pragma unroll
+        for (int nt = 0; nt < NT; nt++) {
+          const uint2 b =
+              *reinterpret_cast<const uint2 *>(Pf + frag_index(q, nt, c, lane, NT, KC));
+#pragma unroll
+          for (int p = 1; p + q <= DMAX; p++) mma16(acc[p + q - 2][nt], a[p - 1], b.x, b.y);
+        }
+    } else {
+      const Ysplit y0 = ysplit(r0[(8 * c) * ks]), y1 = ysplit(r0[(8 * c + 1) * ks]);
+      const Ysplit y2 = ysplit(r1[(8 * c) * ks]), y3 = ysplit(r1[(8 * c + 1) * ks]);
+      unsigned a[SLICES][2];
+#define L2C_OZ_SLICE(P)                          \
+  a[P - 1][0] = pack2(dig<P>(y0), dig<P>(y1));   \
+  a[P - 1][1] = pack2(dig<P>(y2), dig<P>(y3));
+      L2C_OZ_SLICE(1) L2C_OZ_SLICE(2) L2C_OZ_SLICE(3)
+      L2C_OZ_SLICE(4) L2C_OZ_SLICE(5) L2C_OZ_SLICE(6)
+#undef L2C_OZ_SLICE
+#pragma unroll
+      for (int q = 1; q <= SLICES; q++)
+#pragma unroll
+        for (int nt = 0; nt < NT; nt++) {
+          const unsigned b = Pf[frag_index(q, nt, c, lane, NT, KC)];
+#pragma unroll
+          for (int p = 1; p + q <= DMAX; p++) mma8(acc[p + q - 2][nt], a[p - 1][0], a[p - 1][1], b);
+        }
+    }
+  }
+}
+
+// Column exponents and offset words of a staged tile, in place: Xs holds the
+// raw doubles of 16 columns (column r at Xs[r * ld + k * ks], k < K); on
+// return the same places hold the offset words Y, entries K <= k < KP hold
+// RBAL, and Es[r] the column exponent.  Two lanes per column.
+__device__ __forceinline__ void stage_fix(double *Xs, int ld, int ks, int K, int KP, int *Es) {
+  const int lane = threadIdx.x & 31, r = lane >> 1, h = lane & 1;
+  double *row = Xs + r * ld;
+  int e = EXP_ZERO;
+  for (int k = h; k < K; k += 2) e = max(e, exp_bound(row[k * ks]));
+  e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
+  long long *yr = reinterpret_cast<long long *>(row);
+  for (int k = h; k < KP; k += 2) yr[k * ks] = k < K ? fixbal(row[k * ks], e) : RBAL;
+  if (h == 0) Es[r] = e;
+  __syncwarp();
+}
+#endif
 
 }  // namespace l2c_oz
 
