@@ -339,10 +339,11 @@ template <int VB>
 __global__ void __launch_bounds__(256, VB == 1 ? 5 : VB == 2 ? 4 : 2)
     k_near(const double *__restrict__ x, const double *out, double *__restrict__ y,
            const double *__restrict__ a, const double *__restrict__ an,
-           const double *__restrict__ dn, const double *__restrict__ W, Geo g, int c2l) {
-  const long long ntile = (g.N + blockDim.x - 1) / blockDim.x;
+           const double *__restrict__ dn, const double *__restrict__ W, Geo g, int c2l,
+           long long jbeg) {
+  const long long ntile = (g.N - jbeg + blockDim.x - 1) / blockDim.x;
   const long long tile = blockIdx.x % ntile, vg = blockIdx.x / ntile;
-  const long long j = tile * blockDim.x + threadIdx.x;
+  const long long j = jbeg + tile * blockDim.x + threadIdx.x;
   if (j >= g.N) return;
   const long long v0 = vg * VB;
   double res[VB];
@@ -350,6 +351,72 @@ __global__ void __launch_bounds__(256, VB == 1 ? 5 : VB == 2 ? 4 : 2)
 #pragma unroll
   for (int u = 0; u < VB; u++)
     y[(v0 + u) * g.N + j] = out[(v0 + u) * g.dist + j * g.stride] + res[u];
+}
+
+// Band of the blocks b < nL-1 in pairs: one thread forms outputs i and h-1-i
+// of block b for VB vectors.  Their term counts add up to 3h/2 + 1 for every
+// i, so all lanes of a warp run the same number of FP64 instructions (one
+// output per thread leaves up to half the lanes idle at the end of the loop).
+// Terms are accumulated in order k = 0, 1, ... into one FMA chain per output
+// (the FP64 pipe, not its latency, bounds this loop).  Threads past the pairs
+// of a vector group take the outputs of the last (ragged) block one each, in
+// the same launch, so that block runs beside the others.
+template <int VB>
+__global__ void __launch_bounds__(256, VB <= 2 ? 3 : 2)
+    k_near_pair(const double *__restrict__ x, const double *out, double *__restrict__ y,
+                const double *__restrict__ a, const double *__restrict__ an,
+                const double *__restrict__ dn, const double *__restrict__ W, Geo g, int c2l) {
+  const long long half = g.h >> 1, npair = (g.nL - 1) * half, jlast = (g.nL - 1) * g.h;
+  const long long per_vg = npair + (g.N - jlast);
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long vg = idx / per_vg;
+  if (vg * VB >= g.count) return;
+  const long long r = idx - vg * per_vg;
+  if (r >= npair) {
+    const long long j = jlast + (r - npair), v0 = vg * VB;
+    double res[VB];
+    near_sums<VB>(x + v0 * g.N + j, g.N, a, an, dn, W, g, c2l, j, res);
+#pragma unroll
+    for (int u = 0; u < VB; u++)
+      y[(v0 + u) * g.N + j] = out[(v0 + u) * g.dist + j * g.stride] + res[u];
+    return;
+  }
+  const long long b = r / half, i = r - b * half;
+  const long long jA = b * g.h + i, jB = b * g.h + g.h - 1 - i, lim = (b + 2) * g.h;
+  const long long nkA = (lim - jA + 1) >> 1, total = nkA + ((lim - jB + 1) >> 1);
+  const double *xv = x + vg * VB * g.N;
+  const double *Wb = W ? W + b * (3 * g.s * g.s + g.s) : nullptr;
+  double acc[VB], resA[VB];
+#pragma unroll
+  for (int u = 0; u < VB; u++) acc[u] = resA[u] = 0.0;
+  for (long long t = 0; t < total; t++) {
+    const bool second = t >= nkA;
+    const long long j = second ? jB : jA, k = second ? t - nkA : t;
+    double wt;
+    if (Wb) {
+      // offset of term k in the block's table: k h for k < s, then rows of 2h - 2k'
+      const long long off =
+          k < g.s ? k * g.h : 4 * g.s * k - k * k + k - g.s * g.s - g.s;
+      wt = Wb[off + (j - b * g.h)];
+    } else {
+      wt = near_weight(c2l, k, j, a, an, dn);
+    }
+#pragma unroll
+    for (int u = 0; u < VB; u++) acc[u] = fma(wt, xv[u * g.N + j + 2 * k], acc[u]);
+    if (t == nkA - 1) {
+#pragma unroll
+      for (int u = 0; u < VB; u++) {
+        resA[u] = acc[u];
+        acc[u] = 0.0;
+      }
+    }
+  }
+  const long long v0 = vg * VB;
+#pragma unroll
+  for (int u = 0; u < VB; u++) {
+    y[(v0 + u) * g.N + jA] = out[(v0 + u) * g.dist + jA * g.stride] + resA[u];
+    y[(v0 + u) * g.N + jB] = out[(v0 + u) * g.dist + jB * g.stride] + acc[u];
+  }
 }
 
 // Plan time: the band weights of every output, in the layout k_near reads.
@@ -1091,8 +1158,9 @@ constexpr size_t OZ_TREE_UP_SMEM = (size_t)(OZ_TREE_UP_WORDS + OZ_ROWS + 16 * MX
 // fixed-point frame of the product when the magnitudes allow it.
 __device__ __forceinline__ double oz_add(double existing, long long T, int e) {
   long long X;
-  if (l2c_oz::to_fixed(existing, e, X)) return l2c_oz::to_double(T + X, e);
-  return existing + l2c_oz::to_double(T, e);
+  const bool fits = l2c_oz::to_fixed(existing, e, X);
+  const double r = l2c_oz::to_double(fits ? T + X : T, e);
+  return fits ? r : existing + r;
 }
 
 constexpr int OZ_TREE_DOWN_WORDS = 2 * oz_words(OZ_NT, 3);
@@ -1395,6 +1463,7 @@ struct l2c_gpu_plan {
   size_t use_clock = 0;
   bool use_graphs = true;
   bool overlap = false;  // near field on stream2 beside the far-field chain
+  int near_pair = -1;    // band in pairs: 1 always, 0 never, -1 by leaf size
   // launch accounting and optional per-phase CUDA-event timing
   size_t launches = 0;
   bool profiling = false;
@@ -1626,8 +1695,7 @@ cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t 
 // thread, then the remainder.
 cudaError_t launch_near(const double *x, const double *out, double *y, const double *a,
                         const double *an, const double *dn, const double *W, Geo g, int c2l,
-                        cudaStream_t st) {
-  const long long ntile = (g.N + 255) / 256;
+                        cudaStream_t st, bool pair) {
   long long v = 0;
   while (v < g.count) {
     const long long left = g.count - v;
@@ -1638,12 +1706,27 @@ cudaError_t launch_near(const double *x, const double *out, double *y, const dou
     const double *xs = x + v * g.N;
     const double *os = out + v * g.dist;
     double *ys = y + v * g.N;
-    const unsigned grid = (unsigned)(ntile * groups);
+    if (!pair) {
+      const unsigned grid = (unsigned)(((g.N + 255) / 256) * groups);
+      switch (vb) {
+        case 8: k_near<8><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l, 0); break;
+        case 4: k_near<4><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l, 0); break;
+        case 2: k_near<2><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l, 0); break;
+        default: k_near<1><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l, 0); break;
+      }
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+      v += groups * vb;
+      continue;
+    }
+    // blocks b < nL-1 in pairs and the last (ragged) block one output per thread
+    const long long per_vg = (g.nL - 1) * (g.h / 2) + (g.N - (g.nL - 1) * g.h);
+    const unsigned grid = (unsigned)((groups * per_vg + 255) / 256);
     switch (vb) {
-      case 8: k_near<8><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
-      case 4: k_near<4><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
-      case 2: k_near<2><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
-      default: k_near<1><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
+      case 8: k_near_pair<8><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
+      case 4: k_near_pair<4><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
+      case 2: k_near_pair<2><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
+      default: k_near_pair<1><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
     }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -1651,6 +1734,10 @@ cudaError_t launch_near(const double *x, const double *out, double *y, const dou
   }
   return cudaSuccess;
 }
+
+// Pairs pay off when a warp's outputs have very unequal term counts (small
+// leaves: one warp spans a whole block).
+bool near_pair(const l2c_gpu_plan *p) { return p->near_pair >= 0 ? p->near_pair == 1 : p->s <= 16; }
 
 size_t near_launch_count(size_t count) {
   size_t n = 0, v = 0;
@@ -1689,9 +1776,22 @@ void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStrea
   k_mz_leaf_up<KC><<<grid, 32 * MXW, mz_leaf_up_smem(KC), st>>>(x, p->w, p->oz_lu, p->oz_lue, g);
 }
 
+// Down-sweep levels above lt have too few columns to fill the GPU with
+// tensor-core tiles, whose latency then dominates: they run in FP64 in the
+// shared-memory top kernel (one CTA per vector and parity), the levels from lt
+// on tensor cores.  (Upward, the FP64 top kernel measured slower than the
+// tensor-core levels it would replace.)
+constexpr int MZ_TOP_MAX = 6;
+int mixed_top_level(long long L, long long count) {
+  int lt = 0;
+  while (lt + 1 <= L - 2 && lt < MZ_TOP_MAX && count * 2 * ((4LL << lt) - 2) < 16 * 600) lt++;
+  return lt;
+}
+
 bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir, const Geo &g,
                       cudaStream_t st) {
   const int c2l = dir == 1;
+  const int lt = mixed_top_level(g.L, g.count);
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
     switch (p->oz_kc) {
@@ -1707,7 +1807,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     if (cudaGetLastError() != cudaSuccess) return false;
   }
   {
-    PhaseScope ps(p, L2C_PHASE_TREE_UP, p->L - 1);
+    PhaseScope ps(p, L2C_PHASE_TREE_UP, (size_t)(g.L - 1));
     for (long long l = g.L - 2; l >= 0; l--) {
       const long long np = (long long)slots_at((size_t)l);
       const long long tiles = (g.count * 2 * np + 15) / 16;
@@ -1730,8 +1830,9 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     if (cudaGetLastError() != cudaSuccess) return false;
   }
   {
-    PhaseScope ps(p, L2C_PHASE_TREE_DOWN, p->L - 1);
-    for (long long l = 0; l + 1 < g.L; l++) {
+    PhaseScope ps(p, L2C_PHASE_TREE_DOWN, (size_t)(g.L - 1 - lt) + (lt > 0 ? 1 : 0));
+    if (lt > 0) k_down_top<<<(unsigned)(g.count * 2), 32 * M, top_smem(lt), st>>>(p->c, g, lt);
+    for (long long l = lt; l + 1 < g.L; l++) {
       const long long np = (long long)slots_at((size_t)l);
       const long long tiles = (g.count * 2 * np + 15) / 16;
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
@@ -1796,7 +1897,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   if (near_only) {
     {
       PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count));
-      CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, st));
+      CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, st, near_pair(p)));
     }
     Geo g0 = g;
     g0.K = 0;
@@ -1812,7 +1913,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   }
   {
     PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count), stn);
-    CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn));
+    CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, near_pair(p)));
   }
   if (p->overlap) CK(cudaEventRecord(p->ev_join, st2));
   if (p->mixed) return launch_mixed_far(p, x, out, dir, g, st) ? 1 : 0;
@@ -1957,6 +2058,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   PCK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
   if (const char *env = std::getenv("L2C_NO_GRAPHS")) p->use_graphs = env[0] == '0';
   if (const char *env = std::getenv("L2C_OVERLAP")) p->overlap = env[0] == '1';
+  if (const char *env = std::getenv("L2C_NEAR_PAIR")) p->near_pair = env[0] == '1' ? 1 : 0;
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
     p->Nn = N;
@@ -2091,6 +2193,8 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
                                (int)OZ_TREE_DOWN_SMEM));
       PCK(cudaFuncSetAttribute(k_mz_far, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)OZ_FAR_SMEM));
+      PCK(cudaFuncSetAttribute(k_down_top, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)top_smem(MZ_TOP_MAX)));
 #define L2C_MZ_ATTR(kc)                                                                      \
   PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                            (int)mz_leaf_up_smem(kc)));
@@ -2417,7 +2521,7 @@ extern "C" size_t l2c_gpu_execute_noalloc(l2c_gpu_plan *p, const double *in, dou
   const long long total = g.N;
   k_gather<<<blocks_for(total, 256), 256, 0, st>>>(in, x, g, c2l);
   k_near<1><<<blocks_for(total, 256), 256, 0, st>>>(x, out, y, p->a, p->an, p->dn,
-                                                    p->Wnear[dir], g, c2l);
+                                                    p->Wnear[dir], g, c2l, 0);
   k_leaf_up<<<blocks_for(g.K * 2 * M, 288), 288, 0, st>>>(x, p->T, w, g);
   for (long long l = (long long)p->L - 2; l >= 0; l--) {
     const long long np = (long long)slots_at((size_t)l);

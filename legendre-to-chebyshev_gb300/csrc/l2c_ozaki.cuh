@@ -49,15 +49,15 @@ __host__ __device__ inline int exp_bound(double x) {
   return ex == 0 ? EXP_ZERO : ex - 1022;
 }
 
-// Y = trunc(x 2^(FRAC-E)) + RBAL (|x| < 2^E; RBAL for zero).
+// Y = trunc(x 2^(FRAC-E)) + RBAL (|x| < 2^E; RBAL for zero).  Branch-free.
 __host__ __device__ inline long long fixbal(double x, int E) {
   unsigned long long b;
   memcpy(&b, &x, sizeof(b));
   const int ex = (int)((b >> 52) & 0x7FF);
-  if (ex == 0 || E == EXP_ZERO) return RBAL;
   const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
   const int sh = 1075 + E - ex - FRAC;  // >= 0 when |x| < 2^E
-  const long long q = sh >= 64 ? 0 : (long long)(m >> sh);
+  long long q = (long long)(m >> (sh < 63 ? sh : 63));
+  q = (sh >= 64 || ex == 0 || E == EXP_ZERO) ? 0 : q;
   return (b >> 63) ? RBAL - q : RBAL + q;
 }
 
@@ -140,47 +140,35 @@ __host__ __device__ inline int frag_index(int q, int nt, int c, int lane, int NT
 
 #ifdef __CUDACC__
 // T 2^e rounded to nearest-even as a double (T a signed 64-bit integer).
+// Branch-free, so the independent outputs of a lane interleave.
 __device__ __forceinline__ double to_double(long long T, int e) {
-  if (T == 0) return 0.0;
-  const unsigned long long neg = T < 0 ? 1ull : 0ull;
-  unsigned long long a = neg ? (unsigned long long)(-T) : (unsigned long long)T;
+  const unsigned long long neg = (unsigned long long)T >> 63;
+  const unsigned long long a = neg ? 0ull - (unsigned long long)T : (unsigned long long)T;
   const int lz = __clzll((long long)a);
-  a <<= lz;  // leading one at bit 63
-  unsigned long long mant = a >> 11;
-  const unsigned long long rest = a & 0x7FFull;
-  if (rest > 0x400ull || (rest == 0x400ull && (mant & 1ull))) mant++;
-  int ex = 63 - lz + e;
-  if (mant >> 53) {
-    mant >>= 1;
-    ex++;
-  }
-  if (ex < -1022) return 0.0;  // below the normal range: far under any output's ulp
+  const unsigned long long n = a << (lz & 63);  // leading one at bit 63
+  unsigned long long mant = n >> 11;
+  const unsigned long long rest = n & 0x7FFull;
+  mant += (rest > 0x400ull || (rest == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+  const unsigned long long carry = mant >> 53;
+  mant >>= carry;
+  const int ex = 63 - lz + e + (int)carry;
   const unsigned long long bits =
       (neg << 63) | ((unsigned long long)(ex + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull);
-  return __longlong_as_double((long long)bits);
+  // zero, and values below the normal range (far under any output's ulp), give 0
+  return __longlong_as_double((a == 0 || ex < -1022) ? 0ll : (long long)bits);
 }
 
-// x truncated to a multiple of 2^e as an integer, when |x| < 2^(e+60); returns
-// false (and leaves X alone) otherwise.
+// x truncated to a multiple of 2^e as an integer, when |x| < 2^(e+60) (the
+// return value says whether it was).  Branch-free.
 __device__ __forceinline__ bool to_fixed(double x, int e, long long &X) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const int ex = (int)((b >> 52) & 0x7FF);
-  if (ex == 0) {
-    X = 0;
-    return true;
-  }
-  if (ex - 1022 > e + 60) return false;
   const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-  const int sh = e + 1075 - ex;  // x = m 2^(ex-1075) = (m >> sh) 2^e
-  unsigned long long q;
-  if (sh >= 64)
-    q = 0;
-  else if (sh <= 0)
-    q = m << (-sh);
-  else
-    q = m >> sh;
+  const int sh = e + 1075 - ex;  // x = m 2^(ex-1075) = (m >> sh) 2^e; sh >= -7 when it fits
+  unsigned long long q = sh >= 0 ? m >> (sh < 63 ? sh : 63) : m << ((-sh) & 63);
+  q = (sh >= 64 || ex == 0) ? 0ull : q;
   X = (b >> 63) ? -(long long)q : (long long)q;
-  return true;
+  return ex == 0 || ex - 1022 <= e + 60;
 }
 
 // Combined integer T of output (nt, e) from the NDIAG diagonal accumulators
