@@ -914,10 +914,13 @@ inline unsigned blocks_for(long long n, int threads) {
 // into per-lane fragments (l2c_oz::frag_index) that the CTA copies to shared
 // memory once; each warp streams its tiles through a two-deep cp.async
 // pipeline (the next tile's copies are in flight while one is computed).
+// Between the products the moments w and c stay in the column format of
+// l2c_oz::stage_cols (integers and one exponent per 18-coefficient column).
 // ---------------------------------------------------------------------------
 constexpr int MXW = 4;              // warps per CTA
 constexpr int OZ_NT = 3;            // 18 outputs = 3 n-tiles of 8
 constexpr int OZ_ROWS = 8 * OZ_NT;  // padded output rows
+constexpr int OZ_META = 32;         // per-matrix ints: row shifts [0, 24), exponent offset [24]
 constexpr int OZ_TLD = 42;          // staged row of 36 (K = 2M) values, padded
 constexpr int OZ_CLD = 26;          // staged row of 18 (K = M) values, padded
 __host__ __device__ constexpr int oz_words(int NT, int KC) { return l2c_oz::SLICES * NT * KC * 32; }
@@ -947,33 +950,58 @@ __host__ __device__ void oz_pack_row(Row row, bool live, int n, int K, int NT, i
     }
 }
 
-// Far-field block fragments: block gb, part 0 = [A0 A1] (18 x 36), part 1 = A2
-// (18 x 18); words at F + gb * OZ_FAR_WORDS, exponents at E + gb * 2 * OZ_ROWS.
-constexpr int OZ_FAR_W0 = oz_words(OZ_NT, 5), OZ_FAR_WORDS = OZ_FAR_W0 + oz_words(OZ_NT, 3);
-__global__ void k_oz_pack_far(const double *__restrict__ A, long long nblocks, unsigned *F,
-                              int *E) {
-  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (idx >= nblocks * 2 * OZ_ROWS) return;
-  const long long gb = idx / (2 * OZ_ROWS);
-  const int rr = (int)(idx - gb * 2 * OZ_ROWS), part = rr / OZ_ROWS, n = rr - part * OZ_ROWS;
-  const double *A0 = A + 3 * gb * MM + (n < M ? n : 0) * M;
-  unsigned *Fb = F + gb * OZ_FAR_WORDS + (part ? OZ_FAR_W0 : 0);
-  int *Eb = E + gb * 2 * OZ_ROWS + part * OZ_ROWS;
-  if (part == 0)
-    oz_pack_row([&](int k) { return k < M ? A0[k] : A0[MM + k - M]; }, n < M, n, 2 * M, OZ_NT, 5,
-                Fb, Eb);
-  else
-    oz_pack_row([&](int k) { return A0[2 * MM + k]; }, n < M, n, M, OZ_NT, 3, Fb, Eb);
+// Producer metadata of a matrix with row exponents E[0, M): for a column with
+// exponent Ec (entries below 2^Ec) and K <= 64 terms, output n is below
+// K 2^(E[n] + Ec) <= 2^(Ec + Emax + 6); its integer T (value T 2^(Ec + E[n] - 52))
+// is stored as T 2^(E[n] - Emax + 3) under the column exponent Ec + Emax + 7,
+// so |V| < 2^61.  meta[n] = E[n] - Emax + 3, meta[24] = Emax + 7.
+__host__ __device__ inline void oz_meta(const int *E, int *meta) {
+  int emax = l2c_oz::EXP_ZERO;
+  for (int n = 0; n < M; n++) emax = E[n] > emax ? E[n] : emax;
+  for (int n = 0; n < OZ_META; n++) meta[n] = 0;
+  for (int n = 0; n < M; n++) {
+    const int sft = E[n] - emax + 3;
+    meta[n] = sft < -63 ? -63 : sft;
+  }
+  meta[OZ_ROWS] = emax + 7;
 }
 
-// Copy nwords fragment words (and nexp exponents) into shared memory.
+// Far-field block fragments: block gb, part 0 = [A0 A1] (18 x 36), part 1 = A2
+// (18 x 18); words at F + gb * OZ_FAR_WORDS, metadata at Pm + gb * 2 * OZ_META.
+// One thread per (block, part).
+constexpr int OZ_FAR_W0 = oz_words(OZ_NT, 5), OZ_FAR_WORDS = OZ_FAR_W0 + oz_words(OZ_NT, 3);
+__global__ void k_oz_pack_far(const double *__restrict__ A, long long nblocks, unsigned *F,
+                              int *Pm) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= nblocks * 2) return;
+  const long long gb = idx >> 1;
+  const int part = (int)(idx & 1);
+  unsigned *Fb = F + gb * OZ_FAR_WORDS + (part ? OZ_FAR_W0 : 0);
+  int E[OZ_ROWS];
+  for (int n = 0; n < OZ_ROWS; n++) {
+    const double *A0 = A + 3 * gb * MM + (n < M ? n : 0) * M;
+    if (part == 0)
+      oz_pack_row([&](int k) { return k < M ? A0[k] : A0[MM + k - M]; }, n < M, n, 2 * M, OZ_NT,
+                  5, Fb, E);
+    else
+      oz_pack_row([&](int k) { return A0[2 * MM + k]; }, n < M, n, M, OZ_NT, 3, Fb, E);
+  }
+  oz_meta(E, Pm + (gb * 2 + part) * OZ_META);
+}
+
+// Copy nwords fragment words (and nint metadata ints) into shared memory.
 __device__ __forceinline__ void oz_load_frag(unsigned *dst, const unsigned *__restrict__ src,
-                                             int nwords, int *edst, const int *__restrict__ esrc,
-                                             int nexp) {
+                                             int nwords, int *idst, const int *__restrict__ isrc,
+                                             int nint) {
   const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
   uint4 *d4 = reinterpret_cast<uint4 *>(dst);
   for (int i = threadIdx.x; i < nwords / 4; i += blockDim.x) d4[i] = s4[i];
-  for (int i = threadIdx.x; i < nexp; i += blockDim.x) edst[i] = esrc[i];
+  for (int i = threadIdx.x; i < nint; i += blockDim.x) idst[i] = isrc[i];
+}
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem, int bytes) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(bytes));
 }
 
 // Per-warp two-deep pipeline over tiles first, first + step, ... < ntile:
@@ -1023,21 +1051,48 @@ __device__ __forceinline__ void oz_tile_T(const unsigned *Pf, const long long *Y
   }
 }
 
+// Producer epilogue of a 16 x 24 tile with 18 real output rows: the lane's
+// 9 real outputs are n-tiles 0 and 1 (rows g, g+8; outputs 8nt + 2t, +1) and
+// one element of n-tile 2, whose four real elements all sit in the quad's
+// lane t = 0 and are dealt out one per lane.  put2(r, n, V0, V1) stores
+// outputs n, n+1 of tile row r, put1(r, n, V) one output; rs[n] is the
+// metadata row shift.
+template <class Put2, class Put1>
+__device__ __forceinline__ void oz_put18(const long long (&T)[OZ_NT][4], const int *rs, Put2 put2,
+                                         Put1 put1) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
+#pragma unroll
+  for (int nt = 0; nt < 2; nt++)
+#pragma unroll
+    for (int hr = 0; hr < 2; hr++) {
+      const int n = 8 * nt + 2 * t4;
+      put2(g + 8 * hr, n, l2c_oz::shift_s64(T[nt][2 * hr], rs[n]),
+           l2c_oz::shift_s64(T[nt][2 * hr + 1], rs[n + 1]));
+    }
+  const int src = lane & ~3;
+  const long long v1 = __shfl_sync(0xffffffffu, T[2][1], src);
+  const long long v2 = __shfl_sync(0xffffffffu, T[2][2], src);
+  const long long v3 = __shfl_sync(0xffffffffu, T[2][3], src);
+  const long long t9 = t4 == 0 ? T[2][0] : t4 == 1 ? v1 : t4 == 2 ? v2 : v3;
+  const int n9 = 16 + (t4 & 1);
+  put1(g + 8 * (t4 >> 1), n9, l2c_oz::shift_s64(t9, rs[n9]));
+}
+
 // Leaf up (step 1): tile = 16 consecutive leaf nodes of one vector; both
 // parities from one staged stretch of x (node r's h inputs in row r, parity
 // sg at even/odd positions).  P_sg = T_sg^T (18 x s), KC = ceil(s / 8).
 template <int KC>
 __global__ void __launch_bounds__(32 * MXW)
-    k_mz_leaf_up(const double *__restrict__ x, double *__restrict__ w,
-                 const unsigned *__restrict__ Pf, const int *__restrict__ Pe, Geo g) {
+    k_mz_leaf_up(const double *__restrict__ x, long long *__restrict__ w, int *__restrict__ wE,
+                 const unsigned *__restrict__ Pf, const int *__restrict__ Pm, Geo g) {
   constexpr int XLD = 16 * KC + 1, NW = oz_words(OZ_NT, KC);
   extern __shared__ __align__(16) unsigned char mz_smem[];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
   unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
-  int *sE = reinterpret_cast<int *>(sP + 2 * NW);
-  int *Es = sE + 2 * OZ_ROWS + wid * 32;
-  double *Xw = reinterpret_cast<double *>(sE + 2 * OZ_ROWS + 32 * MXW) + wid * 2 * 16 * XLD;
-  oz_load_frag(sP, Pf, 2 * NW, sE, Pe, 2 * OZ_ROWS);
+  int *sM = reinterpret_cast<int *>(sP + 2 * NW);
+  int *Es = sM + 2 * OZ_META + wid * 32;
+  double *Xw = reinterpret_cast<double *>(sM + 2 * OZ_META + 32 * MXW) + wid * 2 * 16 * XLD;
+  oz_load_frag(sP, Pf, 2 * NW, sM, Pm, 2 * OZ_META);
   __syncthreads();
   const long long tpv = (g.K + 15) / 16, ntile = g.count * tpv;
   auto issue = [&](long long tile, int buf) {
@@ -1063,18 +1118,22 @@ __global__ void __launch_bounds__(32 * MXW)
     for (int sg = 0; sg < 2; sg++) {
       long long T[OZ_NT][4];
       oz_tile_T<OZ_NT, KC>(sP + sg * NW, Ys + sg, XLD, 2, T);
-#pragma unroll
-      for (int nt = 0; nt < OZ_NT; nt++)
-#pragma unroll
+      const int *meta = sM + sg * OZ_META;
+      long long *wcol = w + ((v * 2 + sg) * g.slots + g.leaf_base + node0) * M;
+      const long long nrow = g.K - node0;
+      oz_put18(
+          T, meta,
+          [&](int r, int n, long long a, long long b) {
+            if (r < nrow) *reinterpret_cast<longlong2 *>(wcol + r * M + n) = make_longlong2(a, b);
+          },
+          [&](int r, int n, long long a) {
+            if (r < nrow) wcol[r * M + n] = a;
+          });
+      if (t4 == 0)
         for (int hr = 0; hr < 2; hr++) {
-          const int r = gq + 8 * hr, n = 8 * nt + 2 * t4;
-          if (n >= M || node0 + r >= g.K) continue;
-          const int ec = Es[sg * 16 + r] - 52;
-          double2 o;
-          o.x = l2c_oz::to_double(T[nt][2 * hr], ec + sE[sg * OZ_ROWS + n]);
-          o.y = l2c_oz::to_double(T[nt][2 * hr + 1], ec + sE[sg * OZ_ROWS + n + 1]);
-          *reinterpret_cast<double2 *>(
-              w + ((v * 2 + sg) * g.slots + g.leaf_base + node0 + r) * M + n) = o;
+          const int r = gq + 8 * hr;
+          if (r < nrow)
+            wE[(v * 2 + sg) * g.slots + g.leaf_base + node0 + r] = Es[sg * 16 + r] + meta[OZ_ROWS];
         }
     }
   };
@@ -1082,189 +1141,224 @@ __global__ void __launch_bounds__(32 * MXW)
 }
 
 size_t mz_leaf_up_smem(int KC) {
-  return (size_t)(2 * oz_words(OZ_NT, KC) + 2 * OZ_ROWS + 32 * MXW) * 4 +
+  return (size_t)(2 * oz_words(OZ_NT, KC) + 2 * OZ_META + 32 * MXW) * 4 +
          (size_t)MXW * 2 * 16 * (16 * KC + 1) * sizeof(double);
 }
 
 // Transfer trees, one level.  Columns col = (vector * 2 + parity) * np + j.
 // Up: parent slot j of level l from child slots 2j+2, 2j+3 of level l+1
-// (36 contiguous coefficients), P = [B | B'] (18 x 36).
+// (36 contiguous coefficients, two stored columns), P = [B | B'] (18 x 36).
 constexpr int OZ_TREE_UP_WORDS = oz_words(OZ_NT, 5);
 __global__ void __launch_bounds__(32 * MXW)
-    k_mz_tree_up(double *w, const unsigned *__restrict__ Pf, const int *__restrict__ Pe, Geo g,
-                 long long parent_base, long long child_base, long long np) {
+    k_mz_tree_up(long long *w, int *wE, const unsigned *__restrict__ Pf,
+                 const int *__restrict__ Pm, Geo g, long long parent_base, long long child_base,
+                 long long np) {
   extern __shared__ __align__(16) unsigned char mz_smem[];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
   unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
-  int *sE = reinterpret_cast<int *>(sP + OZ_TREE_UP_WORDS);
-  int *Es = sE + OZ_ROWS + wid * 16;
-  long long *sB = reinterpret_cast<long long *>(sE + OZ_ROWS + 16 * MXW) + wid * 2 * 16;
-  double *Xw = reinterpret_cast<double *>(sB - wid * 2 * 16 + 2 * 16 * MXW) + wid * 2 * 16 * OZ_TLD;
-  oz_load_frag(sP, Pf, OZ_TREE_UP_WORDS, sE, Pe, OZ_ROWS);
+  int *sM = reinterpret_cast<int *>(sP + OZ_TREE_UP_WORDS);
+  int *sI = sM + OZ_META + wid * (16 + 2 * 2 * 16);  // Es[16], then [buf][child][16] exponents
+  int *Es = sI, *sEx = sI + 16;
+  long long *sB = reinterpret_cast<long long *>(sM + OZ_META + MXW * (16 + 4 * 16)) + wid * 2 * 16;
+  long long *X0 = sB - wid * 2 * 16 + MXW * 2 * 16;
+  long long *Xw = X0 + wid * 2 * 16 * OZ_TLD;
+  oz_load_frag(sP, Pf, OZ_TREE_UP_WORDS, sM, Pm, OZ_META);
   __syncthreads();
   const long long ncol = g.count * 2 * np, ntile = (ncol + 15) / 16;
   auto issue = [&](long long tile, int buf) {
     long long *B = sB + buf * 16;
+    int *Ex = sEx + buf * 32;
     if (lane < 16) {
       const long long col = tile * 16 + lane;
       long long b = -1;
       if (col < ncol) {
         const long long vs = col / np, j = col - vs * np;
-        b = (vs * g.slots + child_base + 2 * j + 2) * M;
+        b = vs * g.slots + child_base + 2 * j + 2;  // first child slot
       }
       B[lane] = b;
+      cp_async4(Ex + lane, b >= 0 ? wE + b : wE, b >= 0 ? 4 : 0);
+      cp_async4(Ex + 16 + lane, b >= 0 ? wE + b + 1 : wE, b >= 0 ? 4 : 0);
     }
     __syncwarp();
-    double *X = Xw + buf * 16 * OZ_TLD;
+    long long *X = Xw + buf * 16 * OZ_TLD;
     for (int e = lane; e < 16 * M; e += 32) {  // 16 columns x 18 pairs
       const int r = e / M, k2 = e - r * M;
       const long long b = B[r];
-      l2c_oz::cp_async16(X + r * OZ_TLD + 2 * k2, b >= 0 ? w + b + 2 * k2 : w, b >= 0 ? 16 : 0);
+      l2c_oz::cp_async16(X + r * OZ_TLD + 2 * k2, b >= 0 ? w + b * M + 2 * k2 : w, b >= 0 ? 16 : 0);
     }
   };
   auto work = [&](long long tile, int buf) {
-    double *X = Xw + buf * 16 * OZ_TLD;
-    l2c_oz::stage_fix(X, OZ_TLD, 1, 2 * M, 40, Es);
+    long long *X = Xw + buf * 16 * OZ_TLD;
+    const int *Ex = sEx + buf * 32;
+    l2c_oz::stage_cols(X, OZ_TLD, 2 * M, M, 40, Ex, Ex + 16, Es);
     long long T[OZ_NT][4];
-    oz_tile_T<OZ_NT, 5>(sP, reinterpret_cast<const long long *>(X), OZ_TLD, 1, T);
-#pragma unroll
-    for (int hr = 0; hr < 2; hr++) {
-      const int r = gq + 8 * hr;
-      const long long col = tile * 16 + r;
-      if (col >= ncol) continue;
+    oz_tile_T<OZ_NT, 5>(sP, X, OZ_TLD, 1, T);
+    const long long c0 = tile * 16;
+    auto dst = [&](int r) -> long long {  // parent slot index, -1: none
+      const long long col = c0 + r;
+      if (col >= ncol) return -1;
       const long long vs = col / np, j = col - vs * np;
-      double *dst = w + (vs * g.slots + parent_base + j) * M;
-      const int ec = Es[r] - 52;
-#pragma unroll
-      for (int nt = 0; nt < OZ_NT; nt++) {
-        const int n = 8 * nt + 2 * t4;
-        if (n >= M) continue;
-        double2 o;
-        o.x = l2c_oz::to_double(T[nt][2 * hr], ec + sE[n]);
-        o.y = l2c_oz::to_double(T[nt][2 * hr + 1], ec + sE[n + 1]);
-        *reinterpret_cast<double2 *>(dst + n) = o;
-      }
+      return vs * g.slots + parent_base + j;
+    };
+    const long long d0 = dst(gq), d1 = dst(gq + 8);
+    oz_put18(
+        T, sM,
+        [&](int r, int n, long long a, long long b) {
+          const long long d = r < 8 ? d0 : d1;
+          if (d >= 0) *reinterpret_cast<longlong2 *>(w + d * M + n) = make_longlong2(a, b);
+        },
+        [&](int r, int n, long long a) {
+          const long long d = r < 8 ? d0 : d1;
+          if (d >= 0) w[d * M + n] = a;
+        });
+    if (t4 == 0) {
+      if (d0 >= 0) wE[d0] = Es[gq] + sM[OZ_ROWS];
+      if (d1 >= 0) wE[d1] = Es[gq + 8] + sM[OZ_ROWS];
     }
   };
   oz_tile_loop((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue, work);
 }
 
-constexpr size_t OZ_TREE_UP_SMEM = (size_t)(OZ_TREE_UP_WORDS + OZ_ROWS + 16 * MXW) * 4 +
+constexpr size_t OZ_TREE_UP_SMEM = (size_t)(OZ_TREE_UP_WORDS + OZ_META + MXW * (16 + 4 * 16)) * 4 +
                                    (size_t)MXW * 2 * 16 * 8 +
-                                   (size_t)MXW * 2 * 16 * OZ_TLD * sizeof(double);
+                                   (size_t)MXW * 2 * 16 * OZ_TLD * sizeof(long long);
 
 // Down: child slots 2t, 2t+1 of level l+1 += [B^T; B^T'] c(parent slot t of
-// level l).  The sum with the child's own far field is formed exactly in the
-// fixed-point frame of the product when the magnitudes allow it.
-__device__ __forceinline__ double oz_add(double existing, long long T, int e) {
-  long long X;
-  const bool fits = l2c_oz::to_fixed(existing, e, X);
-  const double r = l2c_oz::to_double(fits ? T + X : T, e);
-  return fits ? r : existing + r;
-}
-
+// level l).  The child's own far field (prefetched with the parent) and the
+// product are added as integers on the coarser of their two scales, one bit
+// above the larger exponent.
 constexpr int OZ_TREE_DOWN_WORDS = 2 * oz_words(OZ_NT, 3);
-// Per warp and buffer: 16 parent columns (18 values, row OZ_CLD) and the 16
-// pairs of child columns they add to (36 contiguous values each).
 __global__ void __launch_bounds__(32 * MXW)
-    k_mz_tree_down(double *c, const unsigned *__restrict__ Pf, const int *__restrict__ Pe, Geo g,
-                   long long parent_base, long long child_base, long long np) {
+    k_mz_tree_down(long long *c, int *cE, const unsigned *__restrict__ Pf,
+                   const int *__restrict__ Pm, Geo g, long long parent_base, long long child_base,
+                   long long np) {
   extern __shared__ __align__(16) unsigned char mz_smem[];
   constexpr int NW = oz_words(OZ_NT, 3);
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
   unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
-  int *sE = reinterpret_cast<int *>(sP + OZ_TREE_DOWN_WORDS);
-  int *Es = sE + 2 * OZ_ROWS + wid * 16;
-  long long *sB0 = reinterpret_cast<long long *>(sE + 2 * OZ_ROWS + 16 * MXW);
-  long long *sB = sB0 + wid * 2 * 2 * 16;  // [buf][parent | child][16]
-  double *X0 = reinterpret_cast<double *>(sB0 + 2 * 2 * 16 * MXW);
-  double *Xw = X0 + wid * 2 * 16 * OZ_CLD;
-  double *Cw = X0 + MXW * 2 * 16 * OZ_CLD + wid * 2 * 16 * 2 * M;
-  oz_load_frag(sP, Pf, OZ_TREE_DOWN_WORDS, sE, Pe, 2 * OZ_ROWS);
+  int *sM = reinterpret_cast<int *>(sP + OZ_TREE_DOWN_WORDS);
+  // per warp: Es[16], then per buffer: parent exponent [16], child exponents [2][16]
+  int *sI = sM + 2 * OZ_META + wid * (16 + 2 * 3 * 16);
+  int *Es = sI, *sEx = sI + 16;
+  long long *sB0 = reinterpret_cast<long long *>(sM + 2 * OZ_META + MXW * (16 + 6 * 16));
+  long long *sB = sB0 + wid * 2 * 2 * 16;  // [buf][parent | child][16] slot indices
+  long long *X0 = sB0 + MXW * 2 * 2 * 16;
+  long long *Xw = X0 + wid * 2 * 16 * OZ_CLD;
+  long long *Cw = X0 + MXW * 2 * 16 * OZ_CLD + wid * 2 * 16 * 2 * M;
+  oz_load_frag(sP, Pf, OZ_TREE_DOWN_WORDS, sM, Pm, 2 * OZ_META);
   __syncthreads();
   const long long ncol = g.count * 2 * np, ntile = (ncol + 15) / 16;
   auto issue = [&](long long tile, int buf) {
     long long *B = sB + buf * 32;
+    int *Ex = sEx + buf * 48;
     if (lane < 16) {
       const long long col = tile * 16 + lane;
       long long b = -1, cb = -1;
       if (col < ncol) {
         const long long vs = col / np, t = col - vs * np;
-        b = (vs * g.slots + parent_base + t) * M;
-        cb = (vs * g.slots + child_base + 2 * t) * M;
+        b = vs * g.slots + parent_base + t;
+        cb = vs * g.slots + child_base + 2 * t;
       }
       B[lane] = b;
       B[16 + lane] = cb;
+      cp_async4(Ex + lane, b >= 0 ? cE + b : cE, b >= 0 ? 4 : 0);
+      cp_async4(Ex + 16 + lane, cb >= 0 ? cE + cb : cE, cb >= 0 ? 4 : 0);
+      cp_async4(Ex + 32 + lane, cb >= 0 ? cE + cb + 1 : cE, cb >= 0 ? 4 : 0);
     }
     __syncwarp();
-    double *X = Xw + buf * 16 * OZ_CLD, *C = Cw + buf * 16 * 2 * M;
-    for (int e = lane; e < 16 * (M / 2); e += 32) {  // 16 columns x 9 pairs
+    long long *X = Xw + buf * 16 * OZ_CLD, *C = Cw + buf * 16 * 2 * M;
+    for (int e = lane; e < 16 * (M / 2); e += 32) {  // 16 parent columns x 9 pairs
       const int r = e / (M / 2), k2 = e - r * (M / 2);
       const long long b = B[r];
-      l2c_oz::cp_async16(X + r * OZ_CLD + 2 * k2, b >= 0 ? c + b + 2 * k2 : c, b >= 0 ? 16 : 0);
+      l2c_oz::cp_async16(X + r * OZ_CLD + 2 * k2, b >= 0 ? c + b * M + 2 * k2 : c, b >= 0 ? 16 : 0);
     }
     for (int e = lane; e < 16 * M; e += 32) {  // 16 child pairs x 18 pairs
       const int r = e / M, k2 = e - r * M;
       const long long b = B[16 + r];
-      l2c_oz::cp_async16(C + r * 2 * M + 2 * k2, b >= 0 ? c + b + 2 * k2 : c, b >= 0 ? 16 : 0);
+      l2c_oz::cp_async16(C + r * 2 * M + 2 * k2, b >= 0 ? c + b * M + 2 * k2 : c, b >= 0 ? 16 : 0);
     }
   };
   auto work = [&](long long tile, int buf) {
-    double *X = Xw + buf * 16 * OZ_CLD;
-    const double *C = Cw + buf * 16 * 2 * M;
+    long long *X = Xw + buf * 16 * OZ_CLD;
+    const long long *C = Cw + buf * 16 * 2 * M;
     const long long *B = sB + buf * 32;
-    l2c_oz::stage_fix(X, OZ_CLD, 1, M, 24, Es);
+    const int *Ex = sEx + buf * 48;
+    l2c_oz::stage_cols(X, OZ_CLD, M, M, 24, Ex, Ex, Es);
+    const long long cb0 = B[16 + gq], cb1 = B[16 + gq + 8];
 #pragma unroll 1
     for (int ch = 0; ch < 2; ch++) {
       long long T[OZ_NT][4];
-      oz_tile_T<OZ_NT, 3>(sP + ch * NW, reinterpret_cast<const long long *>(X), OZ_CLD, 1, T);
+      oz_tile_T<OZ_NT, 3>(sP + ch * NW, X, OZ_CLD, 1, T);
+      const int *meta = sM + ch * OZ_META;
+      // per tile row r: product exponent, child exponent, sum exponent
+      int ep[2], ek[2], es[2];
 #pragma unroll
       for (int hr = 0; hr < 2; hr++) {
         const int r = gq + 8 * hr;
-        const long long cb = B[16 + r];
-        if (cb < 0) continue;
-        double *dst = c + cb + ch * M;
-        const double *old = C + r * 2 * M + ch * M;
-        const int ec = Es[r] - 52;
-#pragma unroll
-        for (int nt = 0; nt < OZ_NT; nt++) {
-          const int n = 8 * nt + 2 * t4;
-          if (n >= M) continue;
-          double2 o;
-          o.x = oz_add(old[n], T[nt][2 * hr], ec + sE[ch * OZ_ROWS + n]);
-          o.y = oz_add(old[n + 1], T[nt][2 * hr + 1], ec + sE[ch * OZ_ROWS + n + 1]);
-          *reinterpret_cast<double2 *>(dst + n) = o;
-        }
+        ep[hr] = Es[r] + meta[OZ_ROWS];
+        ek[hr] = Ex[16 + 16 * ch + r];
+        es[hr] = max(ep[hr], ek[hr]) + 1;
+      }
+      auto sum = [&](int r, int n, long long v) -> long long {
+        const int hr = r >> 3;
+        return l2c_oz::shift_s64(C[r * 2 * M + ch * M + n], ek[hr] - es[hr]) +
+               l2c_oz::shift_s64(v, ep[hr] - es[hr]);
+      };
+      oz_put18(
+          T, meta,
+          [&](int r, int n, long long a, long long b) {
+            const long long d = r < 8 ? cb0 : cb1;
+            if (d >= 0)
+              *reinterpret_cast<longlong2 *>(c + (d + ch) * M + n) =
+                  make_longlong2(sum(r, n, a), sum(r, n + 1, b));
+          },
+          [&](int r, int n, long long a) {
+            const long long d = r < 8 ? cb0 : cb1;
+            if (d >= 0) c[(d + ch) * M + n] = sum(r, n, a);
+          });
+      if (t4 == 0) {
+        if (cb0 >= 0) cE[cb0 + ch] = es[0];
+        if (cb1 >= 0) cE[cb1 + ch] = es[1];
       }
     }
   };
   oz_tile_loop((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue, work);
 }
 
-constexpr size_t OZ_TREE_DOWN_SMEM = (size_t)(OZ_TREE_DOWN_WORDS + 2 * OZ_ROWS + 16 * MXW) * 4 +
-                                     (size_t)MXW * 2 * 2 * 16 * 8 +
-                                     (size_t)MXW * 2 * 16 * (OZ_CLD + 2 * M) * sizeof(double);
+constexpr size_t OZ_TREE_DOWN_SMEM =
+    (size_t)(OZ_TREE_DOWN_WORDS + 2 * OZ_META + MXW * (16 + 6 * 16)) * 4 +
+    (size_t)MXW * 2 * 2 * 16 * 8 + (size_t)MXW * 2 * 16 * (OZ_CLD + 2 * M) * sizeof(long long);
 
 // Far field (step 3): CTA = (block gb, chunk of columns vs = vector * 2 +
 // parity).  c0 = [A0 A1] [w0; w1] (K = 36), c1 = A2 w1 (K = 18); both parts
-// use the exponent of the whole column [w0; w1].
+// use the scale of the whole column [w0; w1].
 constexpr int OZ_FAR_COLS = 16 * MXW * 2;  // columns per CTA
 __global__ void __launch_bounds__(32 * MXW)
-    k_mz_far(const double *__restrict__ w, double *__restrict__ c,
-             const unsigned *__restrict__ Pf, const int *__restrict__ Pe, Geo g) {
+    k_mz_far(const long long *__restrict__ w, const int *__restrict__ wE, long long *__restrict__ c,
+             int *__restrict__ cE, const unsigned *__restrict__ Pf, const int *__restrict__ Pm,
+             Geo g) {
   extern __shared__ __align__(16) unsigned char mz_smem[];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
   unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
-  int *sE = reinterpret_cast<int *>(sP + OZ_FAR_WORDS);
-  int *Es = sE + 2 * OZ_ROWS + wid * 16;
-  double *Xw = reinterpret_cast<double *>(sE + 2 * OZ_ROWS + 16 * MXW) + wid * 2 * 16 * OZ_TLD;
+  int *sM = reinterpret_cast<int *>(sP + OZ_FAR_WORDS);
+  int *sI = sM + 2 * OZ_META + wid * (16 + 2 * 2 * 16);  // Es[16], [buf][slot][16]
+  int *Es = sI, *sEx = sI + 16;
+  long long *Xw = reinterpret_cast<long long *>(sM + 2 * OZ_META + MXW * (16 + 4 * 16)) +
+                  wid * 2 * 16 * OZ_TLD;
   const long long gb = blockIdx.x;
-  oz_load_frag(sP, Pf + gb * OZ_FAR_WORDS, OZ_FAR_WORDS, sE, Pe + gb * 2 * OZ_ROWS, 2 * OZ_ROWS);
+  oz_load_frag(sP, Pf + gb * OZ_FAR_WORDS, OZ_FAR_WORDS, sM, Pm + gb * 2 * OZ_META, 2 * OZ_META);
   __syncthreads();
   const long long ncol = 2 * g.count, c0 = (long long)blockIdx.y * OZ_FAR_COLS;
   const long long ntile = (min(ncol - c0, (long long)OZ_FAR_COLS) + 15) / 16;
   auto issue = [&](long long tile, int buf) {
-    double *X = Xw + buf * 16 * OZ_TLD;
+    long long *X = Xw + buf * 16 * OZ_TLD;
+    int *Ex = sEx + buf * 32;
+    if (lane < 16) {
+      const long long col = c0 + tile * 16 + lane;
+      const bool ok = col < ncol;
+      cp_async4(Ex + lane, ok ? wE + col * g.slots + 2 * gb : wE, ok ? 4 : 0);
+      cp_async4(Ex + 16 + lane, ok ? wE + col * g.slots + 2 * gb + 1 : wE, ok ? 4 : 0);
+    }
     for (int e = lane; e < 16 * M; e += 32) {  // 16 columns x 18 pairs
       const int r = e / M, k2 = e - r * M;
       const long long col = c0 + tile * 16 + r;
@@ -1274,40 +1368,41 @@ __global__ void __launch_bounds__(32 * MXW)
     }
   };
   auto work = [&](long long tile, int buf) {
-    double *X = Xw + buf * 16 * OZ_TLD;
-    l2c_oz::stage_fix(X, OZ_TLD, 1, 2 * M, OZ_TLD, Es);
-    const long long *Ys = reinterpret_cast<const long long *>(X);
+    long long *X = Xw + buf * 16 * OZ_TLD;
+    const int *Ex = sEx + buf * 32;
+    l2c_oz::stage_cols(X, OZ_TLD, 2 * M, M, OZ_TLD, Ex, Ex + 16, Es);
+    const long long cA = c0 + tile * 16 + gq, cB = cA + 8;
 #pragma unroll 1
     for (int part = 0; part < 2; part++) {
       long long T[OZ_NT][4];
       if (part == 0)
-        oz_tile_T<OZ_NT, 5>(sP, Ys, OZ_TLD, 1, T);
+        oz_tile_T<OZ_NT, 5>(sP, X, OZ_TLD, 1, T);
       else
-        oz_tile_T<OZ_NT, 3>(sP + OZ_FAR_W0, Ys + M, OZ_TLD, 1, T);
-#pragma unroll
-      for (int hr = 0; hr < 2; hr++) {
-        const int r = gq + 8 * hr;
-        const long long col = c0 + tile * 16 + r;
-        if (col >= ncol) continue;
-        double *dst = c + (col * g.slots + 2 * gb + part) * M;
-        const int ec = Es[r] - 52;
-#pragma unroll
-        for (int nt = 0; nt < OZ_NT; nt++) {
-          const int n = 8 * nt + 2 * t4;
-          if (n >= M) continue;
-          double2 o;
-          o.x = l2c_oz::to_double(T[nt][2 * hr], ec + sE[part * OZ_ROWS + n]);
-          o.y = l2c_oz::to_double(T[nt][2 * hr + 1], ec + sE[part * OZ_ROWS + n + 1]);
-          *reinterpret_cast<double2 *>(dst + n) = o;
-        }
+        oz_tile_T<OZ_NT, 3>(sP + OZ_FAR_W0, X + M, OZ_TLD, 1, T);
+      const int *meta = sM + part * OZ_META;
+      oz_put18(
+          T, meta,
+          [&](int r, int n, long long a, long long b) {
+            const long long col = r < 8 ? cA : cB;
+            if (col < ncol)
+              *reinterpret_cast<longlong2 *>(c + (col * g.slots + 2 * gb + part) * M + n) =
+                  make_longlong2(a, b);
+          },
+          [&](int r, int n, long long a) {
+            const long long col = r < 8 ? cA : cB;
+            if (col < ncol) c[(col * g.slots + 2 * gb + part) * M + n] = a;
+          });
+      if (t4 == 0) {
+        if (cA < ncol) cE[cA * g.slots + 2 * gb + part] = Es[gq] + meta[OZ_ROWS];
+        if (cB < ncol) cE[cB * g.slots + 2 * gb + part] = Es[gq + 8] + meta[OZ_ROWS];
       }
     }
   };
   oz_tile_loop(wid, MXW, ntile, issue, work);
 }
 
-constexpr size_t OZ_FAR_SMEM = (size_t)(OZ_FAR_WORDS + 2 * OZ_ROWS + 16 * MXW) * 4 +
-                               (size_t)MXW * 2 * 16 * OZ_TLD * sizeof(double);
+constexpr size_t OZ_FAR_SMEM = (size_t)(OZ_FAR_WORDS + 2 * OZ_META + MXW * (16 + 4 * 16)) * 4 +
+                               (size_t)MXW * 2 * 16 * OZ_TLD * sizeof(long long);
 
 // Leaf down (step 5) + final scaling: tile = 16 consecutive leaf targets of one
 // vector, both parities; P_sg = T_sg (s x 18) in passes of 16 output rows
@@ -1316,29 +1411,38 @@ constexpr size_t OZ_FAR_SMEM = (size_t)(OZ_FAR_WORDS + 2 * OZ_ROWS + 16 * MXW) *
 // sum is written, scaled, in output order.
 constexpr int OZ_LD_WORDS = oz_words(2, 3);
 __global__ void __launch_bounds__(32 * MXW)
-    k_mz_leaf_down(const double *__restrict__ c, const double *__restrict__ y, double *out,
-                   const unsigned *__restrict__ Pf, const int *__restrict__ Pe, Geo g, int c2l,
-                   int npass) {
+    k_mz_leaf_down(const long long *__restrict__ c, const int *__restrict__ cE,
+                   const double *__restrict__ y, double *out, const unsigned *__restrict__ Pf,
+                   const int *__restrict__ Pe, Geo g, int c2l, int npass) {
   extern __shared__ __align__(16) unsigned char mz_smem[];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
   const int nw = 2 * npass * OZ_LD_WORDS, ne = 2 * npass * 16;
   unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
   int *sE = reinterpret_cast<int *>(sP + nw);
-  int *Ec = sE + ne + wid * 32;
+  int *Ec = sE + ne + wid * (32 + 2 * 32);  // Ec[2][16], then [buf][parity][16] exponents
+  int *sEx = Ec + 32;
   const long long per_warp = 2 * 2 * 16 * OZ_CLD + 2 * 16 * g.h;
-  double *Xw = reinterpret_cast<double *>(sE + ne + 32 * MXW) + wid * per_warp;
-  double *Ow = Xw + 2 * 2 * 16 * OZ_CLD;  // per buffer 16 rows of h outputs
+  long long *Xw =
+      reinterpret_cast<long long *>(sE + ne + MXW * (32 + 2 * 32)) + wid * per_warp;
+  double *Ow = reinterpret_cast<double *>(Xw + 2 * 2 * 16 * OZ_CLD);  // per buffer 16 x h
   oz_load_frag(sP, Pf, nw, sE, Pe, ne);
   __syncthreads();
   const long long tpv = (g.K + 15) / 16, ntile = g.count * tpv;
   auto issue = [&](long long tile, int buf) {
     const long long v = tile / tpv, tau0 = (tile - v * tpv) * 16;
     const long long nrow = min(16LL, g.K - tau0);
-    double *X = Xw + buf * 2 * 16 * OZ_CLD;
+    long long *X = Xw + buf * 2 * 16 * OZ_CLD;
+    int *Ex = sEx + buf * 32;
+    {
+      const int sg = lane >> 4, r = lane & 15;
+      const bool ok = r < nrow;
+      const long long slot = (v * 2 + sg) * g.slots + g.leaf_base + tau0 + r;
+      cp_async4(Ex + lane, ok ? cE + slot : cE, ok ? 4 : 0);
+    }
     for (int e = lane; e < 2 * 16 * (M / 2); e += 32) {  // 2 parities x 16 rows x 9 pairs
       const int sr = e / (M / 2), k2 = e - sr * (M / 2), sg = sr >> 4, r = sr & 15;
       const bool ok = r < nrow;
-      const double *src = c + ((v * 2 + sg) * g.slots + g.leaf_base + tau0 + r) * M + 2 * k2;
+      const long long *src = c + ((v * 2 + sg) * g.slots + g.leaf_base + tau0 + r) * M + 2 * k2;
       l2c_oz::cp_async16(X + sr * OZ_CLD + 2 * k2, ok ? src : c, ok ? 16 : 0);
     }
     const long long j0 = tau0 * g.h, jn = nrow * g.h;
@@ -1352,15 +1456,15 @@ __global__ void __launch_bounds__(32 * MXW)
   auto work = [&](long long tile, int buf) {
     const long long v = tile / tpv, tau0 = (tile - v * tpv) * 16;
     double *O = Ow + buf * 16 * g.h;
+    const int *Ex = sEx + buf * 32;
 #pragma unroll 1
     for (int sg = 0; sg < 2; sg++) {
-      double *X = Xw + (buf * 2 + sg) * 16 * OZ_CLD;
-      l2c_oz::stage_fix(X, OZ_CLD, 1, M, 24, Ec + 16 * sg);
-      const long long *Ys = reinterpret_cast<const long long *>(X);
+      long long *X = Xw + (buf * 2 + sg) * 16 * OZ_CLD;
+      l2c_oz::stage_cols(X, OZ_CLD, M, M, 24, Ex + 16 * sg, Ex + 16 * sg, Ec + 16 * sg);
 #pragma unroll 1
       for (int ps = 0; ps < npass; ps++) {
         long long T[2][4];
-        oz_tile_T<2, 3>(sP + (sg * npass + ps) * OZ_LD_WORDS, Ys, OZ_CLD, 1, T);
+        oz_tile_T<2, 3>(sP + (sg * npass + ps) * OZ_LD_WORDS, X, OZ_CLD, 1, T);
         const int *Ep = sE + (sg * npass + ps) * 16;
 #pragma unroll
         for (int nt = 0; nt < 2; nt++)
@@ -1392,8 +1496,8 @@ __global__ void __launch_bounds__(32 * MXW)
 }
 
 size_t mz_leaf_down_smem(long long s, int npass) {
-  return (size_t)(2 * npass * OZ_LD_WORDS + 2 * npass * 16 + 32 * MXW) * 4 +
-         (size_t)MXW * (2 * 2 * 16 * OZ_CLD + 2 * 16 * 2 * s) * sizeof(double);
+  return (size_t)(2 * npass * OZ_LD_WORDS + 2 * npass * 16 + MXW * (32 + 2 * 32)) * 4 +
+         (size_t)MXW * (2 * 2 * 16 * OZ_CLD + 2 * 16 * 2 * s) * 8;
 }
 
 // Outputs past the last leaf target node (no far field): scaling only.
@@ -1411,6 +1515,41 @@ __global__ void k_mx_tail(const double *__restrict__ y, double *out, Geo g, int 
   }
   out[v * g.dist + j * g.stride] = val;
 }
+
+// Column format <-> doubles, in place, one thread per 18-coefficient column
+// (for the FP64 far-field kernel of single vectors).
+__global__ void k_oz_cols_to_double(long long *V, const int *__restrict__ E, long long ncol) {
+  const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const int e = E[col] - l2c_oz::VBITS;
+  long long *v = V + col * M;
+  double *d = reinterpret_cast<double *>(v);
+  for (int k = 0; k < M; k++) {
+    const long long t = v[k];
+    d[k] = l2c_oz::to_double(t, e);  // t 2^e, rounded once
+  }
+}
+
+__global__ void k_oz_cols_from_double(double *D, int *__restrict__ E, long long ncol) {
+  const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  double *d = D + col * M;
+  long long *v = reinterpret_cast<long long *>(d);
+  int e = l2c_oz::EXP_ZERO;
+  for (int k = 0; k < M; k++) e = max(e, l2c_oz::exp_bound(d[k]));
+  for (int k = 0; k < M; k++) {
+    // |d| < 2^e: V = trunc(d 2^(VBITS - e)), |V| < 2^VBITS
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d[k]);
+    const int ex = (int)((b >> 52) & 0x7FF);
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = e - l2c_oz::VBITS + 1075 - ex;  // >= -(VBITS - 53)
+    unsigned long long q = sh >= 0 ? m >> (sh < 63 ? sh : 63) : m << ((-sh) & 63);
+    q = ex == 0 ? 0ull : q;
+    v[k] = (b >> 63) ? -(long long)q : (long long)q;
+  }
+  E[col] = e;
+}
+
 // ---------------------------------------------------------------------------
 // Plan
 // ---------------------------------------------------------------------------
@@ -1445,10 +1584,14 @@ struct l2c_gpu_plan {
   // of 16 rows (leaf down), and the far-field blocks (built on the first batched
   // call, per direction)
   unsigned *oz_lu = nullptr, *oz_tu = nullptr, *oz_td = nullptr, *oz_ld = nullptr;
-  int *oz_lue = nullptr, *oz_tue = nullptr, *oz_tde = nullptr, *oz_lde = nullptr;
+  int *oz_lum = nullptr, *oz_tum = nullptr, *oz_tdm = nullptr;  // producer metadata
+  int *oz_lde = nullptr;                                        // leaf-down row exponents
   int oz_kc = 0, oz_npass = 0;  // leaf-up k8 chunks, leaf-down passes
   unsigned *oz_far[2] = {nullptr, nullptr};
-  int *oz_fare[2] = {nullptr, nullptr};
+  int *oz_farm[2] = {nullptr, nullptr};
+  // column exponents of w and c (mixed form: w, c hold column-format integers)
+  int *wE = nullptr, *cE = nullptr;
+  size_t cap_wE = 0, cap_cE = 0;
   // captured launch sequences, keyed by the call's shape and pointers
   struct GraphEntry {
     size_t dir, count, dist, stride;
@@ -1594,6 +1737,18 @@ bool ensure_scratch(l2c_gpu_plan *p, size_t count) {
   if (p->L > 0) {
     if (!grow(&p->w, &cw, need * 2 * p->slots * M) || !grow(&p->c, &cc, need * 2 * p->slots * M))
       return false;
+    if (p->mixed) {
+      // column exponents: ints, sized in doubles for grow()
+      const size_t ne = (need * 2 * p->slots + 1) / 2;
+      double *we = reinterpret_cast<double *>(p->wE), *ce = reinterpret_cast<double *>(p->cE);
+      size_t cwe = p->cap_wE, cce = p->cap_cE;
+      const bool ok = grow(&we, &cwe, ne) && grow(&ce, &cce, ne);
+      p->wE = reinterpret_cast<int *>(we);
+      p->cE = reinterpret_cast<int *>(ce);
+      p->cap_wE = cwe;
+      p->cap_cE = cce;
+      if (!ok) return false;
+    }
   }
   p->cap_vec = need;
   return true;
@@ -1768,30 +1923,20 @@ Geo make_geo(const l2c_gpu_plan *p, size_t count, size_t dist, size_t stride) {
 
 // Far field of the mixed form: leaf, tree and far-field products on tensor
 // cores (the far-field blocks only when the batch gives each block at least 8
-// right-hand sides; single vectors keep the FP64 block products).
+// right-hand sides; single vectors keep the FP64 block products, on doubles
+// converted from and back to the column format in place).
 template <int KC>
 void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStream_t st) {
   const long long tiles = g.count * ((g.K + 15) / 16);
   const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
-  k_mz_leaf_up<KC><<<grid, 32 * MXW, mz_leaf_up_smem(KC), st>>>(x, p->w, p->oz_lu, p->oz_lue, g);
-}
-
-// Down-sweep levels above lt have too few columns to fill the GPU with
-// tensor-core tiles, whose latency then dominates: they run in FP64 in the
-// shared-memory top kernel (one CTA per vector and parity), the levels from lt
-// on tensor cores.  (Upward, the FP64 top kernel measured slower than the
-// tensor-core levels it would replace.)
-constexpr int MZ_TOP_MAX = 6;
-int mixed_top_level(long long L, long long count) {
-  int lt = 0;
-  while (lt + 1 <= L - 2 && lt < MZ_TOP_MAX && count * 2 * ((4LL << lt) - 2) < 16 * 600) lt++;
-  return lt;
+  k_mz_leaf_up<KC><<<grid, 32 * MXW, mz_leaf_up_smem(KC), st>>>(
+      x, reinterpret_cast<long long *>(p->w), p->wE, p->oz_lu, p->oz_lum, g);
 }
 
 bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir, const Geo &g,
                       cudaStream_t st) {
   const int c2l = dir == 1;
-  const int lt = mixed_top_level(g.L, g.count);
+  long long *w = reinterpret_cast<long long *>(p->w), *c = reinterpret_cast<long long *>(p->c);
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
     switch (p->oz_kc) {
@@ -1812,33 +1957,36 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
       const long long np = (long long)slots_at((size_t)l);
       const long long tiles = (g.count * 2 * np + 15) / 16;
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
-      k_mz_tree_up<<<grid, 32 * MXW, OZ_TREE_UP_SMEM, st>>>(p->w, p->oz_tu, p->oz_tue, g,
-                                               2 * (long long)blocks_before((size_t)l),
-                                               2 * (long long)blocks_before((size_t)l + 1), np);
+      k_mz_tree_up<<<grid, 32 * MXW, OZ_TREE_UP_SMEM, st>>>(
+          w, p->wE, p->oz_tu, p->oz_tum, g, 2 * (long long)blocks_before((size_t)l),
+          2 * (long long)blocks_before((size_t)l + 1), np);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
   {
-    PhaseScope ps(p, L2C_PHASE_FAR, 1);
-    if (g.count >= 4 && p->oz_far[dir] != nullptr) {
+    const bool tc = g.count >= 4 && p->oz_far[dir] != nullptr;
+    PhaseScope ps(p, L2C_PHASE_FAR, tc ? 1 : 3);
+    if (tc) {
       const dim3 grid((unsigned)p->Nb, (unsigned)((2 * g.count + OZ_FAR_COLS - 1) / OZ_FAR_COLS));
-      k_mz_far<<<grid, 32 * MXW, OZ_FAR_SMEM, st>>>(p->w, p->c, p->oz_far[dir], p->oz_fare[dir], g);
+      k_mz_far<<<grid, 32 * MXW, OZ_FAR_SMEM, st>>>(w, p->wE, c, p->cE, p->oz_far[dir],
+                                                    p->oz_farm[dir], g);
     } else {
-      const long long n = g.count * 2 * (long long)p->Nb * M;
+      const long long ncol = g.count * 2 * g.slots, n = g.count * 2 * (long long)p->Nb * M;
+      k_oz_cols_to_double<<<blocks_for(ncol, 256), 256, 0, st>>>(w, p->wE, ncol);
       k_far<<<blocks_for(n, 256), 256, 0, st>>>(p->A[dir], p->w, p->c, g, (long long)p->Nb);
+      k_oz_cols_from_double<<<blocks_for(ncol, 256), 256, 0, st>>>(p->c, p->cE, ncol);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
   {
-    PhaseScope ps(p, L2C_PHASE_TREE_DOWN, (size_t)(g.L - 1 - lt) + (lt > 0 ? 1 : 0));
-    if (lt > 0) k_down_top<<<(unsigned)(g.count * 2), 32 * M, top_smem(lt), st>>>(p->c, g, lt);
-    for (long long l = lt; l + 1 < g.L; l++) {
+    PhaseScope ps(p, L2C_PHASE_TREE_DOWN, (size_t)(g.L - 1));
+    for (long long l = 0; l + 1 < g.L; l++) {
       const long long np = (long long)slots_at((size_t)l);
       const long long tiles = (g.count * 2 * np + 15) / 16;
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
-      k_mz_tree_down<<<grid, 32 * MXW, OZ_TREE_DOWN_SMEM, st>>>(p->c, p->oz_td, p->oz_tde, g,
-                                                 2 * (long long)blocks_before((size_t)l),
-                                                 2 * (long long)blocks_before((size_t)l + 1), np);
+      k_mz_tree_down<<<grid, 32 * MXW, OZ_TREE_DOWN_SMEM, st>>>(
+          c, p->cE, p->oz_td, p->oz_tdm, g, 2 * (long long)blocks_before((size_t)l),
+          2 * (long long)blocks_before((size_t)l + 1), np);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -1849,7 +1997,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     const long long tiles = g.count * ((g.K + 15) / 16);
     const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
     k_mz_leaf_down<<<grid, 32 * MXW, mz_leaf_down_smem(g.s, p->oz_npass), st>>>(
-        p->c, p->y, out, p->oz_ld, p->oz_lde, g, c2l, p->oz_npass);
+        c, p->cE, p->y, out, p->oz_ld, p->oz_lde, g, c2l, p->oz_npass);
     if (tail > 0) k_mx_tail<<<blocks_for(tail, 256), 256, 0, st>>>(p->y, out, g, c2l);
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -1861,12 +2009,12 @@ bool ensure_mixed_far(l2c_gpu_plan *p, size_t dir) {
   if (p->oz_far[dir]) return true;
   const size_t nb = p->Nb;
   if (cudaMalloc(&p->oz_far[dir], nb * OZ_FAR_WORDS * sizeof(unsigned)) != cudaSuccess ||
-      cudaMalloc(&p->oz_fare[dir], nb * 2 * OZ_ROWS * sizeof(int)) != cudaSuccess) {
+      cudaMalloc(&p->oz_farm[dir], nb * 2 * OZ_META * sizeof(int)) != cudaSuccess) {
     set_err("cudaMalloc of the mixed-form far-field fragments failed");
     return false;
   }
-  k_oz_pack_far<<<blocks_for((long long)(nb * 2 * OZ_ROWS), 128), 128, 0, p->stream>>>(
-      p->A[dir], (long long)nb, p->oz_far[dir], p->oz_fare[dir]);
+  k_oz_pack_far<<<blocks_for((long long)(nb * 2), 128), 128, 0, p->stream>>>(
+      p->A[dir], (long long)nb, p->oz_far[dir], p->oz_farm[dir]);
   return cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(p->stream) == cudaSuccess;
 }
 
@@ -2150,6 +2298,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
       const int wlu = oz_words(OZ_NT, KC), wtu = oz_words(OZ_NT, 5), wtd = oz_words(OZ_NT, 3);
       std::vector<unsigned> lu(2 * wlu), tu(wtu), td(2 * wtd), ld(2 * npass * OZ_LD_WORDS);
       std::vector<int> lue(2 * OZ_ROWS), tue(OZ_ROWS), tde(2 * OZ_ROWS), lde(2 * npass * 16);
+      std::vector<int> lum(2 * OZ_META), tum(OZ_META), tdm(2 * OZ_META);
       for (int sg = 0; sg < 2; sg++) {
         const double *Ts = T.data() + sg * s * M;  // T_sg(i, m) = Ts[i * M + m]
         for (int n = 0; n < OZ_ROWS; n++)          // leaf up: P[m][i] = T_sg(i, m)
@@ -2170,6 +2319,11 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
           oz_pack_row(RowOf{Bd.data() + (ch * M + (n < M ? n : 0)) * M, 0, 1}, n < M, n, M, OZ_NT,
                       3, td.data() + ch * wtd, tde.data() + ch * OZ_ROWS);
       }
+      for (int k = 0; k < 2; k++) {
+        oz_meta(lue.data() + k * OZ_ROWS, lum.data() + k * OZ_META);
+        oz_meta(tde.data() + k * OZ_ROWS, tdm.data() + k * OZ_META);
+      }
+      oz_meta(tue.data(), tum.data());
       auto upload = [&](auto **dst, const auto &v) -> cudaError_t {
         const size_t bytes = v.size() * sizeof(v[0]);
         cudaError_t e = cudaMalloc(dst, bytes);
@@ -2177,11 +2331,11 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
         return e;
       };
       PCK(upload(&p->oz_lu, lu));
-      PCK(upload(&p->oz_lue, lue));
+      PCK(upload(&p->oz_lum, lum));
       PCK(upload(&p->oz_tu, tu));
-      PCK(upload(&p->oz_tue, tue));
+      PCK(upload(&p->oz_tum, tum));
       PCK(upload(&p->oz_td, td));
-      PCK(upload(&p->oz_tde, tde));
+      PCK(upload(&p->oz_tdm, tdm));
       PCK(upload(&p->oz_ld, ld));
       PCK(upload(&p->oz_lde, lde));
       // kernels whose shared memory can pass the 48 KB default
@@ -2193,8 +2347,6 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
                                (int)OZ_TREE_DOWN_SMEM));
       PCK(cudaFuncSetAttribute(k_mz_far, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)OZ_FAR_SMEM));
-      PCK(cudaFuncSetAttribute(k_down_top, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)top_smem(MZ_TOP_MAX)));
 #define L2C_MZ_ATTR(kc)                                                                      \
   PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                            (int)mz_leaf_up_smem(kc)));
@@ -2236,9 +2388,9 @@ void l2c_gpu_plan_destroy(l2c_gpu_plan *p) {
                     p->st_in, p->st_out, p->Wnear[0], p->Wnear[1]};
   for (double *b : bufs)
     if (b) cudaFree(b);
-  void *obufs[] = {p->oz_lu,  p->oz_tu,     p->oz_td,     p->oz_ld,      p->oz_lue,
-                   p->oz_tue, p->oz_tde,    p->oz_lde,    p->oz_far[0],  p->oz_far[1],
-                   p->oz_fare[0], p->oz_fare[1]};
+  void *obufs[] = {p->oz_lu,     p->oz_tu,     p->oz_td,      p->oz_ld,      p->oz_lum,
+                   p->oz_tum,    p->oz_tdm,    p->oz_lde,     p->oz_far[0],  p->oz_far[1],
+                   p->oz_farm[0], p->oz_farm[1], p->wE,        p->cE};
   for (void *b : obufs)
     if (b) cudaFree(b);
   if (p->stream) cudaStreamDestroy(p->stream);

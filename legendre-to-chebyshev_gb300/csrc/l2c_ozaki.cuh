@@ -263,6 +263,45 @@ __device__ __forceinline__ void stage_fix(double *Xs, int ld, int ks, int K, int
   if (h == 0) Es[r] = e;
   __syncwarp();
 }
+
+// Column format of intermediate coefficient vectors: a column of values x_k
+// is stored as integers V_k and one exponent E, x_k = V_k 2^(E - VBITS),
+// |V_k| < 2^VBITS (E is arbitrary, and every V_k zero, for a zero column).
+// Products leave their result in this form without rounding to double, and
+// the next product re-normalises the column once (stage_cols).
+constexpr int VBITS = 62;
+
+// V 2^s (s >= 0) or floor(V 2^s) (s < 0), s clamped to [-63, 63].
+__device__ __forceinline__ long long shift_s64(long long V, int s) {
+  return s >= 0 ? V << (s < 63 ? s : 63) : V >> (-s < 63 ? -s : 63);
+}
+
+// In-place staging of 16 columns held in column format: column r of the tile
+// is Xs[r * ld + k], k < K; entries k < K0 belong to a stored column with
+// exponent Ea[r], entries k >= K0 to one with exponent Eb[r].  On return the
+// same places hold the offset words Y of the column on a common scale with
+// the largest entry at full precision (entries K <= k < KP hold RBAL) and
+// Es[r] the column exponent (every |x_k| < 2^Es[r]).  Two lanes per column.
+__device__ __forceinline__ void stage_cols(long long *Xs, int ld, int K, int K0, int KP,
+                                           const int *Ea, const int *Eb, int *Es) {
+  const int lane = threadIdx.x & 31, r = lane >> 1, h = lane & 1;
+  long long *row = Xs + r * ld;
+  const int ea = Ea[r], eb = K0 < K ? Eb[r] : ea, ec = max(ea, eb);
+  const int sa = -(ec - ea), sb = -(ec - eb);
+  unsigned long long m = 0;
+  for (int k = h; k < K; k += 2) {
+    const long long v = shift_s64(row[k], k < K0 ? sa : sb);
+    row[k] = v;
+    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    m = a > m ? a : m;
+  }
+  const unsigned long long mo = __shfl_xor_sync(0xffffffffu, m, 1);
+  m = mo > m ? mo : m;
+  const int B = 64 - __clzll((long long)m);  // bits of the largest |V| (0 for a zero column)
+  for (int k = h; k < KP; k += 2) row[k] = k < K ? shift_s64(row[k], FRAC - B) + RBAL : RBAL;
+  if (h == 0) Es[r] = ec - VBITS + B;
+  __syncwarp();
+}
 #endif
 
 }  // namespace l2c_oz
