@@ -206,6 +206,15 @@ __global__ void __launch_bounds__(MM) k_assemble_A(const double *__restrict__ f0
 // w, c: 2 parities x 2 N_b slots x M).
 // ---------------------------------------------------------------------------
 
+// n 2^e as a double, exactly (0 <= n < 2^53), by bit construction: integer
+// instructions instead of a conversion on the FP64 pipe.
+__device__ __forceinline__ double dyadic(unsigned long long n, int e) {
+  const int lz = __clzll((long long)n);
+  const unsigned long long frac = (n << ((lz + 1) & 63)) >> 12;  // bits after the leading one
+  const unsigned long long bits = ((unsigned long long)(1023 + 63 - lz + e) << 52) | frac;
+  return n == 0 ? 0.0 : __longlong_as_double((long long)bits);
+}
+
 struct Geo {
   long long N, s, h, nL, L, K, slots, leaf_base, count, dist, stride;
 };
@@ -218,7 +227,7 @@ struct Geo {
 __device__ __forceinline__ void gather_item(const double *__restrict__ in, double *__restrict__ x,
                                             long long stride, int c2l, long long j) {
   double u = in[j * stride];
-  if (c2l && j >= 2) u = u * (double)j;
+  if (c2l && j >= 2) u = u * dyadic((unsigned long long)j, 0);
   x[j] = u;
 }
 
@@ -845,7 +854,7 @@ __device__ __forceinline__ void leaf_down_item(const double *__restrict__ cv,
     val = val * TWO_OVER_PI;
     if (j == 0) val = val * 0.5;
   } else {
-    val = val * ((double)j + 0.5);
+    val = val * dyadic(2 * (unsigned long long)j + 1, -1);  // j + 1/2
   }
   outv[j * g.stride] = val;
 }
@@ -877,13 +886,13 @@ __device__ __forceinline__ void direct_item(const double *u, double *b,
     if (i == 0) val = val / 2;
     if (i * g.stride >= g.N) val = b[i * g.stride] + val;
   } else {
-    const double vi = (i == 0) ? u[0] : u[i * g.stride] * (double)i;
+    const double vi = (i == 0) ? u[0] : u[i * g.stride] * dyadic((unsigned long long)i, 0);
     val = (SQRT_PI * vi) * an[i];
     for (long long k = 1; i + 2 * k < g.N; k++) {
       const long long n = i + 2 * k;
-      val = fma(-(dn[k] * an[k + i]), u[n * g.stride] * (double)n, val);
+      val = fma(-(dn[k] * an[k + i]), u[n * g.stride] * dyadic((unsigned long long)n, 0), val);
     }
-    val = val * ((double)i + 0.5);
+    val = val * dyadic(2 * (unsigned long long)i + 1, -1);  // i + 1/2
   }
   if (g.stride > 1 && (i % g.stride) != 0) b[i] = 0.0;  // contiguous zeroing of [0, N)
   b[i * g.stride] = val;
@@ -1487,7 +1496,7 @@ __global__ void __launch_bounds__(32 * MXW)
         val = val * TWO_OVER_PI;
         if (j == 0) val = val * 0.5;
       } else {
-        val = val * ((double)j + 0.5);
+        val = val * dyadic(2 * (unsigned long long)j + 1, -1);  // j + 1/2
       }
       out[v * g.dist + j * g.stride] = val;
     }
@@ -1511,7 +1520,7 @@ __global__ void k_mx_tail(const double *__restrict__ y, double *out, Geo g, int 
     val = val * TWO_OVER_PI;
     if (j == 0) val = val * 0.5;
   } else {
-    val = val * ((double)j + 0.5);
+    val = val * dyadic(2 * (unsigned long long)j + 1, -1);  // j + 1/2
   }
   out[v * g.dist + j * g.stride] = val;
 }

@@ -8,10 +8,11 @@
 //  * every row of the constant factor P and every column of the data factor Q
 //    shares a power-of-two scale 2^E with |x| < 2^E for all its entries;
 //  * X = trunc(x 2^(53-E)) (|X| < 2^53) is written with six base-2^9 digits,
-//    X = sum_p d_p 2^(9(6-p)): the five low digits are balanced, d_p in
-//    [-256, 255] (the 9-bit fields of Y = X + R, R = 256 sum_{k<5} 2^(9k), less
-//    256), the top digit is d_1 = floor(Y / 2^45) in [-256, 256].  Every digit
-//    is an exact FP16 value;
+//    X = sum_p d_p 2^(9(6-p)), d_p = u_p - 256 where u_p are the bit fields of
+//    Y = X + R, R = 256 sum_{k<6} 2^(9k) (0 <= Y < 2^55): nine bits for the five
+//    low digits (d_p in [-256, 255]), ten for the top one (d_1 in [-256, 256]).
+//    Every digit is an exact FP16 value, and two of them are formed at once as
+//    the FP16 pair (1024 + u_a, 1024 + u_b) - (1280, 1280) from their bit fields;
 //  * digit products with p + q <= DMAX = 7 are summed per diagonal d = p + q on
 //    the tensor cores (mma.sync m16n8k16 / m16n8k8, FP16 in, FP32 accumulate).
 //    A diagonal holds at most 6 digit pairs of magnitude <= 2^16, so for
@@ -39,7 +40,7 @@ constexpr int DMAX = 7;    // digit pairs p + q <= DMAX
 constexpr int NDIAG = DMAX - 1;
 constexpr int KMAX = 40;   // terms per exact accumulation
 constexpr int EXP_ZERO = -4000;
-constexpr long long RBAL = 0x100804020100ll;  // 256 in each of the five low digits
+constexpr long long RBAL = 0x20100804020100ll;  // 256 in every digit field
 
 // Smallest E with |x| < 2^E (EXP_ZERO for zero and subnormals).
 __host__ __device__ inline int exp_bound(double x) {
@@ -63,7 +64,7 @@ __host__ __device__ inline long long fixbal(double x, int E) {
 
 // Digit p (1 = most significant) of Y as an exact float.
 __host__ __device__ inline float digit_f(long long Y, int p) {
-  if (p == 1) return (float)(Y >> 45);
+  if (p == 1) return (float)(int)((Y >> 45) & 1023) - 256.0f;
   return (float)(int)((Y >> (9 * (SLICES - p))) & 511) - 256.0f;
 }
 
@@ -78,25 +79,28 @@ __host__ __device__ inline unsigned half_bits(int v) {
 }
 
 #ifdef __CUDACC__
-// Y split into two 27-bit words: hi holds digits 1..3 (signed), lo digits 4..6.
+// Y split into two words: hi holds the fields of digits 1..3 (ten, nine and
+// nine bits), lo those of digits 4..6.
 struct Ysplit {
-  int hi;
-  unsigned lo;
+  unsigned hi, lo;
 };
 __device__ __forceinline__ Ysplit ysplit(long long Y) {
-  return {(int)(Y >> 27), (unsigned)Y & 0x7FFFFFFu};
+  return {(unsigned)((unsigned long long)Y >> 27), (unsigned)Y & 0x7FFFFFFu};
 }
-// Digit p of a split word as a float, by exponent-field arithmetic (exact).
+// Digit P of two values as one FP16 pair (value a in the low half): the two
+// fields are placed in the mantissas of FP16 1024 + u (exact for u < 1024)
+// and 1280 is subtracted from both halves.
 template <int P>
-__device__ __forceinline__ float dig(const Ysplit &y) {
-  if (P == 1) return __fsub_rn(__int_as_float(0x4B400000 + (y.hi >> 18)), 12582912.0f);
+__device__ __forceinline__ unsigned dig2(const Ysplit &a, const Ysplit &b) {
   constexpr int sh = P <= 3 ? 9 * (3 - P) : 9 * (6 - P);
-  const unsigned w = P <= 3 ? (unsigned)y.hi : y.lo;
-  return __fsub_rn(__uint_as_float(((w >> sh) & 511u) | 0x4B000000u), 8388864.0f);
-}
-__device__ __forceinline__ unsigned pack2(float lo, float hi) {
-  __half2 h = __floats2half2_rn(lo, hi);
-  return *reinterpret_cast<unsigned *>(&h);
+  constexpr unsigned mask = P == 1 ? 0x3FFu : 0x1FFu;
+  const unsigned wa = P <= 3 ? a.hi : a.lo, wb = P <= 3 ? b.hi : b.lo;
+  const unsigned lo = (wa >> sh) & mask;
+  const unsigned hi = (sh <= 16 ? wb << (16 - sh) : wb >> (sh - 16)) & (mask << 16);
+  const unsigned w = lo | hi | 0x64006400u;
+  const __half2 r = __hsub2(*reinterpret_cast<const __half2 *>(&w),
+                            __halves2half2(__ushort_as_half(0x6500), __ushort_as_half(0x6500)));
+  return *reinterpret_cast<const unsigned *>(&r);
 }
 
 __device__ __forceinline__ void mma16(float (&c)[4], const unsigned (&a)[4], unsigned b0,
@@ -209,11 +213,11 @@ __device__ __forceinline__ void mma_tile(const unsigned *__restrict__ Pf, const 
       const Ysplit y4 = ysplit(r0[(8 * c + 8) * ks]), y5 = ysplit(r0[(8 * c + 9) * ks]);
       const Ysplit y6 = ysplit(r1[(8 * c + 8) * ks]), y7 = ysplit(r1[(8 * c + 9) * ks]);
       unsigned a[SLICES][4];
-#define L2C_OZ_SLICE(P)                                      \
-  a[P - 1][0] = pack2(dig<P>(y0), dig<P>(y1));               \
-  a[P - 1][1] = pack2(dig<P>(y2), dig<P>(y3));               \
-  a[P - 1][2] = pack2(dig<P>(y4), dig<P>(y5));               \
-  a[P - 1][3] = pack2(dig<P>(y6), dig<P>(y7));
+#define L2C_OZ_SLICE(P)           \
+  a[P - 1][0] = dig2<P>(y0, y1);  \
+  a[P - 1][1] = dig2<P>(y2, y3);  \
+  a[P - 1][2] = dig2<P>(y4, y5);  \
+  a[P - 1][3] = dig2<P>(y6, y7);
       L2C_OZ_SLICE(1) L2C_OZ_SLICE(2) L2C_OZ_SLICE(3)
       L2C_OZ_SLICE(4) L2C_OZ_SLICE(5) L2C_OZ_SLICE(6)
 #undef L2C_OZ_SLICE
@@ -230,9 +234,9 @@ __device__ __forceinline__ void mma_tile(const unsigned *__restrict__ Pf, const 
       const Ysplit y0 = ysplit(r0[(8 * c) * ks]), y1 = ysplit(r0[(8 * c + 1) * ks]);
       const Ysplit y2 = ysplit(r1[(8 * c) * ks]), y3 = ysplit(r1[(8 * c + 1) * ks]);
       unsigned a[SLICES][2];
-#define L2C_OZ_SLICE(P)                          \
-  a[P - 1][0] = pack2(dig<P>(y0), dig<P>(y1));   \
-  a[P - 1][1] = pack2(dig<P>(y2), dig<P>(y3));
+#define L2C_OZ_SLICE(P)           \
+  a[P - 1][0] = dig2<P>(y0, y1);  \
+  a[P - 1][1] = dig2<P>(y2, y3);
       L2C_OZ_SLICE(1) L2C_OZ_SLICE(2) L2C_OZ_SLICE(3)
       L2C_OZ_SLICE(4) L2C_OZ_SLICE(5) L2C_OZ_SLICE(6)
 #undef L2C_OZ_SLICE
