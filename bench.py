@@ -10,11 +10,13 @@ coefficients transformed (2 N per step) per second.
 
   value   device-resident: inputs already in HBM, plan built, outputs zeroed
           before each step; L2 flushed (256 MiB write) between steps; CUDA
-          events on the plan's stream around each step.
+          events on the plan's stream around each step; each call replays the
+          CUDA graph the library captured for its shape (as any repeated call).
   e2e     the same through execute() with host (pinned) buffers: host->device
           copies of input and output (execute accumulates into its output, as
           the reference), kernels, device->host copy of the result, per step.
-  roofline  dominant kernel (by time) timed live with per-phase CUDA events;
+  roofline  dominant kernel (by time) timed live with per-phase CUDA events in
+          a second pass of the same K steps (direct launches, no graph);
           FP64 work in the reference's own flop count; peak = FP64 DGEMM
           throughput measured in this run (cuBLAS, float64 matmul).
   cpu_baseline  the oracle port of the reference algorithm (OpenMP, all host
@@ -523,12 +525,8 @@ def main():
     plan.synchronize()
     torch.cuda.synchronize()
 
-    # ---- timed region (device resident), per-phase CUDA events on ----
-    if not ragged:
-        abi.l2c_gpu_profile(plan._gpu, 1)
-        launches0 = abi.l2c_gpu_launch_count(plan._gpu)
-    else:
-        launches0 = plan.launch_count()
+    # ---- timed region (device resident, each call shape replayed as a CUDA graph) ----
+    launches0 = abi.l2c_gpu_launch_count(plan._gpu) if not ragged else plan.launch_count()
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
@@ -540,10 +538,18 @@ def main():
     barrier()
     t_wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
-    ms_step = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+    launches = (abi.l2c_gpu_launch_count(plan._gpu) if not ragged else plan.launch_count()) - launches0
+    ms_step = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / len(evs))
+    value = wl.coefs_per_step * world / (ms_step * 1e-3)
+
+    # ---- the same K steps again with per-phase CUDA events (direct launches) ----
     phases = {}
+    ms_prof = None
     if not ragged:
-        launches = abi.l2c_gpu_launch_count(plan._gpu) - launches0
+        abi.l2c_gpu_profile(plan._gpu, 1)
+        evs = [step() for _ in range(args.steps)]
+        plan.synchronize()
+        ms_prof = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / len(evs))
         pms = (ctypes.c_double * 8)()
         pl = (ctypes.c_size_t * 8)()
         abi.l2c_gpu_profile_read(plan._gpu, pms, pl)
@@ -551,15 +557,6 @@ def main():
         names = ["gather", "near", "leaf_up", "tree_up", "far", "tree_down", "leaf_down", "direct"]
         phases = {names[i]: {"ms_per_step": pms[i] / args.steps,
                              "launches_per_step": pl[i] / args.steps} for i in range(8) if pl[i]}
-    else:
-        launches = plan.launch_count() - launches0
-    ms_step = max_over_ranks(ms_step)
-    value = wl.coefs_per_step * world / (ms_step * 1e-3)
-
-    # ---- graph-replay timing without per-phase events (reported beside value) ----
-    evs = [step() for _ in range(args.steps)]
-    plan.synchronize()
-    ms_graph = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / len(evs))
 
     # ---- e2e through execute() with pinned host buffers ----
     hbuf = {"u": torch.from_numpy(np.ascontiguousarray(wl.u)).pin_memory()}
@@ -621,7 +618,7 @@ def main():
         "clocks": clk,
         "roofline": roof,
         "phases": phases,
-        "ms_per_step_graph_replay": ms_graph,
+        "ms_per_step_phase_profiled": ms_prof,
         "fp64_ref_tflops_whole_step": total_flops / (ms_step * 1e-3) / 1e12,
         "wall_s_timed_region": t_wall,
         "plan": {"L": L, "s": s, "Nb": plan.Nb} if not ragged else {"vectors": count},
