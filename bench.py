@@ -129,6 +129,50 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def rank_env():
+    """(rank, world size, local rank) from the torchrun environment."""
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class Ranks:
+    """Barrier and max-over-ranks for the timed region; one process per GPU.
+    Every rank runs the same workload on its own device (independent replicas,
+    no data-path collective), so the whole-job value is the coefficients of all
+    ranks over the slowest rank's time (aggregate_value)."""
+
+    def __init__(self, world, backend, device):
+        self.world, self.device = world, device
+        if world > 1:
+            import torch.distributed as dist
+
+            if backend == "nccl":
+                dist.init_process_group("nccl", device_id=device)
+            else:
+                dist.init_process_group(backend)
+
+    def barrier(self):
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([x], device=self.device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+
+def aggregate_value(coefs_per_step_per_rank, world, ms_max):
+    """Whole-job coefficients per second: every rank's coefficients over the max time."""
+    return coefs_per_step_per_rank * world / (ms_max * 1e-3)
+
+
 def measured_fp64_peak(torch, dev):
     """FP64 DGEMM throughput (TFLOP/s), best of 5, cuBLAS float64 matmul."""
     n = 4096
@@ -452,30 +496,11 @@ def main():
 
     import torch
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank, world, local = rank_env()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=dev)
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        import torch.distributed as dist
-
-        t = torch.tensor([x], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    ranks = Ranks(world, "nccl", dev)
+    barrier, max_over_ranks = ranks.barrier, ranks.max
 
     sys.path.insert(0, PKG)
     import importlib.util
@@ -540,7 +565,7 @@ def main():
     clk = clocks.stop()
     launches = (abi.l2c_gpu_launch_count(plan._gpu) if not ragged else plan.launch_count()) - launches0
     ms_step = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / len(evs))
-    value = wl.coefs_per_step * world / (ms_step * 1e-3)
+    value = aggregate_value(wl.coefs_per_step, world, ms_step)
 
     # ---- the same K steps again with per-phase CUDA events (direct launches) ----
     phases = {}
