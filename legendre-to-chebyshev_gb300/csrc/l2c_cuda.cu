@@ -351,15 +351,18 @@ __global__ void __launch_bounds__(256, VB == 1 ? 5 : VB == 2 ? 4 : 2)
            const double *__restrict__ dn, const double *__restrict__ W, Geo g, int c2l,
            long long jbeg) {
   const long long ntile = (g.N - jbeg + blockDim.x - 1) / blockDim.x;
-  const long long tile = blockIdx.x % ntile, vg = blockIdx.x / ntile;
-  const long long j = jbeg + tile * blockDim.x + threadIdx.x;
-  if (j >= g.N) return;
-  const long long v0 = vg * VB;
-  double res[VB];
-  near_sums<VB>(x + v0 * g.N + j, g.N, a, an, dn, W, g, c2l, j, res);
+  const long long nblk = ntile * (g.count / VB);
+  for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x) {  // grid may be smaller
+    const long long tile = blk % ntile, vg = blk / ntile;
+    const long long j = jbeg + tile * blockDim.x + threadIdx.x;
+    if (j >= g.N) continue;
+    const long long v0 = vg * VB;
+    double res[VB];
+    near_sums<VB>(x + v0 * g.N + j, g.N, a, an, dn, W, g, c2l, j, res);
 #pragma unroll
-  for (int u = 0; u < VB; u++)
-    y[(v0 + u) * g.N + j] = out[(v0 + u) * g.dist + j * g.stride] + res[u];
+    for (int u = 0; u < VB; u++)
+      y[(v0 + u) * g.N + j] = out[(v0 + u) * g.dist + j * g.stride] + res[u];
+  }
 }
 
 // Band of the blocks b < nL-1 in pairs: one thread forms outputs i and h-1-i
@@ -376,55 +379,56 @@ __global__ void __launch_bounds__(256, VB <= 2 ? 3 : 2)
                 const double *__restrict__ a, const double *__restrict__ an,
                 const double *__restrict__ dn, const double *__restrict__ W, Geo g, int c2l) {
   const long long half = g.h >> 1, npair = (g.nL - 1) * half, jlast = (g.nL - 1) * g.h;
-  const long long per_vg = npair + (g.N - jlast);
-  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long vg = idx / per_vg;
-  if (vg * VB >= g.count) return;
-  const long long r = idx - vg * per_vg;
-  if (r >= npair) {
-    const long long j = jlast + (r - npair), v0 = vg * VB;
-    double res[VB];
-    near_sums<VB>(x + v0 * g.N + j, g.N, a, an, dn, W, g, c2l, j, res);
+  const long long per_vg = npair + (g.N - jlast), nitem = per_vg * (g.count / VB);
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < nitem;
+       idx += (long long)gridDim.x * blockDim.x) {  // the grid may be smaller than the work
+    const long long vg = idx / per_vg;
+    const long long r = idx - vg * per_vg;
+    if (r >= npair) {
+      const long long j = jlast + (r - npair), v0 = vg * VB;
+      double res[VB];
+      near_sums<VB>(x + v0 * g.N + j, g.N, a, an, dn, W, g, c2l, j, res);
 #pragma unroll
-    for (int u = 0; u < VB; u++)
-      y[(v0 + u) * g.N + j] = out[(v0 + u) * g.dist + j * g.stride] + res[u];
-    return;
-  }
-  const long long b = r / half, i = r - b * half;
-  const long long jA = b * g.h + i, jB = b * g.h + g.h - 1 - i, lim = (b + 2) * g.h;
-  const long long nkA = (lim - jA + 1) >> 1, total = nkA + ((lim - jB + 1) >> 1);
-  const double *xv = x + vg * VB * g.N;
-  const double *Wb = W ? W + b * (3 * g.s * g.s + g.s) : nullptr;
-  double acc[VB], resA[VB];
-#pragma unroll
-  for (int u = 0; u < VB; u++) acc[u] = resA[u] = 0.0;
-  for (long long t = 0; t < total; t++) {
-    const bool second = t >= nkA;
-    const long long j = second ? jB : jA, k = second ? t - nkA : t;
-    double wt;
-    if (Wb) {
-      // offset of term k in the block's table: k h for k < s, then rows of 2h - 2k'
-      const long long off =
-          k < g.s ? k * g.h : 4 * g.s * k - k * k + k - g.s * g.s - g.s;
-      wt = Wb[off + (j - b * g.h)];
-    } else {
-      wt = near_weight(c2l, k, j, a, an, dn);
+      for (int u = 0; u < VB; u++)
+        y[(v0 + u) * g.N + j] = out[(v0 + u) * g.dist + j * g.stride] + res[u];
+      continue;
     }
+    const long long b = r / half, i = r - b * half;
+    const long long jA = b * g.h + i, jB = b * g.h + g.h - 1 - i, lim = (b + 2) * g.h;
+    const long long nkA = (lim - jA + 1) >> 1, total = nkA + ((lim - jB + 1) >> 1);
+    const double *xv = x + vg * VB * g.N;
+    const double *Wb = W ? W + b * (3 * g.s * g.s + g.s) : nullptr;
+    double acc[VB], resA[VB];
 #pragma unroll
-    for (int u = 0; u < VB; u++) acc[u] = fma(wt, xv[u * g.N + j + 2 * k], acc[u]);
-    if (t == nkA - 1) {
+    for (int u = 0; u < VB; u++) acc[u] = resA[u] = 0.0;
+    for (long long t = 0; t < total; t++) {
+      const bool second = t >= nkA;
+      const long long j = second ? jB : jA, k = second ? t - nkA : t;
+      double wt;
+      if (Wb) {
+        // offset of term k in the block's table: k h for k < s, then rows of 2h - 2k'
+        const long long off =
+            k < g.s ? k * g.h : 4 * g.s * k - k * k + k - g.s * g.s - g.s;
+        wt = Wb[off + (j - b * g.h)];
+      } else {
+        wt = near_weight(c2l, k, j, a, an, dn);
+      }
 #pragma unroll
-      for (int u = 0; u < VB; u++) {
-        resA[u] = acc[u];
-        acc[u] = 0.0;
+      for (int u = 0; u < VB; u++) acc[u] = fma(wt, xv[u * g.N + j + 2 * k], acc[u]);
+      if (t == nkA - 1) {
+#pragma unroll
+        for (int u = 0; u < VB; u++) {
+          resA[u] = acc[u];
+          acc[u] = 0.0;
+        }
       }
     }
-  }
-  const long long v0 = vg * VB;
+    const long long v0 = vg * VB;
 #pragma unroll
-  for (int u = 0; u < VB; u++) {
-    y[(v0 + u) * g.N + jA] = out[(v0 + u) * g.dist + jA * g.stride] + resA[u];
-    y[(v0 + u) * g.N + jB] = out[(v0 + u) * g.dist + jB * g.stride] + acc[u];
+    for (int u = 0; u < VB; u++) {
+      y[(v0 + u) * g.N + jA] = out[(v0 + u) * g.dist + jA * g.stride] + resA[u];
+      y[(v0 + u) * g.N + jB] = out[(v0 + u) * g.dist + jB * g.stride] + acc[u];
+    }
   }
 }
 
@@ -1615,6 +1619,8 @@ struct l2c_gpu_plan {
   size_t use_clock = 0;
   bool use_graphs = true;
   bool overlap = false;  // near field on stream2 beside the far-field chain
+  unsigned near_ctas = 0;  // band grid cap while it overlaps (0: no cap)
+  int near_vb = 8;         // band vectors per thread while it overlaps
   int near_pair = -1;    // band in pairs: 1 always, 0 never, -1 by leaf size
   // launch accounting and optional per-phase CUDA-event timing
   size_t launches = 0;
@@ -1859,11 +1865,12 @@ cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t 
 // thread, then the remainder.
 cudaError_t launch_near(const double *x, const double *out, double *y, const double *a,
                         const double *an, const double *dn, const double *W, Geo g, int c2l,
-                        cudaStream_t st, bool pair) {
+                        cudaStream_t st, bool pair, unsigned max_ctas, int max_vb) {
   long long v = 0;
   while (v < g.count) {
     const long long left = g.count - v;
-    const int vb = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+    int vb = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+    vb = std::min(vb, max_vb);
     const long long groups = left / vb;
     Geo gg = g;
     gg.count = groups * vb;
@@ -1871,7 +1878,8 @@ cudaError_t launch_near(const double *x, const double *out, double *y, const dou
     const double *os = out + v * g.dist;
     double *ys = y + v * g.N;
     if (!pair) {
-      const unsigned grid = (unsigned)(((g.N + 255) / 256) * groups);
+      unsigned grid = (unsigned)(((g.N + 255) / 256) * groups);
+      if (max_ctas) grid = std::min(grid, max_ctas);
       switch (vb) {
         case 8: k_near<8><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l, 0); break;
         case 4: k_near<4><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l, 0); break;
@@ -1885,7 +1893,8 @@ cudaError_t launch_near(const double *x, const double *out, double *y, const dou
     }
     // blocks b < nL-1 in pairs and the last (ragged) block one output per thread
     const long long per_vg = (g.nL - 1) * (g.h / 2) + (g.N - (g.nL - 1) * g.h);
-    const unsigned grid = (unsigned)((groups * per_vg + 255) / 256);
+    unsigned grid = (unsigned)((groups * per_vg + 255) / 256);
+    if (max_ctas) grid = std::min(grid, max_ctas);
     switch (vb) {
       case 8: k_near_pair<8><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
       case 4: k_near_pair<4><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
@@ -1903,11 +1912,11 @@ cudaError_t launch_near(const double *x, const double *out, double *y, const dou
 // leaves: one warp spans a whole block).
 bool near_pair(const l2c_gpu_plan *p) { return p->near_pair >= 0 ? p->near_pair == 1 : p->s <= 16; }
 
-size_t near_launch_count(size_t count) {
+size_t near_launch_count(size_t count, int max_vb) {
   size_t n = 0, v = 0;
   while (v < count) {
     const size_t left = count - v;
-    const size_t vb = left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1;
+    const size_t vb = std::min<size_t>(left >= 8 ? 8 : left >= 4 ? 4 : left >= 2 ? 2 : 1, max_vb);
     v += (left / vb) * vb;
     n++;
   }
@@ -2053,8 +2062,8 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   const double *W = p->Wnear[dir];
   if (near_only) {
     {
-      PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count));
-      CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, st, near_pair(p)));
+      PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, p->overlap ? p->near_vb : 8));
+      CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, st, near_pair(p), 0, 8));
     }
     Geo g0 = g;
     g0.K = 0;
@@ -2069,8 +2078,9 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaStreamWaitEvent(st2, p->ev_fork, 0));
   }
   {
-    PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count), stn);
-    CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, near_pair(p)));
+    PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, p->overlap ? p->near_vb : 8), stn);
+    CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, near_pair(p),
+                    p->overlap ? p->near_ctas : 0, p->overlap ? p->near_vb : 8));
   }
   if (p->overlap) CK(cudaEventRecord(p->ev_join, st2));
   if (p->mixed) return launch_mixed_far(p, x, out, dir, g, st) ? 1 : 0;
@@ -2215,6 +2225,8 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   PCK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
   if (const char *env = std::getenv("L2C_NO_GRAPHS")) p->use_graphs = env[0] == '0';
   if (const char *env = std::getenv("L2C_OVERLAP")) p->overlap = env[0] == '1';
+  if (const char *env = std::getenv("L2C_NEAR_CTAS")) p->near_ctas = (unsigned)std::atoi(env);
+  if (const char *env = std::getenv("L2C_NEAR_VB")) p->near_vb = std::max(1, std::atoi(env));
   if (const char *env = std::getenv("L2C_NEAR_PAIR")) p->near_pair = env[0] == '1' ? 1 : 0;
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
@@ -2282,6 +2294,12 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
         return fail();
       }
       p->mixed = true;
+      // The band is FP64-pipe work and the tensor-core products are integer and
+      // tensor-pipe work, so they can share SMs: the band runs on the second
+      // stream beside the far-field chain (measured: 1.48 -> 1.41 ms per step
+      // for 256 x 16384; capping the band's grid or its vectors per thread to
+      // leave more room for the far-field kernels measured slower).
+      if (!std::getenv("L2C_OVERLAP")) p->overlap = true;
       const int KC = (int)((s + 7) / 8), npass = (int)((s + 15) / 16);
       p->oz_kc = KC;
       p->oz_npass = npass;
