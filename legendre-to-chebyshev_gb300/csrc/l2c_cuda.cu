@@ -1532,35 +1532,41 @@ __global__ void k_mx_tail(const double *__restrict__ y, double *out, Geo g, int 
 // Column format <-> doubles, in place, one thread per 18-coefficient column
 // (for the FP64 far-field kernel of single vectors).
 __global__ void k_oz_cols_to_double(long long *V, const int *__restrict__ E, long long ncol) {
-  const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (col >= ncol) return;
-  const int e = E[col] - l2c_oz::VBITS;
-  long long *v = V + col * M;
-  double *d = reinterpret_cast<double *>(v);
-  for (int k = 0; k < M; k++) {
-    const long long t = v[k];
-    d[k] = l2c_oz::to_double(t, e);  // t 2^e, rounded once
-  }
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;  // one element
+  if (idx >= ncol * M) return;
+  const long long t = V[idx];
+  reinterpret_cast<double *>(V)[idx] = l2c_oz::to_double(t, E[idx / M] - l2c_oz::VBITS);
 }
 
-__global__ void k_oz_cols_from_double(double *D, int *__restrict__ E, long long ncol) {
-  const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (col >= ncol) return;
-  double *d = D + col * M;
-  long long *v = reinterpret_cast<long long *>(d);
-  int e = l2c_oz::EXP_ZERO;
-  for (int k = 0; k < M; k++) e = max(e, l2c_oz::exp_bound(d[k]));
-  for (int k = 0; k < M; k++) {
-    // |d| < 2^e: V = trunc(d 2^(VBITS - e)), |V| < 2^VBITS
-    const unsigned long long b = (unsigned long long)__double_as_longlong(d[k]);
-    const int ex = (int)((b >> 52) & 0x7FF);
-    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = e - l2c_oz::VBITS + 1075 - ex;  // >= -(VBITS - 53)
-    unsigned long long q = sh >= 0 ? m >> (sh < 63 ? sh : 63) : m << ((-sh) & 63);
-    q = ex == 0 ? 0ull : q;
-    v[k] = (b >> 63) ? -(long long)q : (long long)q;
+// 16 columns per CTA of 16 * 18 threads: coalesced loads, one exponent per column.
+constexpr int OZ_CONV_COLS = 16;
+__global__ void __launch_bounds__(OZ_CONV_COLS * M)
+    k_oz_cols_from_double(double *D, int *__restrict__ E, long long ncol) {
+  __shared__ int ex[OZ_CONV_COLS * M];
+  __shared__ int ecol[OZ_CONV_COLS];
+  const long long idx = blockIdx.x * (long long)(OZ_CONV_COLS * M) + threadIdx.x;
+  const bool live = idx < ncol * M;
+  const double d = live ? D[idx] : 0.0;
+  ex[threadIdx.x] = l2c_oz::exp_bound(d);
+  __syncthreads();
+  if (threadIdx.x < OZ_CONV_COLS) {
+    int e = l2c_oz::EXP_ZERO;
+    for (int k = 0; k < M; k++) e = max(e, ex[threadIdx.x * M + k]);
+    ecol[threadIdx.x] = e;
+    const long long col = blockIdx.x * (long long)OZ_CONV_COLS + threadIdx.x;
+    if (col < ncol) E[col] = e;
   }
-  E[col] = e;
+  __syncthreads();
+  if (!live) return;
+  // |d| < 2^e: V = trunc(d 2^(VBITS - e)), |V| < 2^VBITS
+  const int e = ecol[threadIdx.x / M];
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int exb = (int)((b >> 52) & 0x7FF);
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int sh = e - l2c_oz::VBITS + 1075 - exb;  // >= -(VBITS - 53)
+  unsigned long long q = sh >= 0 ? m >> (sh < 63 ? sh : 63) : m << ((-sh) & 63);
+  q = exb == 0 ? 0ull : q;
+  reinterpret_cast<long long *>(D)[idx] = (b >> 63) ? -(long long)q : (long long)q;
 }
 
 // ---------------------------------------------------------------------------
@@ -1990,9 +1996,10 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
                                                     p->oz_farm[dir], g);
     } else {
       const long long ncol = g.count * 2 * g.slots, n = g.count * 2 * (long long)p->Nb * M;
-      k_oz_cols_to_double<<<blocks_for(ncol, 256), 256, 0, st>>>(w, p->wE, ncol);
+      k_oz_cols_to_double<<<blocks_for(ncol * M, 256), 256, 0, st>>>(w, p->wE, ncol);
       k_far<<<blocks_for(n, 256), 256, 0, st>>>(p->A[dir], p->w, p->c, g, (long long)p->Nb);
-      k_oz_cols_from_double<<<blocks_for(ncol, 256), 256, 0, st>>>(p->c, p->cE, ncol);
+      k_oz_cols_from_double<<<blocks_for(ncol, OZ_CONV_COLS), OZ_CONV_COLS * M, 0, st>>>(
+          p->c, p->cE, ncol);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
