@@ -1124,8 +1124,8 @@ __global__ void __launch_bounds__(32 * MXW)
   auto work = [&](long long tile, int buf) {
     const long long v = tile / tpv, node0 = (tile - v * tpv) * 16;
     double *X = Xw + buf * 16 * XLD;
-    l2c_oz::stage_fix(X, XLD, 2, (int)g.s, 8 * KC, Es);
-    l2c_oz::stage_fix(X + 1, XLD, 2, (int)g.s, 8 * KC, Es + 16);
+    l2c_oz::stage_fix<8 * KC>(X, XLD, 2, (int)g.s, Es);
+    l2c_oz::stage_fix<8 * KC>(X + 1, XLD, 2, (int)g.s, Es + 16);
     const long long *Ys = reinterpret_cast<const long long *>(X);
 #pragma unroll 1
     for (int sg = 0; sg < 2; sg++) {
@@ -1203,7 +1203,7 @@ __global__ void __launch_bounds__(32 * MXW)
   auto work = [&](long long tile, int buf) {
     long long *X = Xw + buf * 16 * OZ_TLD;
     const int *Ex = sEx + buf * 32;
-    l2c_oz::stage_cols(X, OZ_TLD, 2 * M, M, 40, Ex, Ex + 16, Es);
+    l2c_oz::stage_cols<2 * M, M, 40>(X, OZ_TLD, Ex, Ex + 16, Es);
     long long T[OZ_NT][4];
     oz_tile_T<OZ_NT, 5>(sP, X, OZ_TLD, 1, T);
     const long long c0 = tile * 16;
@@ -1296,7 +1296,7 @@ __global__ void __launch_bounds__(32 * MXW)
     const long long *C = Cw + buf * 16 * 2 * M;
     const long long *B = sB + buf * 32;
     const int *Ex = sEx + buf * 48;
-    l2c_oz::stage_cols(X, OZ_CLD, M, M, 24, Ex, Ex, Es);
+    l2c_oz::stage_cols<M, M, 24>(X, OZ_CLD, Ex, Ex, Es);
     const long long cb0 = B[16 + gq], cb1 = B[16 + gq + 8];
 #pragma unroll 1
     for (int ch = 0; ch < 2; ch++) {
@@ -1383,7 +1383,7 @@ __global__ void __launch_bounds__(32 * MXW)
   auto work = [&](long long tile, int buf) {
     long long *X = Xw + buf * 16 * OZ_TLD;
     const int *Ex = sEx + buf * 32;
-    l2c_oz::stage_cols(X, OZ_TLD, 2 * M, M, OZ_TLD, Ex, Ex + 16, Es);
+    l2c_oz::stage_cols<2 * M, M, OZ_TLD>(X, OZ_TLD, Ex, Ex + 16, Es);
     const long long cA = c0 + tile * 16 + gq, cB = cA + 8;
 #pragma unroll 1
     for (int part = 0; part < 2; part++) {
@@ -1473,7 +1473,7 @@ __global__ void __launch_bounds__(32 * MXW)
 #pragma unroll 1
     for (int sg = 0; sg < 2; sg++) {
       long long *X = Xw + (buf * 2 + sg) * 16 * OZ_CLD;
-      l2c_oz::stage_cols(X, OZ_CLD, M, M, 24, Ex + 16 * sg, Ex + 16 * sg, Ec + 16 * sg);
+      l2c_oz::stage_cols<M, M, 24>(X, OZ_CLD, Ex + 16 * sg, Ex + 16 * sg, Ec + 16 * sg);
 #pragma unroll 1
       for (int ps = 0; ps < npass; ps++) {
         long long T[2][4];

@@ -255,15 +255,28 @@ __device__ __forceinline__ void mma_tile(const unsigned *__restrict__ Pf, const 
 // Column exponents and offset words of a staged tile, in place: Xs holds the
 // raw doubles of 16 columns (column r at Xs[r * ld + k * ks], k < K); on
 // return the same places hold the offset words Y, entries K <= k < KP hold
-// RBAL, and Es[r] the column exponent.  Two lanes per column.
-__device__ __forceinline__ void stage_fix(double *Xs, int ld, int ks, int K, int KP, int *Es) {
+// RBAL, and Es[r] the column exponent.  Two lanes per column, each keeping its
+// KP/2 entries in registers between the two passes.
+template <int KP>
+__device__ __forceinline__ void stage_fix(double *Xs, int ld, int ks, int K, int *Es) {
+  constexpr int NV = (KP + 1) / 2;
   const int lane = threadIdx.x & 31, r = lane >> 1, h = lane & 1;
   double *row = Xs + r * ld;
+  double v[NV];
   int e = EXP_ZERO;
-  for (int k = h; k < K; k += 2) e = max(e, exp_bound(row[k * ks]));
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    const int k = 2 * i + h;
+    v[i] = k < K ? row[k * ks] : 0.0;
+    e = max(e, exp_bound(v[i]));
+  }
   e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
   long long *yr = reinterpret_cast<long long *>(row);
-  for (int k = h; k < KP; k += 2) yr[k * ks] = k < K ? fixbal(row[k * ks], e) : RBAL;
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    const int k = 2 * i + h;
+    if (k < KP) yr[k * ks] = k < K ? fixbal(v[i], e) : RBAL;
+  }
   if (h == 0) Es[r] = e;
   __syncwarp();
 }
@@ -285,24 +298,34 @@ __device__ __forceinline__ long long shift_s64(long long V, int s) {
 // exponent Ea[r], entries k >= K0 to one with exponent Eb[r].  On return the
 // same places hold the offset words Y of the column on a common scale with
 // the largest entry at full precision (entries K <= k < KP hold RBAL) and
-// Es[r] the column exponent (every |x_k| < 2^Es[r]).  Two lanes per column.
-__device__ __forceinline__ void stage_cols(long long *Xs, int ld, int K, int K0, int KP,
-                                           const int *Ea, const int *Eb, int *Es) {
+// Es[r] the column exponent (every |x_k| < 2^Es[r]).  Two lanes per column;
+// each lane keeps its (KP+1)/2 entries in registers between the two passes.
+template <int K, int K0, int KP>
+__device__ __forceinline__ void stage_cols(long long *Xs, int ld, const int *Ea, const int *Eb,
+                                           int *Es) {
+  constexpr int NV = (KP + 1) / 2;
   const int lane = threadIdx.x & 31, r = lane >> 1, h = lane & 1;
   long long *row = Xs + r * ld;
   const int ea = Ea[r], eb = K0 < K ? Eb[r] : ea, ec = max(ea, eb);
   const int sa = -(ec - ea), sb = -(ec - eb);
+  long long v[NV];
   unsigned long long m = 0;
-  for (int k = h; k < K; k += 2) {
-    const long long v = shift_s64(row[k], k < K0 ? sa : sb);
-    row[k] = v;
-    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    const int k = 2 * i + h;
+    v[i] = k < K ? shift_s64(row[k], k < K0 ? sa : sb) : 0;
+    const unsigned long long a = v[i] < 0 ? 0ull - (unsigned long long)v[i] : (unsigned long long)v[i];
     m = a > m ? a : m;
   }
   const unsigned long long mo = __shfl_xor_sync(0xffffffffu, m, 1);
   m = mo > m ? mo : m;
   const int B = 64 - __clzll((long long)m);  // bits of the largest |V| (0 for a zero column)
-  for (int k = h; k < KP; k += 2) row[k] = k < K ? shift_s64(row[k], FRAC - B) + RBAL : RBAL;
+  const int sh = FRAC - B;                   // in [-9, 53]
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    const int k = 2 * i + h;
+    if (k < KP) row[k] = (k < K ? (sh >= 0 ? v[i] << sh : v[i] >> -sh) : 0) + RBAL;
+  }
   if (h == 0) Es[r] = ec - VBITS + B;
   __syncwarp();
 }
