@@ -1624,7 +1624,7 @@ struct l2c_gpu_plan {
   std::vector<GraphEntry> graphs;
   size_t use_clock = 0;
   bool use_graphs = true;
-  bool overlap = false;  // near field on stream2 beside the far-field chain
+  int overlap = -1;  // band on stream2 beside the far-field chain: 1 / 0 forced, -1 auto
   unsigned near_ctas = 0;  // band grid cap while it overlaps (0: no cap)
   int near_vb = 8;         // band vectors per thread while it overlaps
   int near_pair = -1;    // band in pairs: 1 always, 0 never, -1 by leaf size
@@ -1958,7 +1958,7 @@ void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStrea
 }
 
 bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir, const Geo &g,
-                      cudaStream_t st) {
+                      cudaStream_t st, bool ov) {
   const int c2l = dir == 1;
   long long *w = reinterpret_cast<long long *>(p->w), *c = reinterpret_cast<long long *>(p->c);
   {
@@ -2015,7 +2015,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
-  if (p->overlap && cudaStreamWaitEvent(st, p->ev_join, 0) != cudaSuccess) return false;
+  if (ov && cudaStreamWaitEvent(st, p->ev_join, 0) != cudaSuccess) return false;
   {
     const long long tail = g.count * (g.N - g.K * g.h);
     PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, tail > 0 ? 2 : 1);
@@ -2069,7 +2069,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   const double *W = p->Wnear[dir];
   if (near_only) {
     {
-      PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, p->overlap ? p->near_vb : 8));
+      PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, 8));
       CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, st, near_pair(p), 0, 8));
     }
     Geo g0 = g;
@@ -2079,18 +2079,24 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaGetLastError());
     return 1;
   }
-  cudaStream_t stn = p->overlap ? st2 : st;
-  if (p->overlap) {
+  // The band runs on the second stream beside the far-field chain for batches
+  // and mixed plans (it then overlaps latency-bound tree levels, and in the
+  // mixed form the tensor-core products, which use other pipes: measured 4 %
+  // faster for 4096 x 1024 plain, 5 % for 256 x 16384 mixed; no change for a
+  // single plain vector, whose far field also runs on the FP64 pipe).
+  const bool ov = p->overlap >= 0 ? p->overlap == 1 : (p->mixed || count > 1);
+  cudaStream_t stn = ov ? st2 : st;
+  if (ov) {
     CK(cudaEventRecord(p->ev_fork, st));
     CK(cudaStreamWaitEvent(st2, p->ev_fork, 0));
   }
   {
-    PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, p->overlap ? p->near_vb : 8), stn);
+    PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, ov ? p->near_vb : 8), stn);
     CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, near_pair(p),
-                    p->overlap ? p->near_ctas : 0, p->overlap ? p->near_vb : 8));
+                    ov ? p->near_ctas : 0, ov ? p->near_vb : 8));
   }
-  if (p->overlap) CK(cudaEventRecord(p->ev_join, st2));
-  if (p->mixed) return launch_mixed_far(p, x, out, dir, g, st) ? 1 : 0;
+  if (ov) CK(cudaEventRecord(p->ev_join, st2));
+  if (p->mixed) return launch_mixed_far(p, x, out, dir, g, st, ov) ? 1 : 0;
   const long long leaf_threads = g.count * g.K * 2 * M;
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
@@ -2112,7 +2118,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     PhaseScope ps(p, L2C_PHASE_TREE_DOWN, tree_launches(tp, p->L));
     CK(sweep_down(p->c, g, tp, st));
   }
-  if (p->overlap) CK(cudaStreamWaitEvent(st, p->ev_join, 0));
+  if (ov) CK(cudaStreamWaitEvent(st, p->ev_join, 0));
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
     k_leaf_down<<<blocks_for(total, 256), 256, 0, st>>>(p->c, p->T, p->y, out, g, c2l);
@@ -2231,7 +2237,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   PCK(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
   PCK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
   if (const char *env = std::getenv("L2C_NO_GRAPHS")) p->use_graphs = env[0] == '0';
-  if (const char *env = std::getenv("L2C_OVERLAP")) p->overlap = env[0] == '1';
+  if (const char *env = std::getenv("L2C_OVERLAP")) p->overlap = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_NEAR_CTAS")) p->near_ctas = (unsigned)std::atoi(env);
   if (const char *env = std::getenv("L2C_NEAR_VB")) p->near_vb = std::max(1, std::atoi(env));
   if (const char *env = std::getenv("L2C_NEAR_PAIR")) p->near_pair = env[0] == '1' ? 1 : 0;
@@ -2301,12 +2307,6 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
         return fail();
       }
       p->mixed = true;
-      // The band is FP64-pipe work and the tensor-core products are integer and
-      // tensor-pipe work, so they can share SMs: the band runs on the second
-      // stream beside the far-field chain (measured: 1.48 -> 1.41 ms per step
-      // for 256 x 16384; capping the band's grid or its vectors per thread to
-      // leave more room for the far-field kernels measured slower).
-      if (!std::getenv("L2C_OVERLAP")) p->overlap = true;
       const int KC = (int)((s + 7) / 8), npass = (int)((s + 15) / 16);
       p->oz_kc = KC;
       p->oz_npass = npass;
