@@ -1040,23 +1040,23 @@ __device__ __forceinline__ void oz_tile_loop(long long first, long long step, lo
 
 // Combined integers of a 16 x (NT*8) tile; K past KMAX is split into two exact
 // accumulations whose integers are added.
-template <int NT, int KC>
+template <int NT, int KC, int QMAX = l2c_oz::SLICES>
 __device__ __forceinline__ void oz_tile_T(const unsigned *Pf, const long long *Ys, int yld, int ks,
                                           long long (&T)[NT][4]) {
   float acc[l2c_oz::NDIAG][NT][4];
   if constexpr (KC <= l2c_oz::KMAX / 8) {
-    l2c_oz::mma_tile<NT, KC>(Pf, Ys, yld, ks, acc);
+    l2c_oz::mma_tile<NT, KC, 0, KC, QMAX>(Pf, Ys, yld, ks, acc);
 #pragma unroll
     for (int nt = 0; nt < NT; nt++)
 #pragma unroll
       for (int e = 0; e < 4; e++) T[nt][e] = l2c_oz::combine(acc, nt, e);
   } else {
-    l2c_oz::mma_tile<NT, KC, 0, KC / 2>(Pf, Ys, yld, ks, acc);
+    l2c_oz::mma_tile<NT, KC, 0, KC / 2, QMAX>(Pf, Ys, yld, ks, acc);
 #pragma unroll
     for (int nt = 0; nt < NT; nt++)
 #pragma unroll
       for (int e = 0; e < 4; e++) T[nt][e] = l2c_oz::combine(acc, nt, e);
-    l2c_oz::mma_tile<NT, KC, KC / 2, KC>(Pf, Ys, yld, ks, acc);
+    l2c_oz::mma_tile<NT, KC, KC / 2, KC, QMAX>(Pf, Ys, yld, ks, acc);
 #pragma unroll
     for (int nt = 0; nt < NT; nt++)
 #pragma unroll
@@ -1162,6 +1162,7 @@ size_t mz_leaf_up_smem(int KC) {
 // Up: parent slot j of level l from child slots 2j+2, 2j+3 of level l+1
 // (36 contiguous coefficients, two stored columns), P = [B | B'] (18 x 36).
 constexpr int OZ_TREE_UP_WORDS = oz_words(OZ_NT, 5);
+template <int QMAX>
 __global__ void __launch_bounds__(32 * MXW)
     k_mz_tree_up(long long *w, int *wE, const unsigned *__restrict__ Pf,
                  const int *__restrict__ Pm, Geo g, long long parent_base, long long child_base,
@@ -1205,7 +1206,7 @@ __global__ void __launch_bounds__(32 * MXW)
     const int *Ex = sEx + buf * 32;
     l2c_oz::stage_cols<2 * M, M, 40>(X, OZ_TLD, Ex, Ex + 16, Es);
     long long T[OZ_NT][4];
-    oz_tile_T<OZ_NT, 5>(sP, X, OZ_TLD, 1, T);
+    oz_tile_T<OZ_NT, 5, QMAX>(sP, X, OZ_TLD, 1, T);
     const long long c0 = tile * 16;
     auto dst = [&](int r) -> long long {  // parent slot index, -1: none
       const long long col = c0 + r;
@@ -1241,6 +1242,7 @@ constexpr size_t OZ_TREE_UP_SMEM = (size_t)(OZ_TREE_UP_WORDS + OZ_META + MXW * (
 // product are added as integers on the coarser of their two scales, one bit
 // above the larger exponent.
 constexpr int OZ_TREE_DOWN_WORDS = 2 * oz_words(OZ_NT, 3);
+template <int QMAX>
 __global__ void __launch_bounds__(32 * MXW)
     k_mz_tree_down(long long *c, int *cE, const unsigned *__restrict__ Pf,
                    const int *__restrict__ Pm, Geo g, long long parent_base, long long child_base,
@@ -1301,7 +1303,7 @@ __global__ void __launch_bounds__(32 * MXW)
 #pragma unroll 1
     for (int ch = 0; ch < 2; ch++) {
       long long T[OZ_NT][4];
-      oz_tile_T<OZ_NT, 3>(sP + ch * NW, X, OZ_CLD, 1, T);
+      oz_tile_T<OZ_NT, 3, QMAX>(sP + ch * NW, X, OZ_CLD, 1, T);
       const int *meta = sM + ch * OZ_META;
       // per tile row r: product exponent, child exponent, sum exponent
       int ep[2], ek[2], es[2];
@@ -1606,6 +1608,7 @@ struct l2c_gpu_plan {
   int *oz_lum = nullptr, *oz_tum = nullptr, *oz_tdm = nullptr;  // producer metadata
   int *oz_lde = nullptr;                                        // leaf-down row exponents
   int oz_kc = 0, oz_npass = 0;  // leaf-up k8 chunks, leaf-down passes
+  int oz_tree_q = l2c_oz::SLICES;  // digit slices of the transfer matrices that are not zero
   unsigned *oz_far[2] = {nullptr, nullptr};
   int *oz_farm[2] = {nullptr, nullptr};
   // column exponents of w and c (mixed form: w, c hold column-format integers)
@@ -1981,9 +1984,14 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
       const long long np = (long long)slots_at((size_t)l);
       const long long tiles = (g.count * 2 * np + 15) / 16;
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
-      k_mz_tree_up<<<grid, 32 * MXW, OZ_TREE_UP_SMEM, st>>>(
-          w, p->wE, p->oz_tu, p->oz_tum, g, 2 * (long long)blocks_before((size_t)l),
-          2 * (long long)blocks_before((size_t)l + 1), np);
+      const long long pb = 2 * (long long)blocks_before((size_t)l);
+      const long long cb = 2 * (long long)blocks_before((size_t)l + 1);
+      if (p->oz_tree_q == 2)
+        k_mz_tree_up<2><<<grid, 32 * MXW, OZ_TREE_UP_SMEM, st>>>(w, p->wE, p->oz_tu, p->oz_tum,
+                                                                 g, pb, cb, np);
+      else
+        k_mz_tree_up<l2c_oz::SLICES><<<grid, 32 * MXW, OZ_TREE_UP_SMEM, st>>>(
+            w, p->wE, p->oz_tu, p->oz_tum, g, pb, cb, np);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -2009,9 +2017,14 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
       const long long np = (long long)slots_at((size_t)l);
       const long long tiles = (g.count * 2 * np + 15) / 16;
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
-      k_mz_tree_down<<<grid, 32 * MXW, OZ_TREE_DOWN_SMEM, st>>>(
-          c, p->cE, p->oz_td, p->oz_tdm, g, 2 * (long long)blocks_before((size_t)l),
-          2 * (long long)blocks_before((size_t)l + 1), np);
+      const long long pb = 2 * (long long)blocks_before((size_t)l);
+      const long long cb = 2 * (long long)blocks_before((size_t)l + 1);
+      if (p->oz_tree_q == 2)
+        k_mz_tree_down<2><<<grid, 32 * MXW, OZ_TREE_DOWN_SMEM, st>>>(c, p->cE, p->oz_td,
+                                                                     p->oz_tdm, g, pb, cb, np);
+      else
+        k_mz_tree_down<l2c_oz::SLICES><<<grid, 32 * MXW, OZ_TREE_DOWN_SMEM, st>>>(
+            c, p->cE, p->oz_td, p->oz_tdm, g, pb, cb, np);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -2358,6 +2371,15 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
         oz_meta(tde.data() + k * OZ_ROWS, tdm.data() + k * OZ_META);
       }
       oz_meta(tue.data(), tum.data());
+      // The transfer matrices are dyadic rationals with at most 17 significant
+      // bits below each row's largest entry, so only their two leading digit
+      // slices are non-zero: the tree kernels then form 11 of the 21 products.
+      {
+        const int qu = l2c_oz::used_slices(tu.data(), OZ_NT, 5);
+        const int qd = std::max(l2c_oz::used_slices(td.data(), OZ_NT, 3),
+                                l2c_oz::used_slices(td.data() + wtd, OZ_NT, 3));
+        p->oz_tree_q = std::max(qu, qd) <= 2 ? 2 : l2c_oz::SLICES;
+      }
       auto upload = [&](auto **dst, const auto &v) -> cudaError_t {
         const size_t bytes = v.size() * sizeof(v[0]);
         cudaError_t e = cudaMalloc(dst, bytes);
@@ -2375,10 +2397,14 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
       // kernels whose shared memory can pass the 48 KB default
       PCK(cudaFuncSetAttribute(k_mz_leaf_down, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)mz_leaf_down_smem(4 * 16, 4)));
-      PCK(cudaFuncSetAttribute(k_mz_tree_up, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      PCK(cudaFuncSetAttribute(k_mz_tree_up<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)OZ_TREE_UP_SMEM));
-      PCK(cudaFuncSetAttribute(k_mz_tree_down, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      PCK(cudaFuncSetAttribute(k_mz_tree_up<l2c_oz::SLICES>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_TREE_UP_SMEM));
+      PCK(cudaFuncSetAttribute(k_mz_tree_down<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)OZ_TREE_DOWN_SMEM));
+      PCK(cudaFuncSetAttribute(k_mz_tree_down<l2c_oz::SLICES>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_TREE_DOWN_SMEM));
       PCK(cudaFuncSetAttribute(k_mz_far, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)OZ_FAR_SMEM));
 #define L2C_MZ_ATTR(kc)                                                                      \

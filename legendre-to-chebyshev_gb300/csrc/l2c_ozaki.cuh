@@ -142,6 +142,18 @@ __host__ __device__ inline int frag_index(int q, int nt, int c, int lane, int NT
   return base + (c & ~1) * 32 + 2 * lane + (c & 1);
 }
 
+// Number of leading digit slices of a packed matrix that hold non-zero words
+// (the later ones are zero for every row and k).
+inline int used_slices(const unsigned *frag, int NT, int KC) {
+  int used = 0;
+  for (int q = 1; q <= SLICES; q++)
+    for (int nt = 0; nt < NT; nt++)
+      for (int c = 0; c < KC; c++)
+        for (int lane = 0; lane < 32; lane++)
+          if (frag[frag_index(q, nt, c, lane, NT, KC)] != 0u) used = q;
+  return used;
+}
+
 #ifdef __CUDACC__
 // T 2^e rounded to nearest-even as a double (T a signed 64-bit integer).
 // Branch-free, so the independent outputs of a lane interleave.
@@ -190,10 +202,11 @@ __device__ __forceinline__ long long combine(const float (&acc)[NDIAG][NT][4], i
 // tile) in Ys.  C1 - C0 <= 5 (K <= 40) keeps the accumulation exact.
 //   Ys : offset words Y of the 16 columns, column r at Ys[r * yld + k * ks],
 //        k < 8 C1 (entries past the true K are RBAL, i.e. zero);
-//   Pf : the fragment words of P^T (frag_index layout with KC chunks).
+//   Pf : the fragment words of P^T (frag_index layout with KC chunks); its
+//        slices past QMAX must be zero (they are not read).
 // Output element (nt, e) of the lane is data column (lane >> 2) + 8 (e >> 1)
 // and output row 8 nt + 2 (lane & 3) + (e & 1).
-template <int NT, int KC, int C0 = 0, int C1 = KC>
+template <int NT, int KC, int C0 = 0, int C1 = KC, int QMAX = SLICES>
 __device__ __forceinline__ void mma_tile(const unsigned *__restrict__ Pf, const long long *Ys,
                                          int yld, int ks, float (&acc)[NDIAG][NT][4]) {
   static_assert(C1 - C0 <= KMAX / 8, "accumulation would not be exact");
@@ -222,7 +235,7 @@ __device__ __forceinline__ void mma_tile(const unsigned *__restrict__ Pf, const 
       L2C_OZ_SLICE(4) L2C_OZ_SLICE(5) L2C_OZ_SLICE(6)
 #undef L2C_OZ_SLICE
 #pragma unroll
-      for (int q = 1; q <= SLICES; q++)
+      for (int q = 1; q <= QMAX; q++)
 #pragma unroll
         for (int nt = 0; nt < NT; nt++) {
           const uint2 b =
@@ -241,7 +254,7 @@ __device__ __forceinline__ void mma_tile(const unsigned *__restrict__ Pf, const 
       L2C_OZ_SLICE(4) L2C_OZ_SLICE(5) L2C_OZ_SLICE(6)
 #undef L2C_OZ_SLICE
 #pragma unroll
-      for (int q = 1; q <= SLICES; q++)
+      for (int q = 1; q <= QMAX; q++)
 #pragma unroll
         for (int nt = 0; nt < NT; nt++) {
           const unsigned b = Pf[frag_index(q, nt, c, lane, NT, KC)];
