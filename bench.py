@@ -408,6 +408,25 @@ def run_mixed(args):
         phases = {names[i]: round(pms[i] / nprof, 4) for i in range(8) if pl[i]}
         return ms, [o.cpu().numpy() for o in outs], launches, phases
 
+    def time_e2e(plan):
+        """The same step through execute_batched() with pinned host buffers
+        (input and zeroed outputs copied in, results copied back, per call)."""
+        hu = torch.from_numpy(np.ascontiguousarray(wl.u)).pin_memory()
+        ho = [torch.zeros_like(hu).pin_memory(), torch.zeros_like(hu).pin_memory()]
+        ts = []
+        for it in range(args.warmup + min(args.steps, 20)):
+            ho[0].zero_()
+            ho[1].zero_()
+            t0 = time.perf_counter()
+            plan.execute_batched(hu, ho[0], 0, count, N, 1)
+            plan.execute_batched(hu, ho[1], 1, count, N, 1)
+            if it >= args.warmup:
+                ts.append(time.perf_counter() - t0)
+        st = sum(ts) / len(ts)
+        nbytes = 8 * wl.u.size
+        return {"value": 2 * count * N / st, "unit": "coef/s", "h2d_bytes_per_step": 4 * nbytes,
+                "d2h_bytes_per_step": 2 * nbytes, "ms_per_step": st * 1e3}
+
     clocks = ClockSampler(0)
     clocks.start()
     results = {}
@@ -419,6 +438,8 @@ def run_mixed(args):
                          "value": 2 * count * N / (ms * 1e-3), "launches": launches,
                          "phases_ms_per_step": phases,
                          "flops": plan.flops(0) + plan.flops(1), "outs": outs}
+        if mixed:
+            e2e_mixed = time_e2e(plan)
         plan.close()
     clk = clocks.stop()
     # accuracy against the oracle port (FP64) on the same inputs
@@ -459,6 +480,8 @@ def run_mixed(args):
         "best_plain": best_plain[1],
         "clocks": clk,
         "fp64_peak_tflops_measured": peak,
+        "gpu_launches": int(mixed["launches"]),
+        "e2e": e2e_mixed,
     }
     print(json.dumps(line))
     return 0
@@ -620,9 +643,17 @@ def main():
         avg_ms = phases["near"]["ms_per_step"] / phases["near"]["launches_per_step"]
         flops_per_launch = nf / launches_near
         achieved = flops_per_launch / (avg_ms * 1e-3) / 1e12
+        # DRAM bytes per band launch from one ncu capture of this same command
+        # (dram__bytes_read.sum + dram__bytes_write.sum, mean of the L2C and C2L
+        # launches); other workloads were not captured.
+        captured = (wl.name == "single" and N == 1 << 20 and maxs == 64
+                    and args.precompute == 0)
         roof = {"bound": "tensor", "pipe": "fp64", "kernel": "k_near (near-field band)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": None,
+                "traffic": 25.2e6 + 256 if captured else None,
+                "traffic_unit": "DRAM bytes per launch",
+                "traffic_source": "profiles/k_near_single_N1048576.md" if captured else None,
+                "algorithmic_bytes_per_launch": 24 * N * count,
                 "peak_source": "FP64 DGEMM measured in this run (cuBLAS float64 matmul 4096^3)",
                 "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_ms,
                 "note": "reference flop count of directM/directL (3 per band term); a term "
