@@ -67,6 +67,37 @@ __constant__ double c_binom_upper[NTRI] = L2C_BINOM_UPPER_INIT;
 __constant__ double c_xj[M];       // cos((i + 1/2) pi / M), host libm values
 __constant__ double c_dct[M * M];  // cos(pi k (n + 1/2) / M), [k][n]
 
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization may start while the previous kernel on its stream is still
+// running; pdl_wait() returns once that kernel has completed and its memory
+// writes are visible (immediately when there is no such kernel), so a kernel
+// reads or writes nothing the previous one touches before it.  pdl_trigger()
+// lets the next kernel launch once every CTA of this one has passed it.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+// Launch on st, with programmatic stream serialization when pdl is set: the
+// kernel may then start while the previous kernel on st finishes, and must call
+// pdl_wait() before it touches anything an earlier kernel writes or reads.
+template <typename... KArgs, typename... Args>
+void launch_k(bool pdl, void (*kern)(KArgs...), dim3 grid, unsigned block, size_t smem,
+              cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  (void)cudaLaunchKernelEx(&cfg, kern, args...);  // errors surface in cudaGetLastError()
+}
+
+
 // ---------------------------------------------------------------------------
 // Tree bookkeeping (leg2cheb.c:125-150), as closed forms.
 //   level l holds nb(l) = 2^(l+1) - 1 blocks and S(l) = 2 nb(l) slots;
@@ -350,6 +381,8 @@ __global__ void __launch_bounds__(256, VB == 1 ? 5 : VB == 2 ? 4 : 2)
            const double *__restrict__ a, const double *__restrict__ an,
            const double *__restrict__ dn, const double *__restrict__ W, Geo g, int c2l,
            long long jbeg) {
+  pdl_wait();
+  pdl_trigger();
   const long long ntile = (g.N - jbeg + blockDim.x - 1) / blockDim.x;
   const long long nblk = ntile * (g.count / VB);
   for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x) {  // grid may be smaller
@@ -378,6 +411,8 @@ __global__ void __launch_bounds__(256, VB <= 2 ? 3 : 2)
     k_near_pair(const double *__restrict__ x, const double *out, double *__restrict__ y,
                 const double *__restrict__ a, const double *__restrict__ an,
                 const double *__restrict__ dn, const double *__restrict__ W, Geo g, int c2l) {
+  pdl_wait();
+  pdl_trigger();
   const long long half = g.h >> 1, npair = (g.nL - 1) * half, jlast = (g.nL - 1) * g.h;
   const long long per_vg = npair + (g.N - jlast), nitem = per_vg * (g.count / VB);
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < nitem;
@@ -484,6 +519,8 @@ __device__ __forceinline__ void leaf_up_item(const double *__restrict__ xv,
 __global__ void __launch_bounds__(288) k_leaf_up(const double *__restrict__ x,
                                                  const double *__restrict__ T,
                                                  double *__restrict__ w, Geo g) {
+  pdl_wait();
+  pdl_trigger();
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long per_vec = g.K * 2 * M;
   if (idx >= g.count * per_vec) return;
@@ -530,6 +567,8 @@ __device__ __forceinline__ void tree_up_tile(const double *const *child, double 
 // blockDim = 32 * M; items (vector * 2 + parity, parent slot) in TREE_TILE tiles.
 __global__ void __launch_bounds__(32 * M) k_tree_up(double *w, Geo g, long long parent_base,
                                                     long long child_base, long long nparent) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double sB[NTRI];
   __shared__ double sx[TREE_TILE * TREE_PAD];
   __shared__ const double *child[TREE_TILE];
@@ -587,6 +626,8 @@ __device__ __forceinline__ void row_down(const double *sB, const double *xp, int
 // Upward, levels L-1 .. l0 of one subtree.  blockIdx.x = vs * R + r, R = 2^(l0+2).
 // Dynamic shared memory: (2^(d+1) - 1) nodes of SUB_PAD doubles.
 __global__ void __launch_bounds__(32 * M) k_up_sub(double *w, Geo g, int l0, int d) {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ double sm[];
   __shared__ double sB[NTRI];
   for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_lower[t];
@@ -626,6 +667,8 @@ __global__ void __launch_bounds__(32 * M) k_up_sub(double *w, Geo g, int l0, int
 // Upward, levels lt-1 .. 0 of one (vector, parity) from level lt in global
 // memory.  Dynamic shared memory: sum over l <= lt of 2^(l+2) nodes.
 __global__ void __launch_bounds__(32 * M) k_up_top(double *w, Geo g, int lt) {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ double sm[];
   __shared__ double sB[NTRI];
   for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_lower[t];
@@ -659,6 +702,8 @@ __global__ void __launch_bounds__(32 * M) k_up_top(double *w, Geo g, int lt) {
 // Downward, levels 0 .. lt of one (vector, parity): c[l+1] += B^T c[l] for
 // l < lt, then levels 1..lt written back.  Dynamic shared memory as k_up_top.
 __global__ void __launch_bounds__(32 * M) k_down_top(double *c, Geo g, int lt) {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ double sm[];
   __shared__ double sB[NTRI];
   for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_upper[t];
@@ -703,6 +748,8 @@ __global__ void __launch_bounds__(32 * M) k_down_top(double *c, Geo g, int lt) {
 // Downward, levels l0 .. L-1 of one subtree (target root r at level l0);
 // writes the final leaf level.  blockIdx.x = vs * R + r.
 __global__ void __launch_bounds__(32 * M) k_down_sub(double *c, Geo g, int l0, int d) {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ double sm[];
   __shared__ double sB[NTRI];
   for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_upper[t];
@@ -775,6 +822,8 @@ __device__ __forceinline__ void far_item(const double *__restrict__ Ablk,
 __global__ void __launch_bounds__(256) k_far(const double *__restrict__ A,
                                              const double *__restrict__ w,
                                              double *__restrict__ c, Geo g, long long nblocks) {
+  pdl_wait();
+  pdl_trigger();
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long per_vs = nblocks * M;
   if (idx >= g.count * 2 * per_vs) return;
@@ -814,6 +863,8 @@ __device__ __forceinline__ void tree_down_tile(const double *const *par, double 
 
 __global__ void __launch_bounds__(32 * M) k_tree_down(double *c, Geo g, long long parent_base,
                                                       long long child_base, long long nparent) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double sB[NTRI];
   __shared__ double sx[TREE_TILE * TREE_PAD];
   __shared__ const double *par[TREE_TILE];
@@ -867,6 +918,8 @@ __global__ void __launch_bounds__(256) k_leaf_down(const double *__restrict__ c,
                                                    const double *__restrict__ T,
                                                    const double *__restrict__ y, double *out,
                                                    Geo g, int c2l) {
+  pdl_wait();
+  pdl_trigger();
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= g.count * g.N) return;
   const long long v = idx / g.N, j = idx - v * g.N;
@@ -1107,6 +1160,8 @@ __global__ void __launch_bounds__(32 * MXW)
   double *Xw = reinterpret_cast<double *>(sM + 2 * OZ_META + 32 * MXW) + wid * 2 * 16 * XLD;
   oz_load_frag(sP, Pf, 2 * NW, sM, Pm, 2 * OZ_META);
   __syncthreads();
+  pdl_wait();
+  pdl_trigger();
   const long long tpv = (g.K + 15) / 16, ntile = g.count * tpv;
   auto issue = [&](long long tile, int buf) {
     const long long v = tile / tpv, node0 = (tile - v * tpv) * 16;
@@ -1178,6 +1233,8 @@ __global__ void __launch_bounds__(32 * MXW)
   long long *Xw = X0 + wid * 2 * 16 * OZ_TLD;
   oz_load_frag(sP, Pf, OZ_TREE_UP_WORDS, sM, Pm, OZ_META);
   __syncthreads();
+  pdl_wait();
+  pdl_trigger();
   const long long ncol = g.count * 2 * np, ntile = (ncol + 15) / 16;
   auto issue = [&](long long tile, int buf) {
     long long *B = sB + buf * 16;
@@ -1262,6 +1319,8 @@ __global__ void __launch_bounds__(32 * MXW)
   long long *Cw = X0 + MXW * 2 * 16 * OZ_CLD + wid * 2 * 16 * 2 * M;
   oz_load_frag(sP, Pf, OZ_TREE_DOWN_WORDS, sM, Pm, 2 * OZ_META);
   __syncthreads();
+  pdl_wait();
+  pdl_trigger();
   const long long ncol = g.count * 2 * np, ntile = (ncol + 15) / 16;
   auto issue = [&](long long tile, int buf) {
     long long *B = sB + buf * 32;
@@ -1363,6 +1422,8 @@ __global__ void __launch_bounds__(32 * MXW)
   const long long gb = blockIdx.x;
   oz_load_frag(sP, Pf + gb * OZ_FAR_WORDS, OZ_FAR_WORDS, sM, Pm + gb * 2 * OZ_META, 2 * OZ_META);
   __syncthreads();
+  pdl_wait();
+  pdl_trigger();
   const long long ncol = 2 * g.count, c0 = (long long)blockIdx.y * OZ_FAR_COLS;
   const long long ntile = (min(ncol - c0, (long long)OZ_FAR_COLS) + 15) / 16;
   auto issue = [&](long long tile, int buf) {
@@ -1442,6 +1503,8 @@ __global__ void __launch_bounds__(32 * MXW)
   double *Ow = reinterpret_cast<double *>(Xw + 2 * 2 * 16 * OZ_CLD);  // per buffer 16 x h
   oz_load_frag(sP, Pf, nw, sE, Pe, ne);
   __syncthreads();
+  pdl_wait();
+  pdl_trigger();
   const long long tpv = (g.K + 15) / 16, ntile = g.count * tpv;
   auto issue = [&](long long tile, int buf) {
     const long long v = tile / tpv, tau0 = (tile - v * tpv) * 16;
@@ -1631,6 +1694,13 @@ struct l2c_gpu_plan {
   unsigned near_ctas = 0;  // band grid cap while it overlaps (0: no cap)
   int near_vb = 8;         // band vectors per thread while it overlaps
   int near_pair = -1;    // band in pairs: 1 always, 0 never, -1 by leaf size
+  // programmatic dependent launch, bit flags: 1 far-field chain kernels,
+  // 2 the band, 4 the first chain kernel after the band on the same stream.
+  // Default: chain kernels of mixed plans, whose fragment prologues then overlap
+  // the previous kernel (measured 5 % faster for 256 x 16384, 3 % for one
+  // N = 2^22 vector); plain plans none (their short tree kernels have no
+  // prologue to hide, and one N = 2^20 vector was 3 % slower with it).
+  int pdl = -1;
   // launch accounting and optional per-phase CUDA-event timing
   size_t launches = 0;
   bool profiling = false;
@@ -1828,45 +1898,45 @@ size_t tree_launches(const TreePlan &t, size_t L) {
 size_t sub_smem(int d) { return ((size_t)(2 << d) - 1) * SUB_PAD * sizeof(double); }
 size_t top_smem(int lt) { return ((size_t)(8LL << lt) - 4) * SUB_PAD * sizeof(double); }
 
-cudaError_t sweep_up(double *w, const Geo &g, const TreePlan &t, cudaStream_t st) {
+cudaError_t sweep_up(double *w, const Geo &g, const TreePlan &t, cudaStream_t st, bool pdl) {
   if (!t.staged) {
     for (long long l = g.L - 2; l >= 0; l--) {
       const long long np = (long long)slots_at((size_t)l);
-      k_tree_up<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
-          w, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
+      launch_k(pdl, k_tree_up, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, w, g,
+               2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
     }
     return cudaGetLastError();
   }
   const unsigned nsub = (unsigned)(g.count * 2 * (4LL << t.l0));
-  k_up_sub<<<nsub, 32 * M, sub_smem(t.d), st>>>(w, g, t.l0, t.d);
+  launch_k(pdl, k_up_sub, nsub, 32 * M, sub_smem(t.d), st, w, g, (int)t.l0, (int)t.d);
   for (long long l = t.l0 - 1; l >= t.lt; l--) {
     const long long np = (long long)slots_at((size_t)l);
-    k_tree_up<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
-        w, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
+    launch_k(pdl, k_tree_up, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, w, g,
+             2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
   }
   if (t.lt > 0)
-    k_up_top<<<(unsigned)(g.count * 2), 32 * M, top_smem(t.lt), st>>>(w, g, t.lt);
+    launch_k(pdl, k_up_top, (unsigned)(g.count * 2), 32 * M, top_smem(t.lt), st, w, g, (int)t.lt);
   return cudaGetLastError();
 }
 
-cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t st) {
+cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t st, bool pdl) {
   if (!t.staged) {
     for (long long l = 0; l + 1 < g.L; l++) {
       const long long np = (long long)slots_at((size_t)l);
-      k_tree_down<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
-          c, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
+      launch_k(pdl, k_tree_down, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, c, g,
+               2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
     }
     return cudaGetLastError();
   }
   if (t.lt > 0)
-    k_down_top<<<(unsigned)(g.count * 2), 32 * M, top_smem(t.lt), st>>>(c, g, t.lt);
+    launch_k(pdl, k_down_top, (unsigned)(g.count * 2), 32 * M, top_smem(t.lt), st, c, g, (int)t.lt);
   for (long long l = t.lt; l < t.l0; l++) {
     const long long np = (long long)slots_at((size_t)l);
-    k_tree_down<<<blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st>>>(
-        c, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
+    launch_k(pdl, k_tree_down, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, c, g,
+             2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
   }
   const unsigned nsub = (unsigned)(g.count * 2 * (4LL << t.l0));
-  k_down_sub<<<nsub, 32 * M, sub_smem(t.d), st>>>(c, g, t.l0, t.d);
+  launch_k(pdl, k_down_sub, nsub, 32 * M, sub_smem(t.d), st, c, g, (int)t.l0, (int)t.d);
   return cudaGetLastError();
 }
 
@@ -1874,7 +1944,8 @@ cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t 
 // thread, then the remainder.
 cudaError_t launch_near(const double *x, const double *out, double *y, const double *a,
                         const double *an, const double *dn, const double *W, Geo g, int c2l,
-                        cudaStream_t st, bool pair, unsigned max_ctas, int max_vb) {
+                        cudaStream_t st, bool pair, unsigned max_ctas, int max_vb,
+                        bool pdl = false) {
   long long v = 0;
   while (v < g.count) {
     const long long left = g.count - v;
@@ -1889,12 +1960,8 @@ cudaError_t launch_near(const double *x, const double *out, double *y, const dou
     if (!pair) {
       unsigned grid = (unsigned)(((g.N + 255) / 256) * groups);
       if (max_ctas) grid = std::min(grid, max_ctas);
-      switch (vb) {
-        case 8: k_near<8><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l, 0); break;
-        case 4: k_near<4><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l, 0); break;
-        case 2: k_near<2><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l, 0); break;
-        default: k_near<1><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l, 0); break;
-      }
+      auto *kern = vb == 8 ? k_near<8> : vb == 4 ? k_near<4> : vb == 2 ? k_near<2> : k_near<1>;
+      launch_k(pdl, kern, grid, 256, 0, st, xs, os, ys, a, an, dn, W, gg, c2l, 0LL);
       const cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
       v += groups * vb;
@@ -1904,12 +1971,11 @@ cudaError_t launch_near(const double *x, const double *out, double *y, const dou
     const long long per_vg = (g.nL - 1) * (g.h / 2) + (g.N - (g.nL - 1) * g.h);
     unsigned grid = (unsigned)((groups * per_vg + 255) / 256);
     if (max_ctas) grid = std::min(grid, max_ctas);
-    switch (vb) {
-      case 8: k_near_pair<8><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
-      case 4: k_near_pair<4><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
-      case 2: k_near_pair<2><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
-      default: k_near_pair<1><<<grid, 256, 0, st>>>(xs, os, ys, a, an, dn, W, gg, c2l); break;
-    }
+    auto *kern = vb == 8   ? k_near_pair<8>
+                 : vb == 4 ? k_near_pair<4>
+                 : vb == 2 ? k_near_pair<2>
+                           : k_near_pair<1>;
+    launch_k(pdl, kern, grid, 256, 0, st, xs, os, ys, a, an, dn, W, gg, c2l);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     v += groups * vb;
@@ -1952,12 +2018,21 @@ Geo make_geo(const l2c_gpu_plan *p, size_t count, size_t dist, size_t stride) {
 // cores (the far-field blocks only when the batch gives each block at least 8
 // right-hand sides; single vectors keep the FP64 block products, on doubles
 // converted from and back to the column format in place).
+unsigned pdl_flags(const l2c_gpu_plan *p) {
+  return p->pdl >= 0 ? (unsigned)p->pdl : p->mixed ? 1u : 0u;
+}
+
+// The first far-field kernel follows the band on the same stream unless the
+// band runs on the second stream.
+bool pdl_after_band(const l2c_gpu_plan *p, bool ov) { return (pdl_flags(p) & (ov ? 1u : 4u)) != 0; }
+
 template <int KC>
-void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStream_t st) {
+void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStream_t st, bool pdl) {
   const long long tiles = g.count * ((g.K + 15) / 16);
   const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
-  k_mz_leaf_up<KC><<<grid, 32 * MXW, mz_leaf_up_smem(KC), st>>>(
-      x, reinterpret_cast<long long *>(p->w), p->wE, p->oz_lu, p->oz_lum, g);
+  launch_k(pdl, k_mz_leaf_up<KC>, grid, 32 * MXW, mz_leaf_up_smem(KC), st, x,
+           reinterpret_cast<long long *>(p->w), p->wE, (const unsigned *)p->oz_lu,
+           (const int *)p->oz_lum, g);
 }
 
 bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir, const Geo &g,
@@ -1966,15 +2041,16 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
   long long *w = reinterpret_cast<long long *>(p->w), *c = reinterpret_cast<long long *>(p->c);
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
+    const bool pdl = pdl_after_band(p, ov);
     switch (p->oz_kc) {
-      case 1: mz_leaf_up_launch<1>(p, x, g, st); break;
-      case 2: mz_leaf_up_launch<2>(p, x, g, st); break;
-      case 3: mz_leaf_up_launch<3>(p, x, g, st); break;
-      case 4: mz_leaf_up_launch<4>(p, x, g, st); break;
-      case 5: mz_leaf_up_launch<5>(p, x, g, st); break;
-      case 6: mz_leaf_up_launch<6>(p, x, g, st); break;
-      case 7: mz_leaf_up_launch<7>(p, x, g, st); break;
-      default: mz_leaf_up_launch<8>(p, x, g, st); break;
+      case 1: mz_leaf_up_launch<1>(p, x, g, st, pdl); break;
+      case 2: mz_leaf_up_launch<2>(p, x, g, st, pdl); break;
+      case 3: mz_leaf_up_launch<3>(p, x, g, st, pdl); break;
+      case 4: mz_leaf_up_launch<4>(p, x, g, st, pdl); break;
+      case 5: mz_leaf_up_launch<5>(p, x, g, st, pdl); break;
+      case 6: mz_leaf_up_launch<6>(p, x, g, st, pdl); break;
+      case 7: mz_leaf_up_launch<7>(p, x, g, st, pdl); break;
+      default: mz_leaf_up_launch<8>(p, x, g, st, pdl); break;
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -1986,12 +2062,10 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
       const long long pb = 2 * (long long)blocks_before((size_t)l);
       const long long cb = 2 * (long long)blocks_before((size_t)l + 1);
-      if (p->oz_tree_q == 2)
-        k_mz_tree_up<2><<<grid, 32 * MXW, OZ_TREE_UP_SMEM, st>>>(w, p->wE, p->oz_tu, p->oz_tum,
-                                                                 g, pb, cb, np);
-      else
-        k_mz_tree_up<l2c_oz::SLICES><<<grid, 32 * MXW, OZ_TREE_UP_SMEM, st>>>(
-            w, p->wE, p->oz_tu, p->oz_tum, g, pb, cb, np);
+      launch_k(pdl_flags(p) & 1,
+               p->oz_tree_q == 2 ? k_mz_tree_up<2> : k_mz_tree_up<l2c_oz::SLICES>, grid,
+               32 * MXW, OZ_TREE_UP_SMEM, st, w, p->wE, (const unsigned *)p->oz_tu,
+               (const int *)p->oz_tum, g, pb, cb, np);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -2000,8 +2074,9 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     PhaseScope ps(p, L2C_PHASE_FAR, tc ? 1 : 3);
     if (tc) {
       const dim3 grid((unsigned)p->Nb, (unsigned)((2 * g.count + OZ_FAR_COLS - 1) / OZ_FAR_COLS));
-      k_mz_far<<<grid, 32 * MXW, OZ_FAR_SMEM, st>>>(w, p->wE, c, p->cE, p->oz_far[dir],
-                                                    p->oz_farm[dir], g);
+      launch_k(pdl_flags(p) & 1, k_mz_far, grid, 32 * MXW, OZ_FAR_SMEM, st, (const long long *)w,
+               (const int *)p->wE, c, p->cE, (const unsigned *)p->oz_far[dir],
+               (const int *)p->oz_farm[dir], g);
     } else {
       const long long ncol = g.count * 2 * g.slots, n = g.count * 2 * (long long)p->Nb * M;
       k_oz_cols_to_double<<<blocks_for(ncol * M, 256), 256, 0, st>>>(w, p->wE, ncol);
@@ -2019,12 +2094,10 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
       const long long pb = 2 * (long long)blocks_before((size_t)l);
       const long long cb = 2 * (long long)blocks_before((size_t)l + 1);
-      if (p->oz_tree_q == 2)
-        k_mz_tree_down<2><<<grid, 32 * MXW, OZ_TREE_DOWN_SMEM, st>>>(c, p->cE, p->oz_td,
-                                                                     p->oz_tdm, g, pb, cb, np);
-      else
-        k_mz_tree_down<l2c_oz::SLICES><<<grid, 32 * MXW, OZ_TREE_DOWN_SMEM, st>>>(
-            c, p->cE, p->oz_td, p->oz_tdm, g, pb, cb, np);
+      launch_k(pdl_flags(p) & 1,
+               p->oz_tree_q == 2 ? k_mz_tree_down<2> : k_mz_tree_down<l2c_oz::SLICES>, grid,
+               32 * MXW, OZ_TREE_DOWN_SMEM, st, c, p->cE, (const unsigned *)p->oz_td,
+               (const int *)p->oz_tdm, g, pb, cb, np);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -2034,8 +2107,10 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, tail > 0 ? 2 : 1);
     const long long tiles = g.count * ((g.K + 15) / 16);
     const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
-    k_mz_leaf_down<<<grid, 32 * MXW, mz_leaf_down_smem(g.s, p->oz_npass), st>>>(
-        c, p->cE, p->y, out, p->oz_ld, p->oz_lde, g, c2l, p->oz_npass);
+    // after the join with the band's stream: a plain launch (full dependency)
+    launch_k((pdl_flags(p) & 1) && !ov, k_mz_leaf_down, grid, 32 * MXW,
+             mz_leaf_down_smem(g.s, p->oz_npass), st, (const long long *)c, (const int *)p->cE,
+             (const double *)p->y, out, (const unsigned *)p->oz_ld, (const int *)p->oz_lde, g, c2l, p->oz_npass);
     if (tail > 0) k_mx_tail<<<blocks_for(tail, 256), 256, 0, st>>>(p->y, out, g, c2l);
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -2106,35 +2181,39 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   {
     PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, ov ? p->near_vb : 8), stn);
     CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, near_pair(p),
-                    ov ? p->near_ctas : 0, ov ? p->near_vb : 8));
+                    ov ? p->near_ctas : 0, ov ? p->near_vb : 8, (pdl_flags(p) & 2) && !ov));
   }
   if (ov) CK(cudaEventRecord(p->ev_join, st2));
   if (p->mixed) return launch_mixed_far(p, x, out, dir, g, st, ov) ? 1 : 0;
   const long long leaf_threads = g.count * g.K * 2 * M;
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
-    k_leaf_up<<<blocks_for(leaf_threads, 288), 288, 0, st>>>(x, p->T, p->w, g);
+    launch_k(pdl_after_band(p, ov), k_leaf_up, blocks_for(leaf_threads, 288), 288, 0, st, x,
+             (const double *)p->T, p->w, g);
     CK(cudaGetLastError());
   }
   const TreePlan tp = tree_plan(p->L, count);
   {
     PhaseScope ps(p, L2C_PHASE_TREE_UP, tree_launches(tp, p->L));
-    CK(sweep_up(p->w, g, tp, st));
+    CK(sweep_up(p->w, g, tp, st, pdl_flags(p) & 1));
   }
   {
     PhaseScope ps(p, L2C_PHASE_FAR, 1);
     const long long n = g.count * 2 * (long long)p->Nb * M;
-    k_far<<<blocks_for(n, 256), 256, 0, st>>>(p->A[dir], p->w, p->c, g, (long long)p->Nb);
+    launch_k(pdl_flags(p) & 1, k_far, blocks_for(n, 256), 256, 0, st, (const double *)p->A[dir],
+             (const double *)p->w, p->c, g, (long long)p->Nb);
     CK(cudaGetLastError());
   }
   {
     PhaseScope ps(p, L2C_PHASE_TREE_DOWN, tree_launches(tp, p->L));
-    CK(sweep_down(p->c, g, tp, st));
+    CK(sweep_down(p->c, g, tp, st, pdl_flags(p) & 1));
   }
   if (ov) CK(cudaStreamWaitEvent(st, p->ev_join, 0));
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
-    k_leaf_down<<<blocks_for(total, 256), 256, 0, st>>>(p->c, p->T, p->y, out, g, c2l);
+    launch_k((pdl_flags(p) & 1) && !ov, k_leaf_down, blocks_for(total, 256), 256, 0, st,
+             (const double *)p->c,
+             (const double *)p->T, (const double *)p->y, out, g, c2l);
     CK(cudaGetLastError());
   }
   return 1;
@@ -2254,6 +2333,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_NEAR_CTAS")) p->near_ctas = (unsigned)std::atoi(env);
   if (const char *env = std::getenv("L2C_NEAR_VB")) p->near_vb = std::max(1, std::atoi(env));
   if (const char *env = std::getenv("L2C_NEAR_PAIR")) p->near_pair = env[0] == '1' ? 1 : 0;
+  if (const char *env = std::getenv("L2C_PDL")) p->pdl = std::max(0, std::atoi(env));
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
     p->Nn = N;

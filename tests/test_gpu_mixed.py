@@ -68,3 +68,35 @@ def test_mixed_wide_dynamic_range(lib, orc):
 def test_mixed_rejects_large_leaves(lib):
     with pytest.raises(lib.L2CError, match="s <= 64"):
         lib.Plan(1 << 16, 200, mixed=True)  # s = 128
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+@pytest.mark.parametrize("count", [1, 16])
+def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
+    """Programmatic dependent launch, the band on the second stream and graph
+    replay change only when kernels start, never what they compute: every
+    combination gives the same bits as the default plan."""
+    N = 16384
+    x = np.ascontiguousarray(make_input(N * count, "gauss", 11).reshape(count, N))
+
+    def run():
+        p = lib.Plan(N, 16, mixed=mixed)
+        outs = []
+        for d in (0, 1):
+            out = np.zeros_like(x)
+            for _ in range(2):  # capture, then replay
+                out[:] = 0
+                p.execute_batched(x, out, d, count, N, 1)
+            outs.append(out)
+        p.close()
+        return outs
+
+    want = run()
+    for env in ({"L2C_PDL": "0"}, {"L2C_PDL": "7"}, {"L2C_PDL": "7", "L2C_OVERLAP": "0"},
+                {"L2C_PDL": "7", "L2C_OVERLAP": "1"}, {"L2C_PDL": "7", "L2C_NO_GRAPHS": "1"}):
+        with monkeypatch.context() as m:
+            for k, v in env.items():
+                m.setenv(k, v)
+            got = run()
+        for d in (0, 1):
+            assert np.array_equal(got[d], want[d]), (env, d)
