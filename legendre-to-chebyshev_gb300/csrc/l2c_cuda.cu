@@ -1070,13 +1070,26 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem, int byte
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(bytes));
 }
 
-// Per-warp two-deep pipeline over tiles first, first + step, ... < ntile:
-// issue(tile, buf) starts the copies of a tile into buffer buf, work(tile, buf)
-// computes it once they have landed.
-template <class Issue, class Work>
+// Per-warp pipeline over tiles first, first + step, ... < ntile: issue(tile,
+// buf) starts the copies of a tile into buffer buf, work(tile, buf) computes it
+// once they have landed.  NBUF = 2 copies the next tile during the current
+// one; NBUF = 1 (half the shared memory per warp, so more warps per SM) waits
+// for each tile's copies.
+template <int NBUF = 2, class Issue, class Work>
 __device__ __forceinline__ void oz_tile_loop(long long first, long long step, long long ntile,
                                              Issue issue, Work work) {
   if (first >= ntile) return;
+  if constexpr (NBUF == 1) {
+    for (long long tile = first; tile < ntile; tile += step) {
+      issue(tile, 0);
+      l2c_oz::cp_commit();
+      l2c_oz::cp_wait0();
+      __syncwarp();
+      work(tile, 0);
+      __syncwarp();
+    }
+    return;
+  }
   issue(first, 0);
   l2c_oz::cp_commit();
   int buf = 0;
@@ -1147,8 +1160,12 @@ __device__ __forceinline__ void oz_put18(const long long (&T)[OZ_NT][4], const i
 // Leaf up (step 1): tile = 16 consecutive leaf nodes of one vector; both
 // parities from one staged stretch of x (node r's h inputs in row r, parity
 // sg at even/odd positions).  P_sg = T_sg^T (18 x s), KC = ceil(s / 8).
-template <int KC>
-__global__ void __launch_bounds__(32 * MXW)
+// Single-buffered kernels (NBUF = 1) are held to 128 registers (four CTAs per
+// SM) so the warps freed from the second buffer can be resident.
+constexpr int oz_min_ctas(int NBUF) { return NBUF == 1 ? 4 : 1; }
+
+template <int KC, int NBUF>
+__global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
     k_mz_leaf_up(const double *__restrict__ x, long long *__restrict__ w, int *__restrict__ wE,
                  const unsigned *__restrict__ Pf, const int *__restrict__ Pm, Geo g) {
   constexpr int XLD = 16 * KC + 1, NW = oz_words(OZ_NT, KC);
@@ -1157,7 +1174,7 @@ __global__ void __launch_bounds__(32 * MXW)
   unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
   int *sM = reinterpret_cast<int *>(sP + 2 * NW);
   int *Es = sM + 2 * OZ_META + wid * 32;
-  double *Xw = reinterpret_cast<double *>(sM + 2 * OZ_META + 32 * MXW) + wid * 2 * 16 * XLD;
+  double *Xw = reinterpret_cast<double *>(sM + 2 * OZ_META + 32 * MXW) + wid * NBUF * 16 * XLD;
   oz_load_frag(sP, Pf, 2 * NW, sM, Pm, 2 * OZ_META);
   __syncthreads();
   pdl_wait();
@@ -1205,33 +1222,38 @@ __global__ void __launch_bounds__(32 * MXW)
         }
     }
   };
-  oz_tile_loop((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue, work);
+  oz_tile_loop<NBUF>((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue,
+                     work);
 }
 
-size_t mz_leaf_up_smem(int KC) {
+size_t mz_leaf_up_smem(int KC, int nbuf) {
   return (size_t)(2 * oz_words(OZ_NT, KC) + 2 * OZ_META + 32 * MXW) * 4 +
-         (size_t)MXW * 2 * 16 * (16 * KC + 1) * sizeof(double);
+         (size_t)MXW * nbuf * 16 * (16 * KC + 1) * sizeof(double);
 }
 
 // Transfer trees, one level.  Columns col = (vector * 2 + parity) * np + j.
 // Up: parent slot j of level l from child slots 2j+2, 2j+3 of level l+1
 // (36 contiguous coefficients, two stored columns), P = [B | B'] (18 x 36).
-constexpr int OZ_TREE_UP_WORDS = oz_words(OZ_NT, 5);
-template <int QMAX>
+// The transfer matrices' fragments hold only their first QMAX digit slices
+// (the slice-major layout makes that a prefix of each matrix's words).
+__host__ __device__ constexpr int oz_tree_words(int QMAX, int KC) { return QMAX * OZ_NT * KC * 32; }
+template <int QMAX, int NBUF>
 __global__ void __launch_bounds__(32 * MXW)
     k_mz_tree_up(long long *w, int *wE, const unsigned *__restrict__ Pf,
                  const int *__restrict__ Pm, Geo g, long long parent_base, long long child_base,
                  long long np) {
   extern __shared__ __align__(16) unsigned char mz_smem[];
+  constexpr int NW = oz_tree_words(QMAX, 5);
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
   unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
-  int *sM = reinterpret_cast<int *>(sP + OZ_TREE_UP_WORDS);
-  int *sI = sM + OZ_META + wid * (16 + 2 * 2 * 16);  // Es[16], then [buf][child][16] exponents
+  int *sM = reinterpret_cast<int *>(sP + NW);
+  // per warp: Es[16], then [buf][child][16] exponents
+  int *sI = sM + OZ_META + wid * (16 + NBUF * 2 * 16);
   int *Es = sI, *sEx = sI + 16;
-  long long *sB = reinterpret_cast<long long *>(sM + OZ_META + MXW * (16 + 4 * 16)) + wid * 2 * 16;
-  long long *X0 = sB - wid * 2 * 16 + MXW * 2 * 16;
-  long long *Xw = X0 + wid * 2 * 16 * OZ_TLD;
-  oz_load_frag(sP, Pf, OZ_TREE_UP_WORDS, sM, Pm, OZ_META);
+  long long *sB0 = reinterpret_cast<long long *>(sM + OZ_META + MXW * (16 + NBUF * 2 * 16));
+  long long *sB = sB0 + wid * NBUF * 16;
+  long long *Xw = sB0 + MXW * NBUF * 16 + wid * NBUF * 16 * OZ_TLD;
+  oz_load_frag(sP, Pf, NW, sM, Pm, OZ_META);
   __syncthreads();
   pdl_wait();
   pdl_trigger();
@@ -1287,37 +1309,38 @@ __global__ void __launch_bounds__(32 * MXW)
       if (d1 >= 0) wE[d1] = Es[gq + 8] + sM[OZ_ROWS];
     }
   };
-  oz_tile_loop((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue, work);
+  oz_tile_loop<NBUF>((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue,
+                     work);
 }
 
-constexpr size_t OZ_TREE_UP_SMEM = (size_t)(OZ_TREE_UP_WORDS + OZ_META + MXW * (16 + 4 * 16)) * 4 +
-                                   (size_t)MXW * 2 * 16 * 8 +
-                                   (size_t)MXW * 2 * 16 * OZ_TLD * sizeof(long long);
+constexpr size_t oz_tree_up_smem(int QMAX, int NBUF) {
+  return (size_t)(oz_tree_words(QMAX, 5) + OZ_META + MXW * (16 + NBUF * 2 * 16)) * 4 +
+         (size_t)MXW * NBUF * 16 * 8 + (size_t)MXW * NBUF * 16 * OZ_TLD * sizeof(long long);
+}
 
 // Down: child slots 2t, 2t+1 of level l+1 += [B^T; B^T'] c(parent slot t of
 // level l).  The child's own far field (prefetched with the parent) and the
 // product are added as integers on the coarser of their two scales, one bit
 // above the larger exponent.
-constexpr int OZ_TREE_DOWN_WORDS = 2 * oz_words(OZ_NT, 3);
-template <int QMAX>
+template <int QMAX, int NBUF>
 __global__ void __launch_bounds__(32 * MXW)
     k_mz_tree_down(long long *c, int *cE, const unsigned *__restrict__ Pf,
                    const int *__restrict__ Pm, Geo g, long long parent_base, long long child_base,
                    long long np) {
   extern __shared__ __align__(16) unsigned char mz_smem[];
-  constexpr int NW = oz_words(OZ_NT, 3);
+  constexpr int NW = oz_tree_words(QMAX, 3);  // per matrix: B^T, then B^T'
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
   unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
-  int *sM = reinterpret_cast<int *>(sP + OZ_TREE_DOWN_WORDS);
+  int *sM = reinterpret_cast<int *>(sP + 2 * NW);
   // per warp: Es[16], then per buffer: parent exponent [16], child exponents [2][16]
-  int *sI = sM + 2 * OZ_META + wid * (16 + 2 * 3 * 16);
+  int *sI = sM + 2 * OZ_META + wid * (16 + NBUF * 3 * 16);
   int *Es = sI, *sEx = sI + 16;
-  long long *sB0 = reinterpret_cast<long long *>(sM + 2 * OZ_META + MXW * (16 + 6 * 16));
-  long long *sB = sB0 + wid * 2 * 2 * 16;  // [buf][parent | child][16] slot indices
-  long long *X0 = sB0 + MXW * 2 * 2 * 16;
-  long long *Xw = X0 + wid * 2 * 16 * OZ_CLD;
-  long long *Cw = X0 + MXW * 2 * 16 * OZ_CLD + wid * 2 * 16 * 2 * M;
-  oz_load_frag(sP, Pf, OZ_TREE_DOWN_WORDS, sM, Pm, 2 * OZ_META);
+  long long *sB0 = reinterpret_cast<long long *>(sM + 2 * OZ_META + MXW * (16 + NBUF * 3 * 16));
+  long long *sB = sB0 + wid * NBUF * 2 * 16;  // [buf][parent | child][16] slot indices
+  long long *X0 = sB0 + MXW * NBUF * 2 * 16;
+  long long *Xw = X0 + wid * NBUF * 16 * OZ_CLD;
+  long long *Cw = X0 + MXW * NBUF * 16 * OZ_CLD + wid * NBUF * 16 * 2 * M;
+  oz_load_frag(sP, Pf, 2 * NW, sM, Pm, 2 * OZ_META);
   __syncthreads();
   pdl_wait();
   pdl_trigger();
@@ -1396,18 +1419,22 @@ __global__ void __launch_bounds__(32 * MXW)
       }
     }
   };
-  oz_tile_loop((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue, work);
+  oz_tile_loop<NBUF>((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue,
+                     work);
 }
 
-constexpr size_t OZ_TREE_DOWN_SMEM =
-    (size_t)(OZ_TREE_DOWN_WORDS + 2 * OZ_META + MXW * (16 + 6 * 16)) * 4 +
-    (size_t)MXW * 2 * 2 * 16 * 8 + (size_t)MXW * 2 * 16 * (OZ_CLD + 2 * M) * sizeof(long long);
+constexpr size_t oz_tree_down_smem(int QMAX, int NBUF) {
+  return (size_t)(2 * oz_tree_words(QMAX, 3) + 2 * OZ_META + MXW * (16 + NBUF * 3 * 16)) * 4 +
+         (size_t)MXW * NBUF * 2 * 16 * 8 +
+         (size_t)MXW * NBUF * 16 * (OZ_CLD + 2 * M) * sizeof(long long);
+}
 
 // Far field (step 3): CTA = (block gb, chunk of columns vs = vector * 2 +
 // parity).  c0 = [A0 A1] [w0; w1] (K = 36), c1 = A2 w1 (K = 18); both parts
 // use the scale of the whole column [w0; w1].
 constexpr int OZ_FAR_COLS = 16 * MXW * 2;  // columns per CTA
-__global__ void __launch_bounds__(32 * MXW)
+template <int NBUF>
+__global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
     k_mz_far(const long long *__restrict__ w, const int *__restrict__ wE, long long *__restrict__ c,
              int *__restrict__ cE, const unsigned *__restrict__ Pf, const int *__restrict__ Pm,
              Geo g) {
@@ -1415,10 +1442,10 @@ __global__ void __launch_bounds__(32 * MXW)
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
   unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
   int *sM = reinterpret_cast<int *>(sP + OZ_FAR_WORDS);
-  int *sI = sM + 2 * OZ_META + wid * (16 + 2 * 2 * 16);  // Es[16], [buf][slot][16]
+  int *sI = sM + 2 * OZ_META + wid * (16 + NBUF * 2 * 16);  // Es[16], [buf][slot][16]
   int *Es = sI, *sEx = sI + 16;
-  long long *Xw = reinterpret_cast<long long *>(sM + 2 * OZ_META + MXW * (16 + 4 * 16)) +
-                  wid * 2 * 16 * OZ_TLD;
+  long long *Xw = reinterpret_cast<long long *>(sM + 2 * OZ_META + MXW * (16 + NBUF * 2 * 16)) +
+                  wid * NBUF * 16 * OZ_TLD;
   const long long gb = blockIdx.x;
   oz_load_frag(sP, Pf + gb * OZ_FAR_WORDS, OZ_FAR_WORDS, sM, Pm + gb * 2 * OZ_META, 2 * OZ_META);
   __syncthreads();
@@ -1474,11 +1501,13 @@ __global__ void __launch_bounds__(32 * MXW)
       }
     }
   };
-  oz_tile_loop(wid, MXW, ntile, issue, work);
+  oz_tile_loop<NBUF>(wid, MXW, ntile, issue, work);
 }
 
-constexpr size_t OZ_FAR_SMEM = (size_t)(OZ_FAR_WORDS + 2 * OZ_META + MXW * (16 + 4 * 16)) * 4 +
-                               (size_t)MXW * 2 * 16 * OZ_TLD * sizeof(long long);
+constexpr size_t oz_far_smem(int NBUF) {
+  return (size_t)(OZ_FAR_WORDS + 2 * OZ_META + MXW * (16 + NBUF * 2 * 16)) * 4 +
+         (size_t)MXW * NBUF * 16 * OZ_TLD * sizeof(long long);
+}
 
 // Leaf down (step 5) + final scaling: tile = 16 consecutive leaf targets of one
 // vector, both parities; P_sg = T_sg (s x 18) in passes of 16 output rows
@@ -1486,6 +1515,7 @@ constexpr size_t OZ_FAR_SMEM = (size_t)(OZ_FAR_WORDS + 2 * OZ_META + MXW * (16 +
 // memory with the tile's coefficients, the far field is added there, and the
 // sum is written, scaled, in output order.
 constexpr int OZ_LD_WORDS = oz_words(2, 3);
+template <int NBUF>
 __global__ void __launch_bounds__(32 * MXW)
     k_mz_leaf_down(const long long *__restrict__ c, const int *__restrict__ cE,
                    const double *__restrict__ y, double *out, const unsigned *__restrict__ Pf,
@@ -1495,12 +1525,12 @@ __global__ void __launch_bounds__(32 * MXW)
   const int nw = 2 * npass * OZ_LD_WORDS, ne = 2 * npass * 16;
   unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
   int *sE = reinterpret_cast<int *>(sP + nw);
-  int *Ec = sE + ne + wid * (32 + 2 * 32);  // Ec[2][16], then [buf][parity][16] exponents
+  int *Ec = sE + ne + wid * (32 + NBUF * 32);  // Ec[2][16], then [buf][parity][16] exponents
   int *sEx = Ec + 32;
-  const long long per_warp = 2 * 2 * 16 * OZ_CLD + 2 * 16 * g.h;
+  const long long per_warp = NBUF * 2 * 16 * OZ_CLD + NBUF * 16 * g.h;
   long long *Xw =
-      reinterpret_cast<long long *>(sE + ne + MXW * (32 + 2 * 32)) + wid * per_warp;
-  double *Ow = reinterpret_cast<double *>(Xw + 2 * 2 * 16 * OZ_CLD);  // per buffer 16 x h
+      reinterpret_cast<long long *>(sE + ne + MXW * (32 + NBUF * 32)) + wid * per_warp;
+  double *Ow = reinterpret_cast<double *>(Xw + NBUF * 2 * 16 * OZ_CLD);  // per buffer 16 x h
   oz_load_frag(sP, Pf, nw, sE, Pe, ne);
   __syncthreads();
   pdl_wait();
@@ -1570,12 +1600,13 @@ __global__ void __launch_bounds__(32 * MXW)
       out[v * g.dist + j * g.stride] = val;
     }
   };
-  oz_tile_loop((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue, work);
+  oz_tile_loop<NBUF>((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue,
+                     work);
 }
 
-size_t mz_leaf_down_smem(long long s, int npass) {
-  return (size_t)(2 * npass * OZ_LD_WORDS + 2 * npass * 16 + MXW * (32 + 2 * 32)) * 4 +
-         (size_t)MXW * (2 * 2 * 16 * OZ_CLD + 2 * 16 * 2 * s) * 8;
+size_t mz_leaf_down_smem(long long s, int npass, int nbuf) {
+  return (size_t)(2 * npass * OZ_LD_WORDS + 2 * npass * 16 + MXW * (32 + nbuf * 32)) * 4 +
+         (size_t)MXW * (nbuf * 2 * 16 * OZ_CLD + nbuf * 16 * 2 * s) * 8;
 }
 
 // Outputs past the last leaf target node (no far field): scaling only.
@@ -1672,6 +1703,10 @@ struct l2c_gpu_plan {
   int *oz_lde = nullptr;                                        // leaf-down row exponents
   int oz_kc = 0, oz_npass = 0;  // leaf-up k8 chunks, leaf-down passes
   int oz_tree_q = l2c_oz::SLICES;  // digit slices of the transfer matrices that are not zero
+  // tile buffers per warp of the mixed-form kernels: 1 (default) leaves room
+  // for twice the warps per SM, which hide more of the products' latency than
+  // a second buffer does (256 x 16384: 1.155 vs 1.253 ms per L2C + C2L)
+  int oz_nbuf = 1;
   unsigned *oz_far[2] = {nullptr, nullptr};
   int *oz_farm[2] = {nullptr, nullptr};
   // column exponents of w and c (mixed form: w, c hold column-format integers)
@@ -2030,7 +2065,8 @@ template <int KC>
 void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStream_t st, bool pdl) {
   const long long tiles = g.count * ((g.K + 15) / 16);
   const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
-  launch_k(pdl, k_mz_leaf_up<KC>, grid, 32 * MXW, mz_leaf_up_smem(KC), st, x,
+  launch_k(pdl, p->oz_nbuf == 1 ? k_mz_leaf_up<KC, 1> : k_mz_leaf_up<KC, 2>, grid, 32 * MXW,
+           mz_leaf_up_smem(KC, p->oz_nbuf), st, x,
            reinterpret_cast<long long *>(p->w), p->wE, (const unsigned *)p->oz_lu,
            (const int *)p->oz_lum, g);
 }
@@ -2056,16 +2092,17 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
   }
   {
     PhaseScope ps(p, L2C_PHASE_TREE_UP, (size_t)(g.L - 1));
+    const bool q2 = p->oz_tree_q == 2, nb1 = p->oz_nbuf == 1;
+    auto *kup = q2 ? (nb1 ? k_mz_tree_up<2, 1> : k_mz_tree_up<2, 2>)
+                   : (nb1 ? k_mz_tree_up<l2c_oz::SLICES, 1> : k_mz_tree_up<l2c_oz::SLICES, 2>);
     for (long long l = g.L - 2; l >= 0; l--) {
       const long long np = (long long)slots_at((size_t)l);
       const long long tiles = (g.count * 2 * np + 15) / 16;
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
       const long long pb = 2 * (long long)blocks_before((size_t)l);
       const long long cb = 2 * (long long)blocks_before((size_t)l + 1);
-      launch_k(pdl_flags(p) & 1,
-               p->oz_tree_q == 2 ? k_mz_tree_up<2> : k_mz_tree_up<l2c_oz::SLICES>, grid,
-               32 * MXW, OZ_TREE_UP_SMEM, st, w, p->wE, (const unsigned *)p->oz_tu,
-               (const int *)p->oz_tum, g, pb, cb, np);
+      launch_k(pdl_flags(p) & 1, kup, grid, 32 * MXW, oz_tree_up_smem(p->oz_tree_q, p->oz_nbuf), st,
+               w, p->wE, (const unsigned *)p->oz_tu, (const int *)p->oz_tum, g, pb, cb, np);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -2074,7 +2111,8 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     PhaseScope ps(p, L2C_PHASE_FAR, tc ? 1 : 3);
     if (tc) {
       const dim3 grid((unsigned)p->Nb, (unsigned)((2 * g.count + OZ_FAR_COLS - 1) / OZ_FAR_COLS));
-      launch_k(pdl_flags(p) & 1, k_mz_far, grid, 32 * MXW, OZ_FAR_SMEM, st, (const long long *)w,
+      launch_k(pdl_flags(p) & 1, p->oz_nbuf == 1 ? k_mz_far<1> : k_mz_far<2>, grid, 32 * MXW,
+               oz_far_smem(p->oz_nbuf), st, (const long long *)w,
                (const int *)p->wE, c, p->cE, (const unsigned *)p->oz_far[dir],
                (const int *)p->oz_farm[dir], g);
     } else {
@@ -2088,16 +2126,18 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
   }
   {
     PhaseScope ps(p, L2C_PHASE_TREE_DOWN, (size_t)(g.L - 1));
+    const bool q2 = p->oz_tree_q == 2, nb1 = p->oz_nbuf == 1;
+    auto *kdown = q2 ? (nb1 ? k_mz_tree_down<2, 1> : k_mz_tree_down<2, 2>)
+                     : (nb1 ? k_mz_tree_down<l2c_oz::SLICES, 1> : k_mz_tree_down<l2c_oz::SLICES, 2>);
     for (long long l = 0; l + 1 < g.L; l++) {
       const long long np = (long long)slots_at((size_t)l);
       const long long tiles = (g.count * 2 * np + 15) / 16;
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
       const long long pb = 2 * (long long)blocks_before((size_t)l);
       const long long cb = 2 * (long long)blocks_before((size_t)l + 1);
-      launch_k(pdl_flags(p) & 1,
-               p->oz_tree_q == 2 ? k_mz_tree_down<2> : k_mz_tree_down<l2c_oz::SLICES>, grid,
-               32 * MXW, OZ_TREE_DOWN_SMEM, st, c, p->cE, (const unsigned *)p->oz_td,
-               (const int *)p->oz_tdm, g, pb, cb, np);
+      launch_k(pdl_flags(p) & 1, kdown, grid, 32 * MXW,
+               oz_tree_down_smem(p->oz_tree_q, p->oz_nbuf), st, c, p->cE,
+               (const unsigned *)p->oz_td, (const int *)p->oz_tdm, g, pb, cb, np);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -2108,8 +2148,8 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     const long long tiles = g.count * ((g.K + 15) / 16);
     const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
     // after the join with the band's stream: a plain launch (full dependency)
-    launch_k((pdl_flags(p) & 1) && !ov, k_mz_leaf_down, grid, 32 * MXW,
-             mz_leaf_down_smem(g.s, p->oz_npass), st, (const long long *)c, (const int *)p->cE,
+    launch_k((pdl_flags(p) & 1) && !ov, p->oz_nbuf == 1 ? k_mz_leaf_down<1> : k_mz_leaf_down<2>,
+             grid, 32 * MXW, mz_leaf_down_smem(g.s, p->oz_npass, p->oz_nbuf), st, (const long long *)c, (const int *)p->cE,
              (const double *)p->y, out, (const unsigned *)p->oz_ld, (const int *)p->oz_lde, g, c2l, p->oz_npass);
     if (tail > 0) k_mx_tail<<<blocks_for(tail, 256), 256, 0, st>>>(p->y, out, g, c2l);
     if (cudaGetLastError() != cudaSuccess) return false;
@@ -2334,6 +2374,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_NEAR_VB")) p->near_vb = std::max(1, std::atoi(env));
   if (const char *env = std::getenv("L2C_NEAR_PAIR")) p->near_pair = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_PDL")) p->pdl = std::max(0, std::atoi(env));
+  if (const char *env = std::getenv("L2C_MZ_NBUF")) p->oz_nbuf = env[0] == '1' ? 1 : 2;
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
     p->Nn = N;
@@ -2459,6 +2500,12 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
         const int qd = std::max(l2c_oz::used_slices(td.data(), OZ_NT, 3),
                                 l2c_oz::used_slices(td.data() + wtd, OZ_NT, 3));
         p->oz_tree_q = std::max(qu, qd) <= 2 ? 2 : l2c_oz::SLICES;
+        // keep each down matrix's leading oz_tree_q slices, back to back
+        const int nq = oz_tree_words(p->oz_tree_q, 3);
+        if (nq < wtd) {
+          std::copy(td.begin() + wtd, td.begin() + wtd + nq, td.begin() + nq);
+          td.resize(2 * (size_t)nq);
+        }
       }
       auto upload = [&](auto **dst, const auto &v) -> cudaError_t {
         const size_t bytes = v.size() * sizeof(v[0]);
@@ -2475,21 +2522,26 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
       PCK(upload(&p->oz_ld, ld));
       PCK(upload(&p->oz_lde, lde));
       // kernels whose shared memory can pass the 48 KB default
-      PCK(cudaFuncSetAttribute(k_mz_leaf_down, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)mz_leaf_down_smem(4 * 16, 4)));
-      PCK(cudaFuncSetAttribute(k_mz_tree_up<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)OZ_TREE_UP_SMEM));
-      PCK(cudaFuncSetAttribute(k_mz_tree_up<l2c_oz::SLICES>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_TREE_UP_SMEM));
-      PCK(cudaFuncSetAttribute(k_mz_tree_down<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)OZ_TREE_DOWN_SMEM));
-      PCK(cudaFuncSetAttribute(k_mz_tree_down<l2c_oz::SLICES>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_TREE_DOWN_SMEM));
-      PCK(cudaFuncSetAttribute(k_mz_far, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)OZ_FAR_SMEM));
-#define L2C_MZ_ATTR(kc)                                                                      \
-  PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                           (int)mz_leaf_up_smem(kc)));
+      const cudaFuncAttribute smax = cudaFuncAttributeMaxDynamicSharedMemorySize;
+      PCK(cudaFuncSetAttribute(k_mz_leaf_down<1>, smax, (int)mz_leaf_down_smem(4 * 16, 4, 1)));
+      PCK(cudaFuncSetAttribute(k_mz_leaf_down<2>, smax, (int)mz_leaf_down_smem(4 * 16, 4, 2)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_up<2, 1>, smax, (int)oz_tree_up_smem(2, 1)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_up<2, 2>, smax, (int)oz_tree_up_smem(2, 2)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_up<l2c_oz::SLICES, 1>, smax,
+                               (int)oz_tree_up_smem(l2c_oz::SLICES, 1)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_up<l2c_oz::SLICES, 2>, smax,
+                               (int)oz_tree_up_smem(l2c_oz::SLICES, 2)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_down<2, 1>, smax, (int)oz_tree_down_smem(2, 1)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_down<2, 2>, smax, (int)oz_tree_down_smem(2, 2)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_down<l2c_oz::SLICES, 1>, smax,
+                               (int)oz_tree_down_smem(l2c_oz::SLICES, 1)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_down<l2c_oz::SLICES, 2>, smax,
+                               (int)oz_tree_down_smem(l2c_oz::SLICES, 2)));
+      PCK(cudaFuncSetAttribute(k_mz_far<1>, smax, (int)oz_far_smem(1)));
+      PCK(cudaFuncSetAttribute(k_mz_far<2>, smax, (int)oz_far_smem(2)));
+#define L2C_MZ_ATTR(kc)                                                                     \
+  PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc, 1>, smax, (int)mz_leaf_up_smem(kc, 1)));        \
+  PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc, 2>, smax, (int)mz_leaf_up_smem(kc, 2)));
       L2C_MZ_ATTR(1) L2C_MZ_ATTR(2) L2C_MZ_ATTR(3) L2C_MZ_ATTR(4)
       L2C_MZ_ATTR(5) L2C_MZ_ATTR(6) L2C_MZ_ATTR(7) L2C_MZ_ATTR(8)
 #undef L2C_MZ_ATTR

@@ -130,6 +130,7 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem, int byte
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+__device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;\n" ::); }
 #endif
 
 // Fragment word of P^T for slice q (1-based), n-tile nt, k8-chunk c and lane

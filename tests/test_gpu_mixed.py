@@ -73,9 +73,9 @@ def test_mixed_rejects_large_leaves(lib):
 @pytest.mark.parametrize("mixed", [False, True])
 @pytest.mark.parametrize("count", [1, 16])
 def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
-    """Programmatic dependent launch, the band on the second stream and graph
-    replay change only when kernels start, never what they compute: every
-    combination gives the same bits as the default plan."""
+    """Programmatic dependent launch, the band on the second stream, graph
+    replay and the tile buffer depth change only when work runs, never what it
+    computes: every combination gives the same bits as the default plan."""
     N = 16384
     x = np.ascontiguousarray(make_input(N * count, "gauss", 11).reshape(count, N))
 
@@ -93,7 +93,8 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
 
     want = run()
     for env in ({"L2C_PDL": "0"}, {"L2C_PDL": "7"}, {"L2C_PDL": "7", "L2C_OVERLAP": "0"},
-                {"L2C_PDL": "7", "L2C_OVERLAP": "1"}, {"L2C_PDL": "7", "L2C_NO_GRAPHS": "1"}):
+                {"L2C_PDL": "7", "L2C_OVERLAP": "1"}, {"L2C_PDL": "7", "L2C_NO_GRAPHS": "1"},
+                {"L2C_MZ_NBUF": "2"}):
         with monkeypatch.context() as m:
             for k, v in env.items():
                 m.setenv(k, v)
