@@ -78,22 +78,37 @@ __device__ __forceinline__ void pdl_trigger() {
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
 }
 
-// Launch on st, with programmatic stream serialization when pdl is set: the
-// kernel may then start while the previous kernel on st finishes, and must call
-// pdl_wait() before it touches anything an earlier kernel writes or reads.
+// Launch options: programmatic stream serialization (the kernel may start
+// while the previous kernel on its stream finishes, and must call pdl_wait()
+// before it touches anything an earlier kernel writes or reads) and a
+// scheduling priority (0: the stream's).
+struct LaunchOpt {
+  bool pdl = false;
+  int prio = 0;
+  LaunchOpt(bool pdl_) : pdl(pdl_) {}
+  LaunchOpt(bool pdl_, int prio_) : pdl(pdl_), prio(prio_) {}
+};
+
 template <typename... KArgs, typename... Args>
-void launch_k(bool pdl, void (*kern)(KArgs...), dim3 grid, unsigned block, size_t smem,
+void launch_k(LaunchOpt o, void (*kern)(KArgs...), dim3 grid, unsigned block, size_t smem,
               cudaStream_t st, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = dim3(block);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchAttribute at[2];
+  unsigned n = 0;
+  if (o.pdl) {
+    at[n].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[n++].val.programmaticStreamSerializationAllowed = 1;
+  }
+  if (o.prio != 0) {
+    at[n].id = cudaLaunchAttributePriority;
+    at[n++].val.priority = o.prio;
+  }
   cfg.attrs = at;
-  cfg.numAttrs = pdl ? 1 : 0;
+  cfg.numAttrs = n;
   (void)cudaLaunchKernelEx(&cfg, kern, args...);  // errors surface in cudaGetLastError()
 }
 
@@ -1736,6 +1751,14 @@ struct l2c_gpu_plan {
   // N = 2^22 vector); plain plans none (their short tree kernels have no
   // prologue to hide, and one N = 2^20 vector was 3 % slower with it).
   int pdl = -1;
+  // Scheduling priority of the far-field chain's kernels while the band runs
+  // beside them: with it, CTAs of the (latency-bound) chain are dispatched
+  // before further CTAs of the band as SMs free up, so the chain is not held
+  // behind the whole band.  Default: the device's greatest priority for mixed
+  // plans (256 x 16384: 1.155 -> 1.080 ms), none for plain plans (whose chain
+  // also runs on the FP64 pipe; 4 % slower with it).  L2C_CHAIN_PRIO=0|1 forces.
+  int chain_prio = 0;
+  int chain_prio_mode = -1;
   // launch accounting and optional per-phase CUDA-event timing
   size_t launches = 0;
   bool profiling = false;
@@ -1933,7 +1956,7 @@ size_t tree_launches(const TreePlan &t, size_t L) {
 size_t sub_smem(int d) { return ((size_t)(2 << d) - 1) * SUB_PAD * sizeof(double); }
 size_t top_smem(int lt) { return ((size_t)(8LL << lt) - 4) * SUB_PAD * sizeof(double); }
 
-cudaError_t sweep_up(double *w, const Geo &g, const TreePlan &t, cudaStream_t st, bool pdl) {
+cudaError_t sweep_up(double *w, const Geo &g, const TreePlan &t, cudaStream_t st, LaunchOpt pdl) {
   if (!t.staged) {
     for (long long l = g.L - 2; l >= 0; l--) {
       const long long np = (long long)slots_at((size_t)l);
@@ -1954,7 +1977,7 @@ cudaError_t sweep_up(double *w, const Geo &g, const TreePlan &t, cudaStream_t st
   return cudaGetLastError();
 }
 
-cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t st, bool pdl) {
+cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t st, LaunchOpt pdl) {
   if (!t.staged) {
     for (long long l = 0; l + 1 < g.L; l++) {
       const long long np = (long long)slots_at((size_t)l);
@@ -2062,7 +2085,8 @@ unsigned pdl_flags(const l2c_gpu_plan *p) {
 bool pdl_after_band(const l2c_gpu_plan *p, bool ov) { return (pdl_flags(p) & (ov ? 1u : 4u)) != 0; }
 
 template <int KC>
-void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStream_t st, bool pdl) {
+void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStream_t st,
+                       LaunchOpt pdl) {
   const long long tiles = g.count * ((g.K + 15) / 16);
   const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
   launch_k(pdl, p->oz_nbuf == 1 ? k_mz_leaf_up<KC, 1> : k_mz_leaf_up<KC, 2>, grid, 32 * MXW,
@@ -2075,9 +2099,10 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
                       cudaStream_t st, bool ov) {
   const int c2l = dir == 1;
   long long *w = reinterpret_cast<long long *>(p->w), *c = reinterpret_cast<long long *>(p->c);
+  const LaunchOpt chain(pdl_flags(p) & 1, ov ? p->chain_prio : 0);
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
-    const bool pdl = pdl_after_band(p, ov);
+    const LaunchOpt pdl(pdl_after_band(p, ov), ov ? p->chain_prio : 0);
     switch (p->oz_kc) {
       case 1: mz_leaf_up_launch<1>(p, x, g, st, pdl); break;
       case 2: mz_leaf_up_launch<2>(p, x, g, st, pdl); break;
@@ -2101,7 +2126,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
       const long long pb = 2 * (long long)blocks_before((size_t)l);
       const long long cb = 2 * (long long)blocks_before((size_t)l + 1);
-      launch_k(pdl_flags(p) & 1, kup, grid, 32 * MXW, oz_tree_up_smem(p->oz_tree_q, p->oz_nbuf), st,
+      launch_k(chain, kup, grid, 32 * MXW, oz_tree_up_smem(p->oz_tree_q, p->oz_nbuf), st,
                w, p->wE, (const unsigned *)p->oz_tu, (const int *)p->oz_tum, g, pb, cb, np);
     }
     if (cudaGetLastError() != cudaSuccess) return false;
@@ -2111,7 +2136,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     PhaseScope ps(p, L2C_PHASE_FAR, tc ? 1 : 3);
     if (tc) {
       const dim3 grid((unsigned)p->Nb, (unsigned)((2 * g.count + OZ_FAR_COLS - 1) / OZ_FAR_COLS));
-      launch_k(pdl_flags(p) & 1, p->oz_nbuf == 1 ? k_mz_far<1> : k_mz_far<2>, grid, 32 * MXW,
+      launch_k(chain, p->oz_nbuf == 1 ? k_mz_far<1> : k_mz_far<2>, grid, 32 * MXW,
                oz_far_smem(p->oz_nbuf), st, (const long long *)w,
                (const int *)p->wE, c, p->cE, (const unsigned *)p->oz_far[dir],
                (const int *)p->oz_farm[dir], g);
@@ -2128,14 +2153,15 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     PhaseScope ps(p, L2C_PHASE_TREE_DOWN, (size_t)(g.L - 1));
     const bool q2 = p->oz_tree_q == 2, nb1 = p->oz_nbuf == 1;
     auto *kdown = q2 ? (nb1 ? k_mz_tree_down<2, 1> : k_mz_tree_down<2, 2>)
-                     : (nb1 ? k_mz_tree_down<l2c_oz::SLICES, 1> : k_mz_tree_down<l2c_oz::SLICES, 2>);
+                     : (nb1 ? k_mz_tree_down<l2c_oz::SLICES, 1>
+                            : k_mz_tree_down<l2c_oz::SLICES, 2>);
     for (long long l = 0; l + 1 < g.L; l++) {
       const long long np = (long long)slots_at((size_t)l);
       const long long tiles = (g.count * 2 * np + 15) / 16;
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
       const long long pb = 2 * (long long)blocks_before((size_t)l);
       const long long cb = 2 * (long long)blocks_before((size_t)l + 1);
-      launch_k(pdl_flags(p) & 1, kdown, grid, 32 * MXW,
+      launch_k(chain, kdown, grid, 32 * MXW,
                oz_tree_down_smem(p->oz_tree_q, p->oz_nbuf), st, c, p->cE,
                (const unsigned *)p->oz_td, (const int *)p->oz_tdm, g, pb, cb, np);
     }
@@ -2149,8 +2175,9 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
     // after the join with the band's stream: a plain launch (full dependency)
     launch_k((pdl_flags(p) & 1) && !ov, p->oz_nbuf == 1 ? k_mz_leaf_down<1> : k_mz_leaf_down<2>,
-             grid, 32 * MXW, mz_leaf_down_smem(g.s, p->oz_npass, p->oz_nbuf), st, (const long long *)c, (const int *)p->cE,
-             (const double *)p->y, out, (const unsigned *)p->oz_ld, (const int *)p->oz_lde, g, c2l, p->oz_npass);
+             grid, 32 * MXW, mz_leaf_down_smem(g.s, p->oz_npass, p->oz_nbuf), st,
+             (const long long *)c, (const int *)p->cE, (const double *)p->y, out,
+             (const unsigned *)p->oz_ld, (const int *)p->oz_lde, g, c2l, p->oz_npass);
     if (tail > 0) k_mx_tail<<<blocks_for(tail, 256), 256, 0, st>>>(p->y, out, g, c2l);
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -2228,25 +2255,27 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   const long long leaf_threads = g.count * g.K * 2 * M;
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
-    launch_k(pdl_after_band(p, ov), k_leaf_up, blocks_for(leaf_threads, 288), 288, 0, st, x,
+    launch_k(LaunchOpt(pdl_after_band(p, ov), ov ? p->chain_prio : 0), k_leaf_up,
+             blocks_for(leaf_threads, 288), 288, 0, st, x,
              (const double *)p->T, p->w, g);
     CK(cudaGetLastError());
   }
   const TreePlan tp = tree_plan(p->L, count);
   {
     PhaseScope ps(p, L2C_PHASE_TREE_UP, tree_launches(tp, p->L));
-    CK(sweep_up(p->w, g, tp, st, pdl_flags(p) & 1));
+    CK(sweep_up(p->w, g, tp, st, LaunchOpt(pdl_flags(p) & 1, ov ? p->chain_prio : 0)));
   }
   {
     PhaseScope ps(p, L2C_PHASE_FAR, 1);
     const long long n = g.count * 2 * (long long)p->Nb * M;
-    launch_k(pdl_flags(p) & 1, k_far, blocks_for(n, 256), 256, 0, st, (const double *)p->A[dir],
+    launch_k(LaunchOpt(pdl_flags(p) & 1, ov ? p->chain_prio : 0), k_far, blocks_for(n, 256), 256,
+             0, st, (const double *)p->A[dir],
              (const double *)p->w, p->c, g, (long long)p->Nb);
     CK(cudaGetLastError());
   }
   {
     PhaseScope ps(p, L2C_PHASE_TREE_DOWN, tree_launches(tp, p->L));
-    CK(sweep_down(p->c, g, tp, st, pdl_flags(p) & 1));
+    CK(sweep_down(p->c, g, tp, st, LaunchOpt(pdl_flags(p) & 1, ov ? p->chain_prio : 0)));
   }
   if (ov) CK(cudaStreamWaitEvent(st, p->ev_join, 0));
   {
@@ -2294,7 +2323,8 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     return 0;
   }
   cudaGraphExec_t exec = nullptr;
-  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  const cudaError_t ei =
+      cudaGraphInstantiate(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(graph);
   if (ei != cudaSuccess) {
     set_err("cudaGraphInstantiate failed: %s", cudaGetErrorString(ei));
@@ -2374,6 +2404,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_NEAR_VB")) p->near_vb = std::max(1, std::atoi(env));
   if (const char *env = std::getenv("L2C_NEAR_PAIR")) p->near_pair = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_PDL")) p->pdl = std::max(0, std::atoi(env));
+  if (const char *env = std::getenv("L2C_CHAIN_PRIO")) p->chain_prio_mode = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_MZ_NBUF")) p->oz_nbuf = env[0] == '1' ? 1 : 2;
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
@@ -2561,6 +2592,11 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   PCK(cudaStreamSynchronize(st));
   for (size_t d = 0; d < 2; d++)
     if (directions == d || directions == 2) p->flops[d] = ref_flops(p, d);
+  if (p->chain_prio_mode == 1 || (p->chain_prio_mode < 0 && p->mixed)) {
+    int least = 0, greatest = 0;
+    PCK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    p->chain_prio = greatest;
+  }
   return p;
 #undef PCK
 }

@@ -74,8 +74,9 @@ def test_mixed_rejects_large_leaves(lib):
 @pytest.mark.parametrize("count", [1, 16])
 def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
     """Programmatic dependent launch, the band on the second stream, graph
-    replay and the tile buffer depth change only when work runs, never what it
-    computes: every combination gives the same bits as the default plan."""
+    replay, the tile buffer depth and the chain's scheduling priority change
+    only when work runs, never what it computes: every combination gives the
+    same bits as the default plan."""
     N = 16384
     x = np.ascontiguousarray(make_input(N * count, "gauss", 11).reshape(count, N))
 
@@ -94,7 +95,7 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
     want = run()
     for env in ({"L2C_PDL": "0"}, {"L2C_PDL": "7"}, {"L2C_PDL": "7", "L2C_OVERLAP": "0"},
                 {"L2C_PDL": "7", "L2C_OVERLAP": "1"}, {"L2C_PDL": "7", "L2C_NO_GRAPHS": "1"},
-                {"L2C_MZ_NBUF": "2"}):
+                {"L2C_MZ_NBUF": "2"}, {"L2C_CHAIN_PRIO": "0"}, {"L2C_CHAIN_PRIO": "1"}):
         with monkeypatch.context() as m:
             for k, v in env.items():
                 m.setenv(k, v)
