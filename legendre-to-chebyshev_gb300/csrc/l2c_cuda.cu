@@ -40,6 +40,14 @@ constexpr int M = 18;
 constexpr int MM = M * M;
 constexpr int NTRI = (MM + M) / 2;
 constexpr double TWO_OVER_PI = 0.63661977236758134308;  // 2/pi
+
+// L2C output scale: 2/pi, halved for output 0.  Halving is exact, so one
+// multiply by the selected factor gives the same double as the reference's two
+// (val * 2/pi, then * 0.5 for j = 0) and costs one FP64 instruction per warp
+// instead of two.
+__host__ __device__ __forceinline__ double l2c_out_scale(long long j) {
+  return j == 0 ? 0.5 * TWO_OVER_PI : TWO_OVER_PI;
+}
 constexpr double SQRT_PI = 1.77245385090551602729816;
 constexpr double TWO_OVER_SQRT_PI = 1.12837916709551257390;
 
@@ -921,8 +929,7 @@ __device__ __forceinline__ void leaf_down_item(const double *__restrict__ cv,
   }
   double val = yv[j] + far;
   if (!c2l) {
-    val = val * TWO_OVER_PI;
-    if (j == 0) val = val * 0.5;
+    val = val * l2c_out_scale(j);
   } else {
     val = val * dyadic(2 * (unsigned long long)j + 1, -1);  // j + 1/2
   }
@@ -1526,12 +1533,15 @@ constexpr size_t oz_far_smem(int NBUF) {
 
 // Leaf down (step 5) + final scaling: tile = 16 consecutive leaf targets of one
 // vector, both parities; P_sg = T_sg (s x 18) in passes of 16 output rows
-// (two n-tiles, KC = 3).  The band sum y of the tile is copied to shared
-// memory with the tile's coefficients, the far field is added there, and the
-// sum is written, scaled, in output order.
+// (two n-tiles, KC = 3).  For tile row r, pass ps and parity sg a lane quad
+// holds the far field of outputs (tau0 + r) h + 32 ps + 2 [0, 16) + sg (lane
+// t: 4t + {0, 2} and 16 + 4t + {0, 2}), so the band sum y is read, the far
+// field added and the scaled sum written straight from registers; the other
+// parity fills the rest of the same sectors.  The outputs past the last leaf
+// target (band only) are scaled by the same CTAs.
 constexpr int OZ_LD_WORDS = oz_words(2, 3);
 template <int NBUF>
-__global__ void __launch_bounds__(32 * MXW)
+__global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 5 : 1)
     k_mz_leaf_down(const long long *__restrict__ c, const int *__restrict__ cE,
                    const double *__restrict__ y, double *out, const unsigned *__restrict__ Pf,
                    const int *__restrict__ Pe, Geo g, int c2l, int npass) {
@@ -1542,14 +1552,20 @@ __global__ void __launch_bounds__(32 * MXW)
   int *sE = reinterpret_cast<int *>(sP + nw);
   int *Ec = sE + ne + wid * (32 + NBUF * 32);  // Ec[2][16], then [buf][parity][16] exponents
   int *sEx = Ec + 32;
-  const long long per_warp = NBUF * 2 * 16 * OZ_CLD + NBUF * 16 * g.h;
-  long long *Xw =
-      reinterpret_cast<long long *>(sE + ne + MXW * (32 + NBUF * 32)) + wid * per_warp;
-  double *Ow = reinterpret_cast<double *>(Xw + NBUF * 2 * 16 * OZ_CLD);  // per buffer 16 x h
+  long long *Xw = reinterpret_cast<long long *>(sE + ne + MXW * (32 + NBUF * 32)) +
+                  wid * NBUF * 2 * 16 * OZ_CLD;
   oz_load_frag(sP, Pf, nw, sE, Pe, ne);
   __syncthreads();
   pdl_wait();
   pdl_trigger();
+  auto scale = [&](double val, long long j) -> double {
+    if (!c2l) {
+      val = val * l2c_out_scale(j);
+    } else {
+      val = val * dyadic(2 * (unsigned long long)j + 1, -1);  // j + 1/2
+    }
+    return val;
+  };
   const long long tpv = (g.K + 15) / 16, ntile = g.count * tpv;
   auto issue = [&](long long tile, int buf) {
     const long long v = tile / tpv, tau0 = (tile - v * tpv) * 16;
@@ -1568,18 +1584,13 @@ __global__ void __launch_bounds__(32 * MXW)
       const long long *src = c + ((v * 2 + sg) * g.slots + g.leaf_base + tau0 + r) * M + 2 * k2;
       l2c_oz::cp_async16(X + sr * OZ_CLD + 2 * k2, ok ? src : c, ok ? 16 : 0);
     }
-    const long long j0 = tau0 * g.h, jn = nrow * g.h;
-    const double *yv = y + v * g.N;
-    double *O = Ow + buf * 16 * g.h;
-    for (long long jj = lane; jj < jn; jj += 32) {
-      const bool ok = j0 + jj < g.N;
-      l2c_oz::cp_async8(O + jj, ok ? yv + j0 + jj : yv, ok ? 8 : 0);
-    }
   };
   auto work = [&](long long tile, int buf) {
     const long long v = tile / tpv, tau0 = (tile - v * tpv) * 16;
-    double *O = Ow + buf * 16 * g.h;
+    const long long nrow = min(16LL, g.K - tau0);
     const int *Ex = sEx + buf * 32;
+    const double *yv = y + v * g.N;
+    double *ov = out + v * g.dist;
 #pragma unroll 1
     for (int sg = 0; sg < 2; sg++) {
       long long *X = Xw + (buf * 2 + sg) * 16 * OZ_CLD;
@@ -1594,50 +1605,28 @@ __global__ void __launch_bounds__(32 * MXW)
 #pragma unroll
           for (int e = 0; e < 4; e++) {
             const int r = gq + 8 * (e >> 1), il = 8 * nt + 2 * t4 + (e & 1), i = 16 * ps + il;
-            if (i >= g.s) continue;
-            O[r * g.h + 2 * i + sg] += l2c_oz::to_double(T[nt][e], Ec[16 * sg + r] - 52 + Ep[il]);
+            if (r >= nrow || i >= g.s) continue;
+            const long long j = (tau0 + r) * g.h + 2 * i + sg;
+            const double f = l2c_oz::to_double(T[nt][e], Ec[16 * sg + r] - 52 + Ep[il]);
+            ov[j * g.stride] = scale(yv[j] + f, j);
           }
       }
-    }
-    __syncwarp();
-    // y + far, scaled, in output order
-    const long long j0 = tau0 * g.h, jn = min(16LL, g.K - tau0) * g.h;
-    for (long long jj = lane; jj < jn; jj += 32) {
-      const long long j = j0 + jj;
-      if (j >= g.N) break;
-      double val = O[jj];
-      if (!c2l) {
-        val = val * TWO_OVER_PI;
-        if (j == 0) val = val * 0.5;
-      } else {
-        val = val * dyadic(2 * (unsigned long long)j + 1, -1);  // j + 1/2
-      }
-      out[v * g.dist + j * g.stride] = val;
     }
   };
   oz_tile_loop<NBUF>((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue,
                      work);
-}
-
-size_t mz_leaf_down_smem(long long s, int npass, int nbuf) {
-  return (size_t)(2 * npass * OZ_LD_WORDS + 2 * npass * 16 + MXW * (32 + nbuf * 32)) * 4 +
-         (size_t)MXW * (nbuf * 2 * 16 * OZ_CLD + nbuf * 16 * 2 * s) * 8;
-}
-
-// Outputs past the last leaf target node (no far field): scaling only.
-__global__ void k_mx_tail(const double *__restrict__ y, double *out, Geo g, int c2l) {
-  const long long j0 = g.K * g.h, nt = g.N - j0;
-  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (nt <= 0 || idx >= g.count * nt) return;
-  const long long v = idx / nt, j = j0 + (idx - v * nt);
-  double val = y[v * g.N + j];
-  if (!c2l) {
-    val = val * TWO_OVER_PI;
-    if (j == 0) val = val * 0.5;
-  } else {
-    val = val * dyadic(2 * (unsigned long long)j + 1, -1);  // j + 1/2
+  // outputs past the last leaf target node: band sum only
+  const long long jt = g.K * g.h, ntail = g.N - jt;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < g.count * ntail;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long v = idx / ntail, j = jt + (idx - v * ntail);
+    out[v * g.dist + j * g.stride] = scale(y[v * g.N + j], j);
   }
-  out[v * g.dist + j * g.stride] = val;
+}
+
+size_t mz_leaf_down_smem(int npass, int nbuf) {
+  return (size_t)(2 * npass * OZ_LD_WORDS + 2 * npass * 16 + MXW * (32 + nbuf * 32)) * 4 +
+         (size_t)MXW * nbuf * 2 * 16 * OZ_CLD * 8;
 }
 
 // Column format <-> doubles, in place, one thread per 18-coefficient column
@@ -2169,16 +2158,15 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
   }
   if (ov && cudaStreamWaitEvent(st, p->ev_join, 0) != cudaSuccess) return false;
   {
-    const long long tail = g.count * (g.N - g.K * g.h);
-    PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, tail > 0 ? 2 : 1);
+    PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
     const long long tiles = g.count * ((g.K + 15) / 16);
-    const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
+    const int per_sm = p->oz_nbuf == 1 ? 5 : 2;  // resident CTAs (registers, shared memory)
+    const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * per_sm);
     // after the join with the band's stream: a plain launch (full dependency)
     launch_k((pdl_flags(p) & 1) && !ov, p->oz_nbuf == 1 ? k_mz_leaf_down<1> : k_mz_leaf_down<2>,
-             grid, 32 * MXW, mz_leaf_down_smem(g.s, p->oz_npass, p->oz_nbuf), st,
+             grid, 32 * MXW, mz_leaf_down_smem(p->oz_npass, p->oz_nbuf), st,
              (const long long *)c, (const int *)p->cE, (const double *)p->y, out,
              (const unsigned *)p->oz_ld, (const int *)p->oz_lde, g, c2l, p->oz_npass);
-    if (tail > 0) k_mx_tail<<<blocks_for(tail, 256), 256, 0, st>>>(p->y, out, g, c2l);
     if (cudaGetLastError() != cudaSuccess) return false;
   }
   return true;
@@ -2554,8 +2542,8 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
       PCK(upload(&p->oz_lde, lde));
       // kernels whose shared memory can pass the 48 KB default
       const cudaFuncAttribute smax = cudaFuncAttributeMaxDynamicSharedMemorySize;
-      PCK(cudaFuncSetAttribute(k_mz_leaf_down<1>, smax, (int)mz_leaf_down_smem(4 * 16, 4, 1)));
-      PCK(cudaFuncSetAttribute(k_mz_leaf_down<2>, smax, (int)mz_leaf_down_smem(4 * 16, 4, 2)));
+      PCK(cudaFuncSetAttribute(k_mz_leaf_down<1>, smax, (int)mz_leaf_down_smem(4, 1)));
+      PCK(cudaFuncSetAttribute(k_mz_leaf_down<2>, smax, (int)mz_leaf_down_smem(4, 2)));
       PCK(cudaFuncSetAttribute(k_mz_tree_up<2, 1>, smax, (int)oz_tree_up_smem(2, 1)));
       PCK(cudaFuncSetAttribute(k_mz_tree_up<2, 2>, smax, (int)oz_tree_up_smem(2, 2)));
       PCK(cudaFuncSetAttribute(k_mz_tree_up<l2c_oz::SLICES, 1>, smax,

@@ -36,11 +36,13 @@ void scipy_openblas_set_num_threads(int);
 
 struct orc_plan {
   size_t N, L, s, Nn, Nb, dirs; /* dirs: ORC_L2C, ORC_C2L or ORC_BOTH */
+  size_t lagrange;              /* 0 modal, 1 nodal                     */
   double *a;                    /* Lambda(i), i < N                     */
   double *an, *dn;              /* C2L tables (NULL for an L2C plan)    */
   double *A[2];                 /* far-field blocks per direction       */
-  double *T;                    /* Chebyshev Vandermonde, even then odd */
+  double *T;                    /* leaf matrices, even rows then odd    */
   double B[ORC_NTRI], BT[ORC_NTRI];
+  double LB[2 * ORC_MM];        /* nodal: child interpolation B0 | B1   */
 };
 
 void orc_set_threads(int n) {
@@ -294,7 +296,11 @@ static void orc_assemble(orc_plan *p) {
                 else
                   F[ix] = 2 * (fpq[ix] / (f1[ix] * (x + y) * (x + y + 1) * (x - y + 1)));
               }
-            orc_dct2(F, &p->A[dir][(kk + 3 * block + r) * ORC_MM]);
+            double *dst = &p->A[dir][(kk + 3 * block + r) * ORC_MM];
+            if (p->lagrange) /* nodal: the samples themselves (leg2cheb.c:938, 973) */
+              memcpy(dst, F, sizeof(F));
+            else
+              orc_dct2(F, dst);
           }
         }
       }
@@ -320,11 +326,75 @@ static void orc_vandermonde(orc_plan *p) {
   p->T = T;
 }
 
+/* Nodal form, leg2cheb.c:997-1031: barycentric Lagrange weights from the M
+ * Chebyshev points x_j = cos((j + 1/2) pi / M) (weights w_j = (-1)^j
+ * sin((j + 1/2) pi / M)) to the 2s equispaced points -1 + i/s, each row divided
+ * by its sum; rows split even | odd as in the modal T. */
+static void orc_lagrange_T(orc_plan *p) {
+  const size_t s = p->s;
+  const double pi = 3.14159265358979323846;
+  double xj[ORC_M], wj[ORC_M];
+  for (int j = 0; j < ORC_M; j++) {
+    xj[j] = cos((j + 0.5) * pi / ORC_M);
+    wj[j] = ((j % 2 == 0) ? 1 : -1) * sin((j + 0.5) * pi / ORC_M);
+  }
+  double *T = (double *)malloc(2 * s * ORC_M * sizeof(double));
+  for (size_t i = 0; i < s; i++) {
+    const double xe = -1 + (double)(2 * i) / (double)s, xo = -1 + (double)(2 * i + 1) / (double)s;
+    double sume = 0.0, sumo = 0.0;
+    for (int j = 0; j < ORC_M; j++) {
+      const double se = wj[j] / (xe - xj[j]), so = wj[j] / (xo - xj[j]);
+      T[i * ORC_M + j] = se;
+      T[(s + i) * ORC_M + j] = so;
+      sume += se;
+      sumo += so;
+    }
+    for (int j = 0; j < ORC_M; j++) {
+      T[i * ORC_M + j] /= sume;
+      T[(s + i) * ORC_M + j] /= sumo;
+    }
+  }
+  p->T = T;
+}
+
+/* Nodal transfer matrices, leg2cheb.c:1076-1100: B_c[i][j] = l_j((x_i - 1)/2)
+ * (child c = 0) and l_j((x_i + 1)/2) (c = 1), l_j the barycentric Lagrange
+ * basis of the Chebyshev points, rows normalised by their sums. */
+static void orc_lagrange_B(double *B) {
+  const double pi = 3.14159265358979323846;
+  double xj[ORC_M], wj[ORC_M];
+  for (int j = 0; j < ORC_M; j++) {
+    xj[j] = cos((j + 0.5) * pi / ORC_M);
+    wj[j] = ((j % 2 == 0) ? 1 : -1) * sin((j + 0.5) * pi / ORC_M);
+  }
+  for (int i = 0; i < ORC_M; i++) {
+    const double x0 = (xj[i] - 1) / 2, x1 = (xj[i] + 1) / 2;
+    double sum0 = 0.0, sum1 = 0.0;
+    for (int j = 0; j < ORC_M; j++) {
+      const double s0 = wj[j] / (x0 - xj[j]), s1 = wj[j] / (x1 - xj[j]);
+      B[i * ORC_M + j] = s0;
+      B[ORC_MM + i * ORC_M + j] = s1;
+      sum0 += s0;
+      sum1 += s1;
+    }
+    for (int j = 0; j < ORC_M; j++) {
+      B[i * ORC_M + j] /= sum0;
+      B[ORC_MM + i * ORC_M + j] /= sum1;
+    }
+  }
+}
+
 orc_plan *orc_create(size_t N, size_t maxs, size_t dirs) {
+  return orc_create_ex(N, maxs, dirs, 0);
+}
+
+orc_plan *orc_create_ex(size_t N, size_t maxs, size_t dirs, size_t lagrange) {
   orc_plan *p = (orc_plan *)calloc(1, sizeof(orc_plan));
   p->N = N;
   p->dirs = dirs;
+  p->lagrange = lagrange ? 1 : 0;
   orc_binomial(p->B, p->BT);
+  orc_lagrange_B(p->LB);
   /* leg2cheb.c:860-871 */
   const int L = (int)ceil(log2((double)N / (double)maxs)) - 2;
   if (L < 1) {
@@ -343,7 +413,10 @@ orc_plan *orc_create(size_t N, size_t maxs, size_t dirs) {
       p->A[d] = (double *)malloc(3 * p->Nb * ORC_MM * sizeof(double));
   }
   orc_assemble(p);
-  orc_vandermonde(p);
+  if (p->lagrange)
+    orc_lagrange_T(p);
+  else
+    orc_vandermonde(p);
   return p;
 }
 
@@ -369,8 +442,8 @@ void orc_plan_info(const orc_plan *p, size_t *info) {
 const double *orc_plan_A(const orc_plan *p, size_t d) { return d < 2 ? p->A[d] : NULL; }
 const double *orc_plan_T(const orc_plan *p) { return p->T; }
 const double *orc_plan_lambda(const orc_plan *p) { return p->a; }
-const double *orc_plan_B(const orc_plan *p) { return p->B; }
-const double *orc_plan_BT(const orc_plan *p) { return p->BT; }
+const double *orc_plan_B(const orc_plan *p) { return p->lagrange ? p->LB : p->B; }
+const double *orc_plan_BT(const orc_plan *p) { return p->lagrange ? NULL : p->BT; }
 
 /* ---------------------------------------------------------------------------
  * Direct O(N^2) transform, leg2cheb.c:152-234 (used when L < 1).  Reproduces
@@ -522,6 +595,32 @@ static void orc_down(const double *BT, const double *x, double *b) {
   }
 }
 
+/* Nodal upward product, leg2cheb.c:1409-1412 (two dgemv, CblasTrans):
+ * b[j] = sum_i B0[i][j] x0[i] + sum_i B1[i][j] x1[i]. */
+static void orc_up_nodal(const double *LB, const double *x, double *b) {
+  for (int j = 0; j < ORC_M; j++) {
+    double acc = 0.0;
+    for (int i = 0; i < ORC_M; i++) acc += LB[i * ORC_M + j] * x[i];
+    b[j] = acc;
+  }
+  for (int j = 0; j < ORC_M; j++) {
+    double acc = 0.0;
+    for (int i = 0; i < ORC_M; i++) acc += LB[ORC_MM + i * ORC_M + j] * x[ORC_M + i];
+    b[j] += acc;
+  }
+}
+
+/* Nodal downward product, leg2cheb.c:1457-1460 (two dgemv, beta = 1):
+ * child0[i] += sum_j B0[i][j] x[j], child1[i] += sum_j B1[i][j] x[j]. */
+static void orc_down_nodal(const double *LB, const double *x, double *b) {
+  for (int c = 0; c < 2; c++)
+    for (int i = 0; i < ORC_M; i++) {
+      double acc = 0.0;
+      for (int j = 0; j < ORC_M; j++) acc += LB[c * ORC_MM + i * ORC_M + j] * x[j];
+      b[c * ORC_M + i] += acc;
+    }
+}
+
 /* One FMM transform, leg2cheb.c:1299-1500. */
 size_t orc_execute(const double *in, double *out, orc_plan *p, size_t dir, size_t stride) {
   if (dir > 1) return 0;
@@ -586,16 +685,20 @@ size_t orc_execute(const double *in, double *out, orc_plan *p, size_t dir, size_
 #endif
     flops += 2 * K * s * M;
 
-    /* step 2: upward transfer, leg2cheb.c:1385-1399 */
+    /* step 2: upward transfer, leg2cheb.c:1385-1399 (modal) and 1401-1416
+     * (nodal: parent = B0^T child0 + B1^T child1) */
     for (size_t level = L; level-- > 1;) {
       double *w1 = &wk[lvl[level - 1]];
       const double *w2 = &wk[lvl[level]];
 #pragma omp parallel for schedule(static)
       for (size_t block = 1; block < nblocks(level); block++) {
         const size_t b0 = (block - 1) / 2, q0 = (block - 1) % 2;
-        orc_up(p->B, &w2[block * 2 * M], &w1[(b0 * 2 + q0) * M]);
+        if (p->lagrange)
+          orc_up_nodal(p->LB, &w2[block * 2 * M], &w1[(b0 * 2 + q0) * M]);
+        else
+          orc_up(p->B, &w2[block * 2 * M], &w1[(b0 * 2 + q0) * M]);
       }
-      flops += (nblocks(level) - 1) * M * M;
+      flops += (nblocks(level) - 1) * M * M * (p->lagrange ? 4 : 1);
     }
 
     /* step 3: far-field blocks, leg2cheb.c:1419-1435 */
@@ -622,14 +725,19 @@ size_t orc_execute(const double *in, double *out, orc_plan *p, size_t dir, size_
     }
     flops += 3 * Nb * 2 * M * M;
 
-    /* step 4: downward transfer, leg2cheb.c:1437-1448 */
+    /* step 4: downward transfer, leg2cheb.c:1437-1448 (modal) and 1450-1464
+     * (nodal: child_c += B_c parent) */
     for (size_t level = 0; level + 1 < L; level++) {
       const double *c0 = &ck[lvl[level]];
       double *c1 = &ck[lvl[level + 1]];
 #pragma omp parallel for schedule(static)
-      for (size_t block = 0; block < nblocks(level + 1) - 1; block++)
-        orc_down(p->BT, &c0[block * M], &c1[block * 2 * M]);
-      flops += (nblocks(level + 1) - 1) * M * M;
+      for (size_t block = 0; block < nblocks(level + 1) - 1; block++) {
+        if (p->lagrange)
+          orc_down_nodal(p->LB, &c0[block * M], &c1[block * 2 * M]);
+        else
+          orc_down(p->BT, &c0[block * M], &c1[block * 2 * M]);
+      }
+      flops += (nblocks(level + 1) - 1) * M * M * (p->lagrange ? 4 : 1);
     }
 
     /* step 5: back to leaf values and scatter, leg2cheb.c:1467-1483 */

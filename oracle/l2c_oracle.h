@@ -30,6 +30,9 @@ double orc_LambdaI(size_t z);
 /* Plan for one transform length, leg2cheb.c:820-1234 (modal form, M = 18).
  * direction: ORC_L2C, ORC_C2L or ORC_BOTH. */
 orc_plan *orc_create(size_t N, size_t maxs, size_t direction);
+/* Same with the form: lagrange = 0 modal, 1 nodal (leg2cheb.c:997-1031,
+ * 1076-1100; the far-field blocks are then the kernel samples, not their DCT). */
+orc_plan *orc_create_ex(size_t N, size_t maxs, size_t direction, size_t lagrange);
 void orc_free(orc_plan *p);
 
 /* One transform, leg2cheb.c:1299-1500 (FMM) or leg2cheb.c:152-234 (direct, L < 1).
@@ -59,8 +62,8 @@ void orc_plan_info(const orc_plan *p, size_t *info);
 const double *orc_plan_A(const orc_plan *p, size_t direction); /* 3*N_b*M*M */
 const double *orc_plan_T(const orc_plan *p);                   /* 2*s*M     */
 const double *orc_plan_lambda(const orc_plan *p);              /* a[0..N)   */
-const double *orc_plan_B(const orc_plan *p);                   /* 171       */
-const double *orc_plan_BT(const orc_plan *p);                  /* 171       */
+const double *orc_plan_B(const orc_plan *p);  /* 171 (modal) or B0 | B1, 2*M*M (nodal) */
+const double *orc_plan_BT(const orc_plan *p); /* 171 (modal), NULL (nodal)            */
 
 void orc_set_threads(int n);
 /* 1 when built against OpenBLAS (steps 1 and 5 through CBLAS dgemm, as the reference). */

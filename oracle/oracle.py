@@ -30,6 +30,8 @@ def load():
     sz, vp = ctypes.c_size_t, ctypes.c_void_p
     lib.orc_create.restype = vp
     lib.orc_create.argtypes = [sz, sz, sz]
+    lib.orc_create_ex.restype = vp
+    lib.orc_create_ex.argtypes = [sz, sz, sz, sz]
     lib.orc_free.argtypes = [vp]
     lib.orc_execute.restype = sz
     lib.orc_execute.argtypes = [vp, vp, vp, sz, sz]
@@ -58,10 +60,11 @@ def load():
 
 
 class Oracle:
-    def __init__(self, N, maxs=64, direction=2):
+    def __init__(self, N, maxs=64, direction=2, lagrange=0):
         lib = load()
         self.N = int(N)
-        self._p = lib.orc_create(N, maxs, direction)
+        self.lagrange = int(lagrange)
+        self._p = lib.orc_create_ex(N, maxs, direction, self.lagrange)
         info = (ctypes.c_size_t * 6)()
         lib.orc_plan_info(self._p, info)
         self.L, self.s, self.Nn, self.Nb = int(info[1]), int(info[2]), int(info[3]), int(info[4])
@@ -98,6 +101,11 @@ class Oracle:
 
     def T(self):
         return np.ctypeslib.as_array(load().orc_plan_T(self._p), (2 * self.s * 18,)).copy()
+
+    def B(self):
+        """Transfer matrices: compact binomial (171, modal) or B0 | B1 (648, nodal)."""
+        n = 2 * 324 if self.lagrange else 171
+        return np.ctypeslib.as_array(load().orc_plan_B(self._p), (n,)).copy()
 
     def close(self):
         if getattr(self, "_p", None):

@@ -56,3 +56,20 @@ def _cases():
 
 
 CASES = _cases()
+
+
+def _nodal_cases():
+    """Nodal form (create_fmm with lagrange = 1): FMM path only (the direct
+    path does not depend on the form)."""
+    c = {}
+    for N, maxs in ((512, 64), (1024, 64), (4096, 32), (6000, 50), (16384, 64)):
+        for d in (0, 1):
+            for dist in ("uniform", "sign"):
+                c[f"nodal_N{N}_s{maxs}_d{d}_st1_{dist}"] = (N, maxs, d, 1, dist, 400 + N + d)
+    for d in (0, 1):
+        c[f"nodal_N1024_s64_d{d}_st3_gauss2"] = (1024, 64, d, 3, "gauss2", 500 + d)
+    c["nodal_N1023_s64_d1_st1_uniform"] = (1023, 64, 1, 1, "uniform", 601)
+    return c
+
+
+NODAL_CASES = _nodal_cases()

@@ -10,6 +10,9 @@ Contents (all produced by the reference's own code):
   * execute() outputs and flop counts for a list of (N, maxs, direction,
     stride, distribution, seed) cases, inputs regenerated from the seed.
   * the reference's round-trip (L2C then C2L, like `l2c -N512 -d2`)
+  * nodal form (lagrange = 1): execute() outputs and flop counts for
+    NODAL_CASES, and the plan's T and B (fmm_plan fields, leg2cheb.h:58-78)
+    for N = 1024, maxs = 64
 
 Output buffers handed to the reference carry 8 doubles of slack: for odd N
 its parity scatter writes one element past the end (leg2cheb.c:1473-1476).
@@ -25,7 +28,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
-from tests.golden.cases import CASES, make_input  # noqa: E402
+from tests.golden.cases import CASES, NODAL_CASES, make_input  # noqa: E402
 
 LIB = os.path.join(REPO, "oracle", "_ref", "libleg2cheb_ref.so")
 
@@ -73,6 +76,26 @@ def main():
         ref.free_fmm(plan)
         out[f"roundtrip_{N}_{maxs}/cheb"] = c[:N].copy()
         out[f"roundtrip_{N}_{maxs}/leg"] = b[:N].copy()
+
+    for key, (N, maxs, direction, stride, dist, seed) in NODAL_CASES.items():
+        u = make_input(N * stride, dist, seed)
+        plan = ref.create_fmm(N, maxs, 18, 2, 1, 0, 0)
+        o = np.zeros(N * stride + 8)
+        flops = ref.execute(u.ctypes.data, o.ctypes.data, plan, direction, stride)
+        ref.free_fmm(plan)
+        out[key + "/out"] = o[: N * stride].copy()
+        out[key + "/flops"] = np.array(flops, dtype=np.uint64)
+
+    # nodal plan data: fmm_plan is 7 size_t (direction, M, N, Nn, L, s,
+    # lagrange), then double **A, double *T, double *B, double *BT
+    plan = ref.create_fmm(1024, 64, 18, 2, 1, 0, 0)
+    fields = (ctypes.c_void_p * 11).from_address(plan)
+    s = ctypes.cast(plan + 5 * 8, ctypes.POINTER(ctypes.c_size_t))[0]
+    Tp = ctypes.cast(fields[8], ctypes.POINTER(ctypes.c_double))
+    Bp = ctypes.cast(fields[9], ctypes.POINTER(ctypes.c_double))
+    out["nodal_plan_N1024_s64/T"] = np.ctypeslib.as_array(Tp, (2 * s * 18,)).copy()
+    out["nodal_plan_N1024_s64/B"] = np.ctypeslib.as_array(Bp, (2 * 324,)).copy()
+    ref.free_fmm(plan)
 
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", len(out), "arrays")

@@ -8,7 +8,7 @@ import pytest
 
 from oracle import direct_ld
 from tests.conftest import relerr
-from tests.golden.cases import CASES, make_input
+from tests.golden.cases import CASES, NODAL_CASES, make_input
 
 # the port follows the reference's arithmetic; differences come only from the
 # DCT and BLAS summation order (~1e-16)
@@ -25,6 +25,37 @@ def test_oracle_matches_reference_execute(orc, golden, key):
     ref = golden[key + "/out"]
     assert flops == int(golden[key + "/flops"])
     assert relerr(out, ref) <= PORT_TOL
+
+
+@pytest.mark.parametrize("key", sorted(NODAL_CASES))
+def test_nodal_oracle_matches_reference_execute(orc, golden, key):
+    # nodal form (lagrange = 1): the same transform through Lagrange
+    # interpolation on the Chebyshev points instead of Chebyshev coefficients
+    N, maxs, d, st, dist, seed = NODAL_CASES[key]
+    u = make_input(N * st, dist, seed)
+    o = orc.Oracle(N, maxs, 2, lagrange=1)
+    out = np.zeros(N * st)
+    flops = o.execute(u, out, d, st)
+    assert flops == int(golden[key + "/flops"])
+    assert relerr(out, golden[key + "/out"]) <= PORT_TOL
+
+
+def test_nodal_plan_tables_bitwise(orc, golden):
+    # barycentric leaf matrices T (leg2cheb.c:997-1031) and the two child
+    # interpolation matrices B0 | B1 (leg2cheb.c:1076-1100)
+    o = orc.Oracle(1024, 64, 2, lagrange=1)
+    assert np.array_equal(o.T(), golden["nodal_plan_N1024_s64/T"])
+    assert np.array_equal(o.B(), golden["nodal_plan_N1024_s64/B"])
+
+
+@pytest.mark.parametrize("d", [0, 1])
+def test_nodal_and_modal_agree(orc, d):
+    # two discretisations of the same far field: equal to rounding
+    N = 8192
+    u = make_input(N, "sign", 9)
+    a = orc.Oracle(N, 64, 2, lagrange=0)(u, d)[:N]
+    b = orc.Oracle(N, 64, 2, lagrange=1)(u, d)[:N]
+    assert relerr(b, a) <= 5e-15
 
 
 def test_known_answers_N20(orc):
