@@ -198,7 +198,7 @@ def ragged_lengths(count, seed, lo=64, hi=65536):
     return np.round(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(np.int64)
 
 
-def workload_config(N, maxs, workload="single", count=1, total=None):
+def workload_config(N, maxs, workload="single", count=1, total=None, lagrange=0):
     if workload == "ragged":
         return {"workload": f"ragged list: {count} vectors, N log-uniform in [64, 65536] (seeded), "
                             f"{total} coefficients in total, iid U[-1,1]; L2C and C2L, "
@@ -208,23 +208,24 @@ def workload_config(N, maxs, workload="single", count=1, total=None):
                 "transforms_per_step": 2 * count}
     L = math.ceil(math.log2(N / maxs)) - 2
     s = math.ceil(N / 2 ** (L + 2)) if L >= 1 else 0
+    form = "nodal (lagrange=1)" if lagrange else "plain FP64"
     if workload == "batch":
         desc = (f"batched lines: {count} transforms of N={N} along the last axis of a "
                 f"64x64x{N} float64 array (dist={N}, stride=1), x = N(0,1)(n+1)^-2; "
-                f"L2C then C2L of the result, maxs={maxs} (s={s}, L={L}), plain FP64")
+                f"L2C then C2L of the result, maxs={maxs} (s={s}, L={L}), {form}")
     else:
         desc = (f"single vector L2C + C2L, N={N}, maxs={maxs} (s={s}, L={L}), "
-                "c_n = s_n/(n+1), plain FP64")
+                f"c_n = s_n/(n+1), {form}")
     return {"workload": desc, "N": N, "maxs": maxs, "s": s, "L": L, "vectors": count,
-            "precision": "fp64", "l2_flush": "256 MiB write between steps",
+            "precision": "fp64", "lagrange": lagrange, "l2_flush": "256 MiB write between steps",
             "transforms_per_step": 2 * count}
 
 
 class Workload:
     """A step: a list of transforms (direction, input, output) on one plan."""
 
-    def __init__(self, name, N, maxs, seed):
-        self.name, self.N, self.maxs = name, N, maxs
+    def __init__(self, name, N, maxs, seed, lagrange=0):
+        self.name, self.N, self.maxs, self.lagrange = name, N, maxs, lagrange
         if name == "single":
             self.count = 1
             self.u = sign_decay_input(N, seed)[None, :]
@@ -258,14 +259,14 @@ class Workload:
 
     def config(self):
         return workload_config(self.N, self.maxs, self.name, self.count,
-                               getattr(self, "total", None))
+                               getattr(self, "total", None), self.lagrange)
 
     def cpu_oracle(self, oracle):
         if self.name == "mixed_batch_ref":
             return oracle.Oracle(self.N, self.maxs, 2)
         if self.name == "ragged":
             return oracle.RaggedOracle(self.Ns, self.maxs, 2)
-        return oracle.Oracle(self.N, self.maxs, 2)
+        return oracle.Oracle(self.N, self.maxs, 2, self.lagrange)
 
     def cpu_call(self, o, src, dst, d):
         if self.name == "ragged":
@@ -305,7 +306,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    wl = Workload(args.workload, args.N, args.maxs, 1)
+    wl = Workload(args.workload, args.N, args.maxs, 1, args.lagrange)
     threads = os.cpu_count() or 1
     sys.path.insert(0, REPO)
     from oracle import oracle
@@ -502,6 +503,8 @@ def main():
     ap.add_argument("--precompute", type=int, default=0,
                     help="1: keep the near-field band weights in device memory (create_fmm's "
                          "precompute argument)")
+    ap.add_argument("--lagrange", type=int, default=0, choices=[0, 1],
+                    help="1: the nodal form (create_fmm's lagrange argument; single, batch)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
@@ -509,6 +512,8 @@ def main():
     if args.N is None:
         args.N = {"single": 1 << 20, "batch": 1024, "ragged": 1024, "mixed_single": 1 << 22,
                   "mixed_batch": 16384}[args.workload]
+    if args.lagrange and args.workload not in ("single", "batch"):
+        ap.error("--lagrange 1 applies to the single and batch workloads")
     if args.workload.startswith("mixed"):
         if args.impl == "reference":
             args.workload = "single" if args.workload == "mixed_single" else "mixed_batch_ref"
@@ -539,13 +544,13 @@ def main():
     import l2c_gb300 as l2c
 
     abi = l2c.cuda_abi()
-    wl = Workload(args.workload, args.N, args.maxs, 1 + rank)
+    wl = Workload(args.workload, args.N, args.maxs, 1 + rank, args.lagrange)
     N, maxs, count = wl.N, wl.maxs, wl.count
     ragged = wl.name == "ragged"
     if ragged:
         plan = l2c.RaggedPlan(wl.Ns, maxs)
     else:
-        plan = l2c.Plan(N, maxs, precompute=args.precompute)
+        plan = l2c.Plan(N, maxs, precompute=args.precompute, lagrange=args.lagrange)
     stream = torch.cuda.ExternalStream(plan.stream, device=dev)
     dbuf = {"u": torch.from_numpy(np.ascontiguousarray(wl.u)).to(dev)}
     dbuf["o0"] = torch.zeros_like(dbuf["u"])
@@ -647,7 +652,7 @@ def main():
         # (dram__bytes_read.sum + dram__bytes_write.sum, mean of the L2C and C2L
         # launches); other workloads were not captured.
         captured = (wl.name == "single" and N == 1 << 20 and maxs == 64
-                    and args.precompute == 0)
+                    and args.precompute == 0 and args.lagrange == 0)
         roof = {"bound": "tensor", "pipe": "fp64", "kernel": "k_near (near-field band)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": 25.2e6 + 256 if captured else None,

@@ -32,6 +32,12 @@ typedef struct l2c_gpu_plan l2c_gpu_plan;
                                 FP64 instructions); near-field band, accumulation and
                                 scaling in FP64.  Leaf sizes s <= 64. */
 
+#define L2C_PLAN_NODAL 8u /* nodal (Lagrange) form, create_fmm's lagrange = 1
+                                (leg2cheb.c:997-1031, 1076-1100): leaf matrices of
+                                barycentric interpolation weights, far-field blocks
+                                of kernel samples, transfer matrices B0 | B1.
+                                Not combinable with L2C_PLAN_MIXED. */
+
 /* Execute flags */
 #define L2C_EXEC_ASYNC 1u       /* return without waiting (device pointers only)  */
 #define L2C_EXEC_NEAR_ONLY 2u   /* near-field band + final scaling only (directM/L) */
@@ -41,9 +47,9 @@ typedef struct l2c_gpu_plan l2c_gpu_plan;
  * Returns L. */
 size_t l2c_geometry(size_t N, size_t maxs, size_t *s, size_t *Nn);
 
-/* Build the device plan: Lambda tables, Chebyshev Vandermonde T, the far-field
+/* Build the device plan: Lambda tables, the leaf matrices T, the far-field
  * blocks A for each planned direction (directions: 0 L2C, 1 C2L, 2 both), all on
- * the current CUDA device.  M = 18 (the modal form). */
+ * the current CUDA device.  M = 18; modal form unless L2C_PLAN_NODAL. */
 l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsigned flags);
 void l2c_gpu_plan_destroy(l2c_gpu_plan *plan);
 
@@ -89,7 +95,8 @@ int l2c_gpu_profile(l2c_gpu_plan *plan, int enable);
 int l2c_gpu_profile_read(l2c_gpu_plan *plan, double *ms, size_t *launches);
 
 /* Copy plan tables to host memory, for checking plan construction.
- * which: 0 = A[L2C], 1 = A[C2L], 2 = Lambda table a, 3 = an, 4 = dn, 5 = T.
+ * which: 0 = A[L2C], 1 = A[C2L], 2 = Lambda table a, 3 = an, 4 = dn, 5 = T,
+ * 6 = nodal transfer matrices B0 | B1 (2 M^2; nodal plans only).
  * Returns the number of doubles copied (n_max caps it), 0 if absent. */
 size_t l2c_gpu_plan_copy(const l2c_gpu_plan *plan, int which, double *dst, size_t n_max);
 

@@ -74,6 +74,9 @@ __constant__ double c_binom_lower[NTRI] = L2C_BINOM_LOWER_INIT;
 __constant__ double c_binom_upper[NTRI] = L2C_BINOM_UPPER_INIT;
 __constant__ double c_xj[M];       // cos((i + 1/2) pi / M), host libm values
 __constant__ double c_dct[M * M];  // cos(pi k (n + 1/2) / M), [k][n]
+// Nodal form: interpolation from the Chebyshev points of a parent interval to
+// those of its two children, B0 | B1 (row-major M x M each, leg2cheb.c:1076-1100)
+__constant__ double c_lag_B[2 * M * M];
 
 // Programmatic dependent launch.  A kernel launched with programmatic stream
 // serialization may start while the previous kernel on its stream is still
@@ -185,10 +188,11 @@ __global__ void k_assemble_f0(double *f0, size_t L, size_t s) {
 
 // One far-field block per CTA: blockIdx.x = 3 g + r, g = global block index,
 // r over (q,p) = (0,0), (1,0), (1,1).  Samples the kernel on the 18x18 Chebyshev
-// grid (leg2cheb.c:924-972) and converts it with a 2D DCT-II,
-// A = (4/M^2) C F C^T with row 0 and column 0 halved (dct.c:582-598).
+// grid (leg2cheb.c:924-972) and, in the modal form, converts it with a 2D
+// DCT-II, A = (4/M^2) C F C^T with row 0 and column 0 halved (dct.c:582-598);
+// the nodal form keeps the samples.
 __global__ void __launch_bounds__(MM) k_assemble_A(const double *__restrict__ f0, double *A_l2c,
-                                                   double *A_c2l, size_t L, size_t s) {
+                                                   double *A_c2l, size_t L, size_t s, int nodal) {
   __shared__ double sF1[MM];
   __shared__ double sF[MM];
   __shared__ double sT[MM];
@@ -228,6 +232,10 @@ __global__ void __launch_bounds__(MM) k_assemble_A(const double *__restrict__ f0
       den = __dmul_rn(den, __dadd_rn(xy, 1.0));
       den = __dmul_rn(den, __dadd_rn(__dsub_rn(x, y), 1.0));
       sF[t] = __dmul_rn(2.0, __ddiv_rn(fpq, den));
+    }
+    if (nodal) {  // the nodal form keeps the kernel samples (leg2cheb.c:938, 973)
+      Ad[(size_t)blockIdx.x * MM + t] = sF[t];
+      continue;
     }
     __syncthreads();
     // rows: sT[i][k] = sum_n F[i][n] C[k][n]
@@ -565,8 +573,73 @@ __global__ void __launch_bounds__(288) k_leaf_up(const double *__restrict__ x,
 constexpr int TREE_TILE = 32;
 constexpr int TREE_PAD = 2 * M + 1;  // padded row of staged children (bank spread)
 
+// Transfer matrices in shared memory: modal, the compact lower (upward) or
+// upper (downward) binomial matrix, NTRI doubles; nodal, B0 | B1 (2 M^2).
+template <bool NODAL>
+__host__ __device__ constexpr int tree_mat_size() {
+  return NODAL ? 2 * MM : NTRI;
+}
+template <bool NODAL, bool UP>
+__device__ __forceinline__ void load_tree_mat(double *sB) {
+  for (int t = threadIdx.x; t < tree_mat_size<NODAL>(); t += blockDim.x)
+    sB[t] = NODAL ? c_lag_B[t] : UP ? c_binom_lower[t] : c_binom_upper[t];
+}
+
+// Row m of a parent from its two children x0, x1.  Modal: the lower binomial
+// row with the +/- parity combination of the second child (leg2cheb.c:537-602);
+// nodal: column m of B0 and of B1, out = B0^T x0 + B1^T x1 (leg2cheb.c:1401-1416).
+template <bool NODAL>
+__device__ __forceinline__ void row_up(const double *sB, const double *x0, const double *x1, int m,
+                                       double &out) {
+  double s0 = 0.0, s1 = 0.0;
+  if (NODAL) {
+    for (int i = 0; i < M; i++) {
+      s0 = fma(sB[i * M + m], x0[i], s0);
+      s1 = fma(sB[MM + i * M + m], x1[i], s1);
+    }
+  } else {
+    const double *Bm = sB + m * (m + 1) / 2;
+    for (int i = 0; i <= m; i++) {
+      const double bmi = Bm[i];
+      s0 = fma(bmi, x0[i], s0);
+      s1 = fma(((m + i) & 1) ? -bmi : bmi, x1[i], s1);
+    }
+  }
+  out = s0 + s1;
+}
+
+// Increments d0, d1 of row i of the two children of parent xp.  Modal: the
+// compact upper binomial row, se/so over the columns of equal/opposite parity
+// to the row, d0 = se + so, d1 = se - so (leg2cheb.c:603-618); nodal: row i of
+// B0 and of B1 (leg2cheb.c:1450-1464).
+template <bool NODAL>
+__device__ __forceinline__ void row_down(const double *sB, const double *xp, int i, double &d0,
+                                         double &d1) {
+  if (NODAL) {
+    double a = 0.0, b = 0.0;
+    for (int j = 0; j < M; j++) {
+      a = fma(sB[i * M + j], xp[j], a);
+      b = fma(sB[MM + i * M + j], xp[j], b);
+    }
+    d0 = a;
+    d1 = b;
+    return;
+  }
+  const double *Bu = sB + i * M - i * (i - 1) / 2 - i;  // Bu[j] = row i, column j
+  double se = 0.0, so = 0.0;
+  int j = i;
+  for (; j + 1 < M; j += 2) {
+    se = fma(Bu[j], xp[j], se);
+    so = fma(Bu[j + 1], xp[j + 1], so);
+  }
+  if (j < M) se = fma(Bu[j], xp[j], se);
+  d0 = se + so;
+  d1 = se - so;
+}
+
 // One tile: child[p] points at the 2M child coefficients of item p, par[p] at
 // its M parent coefficients (nullptr: no item).
+template <bool NODAL = false>
 __device__ __forceinline__ void tree_up_tile(const double *const *child, double *const *par,
                                              const double *sB, double *sx) {
   for (int e = threadIdx.x; e < TREE_TILE * 2 * M; e += blockDim.x) {
@@ -577,26 +650,22 @@ __device__ __forceinline__ void tree_up_tile(const double *const *child, double 
   const int m = threadIdx.x >> 5, p = threadIdx.x & 31;
   if (m >= M || par[p] == nullptr) return;
   const double *x0 = sx + p * TREE_PAD, *x1 = x0 + M;
-  const double *Bm = sB + m * (m + 1) / 2;
-  double s0 = 0.0, s1 = 0.0;
-  for (int i = 0; i <= m; i++) {
-    const double bmi = Bm[i];
-    s0 = fma(bmi, x0[i], s0);
-    s1 = fma(((m + i) & 1) ? -bmi : bmi, x1[i], s1);
-  }
-  par[p][m] = s0 + s1;
+  double out;
+  row_up<NODAL>(sB, x0, x1, m, out);
+  par[p][m] = out;
 }
 
 // blockDim = 32 * M; items (vector * 2 + parity, parent slot) in TREE_TILE tiles.
+template <bool NODAL>
 __global__ void __launch_bounds__(32 * M) k_tree_up(double *w, Geo g, long long parent_base,
                                                     long long child_base, long long nparent) {
   pdl_wait();
   pdl_trigger();
-  __shared__ double sB[NTRI];
+  __shared__ double sB[tree_mat_size<NODAL>()];
   __shared__ double sx[TREE_TILE * TREE_PAD];
   __shared__ const double *child[TREE_TILE];
   __shared__ double *par[TREE_TILE];
-  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_lower[t];
+  load_tree_mat<NODAL, true>(sB);
   if (threadIdx.x < TREE_TILE) {
     const long long item = (long long)blockIdx.x * TREE_TILE + threadIdx.x;
     const long long nitem = g.count * 2 * nparent;
@@ -605,7 +674,7 @@ __global__ void __launch_bounds__(32 * M) k_tree_up(double *w, Geo g, long long 
     par[threadIdx.x] = item < nitem ? w + (vs * g.slots + parent_base + jp) * M : nullptr;
   }
   __syncthreads();
-  tree_up_tile(child, par, sB, sx);
+  tree_up_tile<NODAL>(child, par, sB, sx);
 }
 
 // Two-stage sweeps for deep trees.  Every tree level costs a launch and a chain
@@ -621,39 +690,15 @@ __global__ void __launch_bounds__(32 * M) k_tree_up(double *w, Geo g, long long 
 // slots are nodes 0..2^(l+2)-3.
 constexpr int SUB_PAD = M + 1;  // padded node stride in shared memory
 
-__device__ __forceinline__ void row_up(const double *sB, const double *x0, const double *x1, int m,
-                                       double &out) {
-  const double *Bm = sB + m * (m + 1) / 2;
-  double s0 = 0.0, s1 = 0.0;
-  for (int i = 0; i <= m; i++) {
-    const double bmi = Bm[i];
-    s0 = fma(bmi, x0[i], s0);
-    s1 = fma(((m + i) & 1) ? -bmi : bmi, x1[i], s1);
-  }
-  out = s0 + s1;
-}
-
-__device__ __forceinline__ void row_down(const double *sB, const double *xp, int i, double &se,
-                                         double &so) {
-  const double *Bu = sB + i * M - i * (i - 1) / 2 - i;
-  se = 0.0;
-  so = 0.0;
-  int j = i;
-  for (; j + 1 < M; j += 2) {
-    se = fma(Bu[j], xp[j], se);
-    so = fma(Bu[j + 1], xp[j + 1], so);
-  }
-  if (j < M) se = fma(Bu[j], xp[j], se);
-}
-
 // Upward, levels L-1 .. l0 of one subtree.  blockIdx.x = vs * R + r, R = 2^(l0+2).
 // Dynamic shared memory: (2^(d+1) - 1) nodes of SUB_PAD doubles.
+template <bool NODAL>
 __global__ void __launch_bounds__(32 * M) k_up_sub(double *w, Geo g, int l0, int d) {
   pdl_wait();
   pdl_trigger();
   extern __shared__ double sm[];
-  __shared__ double sB[NTRI];
-  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_lower[t];
+  __shared__ double sB[tree_mat_size<NODAL>()];
+  load_tree_mat<NODAL, true>(sB);
   const long long R = 4LL << l0;
   const long long vs = blockIdx.x / R, r = blockIdx.x - vs * R;
   double *ws = w + vs * g.slots * M;
@@ -677,7 +722,7 @@ __global__ void __launch_bounds__(32 * M) k_up_sub(double *w, Geo g, int l0, int
         const long long u = r * np + p;
         if (u < 2) continue;
         double out;
-        row_up(sB, child + 2 * p * SUB_PAD, child + (2 * p + 1) * SUB_PAD, m, out);
+        row_up<NODAL>(sB, child + 2 * p * SUB_PAD, child + (2 * p + 1) * SUB_PAD, m, out);
         par[p * SUB_PAD + m] = out;
         ws[(base + u - 2) * M + m] = out;
       }
@@ -689,12 +734,13 @@ __global__ void __launch_bounds__(32 * M) k_up_sub(double *w, Geo g, int l0, int
 
 // Upward, levels lt-1 .. 0 of one (vector, parity) from level lt in global
 // memory.  Dynamic shared memory: sum over l <= lt of 2^(l+2) nodes.
+template <bool NODAL>
 __global__ void __launch_bounds__(32 * M) k_up_top(double *w, Geo g, int lt) {
   pdl_wait();
   pdl_trigger();
   extern __shared__ double sm[];
-  __shared__ double sB[NTRI];
-  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_lower[t];
+  __shared__ double sB[tree_mat_size<NODAL>()];
+  load_tree_mat<NODAL, true>(sB);
   const long long vs = blockIdx.x;
   double *ws = w + vs * g.slots * M;
   // node t of level l at sm + (off(l) + t) * SUB_PAD, off(l) = 2^(l+2) - 4
@@ -713,7 +759,7 @@ __global__ void __launch_bounds__(32 * M) k_up_top(double *w, Geo g, int lt) {
     if (m < M) {
       for (long long u = 2 + lane; u < nn; u += 32) {
         double out;
-        row_up(sB, child + 2 * u * SUB_PAD, child + (2 * u + 1) * SUB_PAD, m, out);
+        row_up<NODAL>(sB, child + 2 * u * SUB_PAD, child + (2 * u + 1) * SUB_PAD, m, out);
         par[u * SUB_PAD + m] = out;
         ws[(base + u - 2) * M + m] = out;
       }
@@ -724,12 +770,13 @@ __global__ void __launch_bounds__(32 * M) k_up_top(double *w, Geo g, int lt) {
 
 // Downward, levels 0 .. lt of one (vector, parity): c[l+1] += B^T c[l] for
 // l < lt, then levels 1..lt written back.  Dynamic shared memory as k_up_top.
+template <bool NODAL>
 __global__ void __launch_bounds__(32 * M) k_down_top(double *c, Geo g, int lt) {
   pdl_wait();
   pdl_trigger();
   extern __shared__ double sm[];
-  __shared__ double sB[NTRI];
-  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_upper[t];
+  __shared__ double sB[tree_mat_size<NODAL>()];
+  load_tree_mat<NODAL, false>(sB);
   const long long vs = blockIdx.x;
   double *cs = c + vs * g.slots * M;
   // target node t of level l at sm + (off(l) + t) * SUB_PAD; slots t < 2^(l+2)-2
@@ -749,10 +796,10 @@ __global__ void __launch_bounds__(32 * M) k_down_top(double *c, Geo g, int lt) {
     double *par = sm + ((4LL << l) - 4) * SUB_PAD, *child = sm + ((8LL << l) - 4) * SUB_PAD;
     if (i < M) {
       for (long long t = lane; t < nn; t += 32) {
-        double se, so;
-        row_down(sB, par + t * SUB_PAD, i, se, so);
-        child[(2 * t) * SUB_PAD + i] += se + so;
-        child[(2 * t + 1) * SUB_PAD + i] += se - so;
+        double d0, d1;
+        row_down<NODAL>(sB, par + t * SUB_PAD, i, d0, d1);
+        child[(2 * t) * SUB_PAD + i] += d0;
+        child[(2 * t + 1) * SUB_PAD + i] += d1;
       }
     }
     __syncthreads();
@@ -770,12 +817,13 @@ __global__ void __launch_bounds__(32 * M) k_down_top(double *c, Geo g, int lt) {
 
 // Downward, levels l0 .. L-1 of one subtree (target root r at level l0);
 // writes the final leaf level.  blockIdx.x = vs * R + r.
+template <bool NODAL>
 __global__ void __launch_bounds__(32 * M) k_down_sub(double *c, Geo g, int l0, int d) {
   pdl_wait();
   pdl_trigger();
   extern __shared__ double sm[];
-  __shared__ double sB[NTRI];
-  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_upper[t];
+  __shared__ double sB[tree_mat_size<NODAL>()];
+  load_tree_mat<NODAL, false>(sB);
   const long long R = 4LL << l0;
   const long long vs = blockIdx.x / R, r = blockIdx.x - vs * R;
   double *cs = c + vs * g.slots * M;
@@ -800,10 +848,10 @@ __global__ void __launch_bounds__(32 * M) k_down_sub(double *c, Geo g, int l0, i
     if (i < M) {
       for (int p = lane; p < nk; p += 32) {
         if (r * nk + p >= nslot) continue;
-        double se, so;
-        row_down(sB, par + p * SUB_PAD, i, se, so);
-        child[(2 * p) * SUB_PAD + i] += se + so;
-        child[(2 * p + 1) * SUB_PAD + i] += se - so;
+        double d0, d1;
+        row_down<NODAL>(sB, par + p * SUB_PAD, i, d0, d1);
+        child[(2 * p) * SUB_PAD + i] += d0;
+        child[(2 * p + 1) * SUB_PAD + i] += d1;
       }
     }
     __syncthreads();
@@ -861,6 +909,7 @@ __global__ void __launch_bounds__(256) k_far(const double *__restrict__ A,
 // columns of equal/opposite parity to the row, child0 += se + so,
 // child1 += se - so (leg2cheb.c:603-618).  Tiled as k_tree_up: the M parent
 // coefficients of TREE_TILE parents staged in shared memory, warp i computes row i.
+template <bool NODAL = false>
 __device__ __forceinline__ void tree_down_tile(const double *const *par, double *const *child,
                                                const double *sB, double *sx) {
   for (int e = threadIdx.x; e < TREE_TILE * M; e += blockDim.x) {
@@ -870,29 +919,23 @@ __device__ __forceinline__ void tree_down_tile(const double *const *par, double 
   __syncthreads();
   const int i = threadIdx.x >> 5, p = threadIdx.x & 31;
   if (i >= M || child[p] == nullptr) return;
-  const double *xp = sx + p * TREE_PAD;
-  const double *Bu = sB + i * M - i * (i - 1) / 2 - i;  // Bu[j] = row i, column j
-  double se = 0.0, so = 0.0;
-  int j = i;
-  for (; j + 1 < M; j += 2) {
-    se = fma(Bu[j], xp[j], se);
-    so = fma(Bu[j + 1], xp[j + 1], so);
-  }
-  if (j < M) se = fma(Bu[j], xp[j], se);
+  double d0, d1;
+  row_down<NODAL>(sB, sx + p * TREE_PAD, i, d0, d1);
   double *ch = child[p];
-  ch[i] += se + so;
-  ch[M + i] += se - so;
+  ch[i] += d0;
+  ch[M + i] += d1;
 }
 
+template <bool NODAL>
 __global__ void __launch_bounds__(32 * M) k_tree_down(double *c, Geo g, long long parent_base,
                                                       long long child_base, long long nparent) {
   pdl_wait();
   pdl_trigger();
-  __shared__ double sB[NTRI];
+  __shared__ double sB[tree_mat_size<NODAL>()];
   __shared__ double sx[TREE_TILE * TREE_PAD];
   __shared__ const double *par[TREE_TILE];
   __shared__ double *child[TREE_TILE];
-  for (int t = threadIdx.x; t < NTRI; t += blockDim.x) sB[t] = c_binom_upper[t];
+  load_tree_mat<NODAL, false>(sB);
   if (threadIdx.x < TREE_TILE) {
     const long long item = (long long)blockIdx.x * TREE_TILE + threadIdx.x;
     const long long nitem = g.count * 2 * nparent;
@@ -901,7 +944,7 @@ __global__ void __launch_bounds__(32 * M) k_tree_down(double *c, Geo g, long lon
     child[threadIdx.x] = item < nitem ? c + (vs * g.slots + child_base + 2 * tp) * M : nullptr;
   }
   __syncthreads();
-  tree_down_tile(par, child, sB, sx);
+  tree_down_tile<NODAL>(par, child, sB, sx);
 }
 
 // Step 5 + scaling: out[j] = scale_j (y[j] + sum_m c[L-1][tau][m] T_sg[i][m]) with
@@ -1696,6 +1739,10 @@ struct l2c_gpu_plan {
   cudaStream_t stream2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double *Wnear[2] = {nullptr, nullptr};  // precomputed band weights (optional)
+  // nodal (Lagrange) form: T holds barycentric interpolation weights, A the
+  // kernel samples, and the trees use B0 | B1 (c_lag_B; host copy lagB)
+  bool nodal = false;
+  double lagB[2 * MM] = {0};
   // mixed precision (L2C_PLAN_MIXED): sliced constant factors
   bool mixed = false;
   // fragment words (l2c_oz::frag_index layout) and row exponents of: T_parity^T
@@ -1761,10 +1808,14 @@ namespace {
 
 // Reference flop count (the value execute() returns), reproduced term by term,
 // including its unsigned wrap-around in directL's last block (leg2cheb.c:507-516).
-size_t ref_flops_geo(size_t N, size_t L, size_t s, size_t Nb, size_t dir);
-size_t ref_flops(const l2c_gpu_plan *p, size_t dir) { return ref_flops_geo(p->N, p->L, p->s, p->Nb, dir); }
+size_t ref_flops_geo(size_t N, size_t L, size_t s, size_t Nb, size_t dir, bool nodal = false);
+size_t ref_flops(const l2c_gpu_plan *p, size_t dir) {
+  return ref_flops_geo(p->N, p->L, p->s, p->Nb, dir, p->nodal);
+}
 
-size_t ref_flops_geo(size_t N, size_t L_, size_t s_, size_t Nb, size_t dir) {
+// The reference's flop count (execute's return value): transfer steps count
+// M^2 per block (modal) or 4 M^2 (nodal, leg2cheb.c:1414, 1462).
+size_t ref_flops_geo(size_t N, size_t L_, size_t s_, size_t Nb, size_t dir, bool nodal) {
   struct {
     size_t L, s, Nb;
   } q{L_, s_, Nb}, *p = &q;
@@ -1774,12 +1825,12 @@ size_t ref_flops_geo(size_t N, size_t L_, size_t s_, size_t Nb, size_t dir) {
     for (size_t n = (dir == 0 ? 0 : 2); n < N; n += 2) f += 3 * (N - n);
     return f + N;
   }
-  const size_t L = p->L, s = p->s, MMs = (size_t)MM;
+  const size_t L = p->L, s = p->s, MMs = (size_t)MM, MMt = (nodal ? 4 : 1) * MMs;
   const size_t K = 2 * (((size_t)2 << (L - 1)) - 1);
   size_t far = 4 * K * s * M;
-  for (size_t l = 1; l < L; l++) far += (((size_t)2 << l) - 2) * MMs;       // step 2
+  for (size_t l = 1; l < L; l++) far += (((size_t)2 << l) - 2) * MMt;       // step 2
   far += 3 * p->Nb * 2 * MMs;                                              // step 3
-  for (size_t l = 0; l + 1 < L; l++) far += (((size_t)2 << (l + 1)) - 2) * MMs;  // step 4
+  for (size_t l = 0; l + 1 < L; l++) far += (((size_t)2 << (l + 1)) - 2) * MMt;  // step 4
   f = 2 * far;
   const size_t h = 2 * s, nL = N / h, i0 = (nL - 1) * h;
   size_t band = 0;
@@ -1945,46 +1996,60 @@ size_t tree_launches(const TreePlan &t, size_t L) {
 size_t sub_smem(int d) { return ((size_t)(2 << d) - 1) * SUB_PAD * sizeof(double); }
 size_t top_smem(int lt) { return ((size_t)(8LL << lt) - 4) * SUB_PAD * sizeof(double); }
 
-cudaError_t sweep_up(double *w, const Geo &g, const TreePlan &t, cudaStream_t st, LaunchOpt pdl) {
+template <bool NODAL>
+cudaError_t sweep_up_t(double *w, const Geo &g, const TreePlan &t, cudaStream_t st,
+                       LaunchOpt pdl) {
   if (!t.staged) {
     for (long long l = g.L - 2; l >= 0; l--) {
       const long long np = (long long)slots_at((size_t)l);
-      launch_k(pdl, k_tree_up, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, w, g,
+      launch_k(pdl, k_tree_up<NODAL>, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, w, g,
                2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
     }
     return cudaGetLastError();
   }
   const unsigned nsub = (unsigned)(g.count * 2 * (4LL << t.l0));
-  launch_k(pdl, k_up_sub, nsub, 32 * M, sub_smem(t.d), st, w, g, (int)t.l0, (int)t.d);
+  launch_k(pdl, k_up_sub<NODAL>, nsub, 32 * M, sub_smem(t.d), st, w, g, (int)t.l0, (int)t.d);
   for (long long l = t.l0 - 1; l >= t.lt; l--) {
     const long long np = (long long)slots_at((size_t)l);
-    launch_k(pdl, k_tree_up, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, w, g,
+    launch_k(pdl, k_tree_up<NODAL>, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, w, g,
              2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
   }
   if (t.lt > 0)
-    launch_k(pdl, k_up_top, (unsigned)(g.count * 2), 32 * M, top_smem(t.lt), st, w, g, (int)t.lt);
+    launch_k(pdl, k_up_top<NODAL>, (unsigned)(g.count * 2), 32 * M, top_smem(t.lt), st, w, g, (int)t.lt);
   return cudaGetLastError();
 }
 
-cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t st, LaunchOpt pdl) {
+cudaError_t sweep_up(double *w, const Geo &g, const TreePlan &t, cudaStream_t st, LaunchOpt pdl,
+                     bool nodal) {
+  return nodal ? sweep_up_t<true>(w, g, t, st, pdl) : sweep_up_t<false>(w, g, t, st, pdl);
+}
+
+template <bool NODAL>
+cudaError_t sweep_down_t(double *c, const Geo &g, const TreePlan &t, cudaStream_t st,
+                         LaunchOpt pdl) {
   if (!t.staged) {
     for (long long l = 0; l + 1 < g.L; l++) {
       const long long np = (long long)slots_at((size_t)l);
-      launch_k(pdl, k_tree_down, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, c, g,
+      launch_k(pdl, k_tree_down<NODAL>, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, c, g,
                2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
     }
     return cudaGetLastError();
   }
   if (t.lt > 0)
-    launch_k(pdl, k_down_top, (unsigned)(g.count * 2), 32 * M, top_smem(t.lt), st, c, g, (int)t.lt);
+    launch_k(pdl, k_down_top<NODAL>, (unsigned)(g.count * 2), 32 * M, top_smem(t.lt), st, c, g, (int)t.lt);
   for (long long l = t.lt; l < t.l0; l++) {
     const long long np = (long long)slots_at((size_t)l);
-    launch_k(pdl, k_tree_down, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, c, g,
+    launch_k(pdl, k_tree_down<NODAL>, blocks_for(g.count * 2 * np, TREE_TILE), 32 * M, 0, st, c, g,
              2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
   }
   const unsigned nsub = (unsigned)(g.count * 2 * (4LL << t.l0));
-  launch_k(pdl, k_down_sub, nsub, 32 * M, sub_smem(t.d), st, c, g, (int)t.l0, (int)t.d);
+  launch_k(pdl, k_down_sub<NODAL>, nsub, 32 * M, sub_smem(t.d), st, c, g, (int)t.l0, (int)t.d);
   return cudaGetLastError();
+}
+
+cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t st, LaunchOpt pdl,
+                       bool nodal) {
+  return nodal ? sweep_down_t<true>(c, g, t, st, pdl) : sweep_down_t<false>(c, g, t, st, pdl);
 }
 
 // Near field for all vectors of a batch: full groups of 8 (4, 2) vectors per
@@ -2251,7 +2316,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   const TreePlan tp = tree_plan(p->L, count);
   {
     PhaseScope ps(p, L2C_PHASE_TREE_UP, tree_launches(tp, p->L));
-    CK(sweep_up(p->w, g, tp, st, LaunchOpt(pdl_flags(p) & 1, ov ? p->chain_prio : 0)));
+    CK(sweep_up(p->w, g, tp, st, LaunchOpt(pdl_flags(p) & 1, ov ? p->chain_prio : 0), p->nodal));
   }
   {
     PhaseScope ps(p, L2C_PHASE_FAR, 1);
@@ -2263,7 +2328,8 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   }
   {
     PhaseScope ps(p, L2C_PHASE_TREE_DOWN, tree_launches(tp, p->L));
-    CK(sweep_down(p->c, g, tp, st, LaunchOpt(pdl_flags(p) & 1, ov ? p->chain_prio : 0)));
+    CK(sweep_down(p->c, g, tp, st, LaunchOpt(pdl_flags(p) & 1, ov ? p->chain_prio : 0),
+                  p->nodal));
   }
   if (ov) CK(cudaStreamWaitEvent(st, p->ev_join, 0));
   {
@@ -2425,9 +2491,52 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
       for (int n = 0; n < M; n++) cs[k * M + n] = std::cos(M_PI * k * (n + 0.5) / M);
     PCK(cudaMemcpyToSymbolAsync(c_xj, xj, sizeof(xj), 0, cudaMemcpyHostToDevice, st));
     PCK(cudaMemcpyToSymbolAsync(c_dct, cs, sizeof(cs), 0, cudaMemcpyHostToDevice, st));
-    // Vandermonde T_j(-1 + i/s), i < 2s, rows split even | odd (leg2cheb.c:621-648)
+    p->nodal = (flags & L2C_PLAN_NODAL) != 0;
+    if (p->nodal && (flags & L2C_PLAN_MIXED)) {
+      set_err("the mixed form is implemented for the modal form only (lagrange = 0)");
+      return fail();
+    }
     std::vector<double> T(2 * s * M);
-    for (size_t i = 0; i < 2 * s; i++) {
+    if (p->nodal) {
+      // barycentric Lagrange weights from the Chebyshev points to -1 + i/s,
+      // rows normalised by their sums (leg2cheb.c:997-1031), and the child
+      // interpolation matrices B0 | B1 (leg2cheb.c:1076-1100)
+      double wj[M];
+      for (int j = 0; j < M; j++) wj[j] = ((j % 2 == 0) ? 1 : -1) * std::sin((j + 0.5) * M_PI / M);
+      for (size_t i = 0; i < s; i++) {
+        const double xe = -1 + (double)(2 * i) / (double)s, xo = -1 + (double)(2 * i + 1) / (double)s;
+        double sume = 0.0, sumo = 0.0;
+        for (int j = 0; j < M; j++) {
+          const double se = wj[j] / (xe - xj[j]), so = wj[j] / (xo - xj[j]);
+          T[i * M + j] = se;
+          T[(s + i) * M + j] = so;
+          sume += se;
+          sumo += so;
+        }
+        for (int j = 0; j < M; j++) {
+          T[i * M + j] /= sume;
+          T[(s + i) * M + j] /= sumo;
+        }
+      }
+      for (int i = 0; i < M; i++) {
+        const double x0 = (xj[i] - 1) / 2, x1 = (xj[i] + 1) / 2;
+        double sum0 = 0.0, sum1 = 0.0;
+        for (int j = 0; j < M; j++) {
+          const double s0 = wj[j] / (x0 - xj[j]), s1 = wj[j] / (x1 - xj[j]);
+          p->lagB[i * M + j] = s0;
+          p->lagB[MM + i * M + j] = s1;
+          sum0 += s0;
+          sum1 += s1;
+        }
+        for (int j = 0; j < M; j++) {
+          p->lagB[i * M + j] /= sum0;
+          p->lagB[MM + i * M + j] /= sum1;
+        }
+      }
+      PCK(cudaMemcpyToSymbolAsync(c_lag_B, p->lagB, sizeof(p->lagB), 0, cudaMemcpyHostToDevice, st));
+    }
+    // modal: Vandermonde T_j(-1 + i/s), i < 2s, rows split even | odd (leg2cheb.c:621-648)
+    for (size_t i = 0; i < 2 * s && !p->nodal; i++) {
       double row[M];
       const double xv = -1 + (double)i / (double)s;
       const double x2 = 2 * xv;
@@ -2448,7 +2557,8 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
         e = cudaMalloc(&p->A[d], 3 * p->Nb * MM * sizeof(double));
     if (e == cudaSuccess) {
       // one CTA per (block, r); the grid is at most 3 (2^(L+1)) CTAs
-      k_assemble_A<<<(unsigned)(3 * p->Nb), MM, 0, st>>>(f0, p->A[0], p->A[1], L, s);
+      k_assemble_A<<<(unsigned)(3 * p->Nb), MM, 0, st>>>(f0, p->A[0], p->A[1], L, s,
+                                                         p->nodal ? 1 : 0);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -2756,6 +2866,11 @@ size_t l2c_gpu_plan_copy(const l2c_gpu_plan *p, int which, double *dst, size_t n
       src = p->T;
       n = 2 * p->s * M;
       break;
+    case 6:  // nodal transfer matrices B0 | B1 (host copy)
+      if (!p->nodal) return 0;
+      n = std::min(n_max, (size_t)(2 * MM));
+      std::memcpy(dst, p->lagB, n * sizeof(double));
+      return n;
     default:
       return 0;
   }
@@ -2893,14 +3008,16 @@ extern "C" size_t l2c_gpu_execute_noalloc(l2c_gpu_plan *p, const double *in, dou
   k_leaf_up<<<blocks_for(g.K * 2 * M, 288), 288, 0, st>>>(x, p->T, w, g);
   for (long long l = (long long)p->L - 2; l >= 0; l--) {
     const long long np = (long long)slots_at((size_t)l);
-    k_tree_up<<<blocks_for(2 * np, TREE_TILE), 32 * M, 0, st>>>(
+    (p->nodal ? k_tree_up<true> : k_tree_up<false>)<<<blocks_for(2 * np, TREE_TILE), 32 * M, 0,
+                                                      st>>>(
         w, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
   }
   k_far<<<blocks_for(2 * (long long)p->Nb * M, 256), 256, 0, st>>>(p->A[dir], w, c, g,
                                                                    (long long)p->Nb);
   for (long long l = 0; l + 1 < (long long)p->L; l++) {
     const long long np = (long long)slots_at((size_t)l);
-    k_tree_down<<<blocks_for(2 * np, TREE_TILE), 32 * M, 0, st>>>(
+    (p->nodal ? k_tree_down<true> : k_tree_down<false>)<<<blocks_for(2 * np, TREE_TILE), 32 * M,
+                                                          0, st>>>(
         c, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
   }
   k_leaf_down<<<blocks_for(total, 256), 256, 0, st>>>(c, p->T, y, out, g, c2l);

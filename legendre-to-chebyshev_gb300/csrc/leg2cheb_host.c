@@ -276,8 +276,8 @@ fmm_plan *create_fmm_ex(const size_t N, const size_t maxs, const size_t M, const
     herr("only M = 18 is implemented (got M = %zu)", M);
     return NULL;
   }
-  if (lagrange != 0) {
-    herr("the nodal (Lagrange) form is not implemented; use lagrange = 0");
+  if (lagrange > 1) {
+    herr("lagrange must be 0 (modal) or 1 (nodal)");
     return NULL;
   }
   if (direction > 2) {
@@ -298,6 +298,7 @@ fmm_plan *create_fmm_ex(const size_t N, const size_t maxs, const size_t M, const
   const size_t L = l2c_geometry(N, maxs, &s, &Nn);
   unsigned gflags = precompute ? L2C_PLAN_PRECOMPUTE_NEAR : 0;
   if (flags & L2C_FMM_MIXED) gflags |= L2C_PLAN_MIXED;
+  if (lagrange == 1) gflags |= L2C_PLAN_NODAL;
   l2c_gpu_plan *gp = l2c_gpu_plan_create(N, maxs, direction, gflags);
   if (!gp) {
     free(p->A);
@@ -336,9 +337,21 @@ fmm_plan *create_fmm_ex(const size_t N, const size_t maxs, const size_t M, const
   }
   /* host mirrors of the plan fields the reference exposes (leg2cheb.c:1195-1211) */
   p->T = (double *)malloc(2 * s * L2C_M * sizeof(double));
-  vandermonde_host(p->T, s);
-  p->B = (double *)binom_lower;
-  p->BT = (double *)binom_upper;
+  if (lagrange == 1) {
+    /* nodal: T and B0 | B1 as the device plan built them; no BT (leg2cheb.c:1076-1100) */
+    p->B = (double *)malloc(2 * L2C_M * L2C_M * sizeof(double));
+    if (!p->T || !p->B || l2c_gpu_plan_copy(gp, 5, p->T, 2 * s * L2C_M) != 2 * s * L2C_M ||
+        l2c_gpu_plan_copy(gp, 6, p->B, 2 * L2C_M * L2C_M) != 2 * L2C_M * L2C_M) {
+      free_fmm(p);
+      herr("could not copy the nodal plan tables to the host");
+      return NULL;
+    }
+    p->BT = NULL;
+  } else {
+    vandermonde_host(p->T, s);
+    p->B = (double *)binom_lower;
+    p->BT = (double *)binom_upper;
+  }
   const size_t Nb = get_total_number_of_blocks(L);
   p->ia = (double *)calloc(Nn / 2, sizeof(double));
   p->oa = (double *)calloc(Nn / 2, sizeof(double));
@@ -360,6 +373,7 @@ void free_fmm(fmm_plan *p) {
   if (p->gpu) l2c_gpu_plan_destroy((l2c_gpu_plan *)p->gpu);
   if (p->A) free(p->A);
   free(p->T);
+  if (p->lagrange == 1) free(p->B); /* modal B points at the constant binomial table */
   free(p->ia);
   free(p->oa);
   free(p->work);

@@ -211,9 +211,10 @@ class Plan:
         return int(f)
 
     def copy_table(self, which):
-        """Plan data: 0 A[L2C], 1 A[C2L], 2 Lambda a, 3 an, 4 dn, 5 T."""
+        """Plan data: 0 A[L2C], 1 A[C2L], 2 Lambda a, 3 an, 4 dn, 5 T,
+        6 nodal transfer matrices B0 | B1 (nodal plans; empty otherwise)."""
         n = {0: 3 * self.Nb * 324, 1: 3 * self.Nb * 324, 2: self.N, 3: self.N,
-             4: (self.N + 1) // 2, 5: 2 * self.s * 18}[which]
+             4: (self.N + 1) // 2, 5: 2 * self.s * 18, 6: 2 * 324}[which]
         buf = np.zeros(max(n, 1))
         got = _cuda.l2c_gpu_plan_copy(self._gpu, which, _ptr(buf), n)
         return buf[:got]
@@ -349,9 +350,11 @@ class DirectPlan:
 class Plan2D:
     """An fmm_plan_2d (create_fmm_2d / execute2D / free_fmm_2d)."""
 
-    def __init__(self, N0, N1, axis, maxs=36, M=18, direction=BOTH, verbose=0):
+    def __init__(self, N0, N1, axis, maxs=36, M=18, direction=BOTH, verbose=0, lagrange=0,
+                 precompute=0):
         lib = load()
-        self._p = lib.create_fmm_2d(N0, N1, axis, maxs, M, direction, 0, 0, verbose)
+        self._p = lib.create_fmm_2d(N0, N1, axis, maxs, M, direction, lagrange, precompute,
+                                    verbose)
         if not self._p:
             raise L2CError("create_fmm_2d failed: " + last_error())
 
