@@ -1303,7 +1303,7 @@ size_t mz_leaf_up_smem(int KC, int nbuf) {
 // (the slice-major layout makes that a prefix of each matrix's words).
 __host__ __device__ constexpr int oz_tree_words(int QMAX, int KC) { return QMAX * OZ_NT * KC * 32; }
 template <int QMAX, int NBUF>
-__global__ void __launch_bounds__(32 * MXW)
+__global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
     k_mz_tree_up(long long *w, int *wE, const unsigned *__restrict__ Pf,
                  const int *__restrict__ Pm, Geo g, long long parent_base, long long child_base,
                  long long np) {
@@ -1388,7 +1388,7 @@ constexpr size_t oz_tree_up_smem(int QMAX, int NBUF) {
 // product are added as integers on the coarser of their two scales, one bit
 // above the larger exponent.
 template <int QMAX, int NBUF>
-__global__ void __launch_bounds__(32 * MXW)
+__global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
     k_mz_tree_down(long long *c, int *cE, const unsigned *__restrict__ Pf,
                    const int *__restrict__ Pm, Geo g, long long parent_base, long long child_base,
                    long long np) {
@@ -1779,6 +1779,9 @@ struct l2c_gpu_plan {
   int overlap = -1;  // band on stream2 beside the far-field chain: 1 / 0 forced, -1 auto
   unsigned near_ctas = 0;  // band grid cap while it overlaps (0: no cap)
   int near_vb = 8;         // band vectors per thread while it overlaps
+  // band CTA size while it overlaps: 128 threads free registers in pieces the
+  // chain's CTAs fit (256 x 16384 mixed: 1.079 -> 1.067 ms; plain batches +0.1 %)
+  int near_threads = 128;
   int near_pair = -1;    // band in pairs: 1 always, 0 never, -1 by leaf size
   // programmatic dependent launch, bit flags: 1 far-field chain kernels,
   // 2 the band, 4 the first chain kernel after the band on the same stream.
@@ -2057,7 +2060,7 @@ cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t 
 cudaError_t launch_near(const double *x, const double *out, double *y, const double *a,
                         const double *an, const double *dn, const double *W, Geo g, int c2l,
                         cudaStream_t st, bool pair, unsigned max_ctas, int max_vb,
-                        bool pdl = false) {
+                        bool pdl = false, int threads = 256) {
   long long v = 0;
   while (v < g.count) {
     const long long left = g.count - v;
@@ -2070,10 +2073,10 @@ cudaError_t launch_near(const double *x, const double *out, double *y, const dou
     const double *os = out + v * g.dist;
     double *ys = y + v * g.N;
     if (!pair) {
-      unsigned grid = (unsigned)(((g.N + 255) / 256) * groups);
+      unsigned grid = (unsigned)(((g.N + threads - 1) / threads) * groups);
       if (max_ctas) grid = std::min(grid, max_ctas);
       auto *kern = vb == 8 ? k_near<8> : vb == 4 ? k_near<4> : vb == 2 ? k_near<2> : k_near<1>;
-      launch_k(pdl, kern, grid, 256, 0, st, xs, os, ys, a, an, dn, W, gg, c2l, 0LL);
+      launch_k(pdl, kern, grid, threads, 0, st, xs, os, ys, a, an, dn, W, gg, c2l, 0LL);
       const cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
       v += groups * vb;
@@ -2081,13 +2084,13 @@ cudaError_t launch_near(const double *x, const double *out, double *y, const dou
     }
     // blocks b < nL-1 in pairs and the last (ragged) block one output per thread
     const long long per_vg = (g.nL - 1) * (g.h / 2) + (g.N - (g.nL - 1) * g.h);
-    unsigned grid = (unsigned)((groups * per_vg + 255) / 256);
+    unsigned grid = (unsigned)((groups * per_vg + threads - 1) / threads);
     if (max_ctas) grid = std::min(grid, max_ctas);
     auto *kern = vb == 8   ? k_near_pair<8>
                  : vb == 4 ? k_near_pair<4>
                  : vb == 2 ? k_near_pair<2>
                            : k_near_pair<1>;
-    launch_k(pdl, kern, grid, 256, 0, st, xs, os, ys, a, an, dn, W, gg, c2l);
+    launch_k(pdl, kern, grid, threads, 0, st, xs, os, ys, a, an, dn, W, gg, c2l);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     v += groups * vb;
@@ -2301,7 +2304,8 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   {
     PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, ov ? p->near_vb : 8), stn);
     CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, near_pair(p),
-                    ov ? p->near_ctas : 0, ov ? p->near_vb : 8, (pdl_flags(p) & 2) && !ov));
+                    ov ? p->near_ctas : 0, ov ? p->near_vb : 8, (pdl_flags(p) & 2) && !ov,
+                    ov ? p->near_threads : 256));
   }
   if (ov) CK(cudaEventRecord(p->ev_join, st2));
   if (p->mixed) return launch_mixed_far(p, x, out, dir, g, st, ov) ? 1 : 0;
@@ -2456,6 +2460,8 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_OVERLAP")) p->overlap = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_NEAR_CTAS")) p->near_ctas = (unsigned)std::atoi(env);
   if (const char *env = std::getenv("L2C_NEAR_VB")) p->near_vb = std::max(1, std::atoi(env));
+  if (const char *env = std::getenv("L2C_NEAR_THREADS"))
+    p->near_threads = std::atoi(env) == 128 ? 128 : 256;
   if (const char *env = std::getenv("L2C_NEAR_PAIR")) p->near_pair = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_PDL")) p->pdl = std::max(0, std::atoi(env));
   if (const char *env = std::getenv("L2C_CHAIN_PRIO")) p->chain_prio_mode = env[0] == '1' ? 1 : 0;

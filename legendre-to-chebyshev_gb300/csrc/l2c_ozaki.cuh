@@ -189,13 +189,24 @@ __device__ __forceinline__ bool to_fixed(double x, int e, long long &X) {
 }
 
 // Combined integer T of output (nt, e) from the NDIAG diagonal accumulators
-// (each an exact integer below 2^24).
+// (each an exact integer below 2^24):
+//   T = D0 2^36 + D1 2^27 + D2 2^18 + D3 2^9 + D4 + floor(D5 / 2^9),
+// evaluated modulo 2^64 (T itself fits): three 32 x 32 -> 64-bit multiply-adds
+// and the D0 term added to the high word in 32-bit arithmetic
+// ((D0 2^4 mod 2^32) 2^32 = D0 2^36 mod 2^64) -- the same value as the
+// nested form ((D0 2^9 + D1) 2^9 + ...) in half the integer instructions.
 template <int NT>
 __device__ __forceinline__ long long combine(const float (&acc)[NDIAG][NT][4], int nt, int e) {
-  long long T = 0;
-#pragma unroll
-  for (int d = 0; d < NDIAG - 1; d++) T = T * 512 + __float2int_rn(acc[d][nt][e]);
-  return T + (__float2int_rn(acc[NDIAG - 1][nt][e]) >> 9);
+  static_assert(NDIAG == 6, "the expansion below has six diagonals");
+  const int d0 = __float2int_rn(acc[0][nt][e]), d1 = __float2int_rn(acc[1][nt][e]);
+  const int d2 = __float2int_rn(acc[2][nt][e]), d3 = __float2int_rn(acc[3][nt][e]);
+  const int d4 = __float2int_rn(acc[4][nt][e]), d5 = __float2int_rn(acc[5][nt][e]);
+  long long t = (long long)(d4 + (d5 >> 9));
+  t += (long long)d3 * (1 << 9);
+  t += (long long)d2 * (1 << 18);
+  t += (long long)d1 * (1 << 27);
+  const unsigned hi = (unsigned)d0 << 4;
+  return (long long)((unsigned long long)t + ((unsigned long long)hi << 32));
 }
 
 // The warp's 16 x (NT*8) tile over k8-chunks [C0, C1): acc[d-2][nt][.] = sum
