@@ -1222,6 +1222,30 @@ __device__ __forceinline__ void oz_put18(const long long (&T)[OZ_NT][4], const i
   put1(g + 8 * (t4 >> 1), n9, l2c_oz::shift_s64(t9, rs[n9]));
 }
 
+// oz_put18 for one n-tile at a time (T4: that n-tile's four integers), for
+// products computed n-tile by n-tile (mma_nt).
+template <class Put2, class Put1>
+__device__ __forceinline__ void oz_put_nt(int nt, const long long (&T4)[4], const int *rs,
+                                          Put2 put2, Put1 put1) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
+  if (nt < 2) {
+#pragma unroll
+    for (int hr = 0; hr < 2; hr++) {
+      const int n = 8 * nt + 2 * t4;
+      put2(g + 8 * hr, n, l2c_oz::shift_s64(T4[2 * hr], rs[n]),
+           l2c_oz::shift_s64(T4[2 * hr + 1], rs[n + 1]));
+    }
+    return;
+  }
+  const int src = lane & ~3;
+  const long long v1 = __shfl_sync(0xffffffffu, T4[1], src);
+  const long long v2 = __shfl_sync(0xffffffffu, T4[2], src);
+  const long long v3 = __shfl_sync(0xffffffffu, T4[3], src);
+  const long long t9 = t4 == 0 ? T4[0] : t4 == 1 ? v1 : t4 == 2 ? v2 : v3;
+  const int n9 = 16 + (t4 & 1);
+  put1(g + 8 * (t4 >> 1), n9, l2c_oz::shift_s64(t9, rs[n9]));
+}
+
 // Leaf up (step 1): tile = 16 consecutive leaf nodes of one vector; both
 // parities from one staged stretch of x (node r's h inputs in row r, parity
 // sg at even/odd positions).  P_sg = T_sg^T (18 x s), KC = ceil(s / 8).
@@ -1447,10 +1471,11 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
     const int *Ex = sEx + buf * 48;
     l2c_oz::stage_cols<M, M, 24>(X, OZ_CLD, Ex, Ex, Es);
     const long long cb0 = B[16 + gq], cb1 = B[16 + gq + 8];
+    // the parent's digits once, for both children's products
+    l2c_oz::Digits<3> D;
+    l2c_oz::load_digits<3>(X, OZ_CLD, 1, D);
 #pragma unroll 1
     for (int ch = 0; ch < 2; ch++) {
-      long long T[OZ_NT][4];
-      oz_tile_T<OZ_NT, 3, QMAX>(sP + ch * NW, X, OZ_CLD, 1, T);
       const int *meta = sM + ch * OZ_META;
       // per tile row r: product exponent, child exponent, sum exponent
       int ep[2], ek[2], es[2];
@@ -1466,18 +1491,25 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
         return l2c_oz::shift_s64(C[r * 2 * M + ch * M + n], ek[hr] - es[hr]) +
                l2c_oz::shift_s64(v, ep[hr] - es[hr]);
       };
-      oz_put18(
-          T, meta,
-          [&](int r, int n, long long a, long long b) {
-            const long long d = r < 8 ? cb0 : cb1;
-            if (d >= 0)
-              *reinterpret_cast<longlong2 *>(c + (d + ch) * M + n) =
-                  make_longlong2(sum(r, n, a), sum(r, n + 1, b));
-          },
-          [&](int r, int n, long long a) {
-            const long long d = r < 8 ? cb0 : cb1;
-            if (d >= 0) c[(d + ch) * M + n] = sum(r, n, a);
-          });
+      auto put2 = [&](int r, int n, long long a, long long b) {
+        const long long d = r < 8 ? cb0 : cb1;
+        if (d >= 0)
+          *reinterpret_cast<longlong2 *>(c + (d + ch) * M + n) =
+              make_longlong2(sum(r, n, a), sum(r, n + 1, b));
+      };
+      auto put1 = [&](int r, int n, long long a) {
+        const long long d = r < 8 ? cb0 : cb1;
+        if (d >= 0) c[(d + ch) * M + n] = sum(r, n, a);
+      };
+#pragma unroll
+      for (int nt = 0; nt < OZ_NT; nt++) {
+        float acc[l2c_oz::NDIAG][4];
+        l2c_oz::mma_nt<OZ_NT, 3, QMAX>(sP + ch * NW, D, nt, acc);
+        long long T4[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) T4[e] = l2c_oz::combine1(acc, e);
+        oz_put_nt(nt, T4, meta, put2, put1);
+      }
       if (t4 == 0) {
         if (cb0 >= 0) cE[cb0 + ch] = es[0];
         if (cb1 >= 0) cE[cb1 + ch] = es[1];

@@ -277,6 +277,94 @@ __device__ __forceinline__ void mma_tile(const unsigned *__restrict__ Pf, const 
   }
 }
 
+// The FP16 digit fragments of a whole 16 x (8 KC) data tile, extracted once
+// and kept in registers, for tiles multiplied by several constant factors (the
+// two children of a downward transfer): a16 holds the k16 chunk pairs, a8 the
+// trailing k8 chunk when KC is odd.  Same layout as mma_tile's per-chunk a.
+template <int KC>
+struct Digits {
+  unsigned a16[KC / 2 > 0 ? KC / 2 : 1][SLICES][4];
+  unsigned a8[SLICES][2];
+};
+
+template <int KC>
+__device__ __forceinline__ void load_digits(const long long *Ys, int yld, int ks,
+                                            Digits<KC> &D) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const long long *r0 = Ys + g * yld + 2 * t * ks, *r1 = r0 + 8 * yld;
+#pragma unroll
+  for (int cp = 0; cp < KC / 2; cp++) {
+    const int c = 2 * cp;
+    const Ysplit y0 = ysplit(r0[(8 * c) * ks]), y1 = ysplit(r0[(8 * c + 1) * ks]);
+    const Ysplit y2 = ysplit(r1[(8 * c) * ks]), y3 = ysplit(r1[(8 * c + 1) * ks]);
+    const Ysplit y4 = ysplit(r0[(8 * c + 8) * ks]), y5 = ysplit(r0[(8 * c + 9) * ks]);
+    const Ysplit y6 = ysplit(r1[(8 * c + 8) * ks]), y7 = ysplit(r1[(8 * c + 9) * ks]);
+#define L2C_OZ_SLICE(P)                      \
+  D.a16[cp][P - 1][0] = dig2<P>(y0, y1);     \
+  D.a16[cp][P - 1][1] = dig2<P>(y2, y3);     \
+  D.a16[cp][P - 1][2] = dig2<P>(y4, y5);     \
+  D.a16[cp][P - 1][3] = dig2<P>(y6, y7);
+    L2C_OZ_SLICE(1) L2C_OZ_SLICE(2) L2C_OZ_SLICE(3)
+    L2C_OZ_SLICE(4) L2C_OZ_SLICE(5) L2C_OZ_SLICE(6)
+#undef L2C_OZ_SLICE
+  }
+  if constexpr (KC & 1) {
+    const int c = KC - 1;
+    const Ysplit y0 = ysplit(r0[(8 * c) * ks]), y1 = ysplit(r0[(8 * c + 1) * ks]);
+    const Ysplit y2 = ysplit(r1[(8 * c) * ks]), y3 = ysplit(r1[(8 * c + 1) * ks]);
+#define L2C_OZ_SLICE(P)                \
+  D.a8[P - 1][0] = dig2<P>(y0, y1);    \
+  D.a8[P - 1][1] = dig2<P>(y2, y3);
+    L2C_OZ_SLICE(1) L2C_OZ_SLICE(2) L2C_OZ_SLICE(3)
+    L2C_OZ_SLICE(4) L2C_OZ_SLICE(5) L2C_OZ_SLICE(6)
+#undef L2C_OZ_SLICE
+  }
+}
+
+// One n-tile nt of a tile from cached digits: acc[d][.] = the diagonal-d sums
+// over all KC chunks (KC <= KMAX / 8 keeps them exact), as mma_tile does for
+// that n-tile.
+template <int NT, int KC, int QMAX = SLICES>
+__device__ __forceinline__ void mma_nt(const unsigned *__restrict__ Pf, const Digits<KC> &D,
+                                       int nt, float (&acc)[NDIAG][4]) {
+  static_assert(KC <= KMAX / 8, "accumulation would not be exact");
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 0; d < NDIAG; d++)
+#pragma unroll
+    for (int e = 0; e < 4; e++) acc[d][e] = 0.f;
+#pragma unroll
+  for (int cp = 0; cp < KC / 2; cp++) {
+#pragma unroll
+    for (int q = 1; q <= QMAX; q++) {
+      const uint2 b = *reinterpret_cast<const uint2 *>(Pf + frag_index(q, nt, 2 * cp, lane, NT, KC));
+#pragma unroll
+      for (int p = 1; p + q <= DMAX; p++) mma16(acc[p + q - 2], D.a16[cp][p - 1], b.x, b.y);
+    }
+  }
+  if constexpr (KC & 1) {
+#pragma unroll
+    for (int q = 1; q <= QMAX; q++) {
+      const unsigned b = Pf[frag_index(q, nt, KC - 1, lane, NT, KC)];
+#pragma unroll
+      for (int p = 1; p + q <= DMAX; p++) mma8(acc[p + q - 2], D.a8[p - 1][0], D.a8[p - 1][1], b);
+    }
+  }
+}
+
+// combine() for one n-tile's accumulators.
+__device__ __forceinline__ long long combine1(const float (&acc)[NDIAG][4], int e) {
+  const int d0 = __float2int_rn(acc[0][e]), d1 = __float2int_rn(acc[1][e]);
+  const int d2 = __float2int_rn(acc[2][e]), d3 = __float2int_rn(acc[3][e]);
+  const int d4 = __float2int_rn(acc[4][e]), d5 = __float2int_rn(acc[5][e]);
+  long long t = (long long)(d4 + (d5 >> 9));
+  t += (long long)d3 * (1 << 9);
+  t += (long long)d2 * (1 << 18);
+  t += (long long)d1 * (1 << 27);
+  const unsigned hi = (unsigned)d0 << 4;
+  return (long long)((unsigned long long)t + ((unsigned long long)hi << 32));
+}
+
 // Column exponents and offset words of a staged tile, in place: Xs holds the
 // raw doubles of 16 columns (column r at Xs[r * ld + k * ks], k < K); on
 // return the same places hold the offset words Y, entries K <= k < KP hold
