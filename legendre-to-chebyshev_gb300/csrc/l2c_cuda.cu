@@ -1290,19 +1290,33 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
     const long long *Ys = reinterpret_cast<const long long *>(X);
 #pragma unroll 1
     for (int sg = 0; sg < 2; sg++) {
-      long long T[OZ_NT][4];
-      oz_tile_T<OZ_NT, KC>(sP + sg * NW, Ys + sg, XLD, 2, T);
       const int *meta = sM + sg * OZ_META;
       long long *wcol = w + ((v * 2 + sg) * g.slots + g.leaf_base + node0) * M;
       const long long nrow = g.K - node0;
-      oz_put18(
-          T, meta,
-          [&](int r, int n, long long a, long long b) {
-            if (r < nrow) *reinterpret_cast<longlong2 *>(wcol + r * M + n) = make_longlong2(a, b);
-          },
-          [&](int r, int n, long long a) {
-            if (r < nrow) wcol[r * M + n] = a;
-          });
+      auto put2 = [&](int r, int n, long long a, long long b) {
+        if (r < nrow) *reinterpret_cast<longlong2 *>(wcol + r * M + n) = make_longlong2(a, b);
+      };
+      auto put1 = [&](int r, int n, long long a) {
+        if (r < nrow) wcol[r * M + n] = a;
+      };
+      if constexpr (KC <= 3) {
+        // one n-tile at a time from cached digits (fewer live accumulators)
+        l2c_oz::Digits<KC> D;
+        l2c_oz::load_digits<KC>(Ys + sg, XLD, 2, D);
+#pragma unroll
+        for (int nt = 0; nt < OZ_NT; nt++) {
+          float acc[l2c_oz::NDIAG][4];
+          l2c_oz::mma_nt<OZ_NT, KC>(sP + sg * NW, D, nt, acc);
+          long long T4[4];
+#pragma unroll
+          for (int e = 0; e < 4; e++) T4[e] = l2c_oz::combine1(acc, e);
+          oz_put_nt(nt, T4, meta, put2, put1);
+        }
+      } else {
+        long long T[OZ_NT][4];
+        oz_tile_T<OZ_NT, KC>(sP + sg * NW, Ys + sg, XLD, 2, T);
+        oz_put18(T, meta, put2, put1);
+      }
       if (t4 == 0)
         for (int hr = 0; hr < 2; hr++) {
           const int r = gq + 8 * hr;
@@ -1670,21 +1684,25 @@ __global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 5 : 1)
     for (int sg = 0; sg < 2; sg++) {
       long long *X = Xw + (buf * 2 + sg) * 16 * OZ_CLD;
       l2c_oz::stage_cols<M, M, 24>(X, OZ_CLD, Ex + 16 * sg, Ex + 16 * sg, Ec + 16 * sg);
+      l2c_oz::Digits<3> D;
+      l2c_oz::load_digits<3>(X, OZ_CLD, 1, D);
 #pragma unroll 1
       for (int ps = 0; ps < npass; ps++) {
-        long long T[2][4];
-        oz_tile_T<2, 3>(sP + (sg * npass + ps) * OZ_LD_WORDS, X, OZ_CLD, 1, T);
         const int *Ep = sE + (sg * npass + ps) * 16;
 #pragma unroll
-        for (int nt = 0; nt < 2; nt++)
+        for (int nt = 0; nt < 2; nt++) {
+          float acc[l2c_oz::NDIAG][4];
+          l2c_oz::mma_nt<2, 3>(sP + (sg * npass + ps) * OZ_LD_WORDS, D, nt, acc);
 #pragma unroll
           for (int e = 0; e < 4; e++) {
             const int r = gq + 8 * (e >> 1), il = 8 * nt + 2 * t4 + (e & 1), i = 16 * ps + il;
             if (r >= nrow || i >= g.s) continue;
             const long long j = (tau0 + r) * g.h + 2 * i + sg;
-            const double f = l2c_oz::to_double(T[nt][e], Ec[16 * sg + r] - 52 + Ep[il]);
+            const double f =
+                l2c_oz::to_double(l2c_oz::combine1(acc, e), Ec[16 * sg + r] - 52 + Ep[il]);
             ov[j * g.stride] = scale(yv[j] + f, j);
           }
+        }
       }
     }
   };
