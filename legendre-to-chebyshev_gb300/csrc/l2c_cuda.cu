@@ -1630,7 +1630,7 @@ constexpr size_t oz_far_smem(int NBUF) {
 // target (band only) are scaled by the same CTAs.
 constexpr int OZ_LD_WORDS = oz_words(2, 3);
 template <int NBUF>
-__global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 5 : 1)
+__global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 4 : 1)
     k_mz_leaf_down(const long long *__restrict__ c, const int *__restrict__ cE,
                    const double *__restrict__ y, double *out, const unsigned *__restrict__ Pf,
                    const int *__restrict__ Pe, Geo g, int c2l, int npass) {
@@ -2278,7 +2278,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
     const long long tiles = g.count * ((g.K + 15) / 16);
-    const int per_sm = p->oz_nbuf == 1 ? 5 : 2;  // resident CTAs (registers, shared memory)
+    const int per_sm = p->oz_nbuf == 1 ? 4 : 2;  // resident CTAs (registers, shared memory)
     const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * per_sm);
     // after the join with the band's stream: a plain launch (full dependency)
     launch_k((pdl_flags(p) & 1) && !ov, p->oz_nbuf == 1 ? k_mz_leaf_down<1> : k_mz_leaf_down<2>,
