@@ -436,9 +436,13 @@ __global__ void __launch_bounds__(256, VB == 1 ? 5 : VB == 2 ? 4 : 2)
 // Terms are accumulated in order k = 0, 1, ... into one FMA chain per output
 // (the FP64 pipe, not its latency, bounds this loop).  Threads past the pairs
 // of a vector group take the outputs of the last (ragged) block one each, in
-// the same launch, so that block runs beside the others.
+// the same launch, so that block runs beside the others.  Register bound:
+// three 256-thread CTAs per SM (80 registers at VB = 8, a few spilled);
+// the extra resident warps more than pay for the spills (256 x 16384, s = 16:
+// 0.573 -> 0.531 ms per L2C + C2L alone, and room for the far-field chain
+// beside it).
 template <int VB>
-__global__ void __launch_bounds__(256, VB <= 2 ? 3 : 2)
+__global__ void __launch_bounds__(256, 3)
     k_near_pair(const double *__restrict__ x, const double *out, double *__restrict__ y,
                 const double *__restrict__ a, const double *__restrict__ an,
                 const double *__restrict__ dn, const double *__restrict__ W, Geo g, int c2l) {
