@@ -714,22 +714,22 @@ __global__ void __launch_bounds__(32 * M) k_up_sub(double *w, Geo g, int l0, int
     sm[p * SUB_PAD + m] = t >= 2 ? ws[(g.leaf_base + t - 2) * M + m] : 0.0;
   }
   __syncthreads();
-  const int m = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double *child = sm;
   for (int k = 1; k <= d; k++) {
-    const int np = nl >> k;
+    const int np = nl >> k, lg = d - k;  // np = 2^lg parents
     double *par = child + 2 * np * SUB_PAD;
     const int l = g.L - 1 - k;
     const long long base = 2 * (long long)blocks_before((size_t)l);
-    if (m < M) {
-      for (int p = lane; p < np; p += 32) {
-        const long long u = r * np + p;
-        if (u < 2) continue;
-        double out;
-        row_up<NODAL>(sB, child + 2 * p * SUB_PAD, child + (2 * p + 1) * SUB_PAD, m, out);
-        par[p * SUB_PAD + m] = out;
-        ws[(base + u - 2) * M + m] = out;
-      }
+    // (parent, row) items packed densely over the CTA: a warp FP64 instruction
+    // costs the same with idle lanes, so narrow levels use few, full warps
+    for (int it = threadIdx.x; it < np * M; it += blockDim.x) {
+      const int p = it & (np - 1), m = it >> lg;
+      const long long u = r * np + p;
+      if (u < 2) continue;
+      double out;
+      row_up<NODAL>(sB, child + 2 * p * SUB_PAD, child + (2 * p + 1) * SUB_PAD, m, out);
+      par[p * SUB_PAD + m] = out;
+      ws[(base + u - 2) * M + m] = out;
     }
     __syncthreads();
     child = par;
@@ -755,18 +755,16 @@ __global__ void __launch_bounds__(32 * M) k_up_top(double *w, Geo g, int lt) {
     sm[((nt - 4) + j + 2) * SUB_PAD + m] = ws[(2 * (long long)blocks_before((size_t)lt) + j) * M + m];
   }
   __syncthreads();
-  const int m = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int l = lt - 1; l >= 0; l--) {
-    const long long nn = 4LL << l;  // nodes of level l
+    const int nn = 4 << l;  // nodes of level l; sources are nodes 2 .. nn-1
     double *par = sm + (nn - 4) * SUB_PAD, *child = sm + (2 * nn - 4) * SUB_PAD;
     const long long base = 2 * (long long)blocks_before((size_t)l);
-    if (m < M) {
-      for (long long u = 2 + lane; u < nn; u += 32) {
-        double out;
-        row_up<NODAL>(sB, child + 2 * u * SUB_PAD, child + (2 * u + 1) * SUB_PAD, m, out);
-        par[u * SUB_PAD + m] = out;
-        ws[(base + u - 2) * M + m] = out;
-      }
+    for (int it = threadIdx.x; it < (nn - 2) * M; it += blockDim.x) {  // dense items
+      const int u = 2 + it % (nn - 2), m = it / (nn - 2);
+      double out;
+      row_up<NODAL>(sB, child + 2 * u * SUB_PAD, child + (2 * u + 1) * SUB_PAD, m, out);
+      par[u * SUB_PAD + m] = out;
+      ws[(base + u - 2) * M + m] = out;
     }
     __syncthreads();
   }
@@ -794,17 +792,15 @@ __global__ void __launch_bounds__(32 * M) k_down_top(double *c, Geo g, int lt) {
     }
   }
   __syncthreads();
-  const int i = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int l = 0; l < lt; l++) {
-    const long long nn = (4LL << l) - 2;
+    const int nn = (4 << l) - 2;
     double *par = sm + ((4LL << l) - 4) * SUB_PAD, *child = sm + ((8LL << l) - 4) * SUB_PAD;
-    if (i < M) {
-      for (long long t = lane; t < nn; t += 32) {
-        double d0, d1;
-        row_down<NODAL>(sB, par + t * SUB_PAD, i, d0, d1);
-        child[(2 * t) * SUB_PAD + i] += d0;
-        child[(2 * t + 1) * SUB_PAD + i] += d1;
-      }
+    for (int it = threadIdx.x; it < nn * M; it += blockDim.x) {  // dense (target, row) items
+      const int t = it % nn, i = it / nn;
+      double d0, d1;
+      row_down<NODAL>(sB, par + t * SUB_PAD, i, d0, d1);
+      child[(2 * t) * SUB_PAD + i] += d0;
+      child[(2 * t + 1) * SUB_PAD + i] += d1;
     }
     __syncthreads();
   }
@@ -844,19 +840,17 @@ __global__ void __launch_bounds__(32 * M) k_down_sub(double *c, Geo g, int l0, i
     }
   }
   __syncthreads();
-  const int i = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int k = 0; k < d; k++) {
     const int nk = 1 << k;
     const long long nslot = (4LL << (l0 + k)) - 2;
     double *par = sm + (nk - 1) * SUB_PAD, *child = sm + (2 * nk - 1) * SUB_PAD;
-    if (i < M) {
-      for (int p = lane; p < nk; p += 32) {
-        if (r * nk + p >= nslot) continue;
-        double d0, d1;
-        row_down<NODAL>(sB, par + p * SUB_PAD, i, d0, d1);
-        child[(2 * p) * SUB_PAD + i] += d0;
-        child[(2 * p + 1) * SUB_PAD + i] += d1;
-      }
+    for (int it = threadIdx.x; it < nk * M; it += blockDim.x) {  // dense (node, row) items
+      const int p = it & (nk - 1), i = it >> k;
+      if (r * nk + p >= nslot) continue;
+      double d0, d1;
+      row_down<NODAL>(sB, par + p * SUB_PAD, i, d0, d1);
+      child[(2 * p) * SUB_PAD + i] += d0;
+      child[(2 * p + 1) * SUB_PAD + i] += d1;
     }
     __syncthreads();
   }
