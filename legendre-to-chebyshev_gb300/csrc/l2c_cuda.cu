@@ -1824,28 +1824,21 @@ struct l2c_gpu_plan {
   std::vector<GraphEntry> graphs;
   size_t use_clock = 0;
   bool use_graphs = true;
-  int overlap = -1;  // band on stream2 beside the far-field chain: 1 / 0 forced, -1 auto
+  // Scheduling of a call (see sched_for): -1 = by the call's shape, 0/1 forced.
+  //  overlap: the band on stream2 beside the far-field chain;
+  int overlap = -1;
   unsigned near_ctas = 0;  // band grid cap while it overlaps (0: no cap)
   int near_vb = 8;         // band vectors per thread while it overlaps
   // band CTA size while it overlaps: 128 threads free registers in pieces the
   // chain's CTAs fit (256 x 16384 mixed: 1.079 -> 1.067 ms; plain batches +0.1 %)
   int near_threads = 128;
   int near_pair = -1;    // band in pairs: 1 always, 0 never, -1 by leaf size
-  // programmatic dependent launch, bit flags: 1 far-field chain kernels,
-  // 2 the band, 4 the first chain kernel after the band on the same stream.
-  // Default: chain kernels of mixed plans, whose fragment prologues then overlap
-  // the previous kernel (measured 5 % faster for 256 x 16384, 3 % for one
-  // N = 2^22 vector); plain plans none (their short tree kernels have no
-  // prologue to hide, and one N = 2^20 vector was 3 % slower with it).
+  //  pdl: programmatic dependent launch, bit flags: 1 far-field chain kernels,
+  //    2 the band, 4 the first chain kernel after the band on the same stream;
+  //  chain_prio_mode: the chain's kernels at the device's greatest priority.
   int pdl = -1;
-  // Scheduling priority of the far-field chain's kernels while the band runs
-  // beside them: with it, CTAs of the (latency-bound) chain are dispatched
-  // before further CTAs of the band as SMs free up, so the chain is not held
-  // behind the whole band.  Default: the device's greatest priority for mixed
-  // plans (256 x 16384: 1.155 -> 1.080 ms), none for plain plans (whose chain
-  // also runs on the FP64 pipe; 4 % slower with it).  L2C_CHAIN_PRIO=0|1 forces.
-  int chain_prio = 0;
   int chain_prio_mode = -1;
+  int prio_greatest = 0;  // cudaDeviceGetStreamPriorityRange's greatest priority
   // launch accounting and optional per-phase CUDA-event timing
   size_t launches = 0;
   bool profiling = false;
@@ -2181,13 +2174,35 @@ Geo make_geo(const l2c_gpu_plan *p, size_t count, size_t dist, size_t stride) {
 // cores (the far-field blocks only when the batch gives each block at least 8
 // right-hand sides; single vectors keep the FP64 block products, on doubles
 // converted from and back to the column format in place).
-unsigned pdl_flags(const l2c_gpu_plan *p) {
-  return p->pdl >= 0 ? (unsigned)p->pdl : p->mixed ? 1u : 0u;
+// How one call is scheduled.  The band (FP64-bound, many long CTAs) runs on the
+// second stream beside the far-field chain.  When the chain is latency-bound --
+// a single vector, whose tree levels hold few items, or any mixed plan, whose
+// tensor-core kernels are bound by integer latency -- its kernels also carry
+// the device's greatest priority (as band CTAs retire the SMs go to the chain
+// first; graph nodes keep the priority) and programmatic dependent launch
+// (each kernel's prologue and launch overlap the previous kernel).  Measured,
+// L2C + C2L: plain single N = 2^20 1.321 -> 1.177 ms, N = 2^14 0.180 -> 0.135;
+// mixed 256 x 16384 1.276 -> 1.080.  Plain batches keep plain launches (their
+// chain is throughput-bound: 4096 x 1024 2.27 ms, 2.33 with both).
+struct Sched {
+  bool ov;       // band on the second stream
+  unsigned pdl;  // programmatic dependent launch flags (as l2c_gpu_plan::pdl)
+  int prio;      // priority of the chain's kernels (0: the stream's)
+};
+
+Sched sched_for(const l2c_gpu_plan *p, size_t count) {
+  Sched sc;
+  sc.ov = p->overlap >= 0 ? p->overlap == 1 : true;
+  const bool latency = p->mixed || count == 1;
+  sc.pdl = p->pdl >= 0 ? (unsigned)p->pdl : latency ? 1u : 0u;
+  const bool prio = p->chain_prio_mode >= 0 ? p->chain_prio_mode == 1 : latency;
+  sc.prio = prio && sc.ov ? p->prio_greatest : 0;
+  return sc;
 }
 
 // The first far-field kernel follows the band on the same stream unless the
 // band runs on the second stream.
-bool pdl_after_band(const l2c_gpu_plan *p, bool ov) { return (pdl_flags(p) & (ov ? 1u : 4u)) != 0; }
+bool pdl_after_band(const Sched &sc) { return (sc.pdl & (sc.ov ? 1u : 4u)) != 0; }
 
 template <int KC>
 void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStream_t st,
@@ -2201,13 +2216,14 @@ void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStrea
 }
 
 bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir, const Geo &g,
-                      cudaStream_t st, bool ov) {
+                      cudaStream_t st, const Sched &sc) {
+  const bool ov = sc.ov;
   const int c2l = dir == 1;
   long long *w = reinterpret_cast<long long *>(p->w), *c = reinterpret_cast<long long *>(p->c);
-  const LaunchOpt chain(pdl_flags(p) & 1, ov ? p->chain_prio : 0);
+  const LaunchOpt chain(sc.pdl & 1, sc.prio);
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
-    const LaunchOpt pdl(pdl_after_band(p, ov), ov ? p->chain_prio : 0);
+    const LaunchOpt pdl(pdl_after_band(sc), sc.prio);
     switch (p->oz_kc) {
       case 1: mz_leaf_up_launch<1>(p, x, g, st, pdl); break;
       case 2: mz_leaf_up_launch<2>(p, x, g, st, pdl); break;
@@ -2279,7 +2295,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     const int per_sm = p->oz_nbuf == 1 ? 4 : 2;  // resident CTAs (registers, shared memory)
     const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * per_sm);
     // after the join with the band's stream: a plain launch (full dependency)
-    launch_k((pdl_flags(p) & 1) && !ov, p->oz_nbuf == 1 ? k_mz_leaf_down<1> : k_mz_leaf_down<2>,
+    launch_k((sc.pdl & 1) && !ov, p->oz_nbuf == 1 ? k_mz_leaf_down<1> : k_mz_leaf_down<2>,
              grid, 32 * MXW, mz_leaf_down_smem(p->oz_npass, p->oz_nbuf), st,
              (const long long *)c, (const int *)p->cE, (const double *)p->y, out,
              (const unsigned *)p->oz_ld, (const int *)p->oz_lde, g, c2l, p->oz_npass);
@@ -2343,7 +2359,8 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   // mixed form the tensor-core products, which use other pipes: measured 4 %
   // faster for 4096 x 1024 plain, 5 % for 256 x 16384 mixed; no change for a
   // single plain vector, whose far field also runs on the FP64 pipe).
-  const bool ov = p->overlap >= 0 ? p->overlap == 1 : (p->mixed || count > 1);
+  const Sched sc = sched_for(p, count);
+  const bool ov = sc.ov;
   cudaStream_t stn = ov ? st2 : st;
   if (ov) {
     CK(cudaEventRecord(p->ev_fork, st));
@@ -2352,15 +2369,15 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   {
     PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, ov ? p->near_vb : 8), stn);
     CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, near_pair(p),
-                    ov ? p->near_ctas : 0, ov ? p->near_vb : 8, (pdl_flags(p) & 2) && !ov,
+                    ov ? p->near_ctas : 0, ov ? p->near_vb : 8, (sc.pdl & 2) && !ov,
                     ov ? p->near_threads : 256));
   }
   if (ov) CK(cudaEventRecord(p->ev_join, st2));
-  if (p->mixed) return launch_mixed_far(p, x, out, dir, g, st, ov) ? 1 : 0;
+  if (p->mixed) return launch_mixed_far(p, x, out, dir, g, st, sc) ? 1 : 0;
   const long long leaf_threads = g.count * g.K * 2 * M;
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
-    launch_k(LaunchOpt(pdl_after_band(p, ov), ov ? p->chain_prio : 0), k_leaf_up,
+    launch_k(LaunchOpt(pdl_after_band(sc), sc.prio), k_leaf_up,
              blocks_for(leaf_threads, 288), 288, 0, st, x,
              (const double *)p->T, p->w, g);
     CK(cudaGetLastError());
@@ -2368,25 +2385,24 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   const TreePlan tp = tree_plan(p->L, count);
   {
     PhaseScope ps(p, L2C_PHASE_TREE_UP, tree_launches(tp, p->L));
-    CK(sweep_up(p->w, g, tp, st, LaunchOpt(pdl_flags(p) & 1, ov ? p->chain_prio : 0), p->nodal));
+    CK(sweep_up(p->w, g, tp, st, LaunchOpt(sc.pdl & 1, sc.prio), p->nodal));
   }
   {
     PhaseScope ps(p, L2C_PHASE_FAR, 1);
     const long long n = g.count * 2 * (long long)p->Nb * M;
-    launch_k(LaunchOpt(pdl_flags(p) & 1, ov ? p->chain_prio : 0), k_far, blocks_for(n, 256), 256,
+    launch_k(LaunchOpt(sc.pdl & 1, sc.prio), k_far, blocks_for(n, 256), 256,
              0, st, (const double *)p->A[dir],
              (const double *)p->w, p->c, g, (long long)p->Nb);
     CK(cudaGetLastError());
   }
   {
     PhaseScope ps(p, L2C_PHASE_TREE_DOWN, tree_launches(tp, p->L));
-    CK(sweep_down(p->c, g, tp, st, LaunchOpt(pdl_flags(p) & 1, ov ? p->chain_prio : 0),
-                  p->nodal));
+    CK(sweep_down(p->c, g, tp, st, LaunchOpt(sc.pdl & 1, sc.prio), p->nodal));
   }
   if (ov) CK(cudaStreamWaitEvent(st, p->ev_join, 0));
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
-    launch_k((pdl_flags(p) & 1) && !ov, k_leaf_down, blocks_for(total, 256), 256, 0, st,
+    launch_k((sc.pdl & 1) && !ov, k_leaf_down, blocks_for(total, 256), 256, 0, st,
              (const double *)p->c,
              (const double *)p->T, (const double *)p->y, out, g, c2l);
     CK(cudaGetLastError());
@@ -2744,10 +2760,10 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   PCK(cudaStreamSynchronize(st));
   for (size_t d = 0; d < 2; d++)
     if (directions == d || directions == 2) p->flops[d] = ref_flops(p, d);
-  if (p->chain_prio_mode == 1 || (p->chain_prio_mode < 0 && p->mixed)) {
+  {
     int least = 0, greatest = 0;
     PCK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    p->chain_prio = greatest;
+    p->prio_greatest = greatest;
   }
   return p;
 #undef PCK
