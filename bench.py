@@ -558,20 +558,36 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     peak = measured_fp64_peak(torch, dev)
 
-    def step():
-        with torch.cuda.stream(stream):
+    def step(pl=None, st=None):
+        pl, st = pl or plan, st or stream
+        with torch.cuda.stream(st):
             flush.fill_(1)
             dbuf["o0"].zero_()
             dbuf["o1"].zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        e0.record(st)
         for d, src, dst in wl.calls:
             if ragged:
-                plan.execute_async(dbuf[src], dbuf[dst], d)
+                pl.execute_async(dbuf[src], dbuf[dst], d)
             else:
-                plan.execute_async(dbuf[src], dbuf[dst], d, count, N, 1)
-        e1.record(stream)
+                pl.execute_async(dbuf[src], dbuf[dst], d, count, N, 1)
+        e1.record(st)
         return e0, e1
+
+    def phase_pass(pl, st):
+        """args.steps steps with per-phase CUDA events (direct launches)."""
+        abi.l2c_gpu_profile(pl._gpu, 1)
+        evs = [step(pl, st) for _ in range(args.steps)]
+        pl.synchronize()
+        ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / len(evs))
+        pms = (ctypes.c_double * 8)()
+        pl_n = (ctypes.c_size_t * 8)()
+        abi.l2c_gpu_profile_read(pl._gpu, pms, pl_n)
+        abi.l2c_gpu_profile(pl._gpu, 0)
+        names = ["gather", "near", "leaf_up", "tree_up", "far", "tree_down", "leaf_down", "direct"]
+        return ms, {names[i]: {"ms_per_step": pms[i] / args.steps,
+                               "launches_per_step": pl_n[i] / args.steps}
+                    for i in range(8) if pl_n[i]}
 
     for _ in range(args.warmup):
         step()
@@ -596,20 +612,23 @@ def main():
     value = aggregate_value(wl.coefs_per_step, world, ms_step)
 
     # ---- the same K steps again with per-phase CUDA events (direct launches) ----
-    phases = {}
+    phases, phases_iso = {}, {}
     ms_prof = None
     if not ragged:
-        abi.l2c_gpu_profile(plan._gpu, 1)
-        evs = [step() for _ in range(args.steps)]
-        plan.synchronize()
-        ms_prof = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / len(evs))
-        pms = (ctypes.c_double * 8)()
-        pl = (ctypes.c_size_t * 8)()
-        abi.l2c_gpu_profile_read(plan._gpu, pms, pl)
-        abi.l2c_gpu_profile(plan._gpu, 0)
-        names = ["gather", "near", "leaf_up", "tree_up", "far", "tree_down", "leaf_down", "direct"]
-        phases = {names[i]: {"ms_per_step": pms[i] / args.steps,
-                             "launches_per_step": pl[i] / args.steps} for i in range(8) if pl[i]}
+        ms_prof, phases = phase_pass(plan, stream)
+        # the band alone: a plan whose band runs on its own stream, before the
+        # far-field chain (in the step above it shares the SMs with the chain)
+        os.environ["L2C_OVERLAP"] = "0"
+        try:
+            plan_iso = l2c.Plan(N, maxs, precompute=args.precompute, lagrange=args.lagrange)
+        finally:
+            del os.environ["L2C_OVERLAP"]
+        st_iso = torch.cuda.ExternalStream(plan_iso.stream, device=dev)
+        for _ in range(2):
+            step(plan_iso, st_iso)
+        plan_iso.synchronize()
+        _, phases_iso = phase_pass(plan_iso, st_iso)
+        plan_iso.close()
 
     # ---- e2e through execute() with pinned host buffers ----
     hbuf = {"u": torch.from_numpy(np.ascontiguousarray(wl.u)).pin_memory()}
@@ -642,12 +661,16 @@ def main():
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": None,
                 "peak_source": "FP64 DGEMM measured in this run (cuBLAS float64 matmul 4096^3)"}
-    if "near" in phases and L >= 1:
+    if "near" in phases_iso and L >= 1:
         nf = sum(near_flops(N, s, d) for d, _, _ in wl.calls) * count / len(wl.calls)
-        launches_near = phases["near"]["launches_per_step"] / len(wl.calls)
-        avg_ms = phases["near"]["ms_per_step"] / phases["near"]["launches_per_step"]
-        flops_per_launch = nf / launches_near
-        achieved = flops_per_launch / (avg_ms * 1e-3) / 1e12
+
+        def band_rate(ph):
+            launches_near = ph["near"]["launches_per_step"] / len(wl.calls)
+            avg = ph["near"]["ms_per_step"] / ph["near"]["launches_per_step"]
+            return nf / launches_near, avg, nf / launches_near / (avg * 1e-3) / 1e12
+
+        flops_per_launch, avg_ms, achieved = band_rate(phases_iso)
+        _, avg_ms_step, achieved_step = band_rate(phases)
         # DRAM bytes per band launch from one ncu capture of this same command
         # (dram__bytes_read.sum + dram__bytes_write.sum, mean of the L2C and C2L
         # launches); other workloads were not captured.
@@ -661,6 +684,13 @@ def main():
                 "algorithmic_bytes_per_launch": 24 * N * count,
                 "peak_source": "FP64 DGEMM measured in this run (cuBLAS float64 matmul 4096^3)",
                 "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_ms,
+                "timing": "band launches timed with CUDA events on their stream, in a pass "
+                          "of the same workload with the band on the plan's stream (the "
+                          "kernel alone on the GPU)",
+                "achieved_in_step": achieved_step, "frac_in_step": achieved_step / peak,
+                "avg_launch_ms_in_step": avg_ms_step,
+                "in_step_note": "in the timed step the band runs on a second stream beside "
+                                "the far-field chain, whose kernels have scheduling priority",
                 "note": "reference flop count of directM/directL (3 per band term); a term "
                         "costs 2 FP64 issue slots (DMUL+DFMA) unless precompute=1"}
     if not ragged:
