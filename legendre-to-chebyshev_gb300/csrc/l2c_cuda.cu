@@ -589,9 +589,21 @@ __device__ __forceinline__ void load_tree_mat(double *sB) {
     sB[t] = NODAL ? c_lag_B[t] : UP ? c_binom_lower[t] : c_binom_upper[t];
 }
 
-// Row m of a parent from its two children x0, x1.  Modal: the lower binomial
-// row with the +/- parity combination of the second child (leg2cheb.c:537-602);
-// nodal: column m of B0 and of B1, out = B0^T x0 + B1^T x1 (leg2cheb.c:1401-1416).
+// Modal upward transfer, first half (leg2cheb.c:537-602): the children x0, x1
+// of a parent become z+ = x0 + S x1 and z- = x0 - S x1 in place (S = diag(1,
+// -1, 1, ...)), element i of the pair.  Nodal: nothing.
+template <bool NODAL>
+__device__ __forceinline__ void zpm_item(double *x0, double *x1, int i) {
+  if (NODAL) return;
+  const double a = x0[i], b = (i & 1) ? -x1[i] : x1[i];
+  x0[i] = a + b;
+  x1[i] = a - b;
+}
+
+// Row m of a parent from its two children.  Modal: the lower binomial row
+// times z+ (even m) or z- (odd m), the children after zpm_item (leg2cheb.c:
+// 537-602: 36 adds and 171 FMAs per parent); nodal: column m of B0 and of B1,
+// out = B0^T x0 + B1^T x1 (leg2cheb.c:1401-1416).
 template <bool NODAL>
 __device__ __forceinline__ void row_up(const double *sB, const double *x0, const double *x1, int m,
                                        double &out) {
@@ -602,12 +614,13 @@ __device__ __forceinline__ void row_up(const double *sB, const double *x0, const
       s1 = fma(sB[MM + i * M + m], x1[i], s1);
     }
   } else {
-    const double *Bm = sB + m * (m + 1) / 2;
-    for (int i = 0; i <= m; i++) {
-      const double bmi = Bm[i];
-      s0 = fma(bmi, x0[i], s0);
-      s1 = fma(((m + i) & 1) ? -bmi : bmi, x1[i], s1);
+    const double *Bm = sB + m * (m + 1) / 2, *z = (m & 1) ? x1 : x0;
+    int i = 0;
+    for (; i + 1 <= m; i += 2) {  // two chains (even, odd i) halve the latency
+      s0 = fma(Bm[i], z[i], s0);
+      s1 = fma(Bm[i + 1], z[i + 1], s1);
     }
+    if (i <= m) s0 = fma(Bm[i], z[i], s0);
   }
   out = s0 + s1;
 }
@@ -651,6 +664,13 @@ __device__ __forceinline__ void tree_up_tile(const double *const *child, double 
     sx[p * TREE_PAD + q] = par[p] ? child[p][q] : 0.0;
   }
   __syncthreads();
+  if (!NODAL) {
+    for (int e = threadIdx.x; e < TREE_TILE * M; e += blockDim.x) {
+      const int p = e / M, i = e - p * M;
+      zpm_item<NODAL>(sx + p * TREE_PAD, sx + p * TREE_PAD + M, i);
+    }
+    __syncthreads();
+  }
   const int m = threadIdx.x >> 5, p = threadIdx.x & 31;
   if (m >= M || par[p] == nullptr) return;
   const double *x0 = sx + p * TREE_PAD, *x1 = x0 + M;
@@ -722,6 +742,13 @@ __global__ void __launch_bounds__(32 * M) k_up_sub(double *w, Geo g, int l0, int
     const long long base = 2 * (long long)blocks_before((size_t)l);
     // (parent, row) items packed densely over the CTA: a warp FP64 instruction
     // costs the same with idle lanes, so narrow levels use few, full warps
+    if (!NODAL) {
+      for (int it = threadIdx.x; it < np * M; it += blockDim.x) {
+        const int p = it & (np - 1), i = it >> lg;
+        zpm_item<NODAL>(child + 2 * p * SUB_PAD, child + (2 * p + 1) * SUB_PAD, i);
+      }
+      __syncthreads();
+    }
     for (int it = threadIdx.x; it < np * M; it += blockDim.x) {
       const int p = it & (np - 1), m = it >> lg;
       const long long u = r * np + p;
@@ -759,6 +786,13 @@ __global__ void __launch_bounds__(32 * M) k_up_top(double *w, Geo g, int lt) {
     const int nn = 4 << l;  // nodes of level l; sources are nodes 2 .. nn-1
     double *par = sm + (nn - 4) * SUB_PAD, *child = sm + (2 * nn - 4) * SUB_PAD;
     const long long base = 2 * (long long)blocks_before((size_t)l);
+    if (!NODAL) {
+      for (int it = threadIdx.x; it < (nn - 2) * M; it += blockDim.x) {
+        const int u = 2 + it % (nn - 2), i = it / (nn - 2);
+        zpm_item<NODAL>(child + 2 * u * SUB_PAD, child + (2 * u + 1) * SUB_PAD, i);
+      }
+      __syncthreads();
+    }
     for (int it = threadIdx.x; it < (nn - 2) * M; it += blockDim.x) {  // dense items
       const int u = 2 + it % (nn - 2), m = it / (nn - 2);
       double out;
