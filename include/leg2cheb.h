@@ -11,8 +11,9 @@
  *  - execute() returns the reference's flop count on success and 0 on failure
  *    (unplanned direction, CUDA error); l2c_last_error() says why.  The
  *    reference asserts or dereferences NULL in those cases.
- *  - in/out may be host pointers (copied to and from the GPU) or device
- *    pointers (used in place).
+ *  - in/out may be host pointers or device pointers (used in place).  Pageable
+ *    host memory is copied to and from the GPU; page-locked host memory is read
+ *    and written in place by the kernels through its device mapping.
  */
 #ifndef LEG2CHEB_H
 #define LEG2CHEB_H

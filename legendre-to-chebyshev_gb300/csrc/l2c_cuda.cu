@@ -1840,6 +1840,7 @@ struct l2c_gpu_plan {
   // for twice the warps per SM, which hide more of the products' latency than
   // a second buffer does (256 x 16384: 1.155 vs 1.253 ms per L2C + C2L)
   int oz_nbuf = 1;
+  bool zero_copy = true;  // page-locked host buffers used in place (L2C_ZERO_COPY=0: staged)
   unsigned *oz_far[2] = {nullptr, nullptr};
   int *oz_farm[2] = {nullptr, nullptr};
   // column exponents of w and c (mixed form: w, c hold column-format integers)
@@ -2022,6 +2023,17 @@ bool ensure_scratch(l2c_gpu_plan *p, size_t count) {
   }
   p->cap_vec = need;
   return true;
+}
+
+// Device address of page-locked host memory that is mapped into the device's
+// address space (nullptr otherwise: pageable memory, or not mapped).
+void *mapped_host_ptr(const void *ptr) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
 bool is_device_ptr(const void *ptr) {
@@ -2356,7 +2368,8 @@ bool ensure_mixed_far(l2c_gpu_plan *p, size_t dir) {
 // Near field on stream2 beside the far-field chain on stream; joined before the
 // final leaf-down kernel.
 size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, size_t count,
-                  size_t dist, size_t stride, bool near_only, bool input_ready) {
+                  size_t dist, size_t stride, bool near_only, bool input_ready,
+                  bool in_host = false) {
   cudaStream_t st = p->stream, st2 = p->stream2;
   const int c2l = dir == 1;
   Geo g = make_geo(p, count, dist, stride);
@@ -2369,7 +2382,8 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   }
   // contiguous (and for C2L premultiplied) copy of the input
   const double *x = in;
-  if (!input_ready && (c2l || stride != 1 || (count > 1 && dist != p->N))) {
+  // (input in host memory: read once, here, not by every band term)
+  if (!input_ready && (in_host || c2l || stride != 1 || (count > 1 && dist != p->N))) {
     PhaseScope ps(p, L2C_PHASE_GATHER, 1);
     k_gather<<<blocks_for(total, 256), 256, 0, st>>>(in, p->x, g, c2l);
     CK(cudaGetLastError());
@@ -2448,13 +2462,14 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
 // sequence when one exists for this call shape, else capture one (or launch
 // directly while per-phase profiling is on).
 size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, size_t count,
-                  size_t dist, size_t stride, bool near_only, bool input_ready) {
+                  size_t dist, size_t stride, bool near_only, bool input_ready,
+                  bool in_host = false) {
   if (count == 0 || p->N == 0) return 1;
   if (!ensure_scratch(p, count)) return 0;
   if (p->mixed && p->L > 0 && count >= 4 && !ensure_mixed_far(p, dir)) return 0;
-  const unsigned mode = (near_only ? 1u : 0u) | (input_ready ? 2u : 0u);
+  const unsigned mode = (near_only ? 1u : 0u) | (input_ready ? 2u : 0u) | (in_host ? 4u : 0u);
   if (p->profiling || !p->use_graphs) {
-    return launch_all(p, in, out, dir, count, dist, stride, near_only, input_ready);
+    return launch_all(p, in, out, dir, count, dist, stride, near_only, input_ready, in_host);
   }
   p->use_clock++;
   for (auto &e : p->graphs) {
@@ -2468,7 +2483,8 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   }
   const size_t before = p->launches;
   CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
-  const size_t ok = launch_all(p, in, out, dir, count, dist, stride, near_only, input_ready);
+  const size_t ok =
+      launch_all(p, in, out, dir, count, dist, stride, near_only, input_ready, in_host);
   cudaGraph_t graph = nullptr;
   const cudaError_t ec = cudaStreamEndCapture(p->stream, &graph);
   if (!ok || ec != cudaSuccess) {
@@ -2564,6 +2580,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_PDL")) p->pdl = std::max(0, std::atoi(env));
   if (const char *env = std::getenv("L2C_CHAIN_PRIO")) p->chain_prio_mode = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_MZ_NBUF")) p->oz_nbuf = env[0] == '1' ? 1 : 2;
+  if (const char *env = std::getenv("L2C_ZERO_COPY")) p->zero_copy = env[0] != '0';
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
     p->Nn = N;
@@ -2890,7 +2907,29 @@ size_t l2c_gpu_execute(l2c_gpu_plan *p, const double *in, double *out, size_t di
   // directL semantics: contiguous, premultiplied input
   const bool in_contig = near_only && dir == 1;
   const size_t in_span = in_contig ? (count - 1) * dist + N : span;
-  const bool in_dev = is_device_ptr(in), out_dev = is_device_ptr(out);
+  bool in_dev = is_device_ptr(in), out_dev = is_device_ptr(out);
+  // Page-locked host buffers of an FMM transform are used in place through
+  // their device mapping: the gather kernel reads the input once over the
+  // host link, the band reads and the leaf-down kernel writes the output --
+  // no staging copies around the transform (N = 2^20 single vector, L2C + C2L
+  // through host buffers: 1.44e9 -> 1.66e9 coef/s).  Mixed plans stage the
+  // output: their leaf-down writes each lane's outputs at stride 2, which the
+  // host link serves poorly (256 x 16384: 4.1e9 staged, 2.8e9 in place).
+  bool in_host = false, out_host = false;
+  if (p->zero_copy && p->L > 0 && !near_only) {
+    if (!in_dev)
+      if (const void *m = mapped_host_ptr(in)) {
+        in = static_cast<const double *>(m);
+        in_dev = in_host = true;
+      }
+    if (!out_dev && !p->mixed)
+      if (void *m = mapped_host_ptr(out)) {
+        out = static_cast<double *>(m);
+        out_dev = out_host = true;
+      }
+  }
+  // host memory involved: the call returns once the results are there
+  const bool host_side = in_host || out_host || !in_dev || !out_dev;
   if (!in_dev || !out_dev) {
     // host memory: stage the touched span (the layout is kept, so the kernels
     // see the same dist/stride)
@@ -2907,10 +2946,10 @@ size_t l2c_gpu_execute(l2c_gpu_plan *p, const double *in, double *out, size_t di
   }
   const double *din = in_dev ? in : p->st_in;
   double *dout = out_dev ? out : p->st_out;
-  if (!run_device(p, din, dout, dir, count, dist, stride, near_only, in_contig)) return 0;
+  if (!run_device(p, din, dout, dir, count, dist, stride, near_only, in_contig, in_host)) return 0;
   if (!out_dev)
     CK(cudaMemcpyAsync(out, dout, span * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
-  if (!(flags & L2C_EXEC_ASYNC) || !in_dev || !out_dev) CK(cudaStreamSynchronize(p->stream));
+  if (!(flags & L2C_EXEC_ASYNC) || host_side) CK(cudaStreamSynchronize(p->stream));
   size_t f = p->flops[dir];
   if (near_only) f = 1;  // callers of directM/directL get their own count
   return f * count;

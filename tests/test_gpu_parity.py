@@ -355,3 +355,33 @@ def test_ragged_device_pointers_and_launch_count(lib, torch_cuda):
     p.synchronize()
     assert p.launch_count() - before <= 24  # independent of the 500 vectors
     assert np.array_equal(dout.cpu().numpy(), host)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+@pytest.mark.parametrize("count,N,stride", [(1, 1 << 16, 1), (1, 4097, 3), (16, 4096, 1)])
+def test_pinned_host_buffers_in_place(lib, torch_cuda, monkeypatch, mixed, count, N, stride):
+    """Page-locked host buffers are read and written in place through their
+    device mapping (no staging copies); results are the staged path's bits."""
+    torch = torch_cuda
+    maxs = 16 if mixed else 64
+    if mixed and stride != 1:
+        pytest.skip("strided lines are covered by the plain form")
+    dist = N * stride
+    x = make_input(count * dist, "sign", N + count)
+    want = []
+    with monkeypatch.context() as m:
+        m.setenv("L2C_ZERO_COPY", "0")
+        p = lib.Plan(N, maxs, mixed=mixed)
+        for d in (0, 1):
+            out = np.zeros(count * dist)
+            p.execute_batched(x, out, d, count, dist, stride)
+            want.append(out)
+        p.close()
+    p = lib.Plan(N, maxs, mixed=mixed)
+    hx = torch.from_numpy(x).pin_memory()
+    for d in (0, 1):
+        ho = torch.zeros(count * dist, dtype=torch.float64).pin_memory()
+        for _ in range(2):  # capture, then replay
+            ho.zero_()
+            p.execute_batched(hx, ho, d, count, dist, stride)
+        assert np.array_equal(ho.numpy(), want[d]), d
