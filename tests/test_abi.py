@@ -186,3 +186,12 @@ def test_rejects_unsupported_forms(lib):
         lib.Plan(1024, 64, M=20)
     with pytest.raises(lib.L2CError, match="lagrange must be 0"):
         lib.Plan(1024, 64, lagrange=2)
+    # ragged lists: modal form only, refused before any device work
+    import ctypes
+
+    import numpy as np
+
+    L = lib.load()
+    Ns = np.array([1000, 5000], dtype=np.uint64)
+    assert not L.create_fmm_ragged(2, ctypes.c_void_p(Ns.ctypes.data), 64, 18, 2, 1, 0, 0)
+    assert "modal form" in lib.last_error()

@@ -27,12 +27,13 @@ def _abi(lib):
     return c
 
 
-@pytest.mark.parametrize("N,maxs,stride", [(4096, 64, 1), (65536, 32, 1), (5001, 64, 3)])
-def test_noalloc_matches_execute_two_calls(lib, N, maxs, stride):
+@pytest.mark.parametrize("N,maxs,stride,lagrange", [(4096, 64, 1, 0), (65536, 32, 1, 0),
+                                                    (5001, 64, 3, 0), (16384, 32, 1, 1)])
+def test_noalloc_matches_execute_two_calls(lib, N, maxs, stride, lagrange):
     import torch
 
     c = _abi(lib)
-    p = lib.Plan(N, maxs)
+    p = lib.Plan(N, maxs, lagrange=lagrange)
     for d in (0, 1):
         inputs = [make_input(N * stride, "uniform", 10 + d), make_input(N * stride, "sign", 20 + d)]
         for u in inputs:  # two calls in a row
