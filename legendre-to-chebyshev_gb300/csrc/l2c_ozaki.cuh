@@ -195,18 +195,22 @@ __device__ __forceinline__ bool to_fixed(double x, int e, long long &X) {
 // and the D0 term added to the high word in 32-bit arithmetic
 // ((D0 2^4 mod 2^32) 2^32 = D0 2^36 mod 2^64) -- the same value as the
 // nested form ((D0 2^9 + D1) 2^9 + ...) in half the integer instructions.
-template <int NT>
-__device__ __forceinline__ long long combine(const float (&acc)[NDIAG][NT][4], int nt, int e) {
+__device__ __forceinline__ long long combine6(float a0, float a1, float a2, float a3, float a4,
+                                              float a5) {
   static_assert(NDIAG == 6, "the expansion below has six diagonals");
-  const int d0 = __float2int_rn(acc[0][nt][e]), d1 = __float2int_rn(acc[1][nt][e]);
-  const int d2 = __float2int_rn(acc[2][nt][e]), d3 = __float2int_rn(acc[3][nt][e]);
-  const int d4 = __float2int_rn(acc[4][nt][e]), d5 = __float2int_rn(acc[5][nt][e]);
+  const int d0 = __float2int_rn(a0), d1 = __float2int_rn(a1), d2 = __float2int_rn(a2);
+  const int d3 = __float2int_rn(a3), d4 = __float2int_rn(a4), d5 = __float2int_rn(a5);
   long long t = (long long)(d4 + (d5 >> 9));
   t += (long long)d3 * (1 << 9);
   t += (long long)d2 * (1 << 18);
   t += (long long)d1 * (1 << 27);
   const unsigned hi = (unsigned)d0 << 4;
   return (long long)((unsigned long long)t + ((unsigned long long)hi << 32));
+}
+template <int NT>
+__device__ __forceinline__ long long combine(const float (&acc)[NDIAG][NT][4], int nt, int e) {
+  return combine6(acc[0][nt][e], acc[1][nt][e], acc[2][nt][e], acc[3][nt][e], acc[4][nt][e],
+                  acc[5][nt][e]);
 }
 
 // The warp's 16 x (NT*8) tile over k8-chunks [C0, C1): acc[d-2][nt][.] = sum
@@ -354,15 +358,7 @@ __device__ __forceinline__ void mma_nt(const unsigned *__restrict__ Pf, const Di
 
 // combine() for one n-tile's accumulators.
 __device__ __forceinline__ long long combine1(const float (&acc)[NDIAG][4], int e) {
-  const int d0 = __float2int_rn(acc[0][e]), d1 = __float2int_rn(acc[1][e]);
-  const int d2 = __float2int_rn(acc[2][e]), d3 = __float2int_rn(acc[3][e]);
-  const int d4 = __float2int_rn(acc[4][e]), d5 = __float2int_rn(acc[5][e]);
-  long long t = (long long)(d4 + (d5 >> 9));
-  t += (long long)d3 * (1 << 9);
-  t += (long long)d2 * (1 << 18);
-  t += (long long)d1 * (1 << 27);
-  const unsigned hi = (unsigned)d0 << 4;
-  return (long long)((unsigned long long)t + ((unsigned long long)hi << 32));
+  return combine6(acc[0][e], acc[1][e], acc[2][e], acc[3][e], acc[4][e], acc[5][e]);
 }
 
 // Column exponents and offset words of a staged tile, in place: Xs holds the
