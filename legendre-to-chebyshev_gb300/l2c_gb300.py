@@ -127,13 +127,22 @@ def last_error():
 
 
 def _ptr(a):
-    """Address of a numpy array or of a tensor-like object with data_ptr()."""
+    """Address of a numpy array, of a tensor-like object with data_ptr(), or of
+    any DLPack producer (``__dlpack__``: CuPy, JAX, ... device or host arrays,
+    viewed without a copy)."""
     if hasattr(a, "data_ptr"):
         return ctypes.c_void_p(a.data_ptr())
     if isinstance(a, np.ndarray):
         if a.dtype != np.float64:
             raise TypeError("arrays must be float64")
         return ctypes.c_void_p(a.ctypes.data)
+    if hasattr(a, "__dlpack__"):
+        import torch
+
+        t = torch.utils.dlpack.from_dlpack(a)
+        if t.dtype != torch.float64:
+            raise TypeError("arrays must be float64")
+        return ctypes.c_void_p(t.data_ptr())
     raise TypeError(f"unsupported array type {type(a)}")
 
 

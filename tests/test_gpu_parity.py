@@ -385,3 +385,29 @@ def test_pinned_host_buffers_in_place(lib, torch_cuda, monkeypatch, mixed, count
             ho.zero_()
             p.execute_batched(hx, ho, d, count, dist, stride)
         assert np.array_equal(ho.numpy(), want[d]), d
+
+
+def test_dlpack_device_arrays(lib, torch_cuda):
+    """Any DLPack producer is accepted in place (here a minimal one that
+    exports a CUDA tensor only through __dlpack__)."""
+    torch = torch_cuda
+
+    class Producer:
+        def __init__(self, t):
+            self._t = t
+
+        def __dlpack__(self, **kw):
+            return self._t.__dlpack__(**kw)
+
+        def __dlpack_device__(self):
+            return self._t.__dlpack_device__()
+
+    N = 4096
+    u = make_input(N, "sign", 3)
+    p = lib.Plan(N, 64)
+    want = np.zeros(N)
+    p.execute(u, want, 0)
+    du = torch.from_numpy(u).cuda()
+    dout = torch.zeros(N, dtype=torch.float64, device="cuda")
+    p.execute(Producer(du), Producer(dout), 0)
+    assert np.array_equal(dout.cpu().numpy(), want)
