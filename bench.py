@@ -614,13 +614,16 @@ def main():
     # ---- the same K steps again with per-phase CUDA events (direct launches) ----
     phases, phases_iso = {}, {}
     ms_prof = None
+    plan_ms = None
     if not ragged:
         ms_prof, phases = phase_pass(plan, stream)
         # the band alone: a plan whose band runs on its own stream, before the
         # far-field chain (in the step above it shares the SMs with the chain)
         os.environ["L2C_OVERLAP"] = "0"
         try:
+            t_plan0 = time.perf_counter()
             plan_iso = l2c.Plan(N, maxs, precompute=args.precompute, lagrange=args.lagrange)
+            plan_ms = (time.perf_counter() - t_plan0) * 1e3
         finally:
             del os.environ["L2C_OVERLAP"]
         st_iso = torch.cuda.ExternalStream(plan_iso.stream, device=dev)
@@ -712,7 +715,8 @@ def main():
         "ms_per_step_phase_profiled": ms_prof,
         "fp64_ref_tflops_whole_step": total_flops / (ms_step * 1e-3) / 1e12,
         "wall_s_timed_region": t_wall,
-        "plan": {"L": L, "s": s, "Nb": plan.Nb} if not ragged else {"vectors": count},
+        "plan": ({"L": L, "s": s, "Nb": plan.Nb, "create_fmm_ms": plan_ms} if not ragged
+                 else {"vectors": count}),
     }
     got = {k: dbuf[k].cpu().numpy() for k in ("o0", "o1")}
     if wl.name == "batch":
