@@ -921,19 +921,45 @@ __device__ __forceinline__ void far_item(const double *__restrict__ Ablk,
   c0[M + m] = t2 + u2;
 }
 
-// Every level at once: block gb's A blocks start at 3 gb M^2.
+// Every level at once: block gb's A blocks start at 3 gb M^2.  A thread forms
+// row m of block gb for both parities of its vector: its three A rows are read
+// once, 16 bytes at a time (rows are 144 bytes, 16-byte aligned, as are the
+// tree slots), and each parity's sums are accumulated in far_item's order.
 __global__ void __launch_bounds__(256) k_far(const double *__restrict__ A,
                                              const double *__restrict__ w,
                                              double *__restrict__ c, Geo g, long long nblocks) {
   pdl_wait();
   pdl_trigger();
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long per_vs = nblocks * M;
-  if (idx >= g.count * 2 * per_vs) return;
-  const long long vs = idx / per_vs;
-  long long rem = idx - vs * per_vs;
-  const long long gb = rem / M;
-  far_item(A + 3 * gb * MM, w + vs * g.slots * M, c + vs * g.slots * M, gb, (int)(rem % M));
+  const long long per_v = nblocks * M;
+  if (idx >= g.count * per_v) return;
+  const long long v = idx / per_v, rem = idx - v * per_v, gb = rem / M;
+  const int m = (int)(rem - gb * M);
+  const double2 *A0 = reinterpret_cast<const double2 *>(A + 3 * gb * MM + m * M);
+  const double2 *A1 = A0 + MM / 2, *A2 = A1 + MM / 2;
+  double t0[2] = {0.0, 0.0}, t1[2] = {0.0, 0.0}, t2[2] = {0.0, 0.0};
+  double u0[2] = {0.0, 0.0}, u1[2] = {0.0, 0.0}, u2[2] = {0.0, 0.0};
+#pragma unroll
+  for (int k2 = 0; k2 < M / 2; k2++) {
+    const double2 a0 = A0[k2], a1 = A1[k2], a2 = A2[k2];
+#pragma unroll
+    for (int sg = 0; sg < 2; sg++) {
+      const double2 *ws = reinterpret_cast<const double2 *>(w + ((2 * v + sg) * g.slots + 2 * gb) * M);
+      const double2 x0 = ws[k2], x1 = ws[M / 2 + k2];
+      t0[sg] = fma(a0.x, x0.x, t0[sg]);
+      t1[sg] = fma(a1.x, x1.x, t1[sg]);
+      t2[sg] = fma(a2.x, x1.x, t2[sg]);
+      u0[sg] = fma(a0.y, x0.y, u0[sg]);
+      u1[sg] = fma(a1.y, x1.y, u1[sg]);
+      u2[sg] = fma(a2.y, x1.y, u2[sg]);
+    }
+  }
+#pragma unroll
+  for (int sg = 0; sg < 2; sg++) {
+    double *c0 = c + ((2 * v + sg) * g.slots + 2 * gb) * M;
+    c0[m] = (t0[sg] + u0[sg]) + (t1[sg] + u1[sg]);
+    c0[M + m] = t2[sg] + u2[sg];
+  }
 }
 
 // Step 4, one level: parent target slot t of level l into children 2t, 2t+1 of
@@ -2308,7 +2334,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
                (const int *)p->wE, c, p->cE, (const unsigned *)p->oz_far[dir],
                (const int *)p->oz_farm[dir], g);
     } else {
-      const long long ncol = g.count * 2 * g.slots, n = g.count * 2 * (long long)p->Nb * M;
+      const long long ncol = g.count * 2 * g.slots, n = g.count * (long long)p->Nb * M;
       k_oz_cols_to_double<<<blocks_for(ncol * M, 256), 256, 0, st>>>(w, p->wE, ncol);
       k_far<<<blocks_for(n, 256), 256, 0, st>>>(p->A[dir], p->w, p->c, g, (long long)p->Nb);
       k_oz_cols_from_double<<<blocks_for(ncol, OZ_CONV_COLS), OZ_CONV_COLS * M, 0, st>>>(
@@ -2437,7 +2463,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   }
   {
     PhaseScope ps(p, L2C_PHASE_FAR, 1);
-    const long long n = g.count * 2 * (long long)p->Nb * M;
+    const long long n = g.count * (long long)p->Nb * M;  // both parities per thread
     launch_k(LaunchOpt(sc.pdl & 1, sc.prio), k_far, blocks_for(n, 256), 256,
              0, st, (const double *)p->A[dir],
              (const double *)p->w, p->c, g, (long long)p->Nb);
@@ -3155,8 +3181,8 @@ extern "C" size_t l2c_gpu_execute_noalloc(l2c_gpu_plan *p, const double *in, dou
                                                       st>>>(
         w, g, 2 * (long long)blocks_before(l), 2 * (long long)blocks_before(l + 1), np);
   }
-  k_far<<<blocks_for(2 * (long long)p->Nb * M, 256), 256, 0, st>>>(p->A[dir], w, c, g,
-                                                                   (long long)p->Nb);
+  k_far<<<blocks_for((long long)p->Nb * M, 256), 256, 0, st>>>(p->A[dir], w, c, g,
+                                                               (long long)p->Nb);
   for (long long l = 0; l + 1 < (long long)p->L; l++) {
     const long long np = (long long)slots_at((size_t)l);
     (p->nodal ? k_tree_down<true> : k_tree_down<false>)<<<blocks_for(2 * np, TREE_TILE), 32 * M,
