@@ -2428,11 +2428,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaGetLastError());
     return 1;
   }
-  // The band runs on the second stream beside the far-field chain for batches
-  // and mixed plans (it then overlaps latency-bound tree levels, and in the
-  // mixed form the tensor-core products, which use other pipes: measured 4 %
-  // faster for 4096 x 1024 plain, 5 % for 256 x 16384 mixed; no change for a
-  // single plain vector, whose far field also runs on the FP64 pipe).
+  // The band on the second stream beside the far-field chain (sched_for).
   const Sched sc = sched_for(p, count);
   const bool ov = sc.ov;
   cudaStream_t stn = ov ? st2 : st;
