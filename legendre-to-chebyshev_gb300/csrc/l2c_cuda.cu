@@ -2545,8 +2545,9 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
 extern "C" {
 
 size_t l2c_geometry(size_t N, size_t maxs, size_t *s_out, size_t *Nn_out) {
-  const int L = (int)std::ceil(std::log2((double)N / (double)maxs)) - 2;
-  if (L < 1 || maxs == 0) {
+  // N = 0 or maxs = 0: no levels (and no log of zero or division by it)
+  const int L = (N == 0 || maxs == 0) ? 0 : (int)std::ceil(std::log2((double)N / (double)maxs)) - 2;
+  if (L < 1) {
     if (s_out) *s_out = 0;
     if (Nn_out) *Nn_out = N;
     return 0;

@@ -152,6 +152,13 @@ def test_tree_helpers(lib):
     assert (ij[0], ij[1]) == (2 * 3 * 64 * 8, 2 * 3 * 64 * 8 + 2 * 64 * 8)
 
 
+def test_geometry_degenerate(lib):
+    # no levels, and no arithmetic on log(0) or a division by zero
+    assert lib.geometry(0, 64) == (0, 0, 0)
+    assert lib.geometry(1000, 0) == (0, 0, 1000)
+    assert lib.geometry(1, 64) == (0, 0, 1)
+
+
 @pytest.mark.parametrize("N", [20, 256, 257, 300, 512, 1000, 1024, 4097, 65536, 1 << 20, 1 << 24])
 @pytest.mark.parametrize("maxs", [32, 36, 50, 64])
 def test_geometry_matches_oracle(lib, orc, N, maxs):

@@ -411,3 +411,22 @@ def test_dlpack_device_arrays(lib, torch_cuda):
     dout = torch.zeros(N, dtype=torch.float64, device="cuda")
     p.execute(Producer(du), Producer(dout), 0)
     assert np.array_equal(dout.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 5, 8])
+def test_tiny_lengths_match_oracle(lib, orc, N):
+    # the direct path at the smallest lengths, both directions, strides 1 and 2
+    u = make_input(2 * N, "uniform", 40 + N)
+    p = lib.Plan(N, 64)
+    o = orc.Oracle(N, 64, 2)
+    for d in (0, 1):
+        for st in (1, 2):
+            out = np.zeros(2 * N)
+            want = np.zeros(2 * N)
+            assert p.execute(u, out, d, st) == o.execute(u, want, d, st)
+            assert relerr(out, want) <= TOL
+
+
+def test_empty_length_is_refused(lib):
+    with pytest.raises(lib.L2CError, match="positive"):
+        lib.Plan(0, 64)
