@@ -75,6 +75,56 @@ def near_flops(N, s, direction):
     return f + 2 * N
 
 
+def hbm_peak_gbs():
+    """Measured copy bandwidth (MEASURED_PEAKS.json), else the 6.8 TB/s fallback."""
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            v = json.load(f).get("hbm_gbs")
+        if v:
+            return float(v), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, ValueError):
+        pass
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def phase_roofline(wl, L, s, Nb, phases, fp64_tf, hbm_gbs, lagrange):
+    """Per FMM step of one bench step (both calls): the reference's flop count
+    and the algorithmic DRAM bytes of that step, over its CUDA-event time, as
+    fractions of the measured FP64 DGEMM rate and HBM copy bandwidth."""
+    N, count, M = wl.N, wl.count, 18
+    MM, K = M * M, 2 * ((2 << (L - 1)) - 1)
+    slots = 2 * Nb
+    calls = len(wl.calls)
+    c2l_calls = sum(1 for d, _, _ in wl.calls if d == 1)
+    tr = 4 if lagrange else 1
+    up = sum(((2 << l) - 2) * MM * tr for l in range(1, L))
+    down = sum(((2 << (l + 1)) - 2) * MM * tr for l in range(0, L - 1))
+    col = 2 * slots * M * 8  # one pass over a vector's tree (both parities)
+    work = {  # name: (flops, bytes) per bench step
+        "gather": (c2l_calls * count * N, c2l_calls * count * 16 * N),
+        "near": (sum(near_flops(N, s, d) for d, _, _ in wl.calls) * count,
+                 calls * count * 24 * N),
+        "leaf_up": (calls * count * 2 * 2 * K * s * M, calls * count * (8 * N + 2 * K * M * 8)),
+        "tree_up": (calls * count * 2 * up, calls * count * 2 * col),
+        "far": (calls * count * 2 * 3 * Nb * 2 * MM,
+                calls * (3 * Nb * MM * 8 + count * 2 * col)),
+        "tree_down": (calls * count * 2 * down, calls * count * 2 * col),
+        "leaf_down": (calls * count * 2 * 2 * K * s * M,
+                      calls * count * (2 * K * M * 8 + 16 * N)),
+    }
+    out = {}
+    for name, (fl, by) in work.items():
+        if name not in phases or phases[name]["ms_per_step"] <= 0:
+            continue
+        t = phases[name]["ms_per_step"] * 1e-3
+        out[name] = {"ms_per_step": round(t * 1e3, 4),
+                     "fp64_tflops": round(fl / t / 1e12, 4),
+                     "frac_fp64": round(fl / t / 1e12 / fp64_tf, 3),
+                     "alg_gbs": round(by / t / 1e9, 1),
+                     "frac_hbm": round(by / t / 1e9 / hbm_gbs, 3)}
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 50 ms."""
 
@@ -557,6 +607,7 @@ def main():
     dbuf["o1"] = torch.zeros_like(dbuf["u"])
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     peak = measured_fp64_peak(torch, dev)
+    hbm_peak = hbm_peak_gbs()
 
     def step(pl=None, st=None):
         pl, st = pl or plan, st or stream
@@ -713,6 +764,12 @@ def main():
         "roofline": roof,
         "phases": phases,
         "ms_per_step_phase_profiled": ms_prof,
+        "phase_roofline": (phase_roofline(wl, L, s, plan.Nb, phases_iso, peak, hbm_peak[0],
+                                          args.lagrange) if not ragged and L >= 1 else None),
+        "phase_roofline_note": ("per FMM step, each timed alone (band on the plan's stream); "
+                                "flops: the reference's count (band: 3 per term, 2 FP64 "
+                                "instructions); bytes: algorithmic DRAM bytes; peaks: FP64 "
+                                "DGEMM measured in this run, HBM " + hbm_peak[1]),
         "fp64_ref_tflops_whole_step": total_flops / (ms_step * 1e-3) / 1e12,
         "wall_s_timed_region": t_wall,
         "plan": ({"L": L, "s": s, "Nb": plan.Nb, "create_fmm_ms": plan_ms} if not ragged
