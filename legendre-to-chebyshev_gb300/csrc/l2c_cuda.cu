@@ -1228,7 +1228,9 @@ __device__ __forceinline__ void oz_tile_loop(long long first, long long step, lo
 }
 
 // Combined integers of a 16 x (NT*8) tile; K past KMAX is split into two exact
-// accumulations whose integers are added.
+// accumulations whose integers are added.  The split falls on a chunk pair
+// (chunks 0-3, then 4..KC-1): fragment words are interleaved in pairs of
+// chunks, each pair one 8-byte load.
 template <int NT, int KC, int QMAX = l2c_oz::SLICES>
 __device__ __forceinline__ void oz_tile_T(const unsigned *Pf, const long long *Ys, int yld, int ks,
                                           long long (&T)[NT][4]) {
@@ -1240,12 +1242,14 @@ __device__ __forceinline__ void oz_tile_T(const unsigned *Pf, const long long *Y
 #pragma unroll
       for (int e = 0; e < 4; e++) T[nt][e] = l2c_oz::combine(acc, nt, e);
   } else {
-    l2c_oz::mma_tile<NT, KC, 0, KC / 2, QMAX>(Pf, Ys, yld, ks, acc);
+    constexpr int CM = 4;
+    static_assert(KC - CM <= l2c_oz::KMAX / 8, "two exact accumulations cover at most 10 chunks");
+    l2c_oz::mma_tile<NT, KC, 0, CM, QMAX>(Pf, Ys, yld, ks, acc);
 #pragma unroll
     for (int nt = 0; nt < NT; nt++)
 #pragma unroll
       for (int e = 0; e < 4; e++) T[nt][e] = l2c_oz::combine(acc, nt, e);
-    l2c_oz::mma_tile<NT, KC, KC / 2, KC, QMAX>(Pf, Ys, yld, ks, acc);
+    l2c_oz::mma_tile<NT, KC, CM, KC, QMAX>(Pf, Ys, yld, ks, acc);
 #pragma unroll
     for (int nt = 0; nt < NT; nt++)
 #pragma unroll
@@ -1756,6 +1760,8 @@ __global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 4 : 1)
             const int r = gq + 8 * (e >> 1), il = 8 * nt + 2 * t4 + (e & 1), i = 16 * ps + il;
             if (r >= nrow || i >= g.s) continue;
             const long long j = (tau0 + r) * g.h + 2 * i + sg;
+            // the last leaf targets run past N when N < Nn - 2h (K h > N)
+            if (j >= g.N) continue;
             const double f =
                 l2c_oz::to_double(l2c_oz::combine1(acc, e), Ec[16 * sg + r] - 52 + Ep[il]);
             ov[j * g.stride] = scale(yv[j] + f, j);
@@ -1767,7 +1773,7 @@ __global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 4 : 1)
   oz_tile_loop<NBUF>((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue,
                      work);
   // outputs past the last leaf target node: band sum only
-  const long long jt = g.K * g.h, ntail = g.N - jt;
+  const long long jt = g.K * g.h, ntail = jt < g.N ? g.N - jt : 0;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < g.count * ntail;
        idx += (long long)gridDim.x * blockDim.x) {
     const long long v = idx / ntail, j = jt + (idx - v * ntail);

@@ -226,6 +226,8 @@ template <int NT, int KC, int C0 = 0, int C1 = KC, int QMAX = SLICES>
 __device__ __forceinline__ void mma_tile(const unsigned *__restrict__ Pf, const long long *Ys,
                                          int yld, int ks, float (&acc)[NDIAG][NT][4]) {
   static_assert(C1 - C0 <= KMAX / 8, "accumulation would not be exact");
+  // chunk pairs (2i, 2i+1) share one aligned 8-byte fragment load
+  static_assert(C0 % 2 == 0, "a chunk range starts on a pair");
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
 #pragma unroll
   for (int d = 0; d < NDIAG; d++)

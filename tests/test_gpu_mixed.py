@@ -16,7 +16,8 @@ TOL = 1e-14
 
 
 @pytest.mark.parametrize("N,maxs", [(512, 64), (4096, 16), (4096, 32), (5000, 50), (65536, 16),
-                                    (1 << 20, 32), (1 << 20, 64), (300, 18)])
+                                    (1 << 20, 32), (1 << 20, 64), (300, 18), (1495, 64),
+                                    (1600, 64), (3000, 64)])
 @pytest.mark.parametrize("dist", ["uniform", "sign"])
 def test_mixed_single_vector(lib, orc, N, maxs, dist):
     u = make_input(N, dist, N + maxs)
@@ -29,7 +30,7 @@ def test_mixed_single_vector(lib, orc, N, maxs, dist):
 
 
 @pytest.mark.parametrize("N,maxs,count", [(1024, 64, 16), (1024, 16, 64), (16384, 16, 8),
-                                          (2000, 50, 5)])
+                                          (2000, 50, 5), (1495, 64, 12), (1600, 64, 6)])
 def test_mixed_batch(lib, orc, N, maxs, count):
     x = make_input(N * count, "gauss", 3).reshape(count, N) / (np.arange(N) + 1.0)
     x = np.ascontiguousarray(x)
@@ -40,6 +41,29 @@ def test_mixed_batch(lib, orc, N, maxs, count):
         p.execute_batched(x, out, d, count, N, 1)
         for i in (0, count // 2, count - 1):
             assert relerr(out[i], o(x[i], d)[:N]) <= TOL, (i, d)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+@pytest.mark.parametrize("N,maxs,count", [(6902, 16, 4), (7000, 16, 1), (2100, 16, 3),
+                                          (6902, 32, 2)])
+def test_batch_gaps_untouched(lib, orc, mixed, N, maxs, count):
+    """Vectors dist > N apart: the gaps between them keep their contents.  With
+    N < Nn - 2h the last leaf targets cover outputs past N (K h > N); nothing
+    may be read or written there (N = 6902, s = 14: K h = 7112).  The outputs
+    themselves start at zero: like the reference's execute, the transform adds
+    to the output array."""
+    dist = N + 300
+    x = np.full((count, dist), np.nan)
+    x[:, :N] = make_input(count * N, "gauss", 11).reshape(count, N)
+    p = lib.Plan(N, maxs, mixed=mixed)
+    o = orc.Oracle(N, maxs, 2)
+    for d in (0, 1):
+        out = np.full((count, dist), 12345.0)
+        out[:, :N] = 0.0
+        p.execute_batched(x, out, d, count, dist, 1)
+        assert np.all(out[:, N:] == 12345.0), (N, d)
+        for v in range(count):
+            assert relerr(out[v, :N], o(x[v, :N], d)[:N]) <= TOL, (N, maxs, d, v)
 
 
 def test_mixed_vs_extended_precision(lib):

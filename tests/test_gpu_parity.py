@@ -430,3 +430,47 @@ def test_tiny_lengths_match_oracle(lib, orc, N):
 def test_empty_length_is_refused(lib):
     with pytest.raises(lib.L2CError, match="positive"):
         lib.Plan(0, 64)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_shapes_vs_oracle(lib, orc, seed):
+    """Seeded random lengths, leaf sizes, strides and batch counts, both
+    directions and both discretisations (modal, nodal), against the oracle at
+    the 1e-14 bar."""
+    rng = np.random.default_rng(1000 + seed)
+    N = int(np.exp(rng.uniform(np.log(20), np.log(70000))))
+    maxs = int(rng.choice([18, 32, 36, 50, 64, 100]))
+    stride = int(rng.choice([1, 1, 2, 3]))
+    count = int(rng.choice([1, 2, 5]))
+    lagrange = int(rng.integers(0, 2))
+    dist = N * stride + int(rng.integers(0, 3))
+    x = make_input(count * dist, "uniform", seed)
+    p = lib.Plan(N, maxs, lagrange=lagrange)
+    o = orc.Oracle(N, maxs, 2, lagrange=lagrange)
+    for d in (0, 1):
+        out = np.zeros(count * dist + 1)
+        p.execute_batched(x, out, d, count, dist, stride)
+        for v in range(count):
+            want = np.zeros(dist + 1)
+            o.execute(np.ascontiguousarray(x[v * dist:(v + 1) * dist]), want, d, stride)
+            got = out[v * dist:v * dist + (N - 1) * stride + 1:stride]
+            ref = want[:(N - 1) * stride + 1:stride]
+            assert relerr(got, ref) <= TOL, (N, maxs, stride, count, lagrange, d, v)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_shapes_mixed_vs_oracle(lib, orc, seed):
+    """The mixed form on seeded random shapes (leaf sizes s <= 64, batches of
+    1 to 12 vectors: below and above the tensor-core far-field threshold)."""
+    rng = np.random.default_rng(2000 + seed)
+    N = int(np.exp(rng.uniform(np.log(300), np.log(70000))))
+    maxs = int(rng.choice([16, 24, 32, 64]))
+    count = int(rng.choice([1, 3, 4, 12]))
+    x = np.ascontiguousarray(make_input(count * N, "gauss", seed).reshape(count, N))
+    p = lib.Plan(N, maxs, mixed=True)
+    o = orc.Oracle(N, maxs, 2)
+    for d in (0, 1):
+        out = np.zeros_like(x)
+        p.execute_batched(x, out, d, count, N, 1)
+        for v in range(count):
+            assert relerr(out[v], o(x[v], d)[:N]) <= TOL, (N, maxs, count, d, v)
