@@ -474,3 +474,43 @@ def test_random_shapes_mixed_vs_oracle(lib, orc, seed):
         p.execute_batched(x, out, d, count, N, 1)
         for v in range(count):
             assert relerr(out[v], o(x[v], d)[:N]) <= TOL, (N, maxs, count, d, v)
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_layouts_whole_buffer(lib, orc, seed):
+    """Every form (modal, nodal, mixed) on a seeded random shape and layout
+    (N from 2, so the direct path too; any maxs in [8, 64]; strides 1-3;
+    vectors dist >= (N-1) stride + 1 apart with random padding), compared over
+    the WHOLE buffer with the oracle run on an identical buffer: the outputs
+    at j stride to 1e-14, every other position exactly (untouched, or zeroed
+    where the reference's direct path zeroes [0, N) contiguously).  With
+    L >= 1 the input's gaps hold NaN, so a read there would show."""
+    rng = np.random.default_rng(3000 + seed)
+    form = ("modal", "nodal", "mixed")[seed % 3]
+    N = int(np.exp(rng.uniform(np.log(2), np.log(70000))))
+    maxs = int(rng.integers(8, 65))
+    stride = int(rng.integers(1, 4))
+    count = int(rng.integers(1, 13))
+    dist = (N - 1) * stride + 1 + int(rng.integers(0, 40))
+    lagrange = 1 if form == "nodal" else 0
+    p = lib.Plan(N, maxs, lagrange=lagrange, mixed=form == "mixed")
+    o = orc.Oracle(N, maxs, 2, lagrange=lagrange)
+    pos = np.zeros(count * dist + 7, dtype=bool)  # the transform's own positions
+    for v in range(count):
+        pos[v * dist:v * dist + (N - 1) * stride + 1:stride] = True
+    x = np.full(pos.size, np.nan if p.L >= 1 else 3.0)
+    x[pos] = make_input(int(pos.sum()), "gauss", seed)
+    for d in (0, 1):
+        out0 = np.full(pos.size, 7.0)
+        out0[pos] = 0.0
+        got = out0.copy()
+        p.execute_batched(x, got, d, count, dist, stride)
+        want = out0.copy()
+        for v in range(count):
+            seg = slice(v * dist, v * dist + dist)
+            w = np.ascontiguousarray(want[seg])
+            o.execute(np.ascontiguousarray(x[seg]), w, d, stride)
+            want[seg] = w
+        why = (form, N, maxs, stride, count, dist, d)
+        assert np.array_equal(got[~pos], want[~pos]), why
+        assert relerr(got[pos], want[pos]) <= TOL, why
