@@ -2407,6 +2407,22 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   Geo g = make_geo(p, count, dist, stride);
   const long long total = g.count * g.N;
   if (p->L == 0) {
+    // Vectors whose windows overlap (dist < (N-1) stride + 1, e.g. the columns
+    // of a row-major array): each vector's contiguous zeroing of [0, N) and
+    // contiguous L2C read reach the other vectors' elements, so the vectors run
+    // one after another, as the reference's execute2D calls execute() column
+    // by column (leg2cheb.c:1270-1274).  Within one vector the zeroed elements
+    // and the accumulated ones (i stride >= N) are distinct.
+    if (count > 1 && stride > 1 && dist < (p->N - 1) * stride + 1) {
+      PhaseScope ps(p, L2C_PHASE_DIRECT, count);
+      Geo g1 = g;
+      g1.count = 1;
+      for (size_t v = 0; v < count; v++)
+        k_direct<<<blocks_for(g.N, 256), 256, 0, st>>>(in + v * dist, out + v * dist, p->a,
+                                                       p->an, p->dn, g1, c2l);
+      CK(cudaGetLastError());
+      return 1;
+    }
     PhaseScope ps(p, L2C_PHASE_DIRECT, 1);
     k_direct<<<blocks_for(total, 256), 256, 0, st>>>(in, out, p->a, p->an, p->dn, g, c2l);
     CK(cudaGetLastError());

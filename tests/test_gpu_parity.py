@@ -197,6 +197,27 @@ def test_execute2d_matches_lines(lib, orc, axis):
         assert np.sqrt(np.sum((back - x) ** 2)) < 1e-8  # src/bin/l2c.c:386-388
 
 
+@pytest.mark.parametrize("N0,N1", [(5, 7), (30, 11), (64, 200)])
+def test_execute2d_direct_columns_like_reference(lib, orc, N0, N1):
+    """Columns short enough for the direct path (L = 0): the reference's
+    execute2D calls execute() per column with stride N1 (leg2cheb.c:1270-1274),
+    and each call zeroes [0, N0) and reads its L2C input contiguously from the
+    column's start, reaching the neighbouring columns.  The result is that of
+    the calls in order, every time (graph capture, then replay)."""
+    x = np.ascontiguousarray(make_input(N0 * N1, "gauss", N0).reshape(N0, N1))
+    p2 = lib.Plan2D(N0, N1, 0, maxs=64)
+    o = orc.Oracle(N0, 64, 2)
+    assert o.L == 0
+    for d in (0, 1):
+        xf, wf = x.ravel(), np.zeros(N0 * N1)
+        for j in range(N1):
+            o.execute(xf[j:], wf[j:], d, N1)
+        for _ in range(3):
+            out = np.zeros_like(x)
+            p2(x, out, d)
+            assert relerr(out.ravel(), wf) <= TOL, d
+
+
 def test_directM_directL_match_oracle_near_field(lib, orc):
     # near field + final scaling only (leg2cheb.c:236-376, 378-535)
     for N, st in ((2048, 1), (1000, 3)):
@@ -485,13 +506,7 @@ def test_random_layouts_whole_buffer(lib, orc, seed):
     at j stride to 1e-14, every other position exactly (untouched, or zeroed
     where the reference's direct path zeroes [0, N) contiguously).  With
     L >= 1 the input's gaps hold NaN, so a read there would show."""
-    rng = np.random.default_rng(3000 + seed)
-    form = ("modal", "nodal", "mixed")[seed % 3]
-    N = int(np.exp(rng.uniform(np.log(2), np.log(70000))))
-    maxs = int(rng.integers(8, 65))
-    stride = int(rng.integers(1, 4))
-    count = int(rng.integers(1, 13))
-    dist = (N - 1) * stride + 1 + int(rng.integers(0, 40))
+    form, N, maxs, stride, count, dist = random_layout(seed)
     lagrange = 1 if form == "nodal" else 0
     p = lib.Plan(N, maxs, lagrange=lagrange, mixed=form == "mixed")
     o = orc.Oracle(N, maxs, 2, lagrange=lagrange)
@@ -514,3 +529,112 @@ def test_random_layouts_whole_buffer(lib, orc, seed):
         why = (form, N, maxs, stride, count, dist, d)
         assert np.array_equal(got[~pos], want[~pos]), why
         assert relerr(got[pos], want[pos]) <= TOL, why
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_ragged_vs_oracle(lib, orc, seed):
+    """Seeded random ragged lists (1 to 60 vectors, N log-uniform from 1 to
+    70000, so direct-path vectors too; any maxs in [8, 64]) on nonzero
+    incoming outputs, against the oracle per vector; the slots past the last
+    vector keep their contents."""
+    rng = np.random.default_rng(4000 + seed)
+    count = int(rng.integers(1, 61))
+    Ns = [int(n) for n in np.exp(rng.uniform(0, np.log(70000), count))]
+    maxs = int(rng.integers(8, 65))
+    p = lib.RaggedPlan(Ns, maxs)
+    u = make_input(p.total, "gauss", seed)
+    pre = np.concatenate([make_input(p.total, "uniform", seed + 1), np.full(5, 7.0)])
+    for d in (0, 1):
+        out = pre.copy()
+        p(u, out, d)
+        assert np.array_equal(out[p.total:], pre[p.total:])
+        for v, N in enumerate(Ns):
+            a, b = p.offsets[v], p.offsets[v + 1]
+            w = pre[a:b].copy()
+            orc.Oracle(N, maxs, 2).execute(np.ascontiguousarray(u[a:b]), w, d)
+            assert relerr(out[a:b], w) <= TOL, (seed, v, N, maxs, d)
+
+
+def random_layout(seed):
+    """The shape and layout draw of test_random_layouts_whole_buffer."""
+    rng = np.random.default_rng(3000 + seed)
+    form = ("modal", "nodal", "mixed")[seed % 3]
+    N = int(np.exp(rng.uniform(np.log(2), np.log(70000))))
+    maxs = int(rng.integers(8, 65))
+    stride = int(rng.integers(1, 4))
+    count = int(rng.integers(1, 13))
+    dist = (N - 1) * stride + 1 + int(rng.integers(0, 40))
+    return form, N, maxs, stride, count, dist
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_layouts_every_route_bitwise(lib, torch_cuda, seed):
+    """The shapes and layouts of test_random_layouts_whole_buffer (checked
+    there against the oracle) through every memory route: page-locked host
+    buffers used in place, device arrays in place, and a plan with
+    precompute = 1 (band weights from device memory; not for the mixed form,
+    whose band is the same kernel) give the staged call's bits."""
+    torch = torch_cuda
+    form, N, maxs, stride, count, dist = random_layout(seed)
+    lagrange = 1 if form == "nodal" else 0
+    mixed = form == "mixed"
+    size = count * dist + 7
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(size)
+    pre = rng.uniform(-1, 1, size)  # incoming outputs: the transform adds to them
+    p = lib.Plan(N, maxs, lagrange=lagrange, mixed=mixed)
+    routes = {"pinned": lambda: (torch.from_numpy(x).pin_memory(),
+                                 torch.from_numpy(pre.copy()).pin_memory()),
+              "device": lambda: (torch.from_numpy(x).cuda(), torch.from_numpy(pre.copy()).cuda())}
+    for d in (0, 1):
+        want = pre.copy()
+        p.execute_batched(x, want, d, count, dist, stride)
+        for name, make in routes.items():
+            for rep in range(2):  # capture, then replay
+                xi, oi = make()
+                p.execute_batched(xi, oi, d, count, dist, stride)
+                torch.cuda.synchronize()
+                assert np.array_equal(oi.cpu().numpy(), want), (name, rep, form, N, d)
+        if not mixed and p.L >= 1:
+            q = lib.Plan(N, maxs, lagrange=lagrange, precompute=1)
+            got = pre.copy()
+            q.execute_batched(x, got, d, count, dist, stride)
+            assert np.array_equal(got, want), ("precompute", form, N, d)
+            q.close()
+    p.close()
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_2d_vs_lines(lib, orc, seed):
+    """execute2D on seeded random array shapes (from direct-path sizes up),
+    either axis, modal or nodal, precompute 0 or 1, against the oracle applied
+    as the reference's execute2D applies execute() (leg2cheb.c:1267-1280):
+    rows in place, columns one after another with stride N1.  For columns on
+    the direct path (L = 0) that is not the line-by-line transform: each call
+    zeroes [0, N0) and reads its L2C input contiguously from its column's
+    start, reaching the neighbouring columns (sequential semantics, kept)."""
+    rng = np.random.default_rng(5000 + seed)
+    N0, N1 = (int(v) for v in np.exp(rng.uniform(np.log(2), np.log(700), 2)))
+    axis = int(rng.integers(0, 2))
+    maxs = int(rng.integers(8, 65))
+    lagrange = int(rng.integers(0, 2))
+    precompute = int(rng.integers(0, 2))
+    x = np.ascontiguousarray(make_input(N0 * N1, "gauss", seed).reshape(N0, N1))
+    p2 = lib.Plan2D(N0, N1, axis, maxs=maxs, lagrange=lagrange, precompute=precompute)
+    n = (N0, N1)[axis]
+    o = orc.Oracle(n, maxs, 2, lagrange=lagrange)
+    why = (N0, N1, axis, maxs, lagrange, precompute)
+    for d in (0, 1):
+        out = np.zeros_like(x)
+        p2(x, out, d)
+        if axis == 0:
+            xf, wf = x.ravel(), np.zeros(N0 * N1)
+            for j in range(N1):  # views at column j's start: the reference's pointers
+                o.execute(xf[j:], wf[j:], d, N1)
+            want = wf.reshape(N0, N1)
+        else:
+            want = np.stack([o(np.ascontiguousarray(x[i]), d)[:N1] for i in range(N0)])
+        assert relerr(out, want) <= TOL, why + (d,)
+        if axis == 0 and o.L >= 1:  # FMM columns: the line-by-line transform
+            lines = np.stack([o(np.ascontiguousarray(x[:, j]), d)[:N0] for j in range(N1)], axis=1)
+            assert relerr(out, lines) <= TOL, why + (d,)
