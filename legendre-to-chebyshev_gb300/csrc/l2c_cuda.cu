@@ -1686,10 +1686,12 @@ constexpr size_t oz_far_smem(int NBUF) {
 // vector, both parities; P_sg = T_sg (s x 18) in passes of 16 output rows
 // (two n-tiles, KC = 3).  For tile row r, pass ps and parity sg a lane quad
 // holds the far field of outputs (tau0 + r) h + 32 ps + 2 [0, 16) + sg (lane
-// t: 4t + {0, 2} and 16 + 4t + {0, 2}), so the band sum y is read, the far
-// field added and the scaled sum written straight from registers; the other
-// parity fills the rest of the same sectors.  The outputs past the last leaf
-// target (band only) are scaled by the same CTAs.
+// t: 4t + {0, 2} and 16 + 4t + {0, 2}): every other output.  The warp stages
+// both parities' far field of its 16 rows in shared memory (rows of h + 1
+// doubles), then reads y and writes the scaled sums a whole row at a time, so
+// loads and stores are contiguous -- full sectors also when the output is
+// page-locked host memory written over the host link.  The outputs past the
+// last leaf target (band only) are scaled by the same CTAs.
 constexpr int OZ_LD_WORDS = oz_words(2, 3);
 template <int NBUF>
 __global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 4 : 1)
@@ -1703,8 +1705,10 @@ __global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 4 : 1)
   int *sE = reinterpret_cast<int *>(sP + nw);
   int *Ec = sE + ne + wid * (32 + NBUF * 32);  // Ec[2][16], then [buf][parity][16] exponents
   int *sEx = Ec + 32;
-  long long *Xw = reinterpret_cast<long long *>(sE + ne + MXW * (32 + NBUF * 32)) +
-                  wid * NBUF * 2 * 16 * OZ_CLD;
+  long long *X0 = reinterpret_cast<long long *>(sE + ne + MXW * (32 + NBUF * 32));
+  long long *Xw = X0 + wid * NBUF * 2 * 16 * OZ_CLD;
+  const int sld = (int)g.h + 1;  // staged far field: [16][h + 1] doubles per warp
+  double *S = reinterpret_cast<double *>(X0 + MXW * NBUF * 2 * 16 * OZ_CLD) + wid * 16 * sld;
   oz_load_frag(sP, Pf, nw, sE, Pe, ne);
   __syncthreads();
   pdl_wait();
@@ -1740,8 +1744,6 @@ __global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 4 : 1)
     const long long v = tile / tpv, tau0 = (tile - v * tpv) * 16;
     const long long nrow = min(16LL, g.K - tau0);
     const int *Ex = sEx + buf * 32;
-    const double *yv = y + v * g.N;
-    double *ov = out + v * g.dist;
 #pragma unroll 1
     for (int sg = 0; sg < 2; sg++) {
       long long *X = Xw + (buf * 2 + sg) * 16 * OZ_CLD;
@@ -1759,16 +1761,31 @@ __global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 4 : 1)
           for (int e = 0; e < 4; e++) {
             const int r = gq + 8 * (e >> 1), il = 8 * nt + 2 * t4 + (e & 1), i = 16 * ps + il;
             if (r >= nrow || i >= g.s) continue;
-            const long long j = (tau0 + r) * g.h + 2 * i + sg;
-            // the last leaf targets run past N when N < Nn - 2h (K h > N)
-            if (j >= g.N) continue;
-            const double f =
+            S[r * sld + 2 * i + sg] =
                 l2c_oz::to_double(l2c_oz::combine1(acc, e), Ec[16 * sg + r] - 52 + Ep[il]);
-            ov[j * g.stride] = scale(yv[j] + f, j);
           }
         }
       }
     }
+    __syncwarp();
+    const double *yv = y + v * g.N;
+    double *ov = out + v * g.dist;
+    for (long long q = lane; q < g.h; q += 32) {
+      // the 16 rows' band sums first (one latency), then the sums
+      double yy[16];
+#pragma unroll
+      for (int r = 0; r < 16; r++) {
+        const long long j = (tau0 + r) * g.h + q;
+        // the last leaf targets run past N when N < Nn - 2h (K h > N)
+        yy[r] = (r < nrow && j < g.N) ? yv[j] : 0.0;
+      }
+#pragma unroll
+      for (int r = 0; r < 16; r++) {
+        const long long j = (tau0 + r) * g.h + q;
+        if (r < nrow && j < g.N) ov[j * g.stride] = scale(yy[r] + S[r * sld + q], j);
+      }
+    }
+    __syncwarp();
   };
   oz_tile_loop<NBUF>((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue,
                      work);
@@ -1781,9 +1798,9 @@ __global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 4 : 1)
   }
 }
 
-size_t mz_leaf_down_smem(int npass, int nbuf) {
+size_t mz_leaf_down_smem(int npass, int nbuf, long long h) {
   return (size_t)(2 * npass * OZ_LD_WORDS + 2 * npass * 16 + MXW * (32 + nbuf * 32)) * 4 +
-         (size_t)MXW * nbuf * 2 * 16 * OZ_CLD * 8;
+         (size_t)MXW * nbuf * 2 * 16 * OZ_CLD * 8 + (size_t)MXW * 16 * (h + 1) * 8;
 }
 
 // Column format <-> doubles, in place, one thread per 18-coefficient column
@@ -1867,6 +1884,7 @@ struct l2c_gpu_plan {
   int *oz_lum = nullptr, *oz_tum = nullptr, *oz_tdm = nullptr;  // producer metadata
   int *oz_lde = nullptr;                                        // leaf-down row exponents
   int oz_kc = 0, oz_npass = 0;  // leaf-up k8 chunks, leaf-down passes
+  int oz_ld_ctas = 1;           // resident leaf-down CTAs per SM
   int oz_tree_q = l2c_oz::SLICES;  // digit slices of the transfer matrices that are not zero
   // tile buffers per warp of the mixed-form kernels: 1 (default) leaves room
   // for twice the warps per SM, which hide more of the products' latency than
@@ -2370,11 +2388,11 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_DOWN, 1);
     const long long tiles = g.count * ((g.K + 15) / 16);
-    const int per_sm = p->oz_nbuf == 1 ? 4 : 2;  // resident CTAs (registers, shared memory)
-    const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * per_sm);
+    const unsigned grid =
+        (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152LL * p->oz_ld_ctas);
     // after the join with the band's stream: a plain launch (full dependency)
     launch_k((sc.pdl & 1) && !ov, p->oz_nbuf == 1 ? k_mz_leaf_down<1> : k_mz_leaf_down<2>,
-             grid, 32 * MXW, mz_leaf_down_smem(p->oz_npass, p->oz_nbuf), st,
+             grid, 32 * MXW, mz_leaf_down_smem(p->oz_npass, p->oz_nbuf, g.h), st,
              (const long long *)c, (const int *)p->cE, (const double *)p->y, out,
              (const unsigned *)p->oz_ld, (const int *)p->oz_lde, g, c2l, p->oz_npass);
     if (cudaGetLastError() != cudaSuccess) return false;
@@ -2818,8 +2836,14 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
       PCK(upload(&p->oz_lde, lde));
       // kernels whose shared memory can pass the 48 KB default
       const cudaFuncAttribute smax = cudaFuncAttributeMaxDynamicSharedMemorySize;
-      PCK(cudaFuncSetAttribute(k_mz_leaf_down<1>, smax, (int)mz_leaf_down_smem(4, 1)));
-      PCK(cudaFuncSetAttribute(k_mz_leaf_down<2>, smax, (int)mz_leaf_down_smem(4, 2)));
+      // (the attribute is per kernel, not per plan: the largest leaves, s = 64)
+      PCK(cudaFuncSetAttribute(k_mz_leaf_down<1>, smax, (int)mz_leaf_down_smem(4, 1, 128)));
+      PCK(cudaFuncSetAttribute(k_mz_leaf_down<2>, smax, (int)mz_leaf_down_smem(4, 2, 128)));
+      // resident leaf-down CTAs per SM at this plan's leaf size (registers, shared memory)
+      PCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &p->oz_ld_ctas, p->oz_nbuf == 1 ? k_mz_leaf_down<1> : k_mz_leaf_down<2>, 32 * MXW,
+          mz_leaf_down_smem(p->oz_npass, p->oz_nbuf, (long long)p->h)));
+      p->oz_ld_ctas = std::max(1, p->oz_ld_ctas);
       PCK(cudaFuncSetAttribute(k_mz_tree_up<2, 1>, smax, (int)oz_tree_up_smem(2, 1)));
       PCK(cudaFuncSetAttribute(k_mz_tree_up<2, 2>, smax, (int)oz_tree_up_smem(2, 2)));
       PCK(cudaFuncSetAttribute(k_mz_tree_up<l2c_oz::SLICES, 1>, smax,
@@ -2957,9 +2981,7 @@ size_t l2c_gpu_execute(l2c_gpu_plan *p, const double *in, double *out, size_t di
   // their device mapping: the gather kernel reads the input once over the
   // host link, the band reads and the leaf-down kernel writes the output --
   // no staging copies around the transform (N = 2^20 single vector, L2C + C2L
-  // through host buffers: 1.44e9 -> 1.66e9 coef/s).  Mixed plans stage the
-  // output: their leaf-down writes each lane's outputs at stride 2, which the
-  // host link serves poorly (256 x 16384: 4.1e9 staged, 2.8e9 in place).
+  // through host buffers: 1.44e9 -> 1.66e9 coef/s).
   bool in_host = false, out_host = false;
   if (p->zero_copy && p->L > 0 && !near_only) {
     if (!in_dev)
@@ -2967,7 +2989,7 @@ size_t l2c_gpu_execute(l2c_gpu_plan *p, const double *in, double *out, size_t di
         in = static_cast<const double *>(m);
         in_dev = in_host = true;
       }
-    if (!out_dev && !p->mixed)
+    if (!out_dev)
       if (void *m = mapped_host_ptr(out)) {
         out = static_cast<double *>(m);
         out_dev = out_host = true;
