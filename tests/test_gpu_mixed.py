@@ -126,3 +126,18 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
             got = run()
         for d in (0, 1):
             assert np.array_equal(got[d], want[d]), (env, d)
+
+
+@pytest.mark.parametrize("count", [65, 100])
+def test_mixed_far_column_chunks(lib, orc, count):
+    """Batches past one far-field CTA's 128 columns (2 parities x count): the
+    column chunks along the grid's y, the last one partly filled."""
+    N, maxs = 2000, 16
+    x = np.ascontiguousarray(make_input(N * count, "gauss", count).reshape(count, N))
+    p = lib.Plan(N, maxs, mixed=True)
+    o = orc.Oracle(N, maxs, 2)
+    for d in (0, 1):
+        out = np.zeros_like(x)
+        p.execute_batched(x, out, d, count, N, 1)
+        for v in range(count):
+            assert relerr(out[v], o(x[v], d)[:N]) <= TOL, (count, d, v)
