@@ -94,6 +94,29 @@ int l2c_gpu_profile(l2c_gpu_plan *plan, int enable);
  * Returns L2C_NPHASES. */
 int l2c_gpu_profile_read(l2c_gpu_plan *plan, double *ms, size_t *launches);
 
+/* Autotuner (no reference counterpart: the reference runs one code path on
+ * the CPU).  For one call shape -- direction, count, dist, stride, as passed to
+ * l2c_gpu_execute -- it times this plan's launch choices on synthetic device
+ * data and keeps the fastest for every later call of that shape: the band on a
+ * second stream or not, programmatic dependent launch, the chain's priority,
+ * the band's CTA size, vectors per thread and grid cap, and the mixed form's
+ * tile buffers.  No choice changes results: outputs are the same
+ * bits under every setting.  Blocks while it runs (tens of calls of the shape).
+ * Returns the tuned milliseconds per call, 0 on error (l2c_gpu_last_error).
+ * With L2C_AUTOTUNE=1 in the environment at plan creation, each new shape is
+ * tuned on its first call; with L2C_AUTOTUNE_CACHE=path, tuned shapes are
+ * appended to that file and plans of the same device, N, maxs and form read
+ * them back instead of tuning again. */
+double l2c_gpu_autotune(l2c_gpu_plan *plan, size_t direction, size_t count, size_t dist,
+                        size_t stride);
+/* The launch choices a call shape runs with, as text into buf ("overlap=1
+ * pdl=1 ..."); ms (may be NULL) receives the tuned and the default
+ * milliseconds per call when tuned.  Returns 1 if the shape was tuned by this
+ * plan, 2 if its choices came from the cache file, 0 if the plan's own choices
+ * apply, -1 for a null plan. */
+int l2c_gpu_tuned_config(l2c_gpu_plan *plan, size_t direction, size_t count, size_t dist,
+                         size_t stride, char *buf, size_t len, double *ms);
+
 /* Copy plan tables to host memory, for checking plan construction.
  * which: 0 = A[L2C], 1 = A[C2L], 2 = Lambda table a, 3 = an, 4 = dn, 5 = T,
  * 6 = nodal transfer matrices B0 | B1 (2 M^2; nodal plans only).

@@ -1851,6 +1851,32 @@ namespace {
 struct PhaseScope;
 }
 
+// Launch choices of one call shape.  The autotuner searches all but npair;
+// none of those changes results: every setting gives the same bits.
+//   overlap  : the band on a second stream beside the far-field chain (0/1)
+//   pdl      : programmatic dependent launch flags (1 chain, 2 band, 4 the
+//              first chain kernel after the band on the same stream)
+//   prio     : the chain's kernels at the device's greatest priority (0/1)
+//   nthreads : band CTA size while it overlaps (128/256)
+//   nvb      : band vectors per thread while it overlaps (1, 2, 4, 8)
+//   npair    : band kernel forming outputs in pairs (0/1; not searched: the
+//              unpaired kernel splits each sum into even and odd k chains, so
+//              the two round differently)
+//   nctas    : band grid cap while it overlaps (0: none)
+//   nbuf     : tile buffers per warp of the mixed-form kernels (1/2)
+struct TuneCfg {
+  int overlap = -1, pdl = -1, prio = -1, nthreads = 128, nvb = 8, npair = -1, nctas = 0,
+      nbuf = 1;
+};
+
+// A tuned call shape and its choices (dist is 0 for single vectors).
+struct TunedShape {
+  size_t dir, count, dist, stride;
+  TuneCfg cfg;
+  double ms, ms_default;  // per call, tuned and with the plan's defaults
+  bool from_cache;
+};
+
 struct l2c_gpu_plan {
   size_t N = 0, maxs = 0, L = 0, s = 0, Nn = 0, Nb = 0, h = 0, nL = 0, K = 0, slots = 0;
   size_t dirs = 0;
@@ -1902,6 +1928,7 @@ struct l2c_gpu_plan {
     const void *in;
     void *out;
     unsigned mode;
+    unsigned long long sig;  // launch choices the graph was captured with
     cudaGraphExec_t exec;
     size_t launches;
     size_t last_use;
@@ -1924,6 +1951,17 @@ struct l2c_gpu_plan {
   int pdl = -1;
   int chain_prio_mode = -1;
   int prio_greatest = 0;  // cudaDeviceGetStreamPriorityRange's greatest priority
+  // autotuner: the plan's own choices (defaults and environment), the tuned
+  // shapes, a configuration forced while one is timed, and the signature of
+  // the configuration the fields hold (part of every captured graph's key)
+  TuneCfg base;
+  std::vector<TunedShape> tuned;
+  const TuneCfg *forced = nullptr;
+  unsigned long long cfg_sig = 0;
+  bool autotune = false;          // L2C_AUTOTUNE=1: tune each new shape on its first call
+  char tune_cache[1024] = {0};    // L2C_AUTOTUNE_CACHE: file of tuned shapes
+  bool tune_cache_loaded = false;
+  int oz_ld_ctas_nb[3] = {1, 1, 1};  // resident leaf-down CTAs per SM, by tile buffers
   // launch accounting and optional per-phase CUDA-event timing
   size_t launches = 0;
   bool profiling = false;
@@ -2520,13 +2558,58 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   return 1;
 }
 
+// Launch choices -> the plan's fields (and a signature of them).
+unsigned long long cfg_signature(const TuneCfg &c) {
+  unsigned long long v = 0;
+  auto put = [&](long long x, int bits) {
+    v = (v << bits) | ((unsigned long long)(x + 1) & ((1ull << bits) - 1));
+  };
+  put(c.overlap, 2);
+  put(c.pdl, 4);
+  put(c.prio, 2);
+  put(c.nthreads / 128, 2);
+  put(c.nvb, 4);
+  put(c.npair, 2);
+  put(c.nbuf, 2);
+  put(c.nctas, 24);
+  return v;
+}
+
+void cfg_apply(l2c_gpu_plan *p, const TuneCfg &c) {
+  p->overlap = c.overlap;
+  p->pdl = c.pdl;
+  p->chain_prio_mode = c.prio;
+  p->near_threads = c.nthreads;
+  p->near_vb = c.nvb;
+  p->near_pair = c.npair;
+  p->near_ctas = (unsigned)c.nctas;
+  p->oz_nbuf = c.nbuf;
+  p->oz_ld_ctas = p->oz_ld_ctas_nb[c.nbuf == 2 ? 2 : 1];
+  p->cfg_sig = cfg_signature(c);
+}
+
+size_t shape_dist(size_t count, size_t dist) { return count > 1 ? dist : 0; }
+
+const TunedShape *tuned_for(const l2c_gpu_plan *p, size_t dir, size_t count, size_t dist,
+                            size_t stride) {
+  const size_t d = shape_dist(count, dist);
+  for (auto it = p->tuned.rbegin(); it != p->tuned.rend(); ++it)
+    if (it->dir == dir && it->count == count && it->dist == d && it->stride == stride) return &*it;
+  return nullptr;
+}
+
 // Device-pointer execution of one batch: replay a captured graph of the launch
 // sequence when one exists for this call shape, else capture one (or launch
-// directly while per-phase profiling is on).
+// directly while per-phase profiling is on).  The launch choices are the
+// tuned ones of the shape when it has been tuned, else the plan's own.
 size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, size_t count,
                   size_t dist, size_t stride, bool near_only, bool input_ready,
                   bool in_host = false) {
   if (count == 0 || p->N == 0) return 1;
+  {
+    const TunedShape *ts = p->forced ? nullptr : tuned_for(p, dir, count, dist, stride);
+    cfg_apply(p, p->forced ? *p->forced : ts ? ts->cfg : p->base);
+  }
   if (!ensure_scratch(p, count)) return 0;
   if (p->mixed && p->L > 0 && count >= 4 && !ensure_mixed_far(p, dir)) return 0;
   const unsigned mode = (near_only ? 1u : 0u) | (input_ready ? 2u : 0u) | (in_host ? 4u : 0u);
@@ -2536,7 +2619,7 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   p->use_clock++;
   for (auto &e : p->graphs) {
     if (e.dir == dir && e.count == count && e.dist == dist && e.stride == stride && e.in == in &&
-        e.out == out && e.mode == mode) {
+        e.out == out && e.mode == mode && e.sig == p->cfg_sig) {
       e.last_use = p->use_clock;
       CK(cudaGraphLaunch(e.exec, p->stream));
       p->launches += e.launches;
@@ -2564,7 +2647,7 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     set_err("cudaGraphInstantiate failed: %s", cudaGetErrorString(ei));
     return 0;
   }
-  l2c_gpu_plan::GraphEntry e{dir, count, dist, stride, in, out, mode, exec,
+  l2c_gpu_plan::GraphEntry e{dir,  count, dist, stride, in, out, mode, p->cfg_sig, exec,
                              p->launches - before, p->use_clock};
   if (p->graphs.size() >= 8) {
     auto oldest = std::min_element(p->graphs.begin(), p->graphs.end(),
@@ -2578,6 +2661,258 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   p->graphs.push_back(e);
   CK(cudaGraphLaunch(exec, p->stream));
   return 1;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner.  For one call shape (direction, count, dist, stride) it times the
+// launch choices of TuneCfg -- none of which changes results -- on synthetic
+// device data and keeps the fastest: coordinate descent from the plan's own
+// choices, one choice at a time over its values, a change kept when it saves
+// at least 1 %, until a pass keeps none (two passes at most).  Each timing is
+// the captured graph of the call (captured and replayed twice first), the best
+// of three runs of three calls, by CUDA events on the plan's stream (which the
+// band's stream joins).  Tuned shapes are kept in the plan and, with
+// L2C_AUTOTUNE_CACHE=path, appended to that file and read back by later plans
+// of the same device, N, maxs and form.
+// ---------------------------------------------------------------------------
+
+// Uniform [-1, 1) from a counter (splitmix64's output function).
+__global__ void k_tune_fill(double *v, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned long long z = (unsigned long long)i * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  v[i] = (double)(z >> 11) * 0x1.0p-52 - 1.0;
+}
+
+// ms per call under c (< 0 on error).
+double tune_time(l2c_gpu_plan *p, const double *in, double *out, size_t dir, size_t count,
+                 size_t dist, size_t stride, const TuneCfg &c, cudaEvent_t e0, cudaEvent_t e1) {
+  p->forced = &c;
+  double best = -1.0;
+  bool ok = true;
+  for (int i = 0; i < 2 && ok; i++)
+    ok = run_device(p, in, out, dir, count, dist, stride, false, false) != 0;
+  for (int rep = 0; rep < 3 && ok; rep++) {
+    ok = cudaEventRecord(e0, p->stream) == cudaSuccess;
+    for (int i = 0; i < 3 && ok; i++)
+      ok = run_device(p, in, out, dir, count, dist, stride, false, false) != 0;
+    float ms = 0.f;
+    ok = ok && cudaEventRecord(e1, p->stream) == cudaSuccess &&
+         cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+    if (ok && (best < 0.0 || ms / 3.0 < best)) best = ms / 3.0;
+  }
+  p->forced = nullptr;
+  return ok ? best : -1.0;
+}
+
+// The plan's own choices for a shape, with the "by shape" ones resolved as
+// sched_for and near_pair resolve them.
+TuneCfg resolved_cfg(l2c_gpu_plan *p, size_t count) {
+  cfg_apply(p, p->base);
+  const Sched sc = sched_for(p, count);
+  TuneCfg c = p->base;
+  c.overlap = sc.ov ? 1 : 0;
+  c.pdl = (int)sc.pdl;
+  c.prio = p->chain_prio_mode >= 0 ? p->chain_prio_mode : ((p->mixed || count == 1) ? 1 : 0);
+  return c;
+}
+
+void cfg_text(const TuneCfg &c, char *buf, size_t len) {
+  snprintf(buf, len, "overlap=%d pdl=%d prio=%d near_threads=%d near_vb=%d near_pair=%d "
+           "near_ctas=%d nbuf=%d", c.overlap, c.pdl, c.prio, c.nthreads, c.nvb, c.npair,
+           c.nctas, c.nbuf);
+}
+
+// Cache file: one line per tuned shape, fields separated by '|':
+// l2c-tune-1|device|SMs|N|maxs|form|precompute|dir|count|dist|stride|
+//   overlap|pdl|prio|nthreads|nvb|npair|nctas|nbuf|ms|ms_default
+// (form 0 modal, 1 nodal, 2 mixed).  Later lines win.
+constexpr int TUNE_FIELDS = 21;
+
+struct TuneKey {
+  char dev[256];
+  int sms;
+  int form, pre;
+};
+
+TuneKey tune_key(const l2c_gpu_plan *p) {
+  TuneKey k{};
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, p->device) == cudaSuccess) {
+    snprintf(k.dev, sizeof(k.dev), "%s", prop.name);
+    k.sms = prop.multiProcessorCount;
+  } else {
+    cudaGetLastError();
+    snprintf(k.dev, sizeof(k.dev), "unknown");
+  }
+  for (char *c = k.dev; *c; c++)
+    if (*c == '|' || *c == '\n') *c = ' ';
+  k.form = p->mixed ? 2 : p->nodal ? 1 : 0;
+  k.pre = (p->Wnear[0] || p->Wnear[1]) ? 1 : 0;
+  return k;
+}
+
+void cache_append(const l2c_gpu_plan *p, const TunedShape &t) {
+  if (!p->tune_cache[0]) return;
+  const TuneKey k = tune_key(p);
+  FILE *f = std::fopen(p->tune_cache, "a");
+  if (!f) return;  // an unwritable cache leaves the tuning in the plan only
+  const TuneCfg &c = t.cfg;
+  std::fprintf(f, "l2c-tune-1|%s|%d|%zu|%zu|%d|%d|%zu|%zu|%zu|%zu|%d|%d|%d|%d|%d|%d|%d|%d|%.6f|%.6f\n",
+               k.dev, k.sms, p->N, p->maxs, k.form, k.pre, t.dir, t.count, t.dist, t.stride,
+               c.overlap, c.pdl, c.prio, c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, t.ms,
+               t.ms_default);
+  std::fclose(f);
+}
+
+// Entries of the cache file for this plan (device, N, maxs, form, precompute);
+// malformed or foreign lines are skipped.
+void cache_load(l2c_gpu_plan *p) {
+  if (!p->tune_cache[0]) return;
+  FILE *f = std::fopen(p->tune_cache, "r");
+  if (!f) return;
+  const TuneKey k = tune_key(p);
+  char line[2048];
+  while (std::fgets(line, sizeof(line), f)) {
+    char *fld[TUNE_FIELDS];
+    int n = 0;
+    char *q = line;
+    fld[n++] = q;
+    for (; *q && n < TUNE_FIELDS; q++)
+      if (*q == '|') {
+        *q = 0;
+        fld[n++] = q + 1;
+      }
+    if (n != TUNE_FIELDS || std::strcmp(fld[0], "l2c-tune-1") != 0) continue;
+    if (std::strcmp(fld[1], k.dev) != 0 || std::atoi(fld[2]) != k.sms) continue;
+    auto u = [&](int i) { return (size_t)std::strtoull(fld[i], nullptr, 10); };
+    auto iv = [&](int i) { return (int)std::strtol(fld[i], nullptr, 10); };
+    if (u(3) != p->N || u(4) != p->maxs || iv(5) != k.form || iv(6) != k.pre) continue;
+    TunedShape t{};
+    t.dir = u(7);
+    t.count = u(8);
+    t.dist = u(9);
+    t.stride = u(10);
+    t.cfg.overlap = iv(11);
+    t.cfg.pdl = iv(12);
+    t.cfg.prio = iv(13);
+    t.cfg.nthreads = iv(14);
+    t.cfg.nvb = iv(15);
+    t.cfg.npair = iv(16);
+    t.cfg.nctas = iv(17);
+    t.cfg.nbuf = iv(18);
+    t.ms = std::strtod(fld[19], nullptr);
+    t.ms_default = std::strtod(fld[20], nullptr);
+    t.from_cache = true;
+    // only values the launches accept
+    const TuneCfg &c = t.cfg;
+    if (t.dir > 1 || t.count == 0 || t.stride == 0 || c.overlap < 0 || c.overlap > 1 ||
+        c.pdl < 0 || c.pdl > 7 || c.prio < 0 || c.prio > 1 ||
+        (c.nthreads != 128 && c.nthreads != 256) || c.nvb < 1 || c.nvb > 8 || c.npair < -1 ||
+        c.npair > 1 || c.nctas < 0 || c.nbuf < 1 || c.nbuf > 2)
+      continue;
+    p->tuned.push_back(t);
+  }
+  std::fclose(f);
+}
+
+void ensure_tune_cache(l2c_gpu_plan *p) {
+  if (p->tune_cache_loaded) return;
+  p->tune_cache_loaded = true;
+  cache_load(p);
+}
+
+// Tunes one call shape; returns the tuned ms per call (0 on error).
+double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t stride) {
+  if (stride == 0) stride = 1;
+  if (count > 1 && dist == 0) {
+    set_err("dist must be positive for count > 1");
+    return 0.0;
+  }
+  const size_t span = (count - 1) * dist + (p->N - 1) * stride + 1;
+  double *din = nullptr, *dout = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double result = 0.0;
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
+  if (cudaMalloc(&din, span * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&dout, span * sizeof(double)) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    set_err("autotuner: device allocation failed");
+  } else {
+    k_tune_fill<<<blocks_for((long long)span, 256), 256, 0, p->stream>>>(din, (long long)span);
+    cudaMemsetAsync(dout, 0, span * sizeof(double), p->stream);
+    TuneCfg cur = resolved_cfg(p, count);
+    const double t_default = tune_time(p, din, dout, dir, count, dist, stride, cur, e0, e1);
+    double best = t_default;
+    if (best > 0.0 && p->L > 0) {
+      struct Knob {
+        int TuneCfg::*f;
+        std::vector<int> vals;
+      };
+      std::vector<Knob> knobs = {{&TuneCfg::overlap, {0, 1}},
+                                 {&TuneCfg::pdl, {0, 1, 7}},
+                                 {&TuneCfg::prio, {0, 1}},
+                                 {&TuneCfg::nthreads, {128, 256}},
+                                 {&TuneCfg::nctas, {0, 3 * sms, 6 * sms}}};
+      if (count > 1) knobs.push_back({&TuneCfg::nvb, {1, 2, 4, 8}});
+      if (p->mixed) knobs.push_back({&TuneCfg::nbuf, {1, 2}});
+      for (int pass = 0; pass < 2 && best > 0.0; pass++) {
+        bool kept = false;
+        for (const Knob &kb : knobs)
+          for (int v : kb.vals) {
+            if (cur.*(kb.f) == v) continue;
+            TuneCfg c = cur;
+            c.*(kb.f) = v;
+            const double t = tune_time(p, din, dout, dir, count, dist, stride, c, e0, e1);
+            if (t < 0.0) {
+              best = -1.0;
+              break;
+            }
+            if (t < 0.99 * best) {
+              best = t;
+              cur = c;
+              kept = true;
+            }
+          }
+        if (!kept) break;
+      }
+    }
+    if (best > 0.0) {
+      TunedShape t{dir, count, shape_dist(count, dist), stride, cur, best, t_default, false};
+      p->tuned.erase(std::remove_if(p->tuned.begin(), p->tuned.end(),
+                                    [&](const TunedShape &o) {
+                                      return o.dir == t.dir && o.count == t.count &&
+                                             o.dist == t.dist && o.stride == t.stride;
+                                    }),
+                     p->tuned.end());
+      p->tuned.push_back(t);
+      cache_append(p, t);
+      result = best;
+    } else if (!g_err[0]) {
+      set_err("autotuner: a timed call failed");
+    }
+  }
+  // graphs captured on the tuning buffers go with them
+  cudaStreamSynchronize(p->stream);
+  cudaStreamSynchronize(p->stream2);
+  for (auto it = p->graphs.begin(); it != p->graphs.end();) {
+    if (it->in == din || it->out == dout) {
+      cudaGraphExecDestroy(it->exec);
+      it = p->graphs.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (din) cudaFree(din);
+  if (dout) cudaFree(dout);
+  return result;
 }
 
 }  // namespace
@@ -2644,6 +2979,11 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_CHAIN_PRIO")) p->chain_prio_mode = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_MZ_NBUF")) p->oz_nbuf = env[0] == '1' ? 1 : 2;
   if (const char *env = std::getenv("L2C_ZERO_COPY")) p->zero_copy = env[0] != '0';
+  if (const char *env = std::getenv("L2C_AUTOTUNE")) p->autotune = env[0] == '1';
+  if (const char *env = std::getenv("L2C_AUTOTUNE_CACHE"))
+    snprintf(p->tune_cache, sizeof(p->tune_cache), "%s", env);
+  p->base = TuneCfg{p->overlap,    p->pdl,       p->chain_prio_mode, p->near_threads,
+                    p->near_vb,    p->near_pair, (int)p->near_ctas,  p->oz_nbuf};
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
     p->Nn = N;
@@ -2839,11 +3179,16 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
       // (the attribute is per kernel, not per plan: the largest leaves, s = 64)
       PCK(cudaFuncSetAttribute(k_mz_leaf_down<1>, smax, (int)mz_leaf_down_smem(4, 1, 128)));
       PCK(cudaFuncSetAttribute(k_mz_leaf_down<2>, smax, (int)mz_leaf_down_smem(4, 2, 128)));
-      // resident leaf-down CTAs per SM at this plan's leaf size (registers, shared memory)
+      // resident leaf-down CTAs per SM at this plan's leaf size (registers, shared
+      // memory), for either tile-buffer depth
       PCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &p->oz_ld_ctas, p->oz_nbuf == 1 ? k_mz_leaf_down<1> : k_mz_leaf_down<2>, 32 * MXW,
-          mz_leaf_down_smem(p->oz_npass, p->oz_nbuf, (long long)p->h)));
-      p->oz_ld_ctas = std::max(1, p->oz_ld_ctas);
+          &p->oz_ld_ctas_nb[1], k_mz_leaf_down<1>, 32 * MXW,
+          mz_leaf_down_smem(p->oz_npass, 1, (long long)p->h)));
+      PCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &p->oz_ld_ctas_nb[2], k_mz_leaf_down<2>, 32 * MXW,
+          mz_leaf_down_smem(p->oz_npass, 2, (long long)p->h)));
+      for (int b = 1; b <= 2; b++) p->oz_ld_ctas_nb[b] = std::max(1, p->oz_ld_ctas_nb[b]);
+      p->oz_ld_ctas = p->oz_ld_ctas_nb[p->oz_nbuf == 2 ? 2 : 1];
       PCK(cudaFuncSetAttribute(k_mz_tree_up<2, 1>, smax, (int)oz_tree_up_smem(2, 1)));
       PCK(cudaFuncSetAttribute(k_mz_tree_up<2, 2>, smax, (int)oz_tree_up_smem(2, 2)));
       PCK(cudaFuncSetAttribute(k_mz_tree_up<l2c_oz::SLICES, 1>, smax,
@@ -2969,6 +3314,11 @@ size_t l2c_gpu_execute(l2c_gpu_plan *p, const double *in, double *out, size_t di
   }
   std::lock_guard<std::mutex> lock(p->mu);
   DeviceGuard dg(p->device);
+  // tuned launch choices: from the cache file, or tuned now (L2C_AUTOTUNE=1)
+  ensure_tune_cache(p);
+  if (p->autotune && p->L > 0 && !near_only && !p->profiling &&
+      !tuned_for(p, dir, count, dist, stride) && tune_shape(p, dir, count, dist, stride) <= 0.0)
+    return 0;
   const size_t N = p->N;
   // span of caller memory the call touches (the direct path also zeroes [0, N))
   size_t span = (count - 1) * dist + (N - 1) * stride + 1;
@@ -3023,6 +3373,41 @@ size_t l2c_gpu_execute(l2c_gpu_plan *p, const double *in, double *out, size_t di
 }
 
 size_t l2c_gpu_launch_count(const l2c_gpu_plan *p) { return p ? p->launches : 0; }
+
+double l2c_gpu_autotune(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t stride) {
+  g_err[0] = 0;
+  if (!p) {
+    set_err("null plan");
+    return 0.0;
+  }
+  if (dir > 1 || !(p->dirs == dir || p->dirs == 2)) {
+    set_err("direction %zu was not planned", dir);
+    return 0.0;
+  }
+  if (count == 0) {
+    set_err("count must be positive");
+    return 0.0;
+  }
+  std::lock_guard<std::mutex> lock(p->mu);
+  DeviceGuard dg(p->device);
+  ensure_tune_cache(p);
+  return tune_shape(p, dir, count, dist, stride == 0 ? 1 : stride);
+}
+
+int l2c_gpu_tuned_config(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t stride,
+                         char *buf, size_t len, double *ms) {
+  if (!p) return -1;
+  std::lock_guard<std::mutex> lock(p->mu);
+  ensure_tune_cache(p);
+  const TunedShape *t = tuned_for(p, dir, count, dist, stride == 0 ? 1 : stride);
+  const TuneCfg c = t ? t->cfg : resolved_cfg(p, count);
+  if (buf && len) cfg_text(c, buf, len);
+  if (ms) {
+    ms[0] = t ? t->ms : 0.0;
+    ms[1] = t ? t->ms_default : 0.0;
+  }
+  return t ? (t->from_cache ? 2 : 1) : 0;
+}
 
 int l2c_gpu_profile(l2c_gpu_plan *p, int enable) {
   if (!p) return 1;

@@ -113,6 +113,11 @@ def load():
     cuda.l2c_gpu_ragged_launch_count.argtypes = [vp]
     cuda.l2c_gpu_last_error.restype = ctypes.c_char_p
     cuda.l2c_gpu_version.restype = ctypes.c_char_p
+    cuda.l2c_gpu_autotune.restype = ctypes.c_double
+    cuda.l2c_gpu_autotune.argtypes = [vp, sz, sz, sz, sz]
+    cuda.l2c_gpu_tuned_config.restype = ctypes.c_int
+    cuda.l2c_gpu_tuned_config.argtypes = [vp, sz, sz, sz, sz, ctypes.c_char_p, sz,
+                                          ctypes.POINTER(ctypes.c_double)]
     _lib, _cuda = lib, cuda
     return lib
 
@@ -206,6 +211,24 @@ class Plan:
     def synchronize(self):
         if _cuda.l2c_gpu_synchronize(self._gpu) != 0:
             raise L2CError(_cuda.l2c_gpu_last_error().decode())
+
+    def autotune(self, direction, count=1, dist=0, stride=1):
+        """Tune the launch choices of one call shape (l2c_gpu_autotune); returns
+        the tuned milliseconds per call.  Results are the same bits either way."""
+        ms = _cuda.l2c_gpu_autotune(self._gpu, direction, count, dist, stride)
+        if ms <= 0.0:
+            raise L2CError("l2c_gpu_autotune failed: " + _cuda.l2c_gpu_last_error().decode())
+        return float(ms)
+
+    def tuned_config(self, direction, count=1, dist=0, stride=1):
+        """(source, text, ms_tuned, ms_default) of a call shape's launch choices:
+        source "tuned", "cache" or "default" (l2c_gpu_tuned_config)."""
+        buf = ctypes.create_string_buffer(256)
+        ms = (ctypes.c_double * 2)()
+        r = _cuda.l2c_gpu_tuned_config(self._gpu, direction, count, dist, stride, buf, 256, ms)
+        if r < 0:
+            raise L2CError("l2c_gpu_tuned_config failed")
+        return ({1: "tuned", 2: "cache"}.get(r, "default"), buf.value.decode(), ms[0], ms[1])
 
     def directM(self, inp, out, stride=1):
         f = _lib.directM(_ptr(inp), _ptr(out), self._p, stride)

@@ -98,9 +98,10 @@ def test_mixed_rejects_large_leaves(lib):
 @pytest.mark.parametrize("count", [1, 16])
 def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
     """Programmatic dependent launch, the band on the second stream, graph
-    replay, the tile buffer depth and the chain's scheduling priority change
-    only when work runs, never what it computes: every combination gives the
-    same bits as the default plan."""
+    replay, the tile buffer depth, the chain's scheduling priority and the
+    band's CTA size, vectors per thread and grid cap change only
+    when work runs, never what it computes: every setting gives the same bits
+    as the default plan."""
     N = 16384
     x = np.ascontiguousarray(make_input(N * count, "gauss", 11).reshape(count, N))
 
@@ -119,7 +120,11 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
     want = run()
     for env in ({"L2C_PDL": "0"}, {"L2C_PDL": "7"}, {"L2C_PDL": "7", "L2C_OVERLAP": "0"},
                 {"L2C_PDL": "7", "L2C_OVERLAP": "1"}, {"L2C_PDL": "7", "L2C_NO_GRAPHS": "1"},
-                {"L2C_MZ_NBUF": "2"}, {"L2C_CHAIN_PRIO": "0"}, {"L2C_CHAIN_PRIO": "1"}):
+                {"L2C_MZ_NBUF": "2"}, {"L2C_CHAIN_PRIO": "0"}, {"L2C_CHAIN_PRIO": "1"},
+                # the band's launch choices (the autotuner searches these too)
+                {"L2C_NEAR_VB": "1"}, {"L2C_NEAR_VB": "2"}, {"L2C_NEAR_VB": "4"},
+                {"L2C_NEAR_THREADS": "256"}, {"L2C_NEAR_CTAS": "456"},
+                {"L2C_NEAR_THREADS": "256", "L2C_NEAR_VB": "2", "L2C_NEAR_CTAS": "912"}):
         with monkeypatch.context() as m:
             for k, v in env.items():
                 m.setenv(k, v)
