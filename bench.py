@@ -395,6 +395,21 @@ def run_reference(args):
     return 0
 
 
+def autotune_plan(plan, calls, count, N):
+    """Tune the plan's launch choices for the call shapes the bench times
+    (l2c_gpu_autotune; results are the same bits under every choice).  Returns
+    the record for the JSON line: per direction the choices, tuned and default
+    ms per call, and the tuning time (plan-time work, outside the timed region)."""
+    t0 = time.perf_counter()
+    shapes = {}
+    for d in sorted({c[0] for c in calls}):
+        plan.autotune(d, count, N, 1)
+        src, text, mt, md = plan.tuned_config(d, count, N, 1)
+        shapes[("L2C", "C2L")[d]] = {"choices": text, "ms_per_call": round(mt, 4),
+                                     "ms_per_call_default": round(md, 4)}
+    return {"seconds": round(time.perf_counter() - t0, 3), "shapes": shapes}
+
+
 def run_mixed(args):
     """Mixed form against plain FP64 on the same inputs: single vector N = 2^22
     (mixed_single) or 256 vectors of N = 16384 (mixed_batch), iid N(0,1), L2C and
@@ -484,10 +499,11 @@ def run_mixed(args):
     for name, maxs, mixed in (("plain_maxs64", 64, False), ("plain_maxs32", 32, False),
                               ("mixed", args.maxs_mixed, True)):
         plan = l2c.Plan(N, maxs, mixed=mixed)
+        tuned = autotune_plan(plan, ((0,), (1,)), count, N) if args.autotune else None
         ms, outs, launches, phases = time_plan(plan)
         results[name] = {"maxs": maxs, "s": plan.s, "L": plan.L, "ms_per_step": ms,
                          "value": 2 * count * N / (ms * 1e-3), "launches": launches,
-                         "phases_ms_per_step": phases,
+                         "phases_ms_per_step": phases, "autotune": tuned,
                          "flops": plan.flops(0) + plan.flops(1), "outs": outs}
         if mixed:
             e2e_mixed = time_e2e(plan)
@@ -556,6 +572,9 @@ def main():
     ap.add_argument("--lagrange", type=int, default=0, choices=[0, 1],
                     help="1: the nodal form (create_fmm's lagrange argument; single, batch)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--autotune", type=int, default=1, choices=[0, 1],
+                    help="tune each plan's launch choices for the timed call shapes first "
+                         "(same bits under every choice; tuning time reported, not timed)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -640,6 +659,7 @@ def main():
                                "launches_per_step": pl_n[i] / args.steps}
                     for i in range(8) if pl_n[i]}
 
+    tuned = autotune_plan(plan, wl.calls, count, N) if args.autotune and not ragged else None
     for _ in range(args.warmup):
         step()
     plan.synchronize()
@@ -774,6 +794,7 @@ def main():
         "wall_s_timed_region": t_wall,
         "plan": ({"L": L, "s": s, "Nb": plan.Nb, "create_fmm_ms": plan_ms} if not ragged
                  else {"vectors": count}),
+        "autotune": tuned,
     }
     got = {k: dbuf[k].cpu().numpy() for k in ("o0", "o1")}
     if wl.name == "batch":
