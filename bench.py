@@ -659,7 +659,18 @@ def main():
                                "launches_per_step": pl_n[i] / args.steps}
                     for i in range(8) if pl_n[i]}
 
-    tuned = autotune_plan(plan, wl.calls, count, N) if args.autotune and not ragged else None
+    tuned = None
+    if args.autotune and ragged:
+        t_tune0 = time.perf_counter()
+        shapes = {}
+        for d in sorted({c[0] for c in wl.calls}):
+            plan.autotune(d)
+            src, text, mt, md = plan.tuned_config(d)
+            shapes[("L2C", "C2L")[d]] = {"choices": text, "ms_per_call": round(mt, 4),
+                                         "ms_per_call_default": round(md, 4)}
+        tuned = {"seconds": round(time.perf_counter() - t_tune0, 3), "shapes": shapes}
+    elif args.autotune:
+        tuned = autotune_plan(plan, wl.calls, count, N)
     for _ in range(args.warmup):
         step()
     plan.synchronize()

@@ -161,6 +161,18 @@ size_t l2c_gpu_ragged_total(const l2c_gpu_ragged *plan);            /* sum of N 
 size_t l2c_gpu_ragged_flops(const l2c_gpu_ragged *plan, size_t direction);
 void *l2c_gpu_ragged_stream(l2c_gpu_ragged *plan);
 size_t l2c_gpu_ragged_launch_count(const l2c_gpu_ragged *plan);
+/* Autotuner of a ragged list, per direction: the band (and the direct-method
+ * vectors) on a second stream beside the far-field chain or not, and the
+ * chain's kernels at the device's greatest priority or not, timed on synthetic
+ * data of the list (the same bits under every choice).  Returns the tuned ms
+ * per call, 0 on error.  L2C_AUTOTUNE=1 at creation tunes on each direction's
+ * first call; L2C_OVERLAP / L2C_CHAIN_PRIO set the untuned choices. */
+double l2c_gpu_ragged_autotune(l2c_gpu_ragged *plan, size_t direction);
+/* "overlap=.. prio=.." into buf; ms (may be NULL) gets the tuned and default
+ * ms per call.  Returns 1 if tuned, 0 if the plan's own choices apply, -1 on a
+ * bad argument. */
+int l2c_gpu_ragged_tuned_config(l2c_gpu_ragged *plan, size_t direction, char *buf, size_t len,
+                                double *ms);
 
 /* Lambda(z) and Lambda at integer z, host side, bit-identical to the device. */
 double l2c_lambda(double z);

@@ -3834,6 +3834,16 @@ struct l2c_gpu_ragged {
   size_t flops[2] = {0, 0};
   size_t launches = 0;
   std::mutex mu;
+  // The band (and the direct-method vectors) on stream2 beside the far-field
+  // chain, whose kernels then carry the device's greatest priority; joined
+  // before leaf-down.  overlap / chain_prio: the plan's choices (L2C_OVERLAP,
+  // L2C_CHAIN_PRIO); tuned_*: the autotuner's, per direction (-1: none).
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int overlap = 1, chain_prio = 1, prio_greatest = 0;
+  int tuned_ov[2] = {-1, -1}, tuned_prio[2] = {-1, -1};
+  double tuned_ms[2] = {0, 0}, tuned_ms_default[2] = {0, 0};
+  bool autotune = false;
 };
 
 namespace {
@@ -3841,6 +3851,10 @@ namespace {
 size_t ragged_launch(l2c_gpu_ragged *r, const double *in, double *out, size_t dir) {
   cudaStream_t st = r->stream;
   const int c2l = dir == 1, n = (int)r->count;
+  const bool ov = r->any_fmm && (r->tuned_ov[dir] >= 0 ? r->tuned_ov[dir] : r->overlap) == 1;
+  const bool hi = ov && (r->tuned_prio[dir] >= 0 ? r->tuned_prio[dir] : r->chain_prio) == 1;
+  const LaunchOpt chain(false, hi ? r->prio_greatest : 0);
+  cudaStream_t sb = ov ? r->stream2 : st;  // band and direct vectors
   if (r->any_fmm) {
     const double *x = in;  // L2C reads the caller's packed input directly
     if (c2l) {
@@ -3848,30 +3862,44 @@ size_t ragged_launch(l2c_gpu_ragged *r, const double *in, double *out, size_t di
       x = r->x;
       r->launches++;
     }
-    k_r_near<<<blocks_for(r->tot_coef, 256), 256, 0, st>>>(x, out, r->y, r->V, r->D, r->pre_coef,
+    if (ov) {
+      CK(cudaEventRecord(r->ev_fork, st));
+      CK(cudaStreamWaitEvent(r->stream2, r->ev_fork, 0));
+    }
+    k_r_near<<<blocks_for(r->tot_coef, 256), 256, 0, sb>>>(x, out, r->y, r->V, r->D, r->pre_coef,
                                                            n, c2l);
-    k_r_leaf_up<<<blocks_for(r->tot_leaf, 288), 288, 0, st>>>(x, r->w, r->V, r->D, r->pre_leaf, n);
-    r->launches += 2;
-    for (int d = 1; d < r->Lmax; d++) {
-      if (r->tot_up[d] == 0) continue;
-      k_r_tree_up<<<blocks_for(r->tot_up[d], TREE_TILE), 32 * M, 0, st>>>(r->w, r->V,
-                                                                        r->pre_up[d], n, d);
+    r->launches++;
+    if (ov && r->any_direct) {  // other vectors' outputs: no order with the chain
+      k_r_direct<<<blocks_for(r->tot_coef, 256), 256, 0, sb>>>(in, out, r->V, r->D, r->pre_coef,
+                                                               n, c2l);
       r->launches++;
     }
-    k_r_far<<<blocks_for(r->tot_far, 256), 256, 0, st>>>(r->w, r->c, r->V, r->D, r->pre_far, n,
-                                                         (int)dir);
+    if (ov) CK(cudaEventRecord(r->ev_join, sb));
+    launch_k(chain, k_r_leaf_up, blocks_for(r->tot_leaf, 288), 288, 0, st, x, r->w,
+             (const RVec *)r->V, (const RDonor *)r->D, (const long long *)r->pre_leaf, n);
+    r->launches++;
+    for (int d = 1; d < r->Lmax; d++) {
+      if (r->tot_up[d] == 0) continue;
+      launch_k(chain, k_r_tree_up, blocks_for(r->tot_up[d], TREE_TILE), 32 * M, 0, st, r->w,
+               (const RVec *)r->V, (const long long *)r->pre_up[d], n, d);
+      r->launches++;
+    }
+    launch_k(chain, k_r_far, blocks_for(r->tot_far, 256), 256, 0, st, (const double *)r->w, r->c,
+             (const RVec *)r->V, (const RDonor *)r->D, (const long long *)r->pre_far, n,
+             (int)dir);
     r->launches++;
     for (int l = 0; l + 1 < r->Lmax; l++) {
       if (r->tot_down[l] == 0) continue;
-      k_r_tree_down<<<blocks_for(r->tot_down[l], TREE_TILE), 32 * M, 0, st>>>(r->c, r->V,
-                                                                            r->pre_down[l], n, l);
+      launch_k(chain, k_r_tree_down, blocks_for(r->tot_down[l], TREE_TILE), 32 * M, 0, st, r->c,
+               (const RVec *)r->V, (const long long *)r->pre_down[l], n, l);
       r->launches++;
     }
+    if (ov) CK(cudaStreamWaitEvent(st, r->ev_join, 0));
     k_r_leaf_down<<<blocks_for(r->tot_coef, 256), 256, 0, st>>>(r->c, r->y, out, r->V, r->D,
                                                                 r->pre_coef, n, c2l);
     r->launches++;
   }
-  if (r->any_direct) {
+  if (r->any_direct && !ov) {
     k_r_direct<<<blocks_for(r->tot_coef, 256), 256, 0, st>>>(in, out, r->V, r->D, r->pre_coef, n,
                                                              c2l);
     r->launches++;
@@ -3888,10 +3916,14 @@ void l2c_gpu_ragged_destroy(l2c_gpu_ragged *r) {
   if (!r) return;
   DeviceGuard dg(r->device);
   if (r->stream) cudaStreamSynchronize(r->stream);
+  if (r->stream2) cudaStreamSynchronize(r->stream2);
   for (auto *d : r->donors) l2c_gpu_plan_destroy(d);
   void *bufs[] = {r->V, r->D, r->pre_all, r->x, r->y, r->w, r->c, r->st_in, r->st_out};
   for (void *b : bufs)
     if (b) cudaFree(b);
+  if (r->ev_fork) cudaEventDestroy(r->ev_fork);
+  if (r->ev_join) cudaEventDestroy(r->ev_join);
+  if (r->stream2) cudaStreamDestroy(r->stream2);
   if (r->stream) cudaStreamDestroy(r->stream);
   delete r;
 }
@@ -3923,6 +3955,17 @@ l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *Ns, size_t max
   r->dirs = directions;
   RCK(cudaGetDevice(&r->device));
   RCK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+  RCK(cudaStreamCreateWithFlags(&r->stream2, cudaStreamNonBlocking));
+  RCK(cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming));
+  RCK(cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming));
+  {
+    int least = 0, greatest = 0;
+    RCK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    r->prio_greatest = greatest;
+  }
+  if (const char *env = std::getenv("L2C_OVERLAP")) r->overlap = env[0] == '1' ? 1 : 0;
+  if (const char *env = std::getenv("L2C_CHAIN_PRIO")) r->chain_prio = env[0] == '1' ? 1 : 0;
+  if (const char *env = std::getenv("L2C_AUTOTUNE")) r->autotune = env[0] == '1';
   // geometry of every vector; largest level count per leaf size s
   std::vector<size_t> L(count), S(count);
   std::vector<std::pair<size_t, size_t>> smax;  // (s, Lmax)
@@ -4080,6 +4123,111 @@ void *l2c_gpu_ragged_stream(l2c_gpu_ragged *r) { return r ? (void *)r->stream : 
 
 size_t l2c_gpu_ragged_launch_count(const l2c_gpu_ragged *r) { return r ? r->launches : 0; }
 
+}  // extern "C"
+
+namespace {
+
+// ms per ragged call with the band beside the chain or not (ov) and the chain
+// at the greatest priority or not (pr), on device buffers: a warm-up call,
+// then the best of three runs of two calls (CUDA events on the plan's stream,
+// which stream2 joins).  < 0 on error.
+double ragged_time(l2c_gpu_ragged *r, const double *in, double *out, size_t dir, int ov, int pr,
+                   cudaEvent_t e0, cudaEvent_t e1) {
+  r->tuned_ov[dir] = ov;
+  r->tuned_prio[dir] = pr;
+  bool ok = ragged_launch(r, in, out, dir) != 0;
+  double best = -1.0;
+  for (int rep = 0; rep < 3 && ok; rep++) {
+    ok = cudaEventRecord(e0, r->stream) == cudaSuccess;
+    for (int i = 0; i < 2 && ok; i++) ok = ragged_launch(r, in, out, dir) != 0;
+    float ms = 0.f;
+    ok = ok && cudaEventRecord(e1, r->stream) == cudaSuccess &&
+         cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+    if (ok && (best < 0.0 || ms / 2.0 < best)) best = ms / 2.0;
+  }
+  return ok ? best : -1.0;
+}
+
+// The ragged list's autotuner: per direction, the band beside the chain or
+// not and the chain's priority, timed on synthetic data of the list (the same
+// bits under every choice).  Returns the tuned ms per call, 0 on error.
+double ragged_tune(l2c_gpu_ragged *r, size_t dir) {
+  double *din = nullptr, *dout = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double result = 0.0;
+  const size_t n = r->total;
+  if (cudaMalloc(&din, n * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&dout, n * sizeof(double)) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+      cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    set_err("autotuner: device allocation failed");
+  } else {
+    k_tune_fill<<<blocks_for((long long)n, 256), 256, 0, r->stream>>>(din, (long long)n);
+    cudaMemsetAsync(dout, 0, n * sizeof(double), r->stream);
+    int bo = r->overlap, bp = r->chain_prio;
+    const double t_default = ragged_time(r, din, dout, dir, bo, bp, e0, e1);
+    double best = t_default;
+    const int cand[3][2] = {{0, 0}, {1, 0}, {1, 1}};
+    for (int i = 0; i < 3 && best > 0.0 && r->any_fmm; i++) {
+      if (cand[i][0] == r->overlap && (cand[i][0] == 0 || cand[i][1] == r->chain_prio)) continue;
+      const double t = ragged_time(r, din, dout, dir, cand[i][0], cand[i][1], e0, e1);
+      if (t < 0.0) {
+        best = -1.0;
+      } else if (t < 0.99 * best) {
+        best = t;
+        bo = cand[i][0];
+        bp = cand[i][1];
+      }
+    }
+    r->tuned_ov[dir] = bo;
+    r->tuned_prio[dir] = bp;
+    if (best > 0.0) {
+      r->tuned_ms[dir] = best;
+      r->tuned_ms_default[dir] = t_default;
+      result = best;
+    } else {
+      r->tuned_ov[dir] = r->tuned_prio[dir] = -1;
+      if (!g_err[0]) set_err("autotuner: a timed call failed");
+    }
+  }
+  cudaStreamSynchronize(r->stream);
+  cudaStreamSynchronize(r->stream2);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (din) cudaFree(din);
+  if (dout) cudaFree(dout);
+  return result;
+}
+
+}  // namespace
+
+extern "C" {
+
+double l2c_gpu_ragged_autotune(l2c_gpu_ragged *r, size_t dir) {
+  g_err[0] = 0;
+  if (!r || dir > 1 || !(r->dirs == dir || r->dirs == 2)) {
+    set_err("null plan, or direction not planned");
+    return 0.0;
+  }
+  std::lock_guard<std::mutex> lock(r->mu);
+  DeviceGuard dg(r->device);
+  return ragged_tune(r, dir);
+}
+
+int l2c_gpu_ragged_tuned_config(l2c_gpu_ragged *r, size_t dir, char *buf, size_t len,
+                                double *ms) {
+  if (!r || dir > 1) return -1;
+  std::lock_guard<std::mutex> lock(r->mu);
+  const bool t = r->tuned_ov[dir] >= 0;
+  const int ov = t ? r->tuned_ov[dir] : r->overlap, pr = t ? r->tuned_prio[dir] : r->chain_prio;
+  if (buf && len) snprintf(buf, len, "overlap=%d prio=%d", ov, pr);
+  if (ms) {
+    ms[0] = t ? r->tuned_ms[dir] : 0.0;
+    ms[1] = t ? r->tuned_ms_default[dir] : 0.0;
+  }
+  return t ? 1 : 0;
+}
+
 size_t l2c_gpu_ragged_execute(l2c_gpu_ragged *r, const double *in, double *out, size_t dir,
                               unsigned flags) {
   g_err[0] = 0;
@@ -4093,6 +4241,7 @@ size_t l2c_gpu_ragged_execute(l2c_gpu_ragged *r, const double *in, double *out, 
   }
   std::lock_guard<std::mutex> lock(r->mu);
   DeviceGuard dg(r->device);
+  if (r->autotune && r->any_fmm && r->tuned_ov[dir] < 0 && ragged_tune(r, dir) <= 0.0) return 0;
   const bool in_dev = is_device_ptr(in), out_dev = is_device_ptr(out);
   const size_t n = r->total;
   if (!in_dev) {

@@ -113,6 +113,11 @@ def load():
     cuda.l2c_gpu_ragged_launch_count.argtypes = [vp]
     cuda.l2c_gpu_last_error.restype = ctypes.c_char_p
     cuda.l2c_gpu_version.restype = ctypes.c_char_p
+    cuda.l2c_gpu_ragged_autotune.restype = ctypes.c_double
+    cuda.l2c_gpu_ragged_autotune.argtypes = [vp, sz]
+    cuda.l2c_gpu_ragged_tuned_config.restype = ctypes.c_int
+    cuda.l2c_gpu_ragged_tuned_config.argtypes = [vp, sz, ctypes.c_char_p, sz,
+                                                 ctypes.POINTER(ctypes.c_double)]
     cuda.l2c_gpu_autotune.restype = ctypes.c_double
     cuda.l2c_gpu_autotune.argtypes = [vp, sz, sz, sz, sz]
     cuda.l2c_gpu_tuned_config.restype = ctypes.c_int
@@ -322,6 +327,24 @@ class RaggedPlan:
 
     def launch_count(self):
         return int(_cuda.l2c_gpu_ragged_launch_count(self._gpu))
+
+    def autotune(self, direction):
+        """Tune this list's launch choices for one direction
+        (l2c_gpu_ragged_autotune); returns the tuned ms per call."""
+        ms = _cuda.l2c_gpu_ragged_autotune(self._gpu, direction)
+        if ms <= 0.0:
+            raise L2CError("l2c_gpu_ragged_autotune failed: " +
+                           _cuda.l2c_gpu_last_error().decode())
+        return float(ms)
+
+    def tuned_config(self, direction):
+        """(source, text, ms_tuned, ms_default): source "tuned" or "default"."""
+        buf = ctypes.create_string_buffer(64)
+        ms = (ctypes.c_double * 2)()
+        r = _cuda.l2c_gpu_ragged_tuned_config(self._gpu, direction, buf, 64, ms)
+        if r < 0:
+            raise L2CError("l2c_gpu_ragged_tuned_config failed")
+        return ("tuned" if r == 1 else "default", buf.value.decode(), ms[0], ms[1])
 
     def __call__(self, inp, out, direction):
         f = _lib.execute_ragged(_ptr(inp), _ptr(out), self._p, direction)

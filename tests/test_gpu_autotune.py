@@ -97,3 +97,45 @@ def test_autotune_rejects_bad_shapes(lib, monkeypatch):
         p.autotune(0, 0, 0, 1)
     with pytest.raises(lib.L2CError, match="dist"):
         p.autotune(0, 4, 0, 1)
+
+
+def test_ragged_overlap_and_tuning_same_bits(lib, monkeypatch):
+    """Ragged lists: the band and the direct-method vectors beside the
+    far-field chain or not, the chain's priority, and the tuned choice give
+    the same bits."""
+    monkeypatch.delenv("L2C_AUTOTUNE", raising=False)
+    rng = np.random.default_rng(8)
+    Ns = [int(n) for n in np.exp(rng.uniform(np.log(20), np.log(40000), 60))]
+    Ns += [3, 100, 256, 257]  # direct-path vectors beside FMM ones
+
+    def run(env):
+        with monkeypatch.context() as m:
+            for k, v in env.items():
+                m.setenv(k, v)
+            p = lib.RaggedPlan(Ns, 64)
+        u = make_input(p.total, "gauss", 4)
+        pre = make_input(p.total, "uniform", 5)
+        outs = []
+        for d in (0, 1):
+            out = pre.copy()
+            p(u, out, d)
+            outs.append(out)
+        return p, outs
+
+    _, want = run({"L2C_OVERLAP": "0"})
+    for env in ({}, {"L2C_CHAIN_PRIO": "0"}, {"L2C_OVERLAP": "1", "L2C_CHAIN_PRIO": "1"}):
+        _, got = run(env)
+        for d in (0, 1):
+            assert np.array_equal(got[d], want[d]), (env, d)
+    p, _ = run({})
+    for d in (0, 1):
+        assert p.tuned_config(d)[0] == "default"
+        ms = p.autotune(d)
+        src, text, mt, md = p.tuned_config(d)
+        assert src == "tuned" and mt == ms and 0 < mt <= md and text.startswith("overlap="), text
+    u = make_input(p.total, "gauss", 4)
+    pre = make_input(p.total, "uniform", 5)
+    for d in (0, 1):
+        out = pre.copy()
+        p(u, out, d)
+        assert np.array_equal(out, want[d]), d
