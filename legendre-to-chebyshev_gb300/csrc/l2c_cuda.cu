@@ -1864,9 +1864,15 @@ struct PhaseScope;
 //              the two round differently)
 //   nctas    : band grid cap while it overlaps (0: none)
 //   nbuf     : tile buffers per warp of the mixed-form kernels (1/2)
+//   wtab     : band weights from a table in device memory (the reference's
+//              precompute; one DFMA per term instead of DMUL + DFMA, the same
+//              products): 1 always, 0 never, -1 by size -- batches whose table
+//              is no larger than their input (one table serves every vector of
+//              the batch; a single vector's is ~1.5 s times the vector), and
+//              plans created with precompute
 struct TuneCfg {
   int overlap = -1, pdl = -1, prio = -1, nthreads = 128, nvb = 8, npair = -1, nctas = 0,
-      nbuf = 1;
+      nbuf = 1, wtab = -1;
 };
 
 // A tuned call shape and its choices (dist is 0 for single vectors).
@@ -1896,6 +1902,8 @@ struct l2c_gpu_plan {
   cudaStream_t stream2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double *Wnear[2] = {nullptr, nullptr};  // precomputed band weights (optional)
+  bool precompute = false;  // created with L2C_PLAN_PRECOMPUTE_NEAR
+  bool use_w = false;       // this call's band reads Wnear (see TuneCfg::wtab)
   // nodal (Lagrange) form: T holds barycentric interpolation weights, A the
   // kernel samples, and the trees use B0 | B1 (c_lag_B; host copy lagB)
   bool nodal = false;
@@ -2493,7 +2501,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaGetLastError());
     x = p->x;
   }
-  const double *W = p->Wnear[dir];
+  const double *W = p->use_w ? p->Wnear[dir] : nullptr;
   if (near_only) {
     {
       PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, 8));
@@ -2572,6 +2580,7 @@ unsigned long long cfg_signature(const TuneCfg &c) {
   put(c.npair, 2);
   put(c.nbuf, 2);
   put(c.nctas, 24);
+  put(c.wtab, 2);
   return v;
 }
 
@@ -2586,6 +2595,30 @@ void cfg_apply(l2c_gpu_plan *p, const TuneCfg &c) {
   p->oz_nbuf = c.nbuf;
   p->oz_ld_ctas = p->oz_ld_ctas_nb[c.nbuf == 2 ? 2 : 1];
   p->cfg_sig = cfg_signature(c);
+}
+
+// Whether a call's band reads the weight table (TuneCfg::wtab).
+bool wants_table(const l2c_gpu_plan *p, const TuneCfg &c, size_t count) {
+  if (p->L == 0 || c.wtab == 0) return false;
+  if (c.wtab == 1 || p->precompute) return true;
+  return count > 1 && near_table_size(p->N, p->s) <= count * p->N;
+}
+
+// The band weights of one direction, built on first use (outside any capture).
+bool ensure_near_table(l2c_gpu_plan *p, size_t dir) {
+  if (p->Wnear[dir]) return true;
+  const size_t nw = near_table_size(p->N, p->s);
+  if (cudaMalloc(&p->Wnear[dir], nw * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    p->Wnear[dir] = nullptr;
+    set_err("cudaMalloc of the band weight table failed");
+    return false;
+  }
+  Geo g = make_geo(p, 1, p->N, 1);
+  k_near_weights<<<blocks_for((long long)p->N, 256), 256, 0, p->stream>>>(p->Wnear[dir], p->a,
+                                                                          p->an, p->dn, g,
+                                                                          (int)dir);
+  return cudaGetLastError() == cudaSuccess;
 }
 
 size_t shape_dist(size_t count, size_t dist) { return count > 1 ? dist : 0; }
@@ -2608,7 +2641,11 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   if (count == 0 || p->N == 0) return 1;
   {
     const TunedShape *ts = p->forced ? nullptr : tuned_for(p, dir, count, dist, stride);
-    cfg_apply(p, p->forced ? *p->forced : ts ? ts->cfg : p->base);
+    const TuneCfg &c = p->forced ? *p->forced : ts ? ts->cfg : p->base;
+    cfg_apply(p, c);
+    p->use_w = wants_table(p, c, count);
+    if (p->use_w && !ensure_near_table(p, dir)) return 0;
+    if (p->use_w) p->cfg_sig |= 1ull << 63;
   }
   if (!ensure_scratch(p, count)) return 0;
   if (p->mixed && p->L > 0 && count >= 4 && !ensure_mixed_far(p, dir)) return 0;
@@ -2722,15 +2759,15 @@ TuneCfg resolved_cfg(l2c_gpu_plan *p, size_t count) {
 
 void cfg_text(const TuneCfg &c, char *buf, size_t len) {
   snprintf(buf, len, "overlap=%d pdl=%d prio=%d near_threads=%d near_vb=%d near_pair=%d "
-           "near_ctas=%d nbuf=%d", c.overlap, c.pdl, c.prio, c.nthreads, c.nvb, c.npair,
-           c.nctas, c.nbuf);
+           "near_ctas=%d nbuf=%d near_table=%d", c.overlap, c.pdl, c.prio, c.nthreads, c.nvb,
+           c.npair, c.nctas, c.nbuf, c.wtab);
 }
 
 // Cache file: one line per tuned shape, fields separated by '|':
-// l2c-tune-1|device|SMs|N|maxs|form|precompute|dir|count|dist|stride|
-//   overlap|pdl|prio|nthreads|nvb|npair|nctas|nbuf|ms|ms_default
+// l2c-tune-2|device|SMs|N|maxs|form|precompute|dir|count|dist|stride|
+//   overlap|pdl|prio|nthreads|nvb|npair|nctas|nbuf|wtab|ms|ms_default
 // (form 0 modal, 1 nodal, 2 mixed).  Later lines win.
-constexpr int TUNE_FIELDS = 21;
+constexpr int TUNE_FIELDS = 22;
 
 struct TuneKey {
   char dev[256];
@@ -2751,7 +2788,7 @@ TuneKey tune_key(const l2c_gpu_plan *p) {
   for (char *c = k.dev; *c; c++)
     if (*c == '|' || *c == '\n') *c = ' ';
   k.form = p->mixed ? 2 : p->nodal ? 1 : 0;
-  k.pre = (p->Wnear[0] || p->Wnear[1]) ? 1 : 0;
+  k.pre = p->precompute ? 1 : 0;
   return k;
 }
 
@@ -2761,9 +2798,11 @@ void cache_append(const l2c_gpu_plan *p, const TunedShape &t) {
   FILE *f = std::fopen(p->tune_cache, "a");
   if (!f) return;  // an unwritable cache leaves the tuning in the plan only
   const TuneCfg &c = t.cfg;
-  std::fprintf(f, "l2c-tune-1|%s|%d|%zu|%zu|%d|%d|%zu|%zu|%zu|%zu|%d|%d|%d|%d|%d|%d|%d|%d|%.6f|%.6f\n",
+  std::fprintf(f,
+               "l2c-tune-2|%s|%d|%zu|%zu|%d|%d|%zu|%zu|%zu|%zu|%d|%d|%d|%d|%d|%d|%d|%d|%d|%.6f|"
+               "%.6f\n",
                k.dev, k.sms, p->N, p->maxs, k.form, k.pre, t.dir, t.count, t.dist, t.stride,
-               c.overlap, c.pdl, c.prio, c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, t.ms,
+               c.overlap, c.pdl, c.prio, c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, c.wtab, t.ms,
                t.ms_default);
   std::fclose(f);
 }
@@ -2786,7 +2825,7 @@ void cache_load(l2c_gpu_plan *p) {
         *q = 0;
         fld[n++] = q + 1;
       }
-    if (n != TUNE_FIELDS || std::strcmp(fld[0], "l2c-tune-1") != 0) continue;
+    if (n != TUNE_FIELDS || std::strcmp(fld[0], "l2c-tune-2") != 0) continue;
     if (std::strcmp(fld[1], k.dev) != 0 || std::atoi(fld[2]) != k.sms) continue;
     auto u = [&](int i) { return (size_t)std::strtoull(fld[i], nullptr, 10); };
     auto iv = [&](int i) { return (int)std::strtol(fld[i], nullptr, 10); };
@@ -2804,15 +2843,16 @@ void cache_load(l2c_gpu_plan *p) {
     t.cfg.npair = iv(16);
     t.cfg.nctas = iv(17);
     t.cfg.nbuf = iv(18);
-    t.ms = std::strtod(fld[19], nullptr);
-    t.ms_default = std::strtod(fld[20], nullptr);
+    t.cfg.wtab = iv(19);
+    t.ms = std::strtod(fld[20], nullptr);
+    t.ms_default = std::strtod(fld[21], nullptr);
     t.from_cache = true;
     // only values the launches accept
     const TuneCfg &c = t.cfg;
     if (t.dir > 1 || t.count == 0 || t.stride == 0 || c.overlap < 0 || c.overlap > 1 ||
         c.pdl < 0 || c.pdl > 7 || c.prio < 0 || c.prio > 1 ||
         (c.nthreads != 128 && c.nthreads != 256) || c.nvb < 1 || c.nvb > 8 || c.npair < -1 ||
-        c.npair > 1 || c.nctas < 0 || c.nbuf < 1 || c.nbuf > 2)
+        c.npair > 1 || c.nctas < 0 || c.nbuf < 1 || c.nbuf > 2 || c.wtab < -1 || c.wtab > 1)
       continue;
     p->tuned.push_back(t);
   }
@@ -2860,6 +2900,9 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
                                  {&TuneCfg::nthreads, {128, 256}},
                                  {&TuneCfg::nctas, {0, 3 * sms, 6 * sms}}};
       if (count > 1) knobs.push_back({&TuneCfg::nvb, {1, 2, 4, 8}});
+      // the weight table: when the plan has one, or a batch's would be small
+      if (p->precompute || (count > 1 && near_table_size(p->N, p->s) <= count * p->N))
+        knobs.push_back({&TuneCfg::wtab, {0, 1}});
       if (p->mixed) knobs.push_back({&TuneCfg::nbuf, {1, 2}});
       for (int pass = 0; pass < 2 && best > 0.0; pass++) {
         bool kept = false;
@@ -2984,6 +3027,8 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
     snprintf(p->tune_cache, sizeof(p->tune_cache), "%s", env);
   p->base = TuneCfg{p->overlap,    p->pdl,       p->chain_prio_mode, p->near_threads,
                     p->near_vb,    p->near_pair, (int)p->near_ctas,  p->oz_nbuf};
+  if (const char *env = std::getenv("L2C_NEAR_TABLE")) p->base.wtab = env[0] == '1' ? 1 : 0;
+  p->precompute = (flags & L2C_PLAN_PRECOMPUTE_NEAR) != 0;
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
     p->Nn = N;
