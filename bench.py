@@ -777,7 +777,10 @@ def main():
                 "in_step_note": "in the timed step the band runs on a second stream beside "
                                 "the far-field chain, whose kernels have scheduling priority",
                 "note": "reference flop count of directM/directL (3 per band term); a term "
-                        "costs 2 FP64 issue slots (DMUL+DFMA) unless precompute=1"}
+                        "costs 2 FP64 issue slots (DMUL+DFMA), or 1 (DFMA) when the band "
+                        "reads its weights from a table (precompute=1, and batches whose "
+                        "table is no larger than their input); with a table, or with one "
+                        "weight shared by 8 vectors, frac can pass 1"}
     if not ragged:
         total_flops = sum(plan.flops(d) for d, _, _ in wl.calls) * count
 
