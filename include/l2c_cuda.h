@@ -98,7 +98,8 @@ int l2c_gpu_profile_read(l2c_gpu_plan *plan, double *ms, size_t *launches);
  * the CPU).  For one call shape -- direction, count, dist, stride, as passed to
  * l2c_gpu_execute -- it times this plan's launch choices on synthetic device
  * data and keeps the fastest for every later call of that shape: the band on a
- * second stream or not, programmatic dependent launch, the chain's priority,
+ * second stream or not and the chain step after which it starts, programmatic
+ * dependent launch, the chain's priority,
  * the band's CTA size, vectors per thread and grid cap, the mixed form's tile
  * buffers, and whether the band reads its weights from a table in device memory
  * (by default: batches whose table is no larger than their input).  No choice

@@ -28,6 +28,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <functional>
 #include <vector>
 
 #include "../../include/l2c_cuda.h"
@@ -1870,9 +1871,12 @@ struct PhaseScope;
 //              is no larger than their input (one table serves every vector of
 //              the batch; a single vector's is ~1.5 s times the vector), and
 //              plans created with precompute
+//   fork     : where the band joins the chain's stream order when it overlaps:
+//              0 from the start, 1 after leaf-up, 2 after the upward sweep,
+//              3 after the far field (it always finishes before leaf-down)
 struct TuneCfg {
   int overlap = -1, pdl = -1, prio = -1, nthreads = 128, nvb = 8, npair = -1, nctas = 0,
-      nbuf = 1, wtab = -1;
+      nbuf = 1, wtab = -1, fork = 0;
 };
 
 // A tuned call shape and its choices (dist is 0 for single vectors).
@@ -1958,6 +1962,7 @@ struct l2c_gpu_plan {
   //  chain_prio_mode: the chain's kernels at the device's greatest priority.
   int pdl = -1;
   int chain_prio_mode = -1;
+  int band_fork = 0;  // TuneCfg::fork
   int prio_greatest = 0;  // cudaDeviceGetStreamPriorityRange's greatest priority
   // autotuner: the plan's own choices (defaults and environment), the tuned
   // shapes, a configuration forced while one is timed, and the signature of
@@ -2358,9 +2363,10 @@ void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStrea
 }
 
 bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir, const Geo &g,
-                      cudaStream_t st, const Sched &sc) {
+                      cudaStream_t st, const Sched &sc, const std::function<bool(int)> &band) {
   const bool ov = sc.ov;
   const int c2l = dir == 1;
+  if (!band(0)) return false;
   long long *w = reinterpret_cast<long long *>(p->w), *c = reinterpret_cast<long long *>(p->c);
   const LaunchOpt chain(sc.pdl & 1, sc.prio);
   {
@@ -2378,6 +2384,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
+  if (!band(1)) return false;
   {
     PhaseScope ps(p, L2C_PHASE_TREE_UP, (size_t)(g.L - 1));
     const bool q2 = p->oz_tree_q == 2, nb1 = p->oz_nbuf == 1;
@@ -2394,6 +2401,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
+  if (!band(2)) return false;
   {
     const bool tc = g.count >= 4 && p->oz_far[dir] != nullptr;
     PhaseScope ps(p, L2C_PHASE_FAR, tc ? 1 : 3);
@@ -2412,6 +2420,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
+  if (!band(3)) return false;
   {
     PhaseScope ps(p, L2C_PHASE_TREE_DOWN, (size_t)(g.L - 1));
     const bool q2 = p->oz_tree_q == 2, nb1 = p->oz_nbuf == 1;
@@ -2514,22 +2523,32 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaGetLastError());
     return 1;
   }
-  // The band on the second stream beside the far-field chain (sched_for).
+  // The band on the second stream beside the far-field chain (sched_for),
+  // entering it at fork point band_fork of the chain (TuneCfg::fork); it
+  // always finishes before leaf-down.  Without the second stream it runs
+  // first, on the chain's stream.
   const Sched sc = sched_for(p, count);
   const bool ov = sc.ov;
   cudaStream_t stn = ov ? st2 : st;
-  if (ov) {
-    CK(cudaEventRecord(p->ev_fork, st));
-    CK(cudaStreamWaitEvent(st2, p->ev_fork, 0));
-  }
-  {
-    PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, ov ? p->near_vb : 8), stn);
-    CK(launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, near_pair(p),
-                    ov ? p->near_ctas : 0, ov ? p->near_vb : 8, (sc.pdl & 2) && !ov,
-                    ov ? p->near_threads : 256));
-  }
-  if (ov) CK(cudaEventRecord(p->ev_join, st2));
-  if (p->mixed) return launch_mixed_far(p, x, out, dir, g, st, sc) ? 1 : 0;
+  const int fork = ov ? std::min(std::max(p->band_fork, 0), 3) : 0;
+  bool band_done = false;
+  auto band = [&](int pos) -> bool {
+    if (band_done || pos < fork) return true;
+    band_done = true;
+    if (ov && (cudaEventRecord(p->ev_fork, st) != cudaSuccess ||
+               cudaStreamWaitEvent(st2, p->ev_fork, 0) != cudaSuccess))
+      return false;
+    {
+      PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, ov ? p->near_vb : 8), stn);
+      if (launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, near_pair(p),
+                      ov ? p->near_ctas : 0, ov ? p->near_vb : 8, (sc.pdl & 2) && !ov,
+                      ov ? p->near_threads : 256) != cudaSuccess)
+        return false;
+    }
+    return !ov || cudaEventRecord(p->ev_join, st2) == cudaSuccess;
+  };
+  if (p->mixed) return launch_mixed_far(p, x, out, dir, g, st, sc, band) ? 1 : 0;
+  if (!band(0)) return 0;
   const long long leaf_threads = g.count * g.K * 2 * M;
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
@@ -2538,11 +2557,13 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
              (const double *)p->T, p->w, g);
     CK(cudaGetLastError());
   }
+  if (!band(1)) return 0;
   const TreePlan tp = tree_plan(p->L, count);
   {
     PhaseScope ps(p, L2C_PHASE_TREE_UP, tree_launches(tp, p->L));
     CK(sweep_up(p->w, g, tp, st, LaunchOpt(sc.pdl & 1, sc.prio), p->nodal));
   }
+  if (!band(2)) return 0;
   {
     PhaseScope ps(p, L2C_PHASE_FAR, 1);
     const long long n = g.count * (long long)p->Nb * M;  // both parities per thread
@@ -2551,6 +2572,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
              (const double *)p->w, p->c, g, (long long)p->Nb);
     CK(cudaGetLastError());
   }
+  if (!band(3)) return 0;
   {
     PhaseScope ps(p, L2C_PHASE_TREE_DOWN, tree_launches(tp, p->L));
     CK(sweep_down(p->c, g, tp, st, LaunchOpt(sc.pdl & 1, sc.prio), p->nodal));
@@ -2581,6 +2603,7 @@ unsigned long long cfg_signature(const TuneCfg &c) {
   put(c.nbuf, 2);
   put(c.nctas, 24);
   put(c.wtab, 2);
+  put(c.fork, 3);
   return v;
 }
 
@@ -2593,6 +2616,7 @@ void cfg_apply(l2c_gpu_plan *p, const TuneCfg &c) {
   p->near_pair = c.npair;
   p->near_ctas = (unsigned)c.nctas;
   p->oz_nbuf = c.nbuf;
+  p->band_fork = c.fork;
   p->oz_ld_ctas = p->oz_ld_ctas_nb[c.nbuf == 2 ? 2 : 1];
   p->cfg_sig = cfg_signature(c);
 }
@@ -2758,16 +2782,16 @@ TuneCfg resolved_cfg(l2c_gpu_plan *p, size_t count) {
 }
 
 void cfg_text(const TuneCfg &c, char *buf, size_t len) {
-  snprintf(buf, len, "overlap=%d pdl=%d prio=%d near_threads=%d near_vb=%d near_pair=%d "
-           "near_ctas=%d nbuf=%d near_table=%d", c.overlap, c.pdl, c.prio, c.nthreads, c.nvb,
-           c.npair, c.nctas, c.nbuf, c.wtab);
+  snprintf(buf, len, "overlap=%d band_fork=%d pdl=%d prio=%d near_threads=%d near_vb=%d "
+           "near_pair=%d near_ctas=%d nbuf=%d near_table=%d", c.overlap, c.fork, c.pdl, c.prio,
+           c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, c.wtab);
 }
 
 // Cache file: one line per tuned shape, fields separated by '|':
-// l2c-tune-2|device|SMs|N|maxs|form|precompute|dir|count|dist|stride|
-//   overlap|pdl|prio|nthreads|nvb|npair|nctas|nbuf|wtab|ms|ms_default
+// l2c-tune-3|device|SMs|N|maxs|form|precompute|dir|count|dist|stride|
+//   overlap|pdl|prio|nthreads|nvb|npair|nctas|nbuf|wtab|fork|ms|ms_default
 // (form 0 modal, 1 nodal, 2 mixed).  Later lines win.
-constexpr int TUNE_FIELDS = 22;
+constexpr int TUNE_FIELDS = 23;
 
 struct TuneKey {
   char dev[256];
@@ -2799,11 +2823,11 @@ void cache_append(const l2c_gpu_plan *p, const TunedShape &t) {
   if (!f) return;  // an unwritable cache leaves the tuning in the plan only
   const TuneCfg &c = t.cfg;
   std::fprintf(f,
-               "l2c-tune-2|%s|%d|%zu|%zu|%d|%d|%zu|%zu|%zu|%zu|%d|%d|%d|%d|%d|%d|%d|%d|%d|%.6f|"
-               "%.6f\n",
+               "l2c-tune-3|%s|%d|%zu|%zu|%d|%d|%zu|%zu|%zu|%zu|%d|%d|%d|%d|%d|%d|%d|%d|%d|%d|"
+               "%.6f|%.6f\n",
                k.dev, k.sms, p->N, p->maxs, k.form, k.pre, t.dir, t.count, t.dist, t.stride,
-               c.overlap, c.pdl, c.prio, c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, c.wtab, t.ms,
-               t.ms_default);
+               c.overlap, c.pdl, c.prio, c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, c.wtab,
+               c.fork, t.ms, t.ms_default);
   std::fclose(f);
 }
 
@@ -2825,7 +2849,7 @@ void cache_load(l2c_gpu_plan *p) {
         *q = 0;
         fld[n++] = q + 1;
       }
-    if (n != TUNE_FIELDS || std::strcmp(fld[0], "l2c-tune-2") != 0) continue;
+    if (n != TUNE_FIELDS || std::strcmp(fld[0], "l2c-tune-3") != 0) continue;
     if (std::strcmp(fld[1], k.dev) != 0 || std::atoi(fld[2]) != k.sms) continue;
     auto u = [&](int i) { return (size_t)std::strtoull(fld[i], nullptr, 10); };
     auto iv = [&](int i) { return (int)std::strtol(fld[i], nullptr, 10); };
@@ -2844,15 +2868,17 @@ void cache_load(l2c_gpu_plan *p) {
     t.cfg.nctas = iv(17);
     t.cfg.nbuf = iv(18);
     t.cfg.wtab = iv(19);
-    t.ms = std::strtod(fld[20], nullptr);
-    t.ms_default = std::strtod(fld[21], nullptr);
+    t.cfg.fork = iv(20);
+    t.ms = std::strtod(fld[21], nullptr);
+    t.ms_default = std::strtod(fld[22], nullptr);
     t.from_cache = true;
     // only values the launches accept
     const TuneCfg &c = t.cfg;
     if (t.dir > 1 || t.count == 0 || t.stride == 0 || c.overlap < 0 || c.overlap > 1 ||
         c.pdl < 0 || c.pdl > 7 || c.prio < 0 || c.prio > 1 ||
         (c.nthreads != 128 && c.nthreads != 256) || c.nvb < 1 || c.nvb > 8 || c.npair < -1 ||
-        c.npair > 1 || c.nctas < 0 || c.nbuf < 1 || c.nbuf > 2 || c.wtab < -1 || c.wtab > 1)
+        c.npair > 1 || c.nctas < 0 || c.nbuf < 1 || c.nbuf > 2 || c.wtab < -1 || c.wtab > 1 ||
+        c.fork < 0 || c.fork > 3)
       continue;
     p->tuned.push_back(t);
   }
@@ -2895,6 +2921,7 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
         std::vector<int> vals;
       };
       std::vector<Knob> knobs = {{&TuneCfg::overlap, {0, 1}},
+                                 {&TuneCfg::fork, {0, 1, 2, 3}},
                                  {&TuneCfg::pdl, {0, 1, 7}},
                                  {&TuneCfg::prio, {0, 1}},
                                  {&TuneCfg::nthreads, {128, 256}},
@@ -3028,6 +3055,8 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   p->base = TuneCfg{p->overlap,    p->pdl,       p->chain_prio_mode, p->near_threads,
                     p->near_vb,    p->near_pair, (int)p->near_ctas,  p->oz_nbuf};
   if (const char *env = std::getenv("L2C_NEAR_TABLE")) p->base.wtab = env[0] == '1' ? 1 : 0;
+  if (const char *env = std::getenv("L2C_BAND_FORK"))
+    p->base.fork = std::min(3, std::max(0, std::atoi(env)));
   p->precompute = (flags & L2C_PLAN_PRECOMPUTE_NEAR) != 0;
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;

@@ -99,9 +99,9 @@ def test_mixed_rejects_large_leaves(lib):
 def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
     """Programmatic dependent launch, the band on the second stream, graph
     replay, the tile buffer depth, the chain's scheduling priority and the
-    band's CTA size, vectors per thread, grid cap and weight table change only
-    when work runs, never what it computes: every setting gives the same bits
-    as the default plan."""
+    band's CTA size, vectors per thread, grid cap, weight table and fork point
+    change only when work runs, never what it computes: every setting gives
+    the same bits as the default plan."""
     N = 16384
     x = np.ascontiguousarray(make_input(N * count, "gauss", 11).reshape(count, N))
 
@@ -125,7 +125,9 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
                 {"L2C_NEAR_VB": "1"}, {"L2C_NEAR_VB": "2"}, {"L2C_NEAR_VB": "4"},
                 {"L2C_NEAR_THREADS": "256"}, {"L2C_NEAR_CTAS": "456"},
                 {"L2C_NEAR_THREADS": "256", "L2C_NEAR_VB": "2", "L2C_NEAR_CTAS": "912"},
-                {"L2C_NEAR_TABLE": "0"}, {"L2C_NEAR_TABLE": "1"}):
+                {"L2C_NEAR_TABLE": "0"}, {"L2C_NEAR_TABLE": "1"},
+                {"L2C_BAND_FORK": "1"}, {"L2C_BAND_FORK": "2"}, {"L2C_BAND_FORK": "3"},
+                {"L2C_BAND_FORK": "2", "L2C_PDL": "7"}):
         with monkeypatch.context() as m:
             for k, v in env.items():
                 m.setenv(k, v)
