@@ -99,12 +99,12 @@ int l2c_gpu_profile_read(l2c_gpu_plan *plan, double *ms, size_t *launches);
  * l2c_gpu_execute -- it times this plan's launch choices on synthetic device
  * data and keeps the fastest for every later call of that shape: the band on a
  * second stream or not and the chain step after which it starts, programmatic
- * dependent launch, the chain's priority,
- * the band's CTA size, vectors per thread and grid cap, the mixed form's tile
- * buffers, and whether the band reads its weights from a table in device memory
- * (by default: batches whose table is no larger than their input).  No choice
- * changes results: outputs are the same bits under every setting.  Blocks
- * while it runs (tens of calls of the shape).
+ * dependent launch, the chain's priority, the band's CTA size, vectors per
+ * thread and grid cap, the mixed form's tile buffers, and whether the band
+ * reads its weights from a table in device memory (by default: batches whose
+ * table is no larger than their input).  No choice changes results: outputs
+ * are the same bits under every setting.  Blocks while it runs (tens of calls
+ * of the shape).
  * Returns the tuned milliseconds per call, 0 on error (l2c_gpu_last_error).
  * With L2C_AUTOTUNE=1 in the environment at plan creation, each new shape is
  * tuned on its first call; with L2C_AUTOTUNE_CACHE=path, tuned shapes are
