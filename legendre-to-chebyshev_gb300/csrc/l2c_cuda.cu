@@ -1319,7 +1319,8 @@ constexpr int oz_min_ctas(int NBUF) { return NBUF == 1 ? 4 : 1; }
 template <int KC, int NBUF>
 __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
     k_mz_leaf_up(const double *__restrict__ x, long long *__restrict__ w, int *__restrict__ wE,
-                 const unsigned *__restrict__ Pf, const int *__restrict__ Pm, Geo g) {
+                 const unsigned *__restrict__ Pf, const int *__restrict__ Pm, Geo g,
+                 int *__restrict__ bad) {
   constexpr int XLD = 16 * KC + 1, NW = oz_words(OZ_NT, KC);
   extern __shared__ __align__(16) unsigned char mz_smem[];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
@@ -1383,8 +1384,12 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
       if (t4 == 0)
         for (int hr = 0; hr < 2; hr++) {
           const int r = gq + 8 * hr;
-          if (r < nrow)
+          if (r < nrow) {
             wE[(v * 2 + sg) * g.slots + g.leaf_base + node0 + r] = Es[sg * 16 + r] + meta[OZ_ROWS];
+            // an Inf or NaN input (exponent bound past the largest finite
+            // double's): the vector's far field is not defined
+            if (Es[sg * 16 + r] > 1024) bad[v] = 1;
+          }
         }
     }
   };
@@ -1698,7 +1703,8 @@ template <int NBUF>
 __global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 4 : 1)
     k_mz_leaf_down(const long long *__restrict__ c, const int *__restrict__ cE,
                    const double *__restrict__ y, double *out, const unsigned *__restrict__ Pf,
-                   const int *__restrict__ Pe, Geo g, int c2l, int npass) {
+                   const int *__restrict__ Pe, Geo g, int c2l, int npass,
+                   const int *__restrict__ bad) {
   extern __shared__ __align__(16) unsigned char mz_smem[];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
   const int nw = 2 * npass * OZ_LD_WORDS, ne = 2 * npass * 16;
@@ -1771,6 +1777,10 @@ __global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 4 : 1)
     __syncwarp();
     const double *yv = y + v * g.N;
     double *ov = out + v * g.dist;
+    // a vector with an Inf or NaN input: NaN far field (the FP64 form's NaN
+    // reaches the outputs the bad input's blocks interact with)
+    const bool nan_v = bad[v] != 0;
+    const double qnan = __longlong_as_double(0x7ff8000000000000ll);
     for (long long q = lane; q < g.h; q += 32) {
       // the 16 rows' band sums first (one latency), then the sums
       double yy[16];
@@ -1783,7 +1793,8 @@ __global__ void __launch_bounds__(32 * MXW, NBUF == 1 ? 4 : 1)
 #pragma unroll
       for (int r = 0; r < 16; r++) {
         const long long j = (tau0 + r) * g.h + q;
-        if (r < nrow && j < g.N) ov[j * g.stride] = scale(yy[r] + S[r * sld + q], j);
+        if (r < nrow && j < g.N)
+          ov[j * g.stride] = scale(yy[r] + (nan_v ? qnan : S[r * sld + q]), j);
       }
     }
     __syncwarp();
@@ -1934,6 +1945,7 @@ struct l2c_gpu_plan {
   // column exponents of w and c (mixed form: w, c hold column-format integers)
   int *wE = nullptr, *cE = nullptr;
   size_t cap_wE = 0, cap_cE = 0;
+  int *bad = nullptr;  // per vector: an Inf or NaN input seen (mixed form)
   // captured launch sequences, keyed by the call's shape and pointers
   struct GraphEntry {
     size_t dir, count, dist, stride;
@@ -2120,6 +2132,13 @@ bool ensure_scratch(l2c_gpu_plan *p, size_t count) {
       p->cap_wE = cwe;
       p->cap_cE = cce;
       if (!ok) return false;
+      if (p->bad) cudaFree(p->bad);
+      p->bad = nullptr;
+      if (cudaMalloc(&p->bad, need * sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        set_err("cudaMalloc of the mixed-form vector flags failed");
+        return false;
+      }
     }
   }
   p->cap_vec = need;
@@ -2359,7 +2378,7 @@ void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStrea
   launch_k(pdl, p->oz_nbuf == 1 ? k_mz_leaf_up<KC, 1> : k_mz_leaf_up<KC, 2>, grid, 32 * MXW,
            mz_leaf_up_smem(KC, p->oz_nbuf), st, x,
            reinterpret_cast<long long *>(p->w), p->wE, (const unsigned *)p->oz_lu,
-           (const int *)p->oz_lum, g);
+           (const int *)p->oz_lum, g, p->bad);
 }
 
 bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir, const Geo &g,
@@ -2369,6 +2388,7 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
   if (!band(0)) return false;
   long long *w = reinterpret_cast<long long *>(p->w), *c = reinterpret_cast<long long *>(p->c);
   const LaunchOpt chain(sc.pdl & 1, sc.prio);
+  if (cudaMemsetAsync(p->bad, 0, (size_t)g.count * sizeof(int), st) != cudaSuccess) return false;
   {
     PhaseScope ps(p, L2C_PHASE_LEAF_UP, 1);
     const LaunchOpt pdl(pdl_after_band(sc), sc.prio);
@@ -2449,7 +2469,8 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     launch_k((sc.pdl & 1) && !ov, p->oz_nbuf == 1 ? k_mz_leaf_down<1> : k_mz_leaf_down<2>,
              grid, 32 * MXW, mz_leaf_down_smem(p->oz_npass, p->oz_nbuf, g.h), st,
              (const long long *)c, (const int *)p->cE, (const double *)p->y, out,
-             (const unsigned *)p->oz_ld, (const int *)p->oz_lde, g, c2l, p->oz_npass);
+             (const unsigned *)p->oz_ld, (const int *)p->oz_lde, g, c2l, p->oz_npass,
+             (const int *)p->bad);
     if (cudaGetLastError() != cudaSuccess) return false;
   }
   return true;
@@ -3325,7 +3346,7 @@ void l2c_gpu_plan_destroy(l2c_gpu_plan *p) {
     if (b) cudaFree(b);
   void *obufs[] = {p->oz_lu,     p->oz_tu,     p->oz_td,      p->oz_ld,      p->oz_lum,
                    p->oz_tum,    p->oz_tdm,    p->oz_lde,     p->oz_far[0],  p->oz_far[1],
-                   p->oz_farm[0], p->oz_farm[1], p->wE,        p->cE};
+                   p->oz_farm[0], p->oz_farm[1], p->wE,        p->cE,         p->bad};
   for (void *b : obufs)
     if (b) cudaFree(b);
   if (p->stream) cudaStreamDestroy(p->stream);

@@ -149,3 +149,31 @@ def test_mixed_far_column_chunks(lib, orc, count):
         p.execute_batched(x, out, d, count, N, 1)
         for v in range(count):
             assert relerr(out[v], o(x[v], d)[:N]) <= TOL, (count, d, v)
+
+
+@pytest.mark.parametrize("bad", [np.nan, np.inf])
+def test_non_finite_inputs(lib, orc, bad):
+    """Inf and NaN inputs.  The plain form gives the oracle's pattern of
+    non-finite outputs exactly (they spread through the same sums).  The mixed
+    form's fixed-point far field cannot carry them: a vector holding one gets
+    non-finite outputs wherever the oracle does (and more), and the other
+    vectors of the batch keep their bits."""
+    N, maxs, count = 4096, 16, 6
+    x = np.ascontiguousarray(make_input(N * count, "gauss", 21).reshape(count, N))
+    xb = x.copy()
+    xb[2, 1500] = bad
+    o = orc.Oracle(N, maxs, 2)
+    for d in (0, 1):
+        want = ~np.isfinite(o(xb[2], d)[:N])
+        assert want.any()
+        p = lib.Plan(N, maxs)
+        out = np.zeros_like(xb)
+        p.execute_batched(xb, out, d, count, N, 1)
+        assert np.array_equal(~np.isfinite(out[2]), want), d
+        q = lib.Plan(N, maxs, mixed=True)
+        clean, got = np.zeros_like(x), np.zeros_like(xb)
+        q.execute_batched(x, clean, d, count, N, 1)
+        q.execute_batched(xb, got, d, count, N, 1)
+        assert np.all(~np.isfinite(got[2]) >= want), d
+        for v in (0, 1, 3, 4, 5):
+            assert np.array_equal(got[v], clean[v]), (d, v)
