@@ -38,3 +38,29 @@ def test_hbm_peak_source():
 
     v, src = bench.hbm_peak_gbs()
     assert v > 1000 and ("measured" in src or "fallback" in src)
+
+
+def test_autotune_record():
+    """autotune_plan tunes each direction the workload calls once and reports
+    the choices and timings the plan gives back."""
+    sys.path.insert(0, REPO)
+    import bench
+
+    class FakePlan:
+        def __init__(self):
+            self.tuned = []
+
+        def autotune(self, d, count, dist, stride):
+            self.tuned.append((d, count, dist, stride))
+            return 0.5 + d
+
+        def tuned_config(self, d, count, dist, stride):
+            return ("tuned", f"overlap=1 dir={d}", 0.5 + d, 0.6 + d)
+
+    p = FakePlan()
+    calls = [(0, "u", "o0"), (1, "o0", "o1"), (0, "u", "o2")]
+    rec = bench.autotune_plan(p, calls, 4096, 1024)
+    assert p.tuned == [(0, 4096, 1024, 1), (1, 4096, 1024, 1)]
+    assert rec["shapes"]["L2C"] == {"choices": "overlap=1 dir=0", "ms_per_call": 0.5,
+                                    "ms_per_call_default": 0.6}
+    assert rec["shapes"]["C2L"]["ms_per_call"] == 1.5 and rec["seconds"] >= 0
