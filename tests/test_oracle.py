@@ -110,6 +110,20 @@ def test_oracle_vs_extended_precision(orc, N, maxs, dist):
     assert direct_ld.rel_maxnorm(o(u, 1)[:N], direct_ld.c2l_direct(u)) < 5e-15
 
 
+@pytest.mark.parametrize("seed", range(12))
+def test_oracle_random_shapes_vs_extended_precision(orc, seed):
+    """The checker itself on seeded random lengths (from 2, so the direct
+    method too), leaf sizes and input distributions, against the
+    extended-precision direct sums: at most 1.7e-15 measured, bar 5e-15."""
+    rng = np.random.default_rng(6000 + seed)
+    N = int(np.exp(rng.uniform(np.log(2), np.log(6000))))
+    maxs = int(rng.integers(8, 65))
+    u = make_input(N, ("uniform", "sign", "gauss")[seed % 3], seed)
+    o = orc.Oracle(N, maxs, 2)
+    assert direct_ld.rel_maxnorm(o(u, 0)[:N], direct_ld.l2c_direct(u)) < 5e-15, (N, maxs)
+    assert direct_ld.rel_maxnorm(o(u, 1)[:N], direct_ld.c2l_direct(u)) < 5e-15, (N, maxs)
+
+
 @pytest.mark.parametrize("N", [257, 1023, 4097])
 def test_oracle_odd_N_l2c_vs_extended_precision(orc, N):
     # the reference itself cannot run these (leg2cheb.c:283-294 overruns for odd N)
