@@ -87,6 +87,34 @@ def hbm_peak_gbs():
     return 6800.0, "fallback 6.8 TB/s"
 
 
+FP64_PEAK_SOURCE = ("FP64 DGEMM measured in this run (cuBLAS float64 matmul 4096^3); "
+                    "MEASURED_PEAKS.json holds no FP64 figure")
+BAND_PROFILE = "profiles/k_near_single_N1048576.md"
+
+
+def profile_traffic(rel_path):
+    """DRAM bytes per launch from a committed ncu summary: the mean over its
+    launch columns of dram__bytes_read.sum + dram__bytes_write.sum, read from
+    the summary's table rows ("| dram__bytes_read.sum | 25.2 MB | 25.2 MB |")."""
+    units = {"B": 1.0, "KB": 1e3, "MB": 1e6, "GB": 1e9}
+    try:
+        with open(os.path.join(REPO, rel_path)) as f:
+            rows = [ln for ln in f if ln.startswith("| dram__bytes_")]
+    except OSError:
+        return None
+    cols = None
+    for ln in rows:
+        name = ln.split("|")[1].strip()
+        if name not in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+            continue
+        vals = []
+        for cell in ln.strip().strip("|").split("|")[1:]:
+            parts = cell.split()
+            vals.append(float(parts[0]) * units[parts[1] if len(parts) > 1 else "B"])
+        cols = vals if cols is None else [a + b for a, b in zip(cols, vals)]
+    return sum(cols) / len(cols) if cols else None
+
+
 def phase_roofline(wl, L, s, Nb, phases, fp64_tf, hbm_gbs, lagrange):
     """Per FMM step of one bench step (both calls): the reference's flop count
     and the algorithmic DRAM bytes of that step, over its CUDA-event time, as
@@ -329,14 +357,133 @@ class Workload:
             o.execute_batch(src, dst, d, self.count, self.N)
 
 
-def cpu_run(wl, seconds, threads):
-    """Oracle port on all host cores: the workload's step repeated for about
-    `seconds`; returns (coefficients per second, outputs, reps)."""
-    sys.path.insert(0, REPO)
-    from oracle import oracle
+REF_DIR = os.path.join(REPO, "oracle", "_ref")
+REF_LIB = os.path.join(REF_DIR, "libleg2cheb_ref.so")
+REF_BATCH = os.path.join(REF_DIR, "libref_batch.so")
 
-    oracle.set_threads(threads)
-    o = wl.cpu_oracle(oracle)
+
+class PortCPU:
+    """The oracle port of the reference algorithm (oracle/l2c_oracle.c, OpenMP)."""
+
+    kind = "port"
+
+    def __init__(self, wl, threads, why):
+        sys.path.insert(0, REPO)
+        from oracle import oracle
+
+        oracle.set_threads(threads)
+        self.wl, self.o = wl, wl.cpu_oracle(oracle)
+        self.note = f"oracle port of the reference algorithm with OpenMP ({why})"
+
+    def call(self, src, dst, d):
+        self.wl.cpu_call(self.o, src, dst, d)
+
+
+class ReferenceCPU:
+    """The reference's own execute() (src/C/leg2cheb.c:1299-1500), compiled
+    from its unmodified sources into oracle/_ref by oracle/Makefile, called
+    through ctypes.  A single vector runs on one plan with every host thread
+    (the reference's OpenMP loops and OpenBLAS threads); a batch loops execute
+    over the vectors with one plan per OpenMP thread (oracle/ref_batch.c)."""
+
+    kind = "reference"
+
+    def __init__(self, wl, threads):
+        import ctypes
+
+        sz, vp = ctypes.c_size_t, ctypes.c_void_p
+        self.lib = ctypes.CDLL(REF_LIB, mode=ctypes.RTLD_GLOBAL)
+        self.batch = ctypes.CDLL(REF_BATCH)
+        self.lib.create_fmm.restype = vp
+        self.lib.create_fmm.argtypes = [sz] * 7
+        self.lib.execute.restype = sz
+        self.lib.execute.argtypes = [vp, vp, vp, sz, sz]
+        self.lib.free_fmm.argtypes = [vp]
+        self.batch.ref_batch_create.restype = vp
+        self.batch.ref_batch_create.argtypes = [sz, vp, sz, sz]
+        self.batch.ref_batch_execute.restype = sz
+        self.batch.ref_batch_execute.argtypes = [vp, vp, vp, sz]
+        self.batch.ref_batch_free.argtypes = [vp]
+        self.batch.ref_set_threads.argtypes = [ctypes.c_int, ctypes.c_int]
+        self.wl, self.plan, self.handle = wl, None, None
+        if wl.count == 1:
+            self.plan = self.lib.create_fmm(wl.N, wl.maxs, 18, 2, wl.lagrange, 0, 0)
+            if not self.plan:
+                raise RuntimeError("reference create_fmm failed")
+            omp_t, blas_t = self._pick_threads(threads)
+            self.note = (f"the reference's execute() built from its unmodified sources, one plan, "
+                         f"{omp_t} OpenMP threads and {blas_t} OpenBLAS threads (the fastest of "
+                         f"the settings tried: {self.tried})")
+        else:
+            Ns = np.full(wl.count, wl.N, dtype=np.uint64)
+            self.handle = self.batch.ref_batch_create(wl.count, Ns.ctypes.data, wl.maxs, threads)
+            if not self.handle:
+                raise RuntimeError("reference batch plans failed")
+            self.note = (f"the reference's execute() built from its unmodified sources, looped "
+                         f"over the {wl.count} vectors with one plan per OpenMP thread "
+                         f"({threads} threads)")
+
+    def _pick_threads(self, threads):
+        """The reference's fastest thread setting for this vector: OpenMP on
+        every core with OpenBLAS serial or on every core, or OpenMP on half the
+        cores (each timed on two steps after one)."""
+        u = np.ascontiguousarray(self.wl.u[0])
+        out = np.zeros_like(u)
+        best, self.tried = None, {}
+        for omp_t, blas_t in ((threads, 1), (threads, threads), (max(1, threads // 2), 1)):
+            self.batch.ref_set_threads(omp_t, blas_t)
+            ts = []
+            for _ in range(3):
+                out[:] = 0
+                t0 = time.perf_counter()
+                for d, _, _ in self.wl.calls:
+                    self.lib.execute(u.ctypes.data, out.ctypes.data, self.plan, d, 1)
+                ts.append(time.perf_counter() - t0)
+            t = min(ts[1:])
+            self.tried[f"{omp_t}x{blas_t}"] = round(t * 1e3, 2)
+            if best is None or t < best[0]:
+                best = (t, omp_t, blas_t)
+        self.batch.ref_set_threads(best[1], best[2])
+        return best[1], best[2]
+
+    def call(self, src, dst, d):
+        src = np.ascontiguousarray(src)
+        if self.plan:
+            self.lib.execute(src.ctypes.data, dst.ctypes.data, self.plan, d, 1)
+        else:
+            self.batch.ref_batch_execute(self.handle, src.ctypes.data, dst.ctypes.data, d)
+
+    def close(self):
+        if self.plan:
+            self.lib.free_fmm(self.plan)
+            self.plan = None
+        if self.handle:
+            self.batch.ref_batch_free(self.handle)
+            self.handle = None
+
+
+def cpu_impl(wl, threads):
+    """The CPU implementation the reference arm and the CPU baseline time: the
+    reference itself where it was built (oracle/_ref) and can run the workload,
+    else the oracle port."""
+    if wl.name == "ragged":
+        # the reference's L2C of an odd N with L >= 1 runs past its arrays
+        # (leg2cheb.c:283-294: an unsigned test that never ends the last block's
+        # loop), and the list holds odd lengths
+        return PortCPU(wl, threads, "the reference itself cannot run odd-length L2C")
+    if not (os.path.exists(REF_LIB) and os.path.exists(REF_BATCH)):
+        return PortCPU(wl, threads, "the reference was not built on this machine")
+    try:
+        return ReferenceCPU(wl, threads)
+    except (OSError, RuntimeError) as exc:
+        return PortCPU(wl, threads, f"the reference build did not load: {exc}")
+
+
+def cpu_run(wl, seconds, threads):
+    """CPU implementation (cpu_impl) on all host cores: the workload's step
+    repeated for about `seconds`; returns (coefficients per second, outputs,
+    reps, implementation)."""
+    impl = cpu_impl(wl, threads)
     bufs = {"u": np.ascontiguousarray(wl.u), "o0": np.zeros_like(wl.u), "o1": np.zeros_like(wl.u)}
     times = []
     t_start = time.perf_counter()
@@ -345,11 +492,11 @@ def cpu_run(wl, seconds, threads):
         bufs["o1"][:] = 0
         t0 = time.perf_counter()
         for d, src, dst in wl.calls:
-            wl.cpu_call(o, bufs[src], bufs[dst], d)
+            impl.call(bufs[src], bufs[dst], d)
         times.append(time.perf_counter() - t0)
         if time.perf_counter() - t_start > seconds and len(times) >= 2:
             break
-    return wl.coefs_per_step / statistics.median(times), bufs, len(times)
+    return wl.coefs_per_step / statistics.median(times), bufs, len(times), impl
 
 
 def run_reference(args):
@@ -358,11 +505,7 @@ def run_reference(args):
         return 0
     wl = Workload(args.workload, args.N, args.maxs, 1, args.lagrange)
     threads = os.cpu_count() or 1
-    sys.path.insert(0, REPO)
-    from oracle import oracle
-
-    oracle.set_threads(threads)
-    o = wl.cpu_oracle(oracle)
+    impl = cpu_impl(wl, threads)
     bufs = {"u": np.ascontiguousarray(wl.u), "o0": np.zeros_like(wl.u), "o1": np.zeros_like(wl.u)}
 
     def step():
@@ -370,7 +513,7 @@ def run_reference(args):
         bufs["o1"][:] = 0
         t0 = time.perf_counter()
         for d, src, dst in wl.calls:
-            wl.cpu_call(o, bufs[src], bufs[dst], d)
+            impl.call(bufs[src], bufs[dst], d)
         return time.perf_counter() - t0
 
     for _ in range(args.warmup):
@@ -384,10 +527,9 @@ def run_reference(args):
         "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": wl.config(),
-        "cpu_baseline": {"value": value, "unit": "coef/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": "coef/s", "cores": threads, "kind": impl.kind,
                          "sample": f"full workload per step ({wl.coefs_per_step} coefficients), "
-                                   f"{args.steps} steps; oracle port of the reference algorithm "
-                                   "with OpenMP (the reference sources are not on this machine)"},
+                                   f"{args.steps} steps; {impl.note}"},
         "e2e": {"value": value, "unit": "coef/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -410,16 +552,8 @@ def autotune_plan(plan, calls, count, N):
     return {"seconds": round(time.perf_counter() - t0, 3), "shapes": shapes}
 
 
-def run_mixed(args):
-    """Mixed form against plain FP64 on the same inputs: single vector N = 2^22
-    (mixed_single) or 256 vectors of N = 16384 (mixed_batch), iid N(0,1), L2C and
-    C2L of the same input per step.  value = the mixed form's throughput."""
-    import ctypes
-
-    import torch
-
-    torch.cuda.set_device(0)
-    dev = torch.device("cuda", 0)
+def load_library():
+    """Build (if stale) and import the in-tree library front end."""
     sys.path.insert(0, PKG)
     import importlib.util
 
@@ -427,13 +561,29 @@ def run_mixed(args):
     bmod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(bmod)
     bmod.build()
-    import l2c_gb300 as l2c
+    import l2c_gb300
 
-    wl = Workload(args.workload, args.N, args.maxs, 1)
+    return l2c_gb300
+
+
+MIXED_FORM = ("f64 (mixed: far-field, leaf and transfer products on FP16 tensor cores from "
+              "exact 9-bit digit slices with exact integer recombination; band, Lambda and "
+              "output accumulation in FP64)")
+
+
+def compare_mixed(l2c, workload, N, maxs_mixed, steps, warmup, autotune, dev, torch):
+    """Mixed form against plain FP64 on the same inputs (single vector N = 2^22
+    or 256 vectors of N = 16384, iid N(0,1), seed 1; L2C and C2L of the same
+    input per step).  Plain plans at maxs 16, 32 and 64 (and the mixed plan's
+    own leaf bound) are each autotuned and timed; every output is compared with
+    the oracle port.  Returns the record: per plan ms, coef/s, launches and
+    phases; errors per direction; the speed-up against the fastest plain plan."""
+    import ctypes
+
+    wl = Workload(workload, N, maxs_mixed, 1)
     N, count = wl.N, wl.count
     du = torch.from_numpy(np.ascontiguousarray(wl.u)).to(dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    peak = measured_fp64_peak(torch, dev)
 
     def time_plan(plan):
         stream = torch.cuda.ExternalStream(plan.stream, device=dev)
@@ -451,18 +601,18 @@ def run_mixed(args):
             e1.record(stream)
             return e0, e1
 
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             step()
         plan.synchronize()
         l0 = l2c.cuda_abi().l2c_gpu_launch_count(plan._gpu)
-        evs = [step() for _ in range(args.steps)]
+        evs = [step() for _ in range(steps)]
         plan.synchronize()
         launches = l2c.cuda_abi().l2c_gpu_launch_count(plan._gpu) - l0
         ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
         # per-phase CUDA events in a separate pass (graph replay off while profiling)
         abi = l2c.cuda_abi()
         abi.l2c_gpu_profile(plan._gpu, 1)
-        nprof = max(1, min(args.steps, 20))
+        nprof = max(1, min(steps, 20))
         for _ in range(nprof):
             step()
         plan.synchronize()
@@ -476,40 +626,43 @@ def run_mixed(args):
 
     def time_e2e(plan):
         """The same step through execute_batched() with pinned host buffers
-        (input and zeroed outputs copied in, results copied back, per call)."""
+        (input and zeroed outputs read over the host link, results written
+        back, per call)."""
         hu = torch.from_numpy(np.ascontiguousarray(wl.u)).pin_memory()
         ho = [torch.zeros_like(hu).pin_memory(), torch.zeros_like(hu).pin_memory()]
         ts = []
-        for it in range(args.warmup + min(args.steps, 20)):
+        for it in range(warmup + min(steps, 20)):
             ho[0].zero_()
             ho[1].zero_()
             t0 = time.perf_counter()
             plan.execute_batched(hu, ho[0], 0, count, N, 1)
             plan.execute_batched(hu, ho[1], 1, count, N, 1)
-            if it >= args.warmup:
+            if it >= warmup:
                 ts.append(time.perf_counter() - t0)
         st = sum(ts) / len(ts)
         nbytes = 8 * wl.u.size
         return {"value": 2 * count * N / st, "unit": "coef/s", "h2d_bytes_per_step": 4 * nbytes,
                 "d2h_bytes_per_step": 2 * nbytes, "ms_per_step": st * 1e3}
 
-    clocks = ClockSampler(0)
-    clocks.start()
     results = {}
-    for name, maxs, mixed in (("plain_maxs64", 64, False), ("plain_maxs32", 32, False),
-                              ("mixed", args.maxs_mixed, True)):
+    e2e_mixed = None
+    plain_bounds = sorted({16, 32, 64, maxs_mixed})
+    for name, maxs, mixed in ([(f"plain_maxs{m}", m, False) for m in plain_bounds]
+                              + [("mixed", maxs_mixed, True)]):
+        t_plan0 = time.perf_counter()
         plan = l2c.Plan(N, maxs, mixed=mixed)
-        tuned = autotune_plan(plan, ((0,), (1,)), count, N) if args.autotune else None
+        plan_ms = (time.perf_counter() - t_plan0) * 1e3
+        tuned = autotune_plan(plan, ((0,), (1,)), count, N) if autotune else None
         ms, outs, launches, phases = time_plan(plan)
         results[name] = {"maxs": maxs, "s": plan.s, "L": plan.L, "ms_per_step": ms,
                          "value": 2 * count * N / (ms * 1e-3), "launches": launches,
                          "phases_ms_per_step": phases, "autotune": tuned,
+                         "create_fmm_ms": round(plan_ms, 3),
                          "flops": plan.flops(0) + plan.flops(1), "outs": outs}
         if mixed:
             e2e_mixed = time_e2e(plan)
         plan.close()
-    clk = clocks.stop()
-    # accuracy against the oracle port (FP64) on the same inputs
+    # accuracy against the oracle port (FP64) on the same inputs, every vector
     sys.path.insert(0, REPO)
     from oracle import oracle
 
@@ -524,31 +677,60 @@ def run_mixed(args):
                 o.execute(np.ascontiguousarray(wl.u[0]), want[0], d)
             else:
                 o.execute_batch(np.ascontiguousarray(wl.u), want, d, count, N)
-            e.append(float(np.max(np.abs(r["outs"][d] - want)) / np.max(np.abs(want))))
+            den = np.max(np.abs(want), axis=1)
+            e.append(float(np.max(np.max(np.abs(r["outs"][d] - want), axis=1) / den)))
+        o.close()
         errs[name] = {"l2c": e[0], "c2l": e[1]}
         del r["outs"]
     mixed = results["mixed"]
     best_plain = min((results[k]["ms_per_step"], k) for k in results if k.startswith("plain"))
-    fp64_flops_mixed = None
+    return {
+        "workload": (f"mixed vs plain FP64, {'single vector' if count == 1 else str(count) + ' vectors'} "
+                     f"of N={N}, iid N(0,1), L2C and C2L of the same input per step"),
+        "N": N, "vectors": count, "maxs_mixed": maxs_mixed, "steps": steps, "warmup": warmup,
+        "ms_per_step_mixed": mixed["ms_per_step"], "value_mixed": mixed["value"],
+        "ms_per_step_best_plain": best_plain[0], "best_plain": best_plain[1],
+        "speedup_vs_best_plain": best_plain[0] / mixed["ms_per_step"],
+        "speedup_vs_plain_maxs64": results["plain_maxs64"]["ms_per_step"] / mixed["ms_per_step"],
+        "max_rel_err_vs_oracle": errs,
+        "error_note": "relative max-norm per vector (max over the batch), per direction, "
+                      "against the oracle port (FP64) on the same inputs",
+        "plans": results, "e2e_mixed": e2e_mixed,
+        "l2_flush": "256 MiB write between steps", "dtype": MIXED_FORM,
+    }
+
+
+def run_mixed(args):
+    """--workload mixed_single | mixed_batch: a line whose value is the mixed
+    form's throughput, with the plain plans beside it (compare_mixed)."""
+    import torch
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    l2c = load_library()
+    peak = measured_fp64_peak(torch, dev)
+    clocks = ClockSampler(0)
+    clocks.start()
+    rec = compare_mixed(l2c, args.workload, args.N, args.maxs_mixed, args.steps, args.warmup,
+                        args.autotune, dev, torch)
+    clk = clocks.stop()
+    mixed = rec["plans"]["mixed"]
     line = {
         "metric": METRIC, "value": mixed["value"], "unit": "coef/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 (mixed: split-bf16 tensor-core far field, fp64 band)",
-        "data": "synthetic (seeded iid N(0,1))",
-        "config": {"workload": f"mixed vs plain FP64, {'single vector' if count == 1 else str(count) + ' vectors'} "
-                               f"of N={N}, L2C and C2L of the same input per step",
-                   "N": N, "vectors": count, "maxs_mixed": args.maxs_mixed,
-                   "l2_flush": "256 MiB write between steps"},
-        "plans": results,
-        "max_rel_err_vs_oracle": errs,
-        "speedup_mixed_vs_plain_maxs64": results["plain_maxs64"]["ms_per_step"] / mixed["ms_per_step"],
-        "speedup_mixed_vs_best_plain": best_plain[0] / mixed["ms_per_step"],
-        "best_plain": best_plain[1],
+        "dtype": MIXED_FORM, "data": "synthetic (seeded iid N(0,1))",
+        "config": {"workload": rec["workload"], "N": rec["N"], "vectors": rec["vectors"],
+                   "maxs_mixed": args.maxs_mixed, "l2_flush": "256 MiB write between steps"},
+        "plans": rec["plans"],
+        "max_rel_err_vs_oracle": rec["max_rel_err_vs_oracle"],
+        "speedup_mixed_vs_plain_maxs64": rec["speedup_vs_plain_maxs64"],
+        "speedup_mixed_vs_best_plain": rec["speedup_vs_best_plain"],
+        "best_plain": rec["best_plain"],
         "clocks": clk,
         "fp64_peak_tflops_measured": peak,
         "gpu_launches": int(mixed["launches"]),
-        "e2e": e2e_mixed,
+        "e2e": rec["e2e_mixed"],
     }
     print(json.dumps(line))
     return 0
@@ -572,6 +754,8 @@ def main():
     ap.add_argument("--lagrange", type=int, default=0, choices=[0, 1],
                     help="1: the nodal form (create_fmm's lagrange argument; single, batch)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true",
+                    help="leave out the mixed-vs-plain record of the default line")
     ap.add_argument("--autotune", type=int, default=1, choices=[0, 1],
                     help="tune each plan's launch choices for the timed call shapes first "
                          "(same bits under every choice; tuning time reported, not timed)")
@@ -599,14 +783,8 @@ def main():
     ranks = Ranks(world, "nccl", dev)
     barrier, max_over_ranks = ranks.barrier, ranks.max
 
-    sys.path.insert(0, PKG)
-    import importlib.util
-
-    spec = importlib.util.spec_from_file_location("l2c_pkg_build", os.path.join(PKG, "build.py"))
-    bmod = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(bmod)
     if rank == 0:
-        bmod.build()
+        load_library()
     barrier()
     import ctypes
 
@@ -742,10 +920,9 @@ def main():
     if ragged:
         total_flops = sum(plan.flops(d) for d, _, _ in wl.calls)
         achieved = total_flops / (ms_step * 1e-3) / 1e12
-        roof = {"bound": "tensor", "pipe": "fp64", "kernel": "whole step (all ragged kernels)",
+        roof = {"bound": "fp64", "pipe": "fp64", "kernel": "whole step (all ragged kernels)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": None,
-                "peak_source": "FP64 DGEMM measured in this run (cuBLAS float64 matmul 4096^3)"}
+                "traffic": None, "peak_source": FP64_PEAK_SOURCE}
     if "near" in phases_iso and L >= 1:
         nf = sum(near_flops(N, s, d) for d, _, _ in wl.calls) * count / len(wl.calls)
 
@@ -756,18 +933,19 @@ def main():
 
         flops_per_launch, avg_ms, achieved = band_rate(phases_iso)
         _, avg_ms_step, achieved_step = band_rate(phases)
-        # DRAM bytes per band launch from one ncu capture of this same command
-        # (dram__bytes_read.sum + dram__bytes_write.sum, mean of the L2C and C2L
-        # launches); other workloads were not captured.
+        # DRAM bytes per band launch from the committed ncu summary of this same
+        # command (dram__bytes_read.sum + dram__bytes_write.sum, mean of the L2C
+        # and C2L launches); other workloads were not captured.
         captured = (wl.name == "single" and N == 1 << 20 and maxs == 64
                     and args.precompute == 0 and args.lagrange == 0)
-        roof = {"bound": "tensor", "pipe": "fp64", "kernel": "k_near (near-field band)",
+        traffic = profile_traffic(BAND_PROFILE) if captured else None
+        roof = {"bound": "fp64", "pipe": "fp64", "kernel": "k_near (near-field band)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": 25.2e6 + 256 if captured else None,
+                "traffic": traffic,
                 "traffic_unit": "DRAM bytes per launch",
-                "traffic_source": "profiles/k_near_single_N1048576.md" if captured else None,
+                "traffic_source": BAND_PROFILE if traffic is not None else None,
                 "algorithmic_bytes_per_launch": 24 * N * count,
-                "peak_source": "FP64 DGEMM measured in this run (cuBLAS float64 matmul 4096^3)",
+                "peak_source": FP64_PEAK_SOURCE,
                 "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_ms,
                 "timing": "band launches timed with CUDA events on their stream, in a pass "
                           "of the same workload with the band on the plan's stream (the "
@@ -816,14 +994,28 @@ def main():
 
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        cpu_value, outs, reps = cpu_run(wl, args.cpu_seconds, threads)
+        cpu_value, outs, reps, impl = cpu_run(wl, args.cpu_seconds, threads)
         line["cpu_baseline"] = {
-            "value": cpu_value, "unit": "coef/s", "cores": threads, "kind": "port",
+            "value": cpu_value, "unit": "coef/s", "cores": threads, "kind": impl.kind,
             "sample": f"{reps} repetitions of the full step ({wl.coefs_per_step} coefficients), "
-                      "median; oracle port of the reference algorithm with OpenMP"}
+                      f"median; {impl.note}"}
         line["max_rel_err_vs_oracle"] = {
             name: float(np.max(np.abs(got[k] - outs[k])) / np.max(np.abs(outs[k])))
             for name, k in (("l2c", "o0"), ("c2l", "o1"))}
+        line["max_rel_err_vs"] = impl.note
+    if (rank == 0 and world == 1 and not ragged and not args.no_mixed
+            and wl.name == "single" and args.lagrange == 0):
+        # the metric's second half: mixed form against the fastest plain plan,
+        # on the two mixed-precision workloads, each with its own clock record
+        line["mixed"] = {}
+        for key, wname, n_mixed in (("batch", "mixed_batch", 16384),
+                                    ("single", "mixed_single", 1 << 22)):
+            clk_m = ClockSampler(local)
+            clk_m.start()
+            rec = compare_mixed(l2c, wname, n_mixed, args.maxs_mixed, min(args.steps, 20),
+                                args.warmup, args.autotune, dev, torch)
+            rec["clocks"] = clk_m.stop()
+            line["mixed"][key] = rec
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -27,10 +27,11 @@ typedef struct l2c_gpu_plan l2c_gpu_plan;
                                        the reference's `precompute`, leg2cheb.c:1108-1193):
                                        one FP64 FMA per band term instead of two ops */
 
-#define L2C_PLAN_MIXED 4u /* mixed form: leaf, transfer and far-field products as
-                                FP64-accurate split-BF16 tensor-core products (no
-                                FP64 instructions); near-field band, accumulation and
-                                scaling in FP64.  Leaf sizes s <= 64. */
+#define L2C_PLAN_MIXED 4u /* mixed form: leaf, transfer and far-field products on
+                                FP16 tensor cores, FP64-accurate (operands split into
+                                exact 9-bit digit slices, products recombined exactly
+                                in integers; no FP64 instructions); near-field band,
+                                accumulation and scaling in FP64.  Leaf sizes s <= 64. */
 
 #define L2C_PLAN_NODAL 8u /* nodal (Lagrange) form, create_fmm's lagrange = 1
                                 (leg2cheb.c:997-1031, 1076-1100): leaf matrices of
@@ -129,18 +130,25 @@ size_t l2c_gpu_plan_copy(const l2c_gpu_plan *plan, int which, double *dst, size_
 /* One transform that allocates no device memory (no counterpart in the
  * reference).  For callers that cannot allocate at transform time -- an
  * application that reserves the device for its own memory pool, a solver that
- * must not risk allocation latency or failure inside a time step.  Same
- * kernels and results as l2c_gpu_execute (count = 1), but the working buffers
+ * must not risk allocation latency or failure inside a time step.  It runs the
+ * plain FP64 kernels of l2c_gpu_execute (count = 1), but the working buffers
  * live in a fixed array of L2C_NOALLOC_SCRATCH_DOUBLES doubles (4 MiB) that
  * every GPU loading this library holds until the process exits; the plan's own
  * tables are built beforehand by l2c_gpu_plan_create, as set-up.
  *   - in and out must be device pointers; FMM plans only (L >= 1).
  *   - a plan needing more than the fixed array (2N + 144 N_b doubles; e.g.
  *     N up to about 1.2e5 at maxs = 64) is rejected with an error message.
+ *   - plain and nodal plans give the same results as l2c_gpu_execute.  On a
+ *     plan made with L2C_PLAN_MIXED it still runs the FP64 far field (such a
+ *     plan keeps the FP64 blocks; its tensor-core fragments are built on the
+ *     first batched call, which allocates), so the results agree with
+ *     l2c_gpu_execute within 1e-14 but not bit for bit, and a vector holding
+ *     an Inf or NaN gets the plain form's pattern of non-finite outputs.
  *   - the first call on a device looks up the array's device address
  *     (cudaGetSymbolAddress), so make that first call before any stream capture.
- *   - calls on one device are serialised and return after the work has
- *     finished, since all of them share the array.
+ *   - calls on one device are serialised, since all of them share the array:
+ *     each call waits on the host until its work has finished on the GPU (it
+ *     synchronises the plan's stream) before it returns.
  * Returns the reference's flop count, 0 on failure (l2c_gpu_last_error()). */
 #define L2C_NOALLOC_SCRATCH_DOUBLES (1u << 19)
 size_t l2c_gpu_execute_noalloc(l2c_gpu_plan *plan, const double *in, double *out,

@@ -66,6 +66,7 @@ def build(force=False, verbose=False):
     if force or _stale(HOST_LIB, HOST_DEPS + [CUDA_LIB]):
         cc = os.environ.get("CC", "gcc")
         cmd = [cc, "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-Wall",
+               "-Wl,-soname,libleg2cheb.so",
                "-I", INCLUDE, "-o", HOST_LIB + ".tmp", *HOST_SOURCES,
                "-L", LIB, "-l:libl2c_cuda.so", "-Wl,-rpath,$ORIGIN", "-lm"]
         out = _run(cmd)

@@ -1,7 +1,8 @@
 """Generate golden vectors by running the UNMODIFIED reference.
 
-Needs the reference tree (default /root/reference) built into oracle/_ref by
-``make -C oracle ref``.  Writes tests/golden/golden.npz, committed so the
+Needs the reference built into oracle/_ref by ``make -C oracle ref`` (from the
+reference tree given as REF=..., by default ``reference`` beside this
+repository's root directory).  Writes tests/golden/golden.npz, committed so the
 tests run without the reference (on the GPU machine it does not exist).
 
 Contents (all produced by the reference's own code):

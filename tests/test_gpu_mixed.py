@@ -1,5 +1,6 @@
-"""The mixed form (L2C_PLAN_MIXED): leaf, transfer and far-field products as
-split-BF16 tensor-core products with exact integer recombination.  Same
+"""The mixed form (L2C_PLAN_MIXED): leaf, transfer and far-field products on
+FP16 tensor cores from exact 9-bit digit slices of the FP64 operands, with
+exact integer recombination.  Same
 accuracy bar as the FP64 path: 1e-14 relative max-norm against the oracle,
 per direction, on single vectors and on batches (where the far-field blocks
 also run on the tensor cores)."""
