@@ -571,7 +571,8 @@ MIXED_FORM = ("f64 (mixed: far-field, leaf and transfer products on FP16 tensor 
               "output accumulation in FP64)")
 
 
-def compare_mixed(l2c, workload, N, maxs_mixed, steps, warmup, autotune, dev, torch):
+def compare_mixed(l2c, workload, N, maxs_mixed, steps, warmup, autotune, dev, torch,
+                  only=None):
     """Mixed form against plain FP64 on the same inputs (single vector N = 2^22
     or 256 vectors of N = 16384, iid N(0,1), seed 1; L2C and C2L of the same
     input per step).  Plain plans at maxs 16, 32 and 64 (and the mixed plan's
@@ -649,6 +650,8 @@ def compare_mixed(l2c, workload, N, maxs_mixed, steps, warmup, autotune, dev, to
     plain_bounds = sorted({16, 32, 64, maxs_mixed})
     for name, maxs, mixed in ([(f"plain_maxs{m}", m, False) for m in plain_bounds]
                               + [("mixed", maxs_mixed, True)]):
+        if only and name not in only:
+            continue
         t_plan0 = time.perf_counter()
         plan = l2c.Plan(N, maxs, mixed=mixed)
         plan_ms = (time.perf_counter() - t_plan0) * 1e3
@@ -682,6 +685,8 @@ def compare_mixed(l2c, workload, N, maxs_mixed, steps, warmup, autotune, dev, to
         o.close()
         errs[name] = {"l2c": e[0], "c2l": e[1]}
         del r["outs"]
+    if "mixed" not in results or not any(k.startswith("plain") for k in results):
+        return {"plans": results, "max_rel_err_vs_oracle": errs, "e2e_mixed": e2e_mixed}
     mixed = results["mixed"]
     best_plain = min((results[k]["ms_per_step"], k) for k in results if k.startswith("plain"))
     return {
@@ -711,9 +716,14 @@ def run_mixed(args):
     peak = measured_fp64_peak(torch, dev)
     clocks = ClockSampler(0)
     clocks.start()
+    only = set(args.mixed_plans.split(",")) if args.mixed_plans else None
     rec = compare_mixed(l2c, args.workload, args.N, args.maxs_mixed, args.steps, args.warmup,
-                        args.autotune, dev, torch)
+                        args.autotune, dev, torch, only)
     clk = clocks.stop()
+    if "speedup_vs_best_plain" not in rec:  # a subset of the plans (profiling runs)
+        print(json.dumps({"plans": rec["plans"], "errors": rec["max_rel_err_vs_oracle"],
+                          "clocks": clk}))
+        return 0
     mixed = rec["plans"]["mixed"]
     line = {
         "metric": METRIC, "value": mixed["value"], "unit": "coef/s", "n_gpus": 1,
@@ -744,6 +754,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="single",
                     choices=["single", "batch", "ragged", "mixed_single", "mixed_batch"])
+    ap.add_argument("--mixed-plans", default=None,
+                    help="mixed_* workloads: comma-separated subset of the plans to time "
+                         "(plain_maxs16, plain_maxs32, plain_maxs64, mixed), for profiling")
     ap.add_argument("--maxs-mixed", type=int, default=16,
                     help="leaf size bound of the mixed-form plan (mixed_* workloads)")
     ap.add_argument("--N", type=int, default=None)

@@ -1093,6 +1093,244 @@ inline unsigned blocks_for(long long n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
 }
 
+// ---------------------------------------------------------------------------
+// Band of a batch as dense register tiles (batches of at least BT_MIN_COUNT
+// vectors, leaf size s a multiple of 4; the band sums of directM / directL,
+// leg2cheb.c:236-302 and :392-459).
+//
+// For a full block b < nL-1 and parity p the band is a small dense product
+//   Y[i'][v] = sum_{m' = i' .. 2s-1} W'[m'][i'] X[m'][v],
+// output j = b h + 2 i' + p, source x[v][b h + 2 m' + p], and the weight
+// W'[m'][i'] = near_weight(k = m' - i', j) (the term k of output j).  A CTA of
+// BT_WARPS warps owns a chunk of VCH = 32 C vectors and walks a run of
+// consecutive blocks: block b reads the two half windows x[v][(b + e) h + [0, h)]
+// (e = 0, 1), which pass through a ring of three shared-memory slots (rows of
+// 2s + 1 doubles, odd, so the lanes of a warp hit distinct banks), each filled
+// by cp.async one block ahead.  Every lane owns C vectors; every warp owns row
+// groups (4 consecutive rows i' of one parity) dealt in a snake order of their
+// trip counts 2s - i'0, so the warps run equal numbers of FMAs.  A thread
+// thus holds a 4 x C tile: per m' four weights (one address for the whole
+// warp: a table entry or, without the table, the same products formed on the
+// fly) and C shared-memory loads feed 4 C independent FMAs.  With this much
+// independent work a few warps keep the FP64 pipe busy, so the kernel runs on
+// one CTA per SM and leaves the SM's other pipes, most of its registers and
+// shared memory to the far-field chain beside it.  Each output sums its terms
+// in order of k in one FMA chain from zero, then y = out_in + sum, staged
+// through the slot the block no longer needs and written a row at a time.
+// The last (ragged) block is k_near's (jbeg = (nL - 1) h).
+// ---------------------------------------------------------------------------
+constexpr int BT_WARPS = 4;
+constexpr int BT_THREADS = 32 * BT_WARPS;
+constexpr long long BT_MIN_COUNT = 64;
+
+// Vectors per lane: two while a chunk's three slots stay near 100 KB.
+__host__ __device__ inline int band_tile_c(long long s) { return s <= 32 ? 2 : 1; }
+inline size_t band_tile_smem(long long s) {
+  return (size_t)3 * 32 * band_tile_c(s) * (2 * s + 1) * sizeof(double);
+}
+// Entries of the dense weight table: (nL - 1) blocks x 2 parities x 2s x s.
+inline size_t band_tile_table_size(size_t N, size_t s) {
+  const size_t h = 2 * s, nL = N / h;
+  return nL >= 2 ? (nL - 1) * 4 * s * s : 0;
+}
+
+// Weight of row r of the group at i'0 for m' (r <= m' - i'0 is the caller's).
+__device__ __forceinline__ double band_tile_weight(int c2l, long long mp, long long ip,
+                                                   long long j, const double *__restrict__ a,
+                                                   const double *__restrict__ an,
+                                                   const double *__restrict__ dn) {
+  return near_weight(c2l, mp - ip, j, a, an, dn);
+}
+
+// Plan time: the dense table W'[b][p][m'][i'] (zero where m' < i').
+__global__ void k_band_tile_weights(double *__restrict__ Wt, const double *__restrict__ a,
+                                    const double *__restrict__ an,
+                                    const double *__restrict__ dn, Geo g, int c2l) {
+  const long long n = (g.nL - 1) * 4 * g.s * g.s;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const long long ip = idx % g.s, mp = (idx / g.s) % (2 * g.s), bp = idx / (2 * g.s * g.s);
+  const long long b = bp >> 1, p = bp & 1;
+  const long long j = b * g.h + 2 * ip + p;
+  Wt[idx] = mp >= ip ? band_tile_weight(c2l, mp, ip, j, a, an, dn) : 0.0;
+}
+
+template <int C, bool TAB>
+__device__ __forceinline__ void band_tile_step(const double *__restrict__ xs, int ld,
+                                               const double *__restrict__ Wr, long long mp,
+                                               long long ip0, long long j0, int c2l,
+                                               const double *__restrict__ a,
+                                               const double *__restrict__ an,
+                                               const double *__restrict__ dn, int rows,
+                                               double (&acc)[4][C]) {
+  double w[4];
+  if (TAB) {
+    const double2 q0 = __ldg(reinterpret_cast<const double2 *>(Wr));
+    const double2 q1 = __ldg(reinterpret_cast<const double2 *>(Wr) + 1);
+    w[0] = q0.x;
+    w[1] = q0.y;
+    w[2] = q1.x;
+    w[3] = q1.y;
+  } else {
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+      w[r] = r < rows ? band_tile_weight(c2l, mp, ip0 + r, j0 + 2 * r, a, an, dn) : 0.0;
+  }
+  double xv[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) xv[c] = xs[c * 32 * ld];
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+    if (r < rows)
+#pragma unroll
+      for (int c = 0; c < C; c++) acc[r][c] = fma(w[r], xv[c], acc[r][c]);
+}
+
+// One row group (parity p, rows i'0 .. i'0 + 3) of block b for the lane's C
+// vectors; sA / sB: the lane's rows in the two half-window slots.
+template <int C, bool TAB>
+__device__ __forceinline__ void band_tile_group(const double *__restrict__ sA,
+                                                const double *__restrict__ sB, int ld,
+                                                const double *__restrict__ Wt, const Geo &g,
+                                                long long b, int p, long long ip0, int c2l,
+                                                const double *__restrict__ a,
+                                                const double *__restrict__ an,
+                                                const double *__restrict__ dn,
+                                                double (&acc)[4][C]) {
+  const long long s = g.s, j0 = b * g.h + 2 * ip0 + p;
+  const double *Wb = TAB ? Wt + ((b * 2 + p) * 2 * s) * s + ip0 : nullptr;
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+#pragma unroll
+    for (int c = 0; c < C; c++) acc[r][c] = 0.0;
+  // m' = i'0 .. i'0 + 2: only rows r <= m' - i'0 have a term (i'0 + 3 < s)
+#pragma unroll
+  for (int t = 0; t < 3; t++) {
+    const long long mp = ip0 + t;
+    band_tile_step<C, TAB>(sA + 2 * mp + p, ld, TAB ? Wb + mp * s : nullptr, mp, ip0, j0, c2l,
+                           a, an, dn, t + 1, acc);
+  }
+#pragma unroll 4
+  for (long long mp = ip0 + 3; mp < s; mp++)
+    band_tile_step<C, TAB>(sA + 2 * mp + p, ld, TAB ? Wb + mp * s : nullptr, mp, ip0, j0, c2l,
+                           a, an, dn, 4, acc);
+#pragma unroll 4
+  for (long long mp = s; mp < 2 * s; mp++)
+    band_tile_step<C, TAB>(sB + 2 * (mp - s) + p, ld, TAB ? Wb + mp * s : nullptr, mp, ip0, j0,
+                           c2l, a, an, dn, 4, acc);
+}
+
+// Copies of half window hw of the chunk's vectors into slot dst (zeros for
+// vectors past the batch).
+__device__ __forceinline__ void band_tile_fill(double *dst, int ld, const double *__restrict__ x,
+                                               const Geo &g, long long v0, int vch,
+                                               long long hw) {
+  const int n = vch * (int)g.h;
+  for (int idx = threadIdx.x; idx < n; idx += BT_THREADS) {
+    const int vl = idx / (int)g.h, m = idx - vl * (int)g.h;
+    const long long v = v0 + vl;
+    const bool live = v < g.count;
+    l2c_oz::cp_async8(dst + vl * ld + m, live ? x + v * g.N + hw * g.h + m : x, live ? 8 : 0);
+  }
+}
+
+// Work unit u: vector chunk u % nchunk, blocks [seg bseg, (seg + 1) bseg) of
+// the nL - 1 full ones, seg = u / nchunk (a segment's chunks run side by side,
+// so its weights are read from L2 by all of them).  GPW row groups per warp:
+// warp w takes groups q = 8 t' + w and 8 t' + 7 - w (t' = 0, 1, ...), q < s/2.
+template <int C, int GPW, bool TAB>
+__global__ void __launch_bounds__(BT_THREADS)
+    k_band_tile(const double *__restrict__ x, const double *out, double *__restrict__ y,
+                const double *__restrict__ Wt, const double *__restrict__ a,
+                const double *__restrict__ an, const double *__restrict__ dn, Geo g, int c2l,
+                long long nchunk, long long bseg) {
+  extern __shared__ __align__(16) double bt_smem[];
+  pdl_wait();
+  pdl_trigger();
+  constexpr int VCH = 32 * C;
+  const int ld = 2 * (int)g.s + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long nfull = g.nL - 1, nseg = (nfull + bseg - 1) / bseg;
+  const int groups = (int)g.s / 2;  // row groups: 2 parities x s/4
+  for (long long u = blockIdx.x; u < nchunk * nseg; u += gridDim.x) {
+    const long long v0 = (u % nchunk) * VCH, seg = u / nchunk;
+    const long long b0 = seg * bseg, b1 = b0 + bseg < nfull ? b0 + bseg : nfull;
+    // half windows b0 and b0 + 1 (block b0 needs both)
+    band_tile_fill(bt_smem + (b0 % 3) * VCH * ld, ld, x, g, v0, VCH, b0);
+    l2c_oz::cp_commit();
+    band_tile_fill(bt_smem + ((b0 + 1) % 3) * VCH * ld, ld, x, g, v0, VCH, b0 + 1);
+    l2c_oz::cp_commit();
+    for (long long b = b0; b < b1; b++) {
+      // half window b + 2 for the next block, one block ahead
+      if (b + 2 <= b1)
+        band_tile_fill(bt_smem + ((b + 2) % 3) * VCH * ld, ld, x, g, v0, VCH, b + 2);
+      l2c_oz::cp_commit();
+      l2c_oz::cp_wait1();  // halves b and b + 1 have landed
+      __syncthreads();
+      double *sA = bt_smem + (b % 3) * VCH * ld;
+      const double *sB = bt_smem + ((b + 1) % 3) * VCH * ld;
+      double res[GPW][4][C];
+#pragma unroll
+      for (int t = 0; t < GPW; t++) {
+        const int q = 8 * (t >> 1) + ((t & 1) ? 2 * BT_WARPS - 1 - warp : warp);
+        if (q < groups)
+          band_tile_group<C, TAB>(sA + lane * ld, sB + lane * ld, ld, Wt, g, b, q & 1,
+                                  4LL * (q >> 1), c2l, a, an, dn, res[t]);
+      }
+      __syncthreads();  // every warp is done reading slots A and B
+      // the sums, staged in slot A (its inputs are no longer needed)
+#pragma unroll
+      for (int t = 0; t < GPW; t++) {
+        const int q = 8 * (t >> 1) + ((t & 1) ? 2 * BT_WARPS - 1 - warp : warp);
+        if (q < groups)
+#pragma unroll
+          for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < C; c++)
+              sA[(lane + 32 * c) * ld + 2 * (4 * (q >> 1) + r) + (q & 1)] = res[t][r][c];
+      }
+      __syncthreads();
+      // y = out_in + band, a row of h outputs per vector
+      const int n = VCH * (int)g.h;
+      for (int idx = threadIdx.x; idx < n; idx += BT_THREADS) {
+        const int vl = idx / (int)g.h, i = idx - vl * (int)g.h;
+        const long long v = v0 + vl;
+        if (v < g.count) {
+          const long long j = b * g.h + i;
+          y[v * g.N + j] = out[v * g.dist + j * g.stride] + sA[vl * ld + i];
+        }
+      }
+      __syncthreads();  // slot A is refilled next
+    }
+    l2c_oz::cp_wait0();
+    __syncthreads();
+  }
+}
+
+// Whether a batch's band takes k_band_tile: count >= BT_MIN_COUNT, s a
+// multiple of 8 up to 64, at least one full block.
+inline bool band_tile_ok(long long s, long long nL, long long count) {
+  return count >= BT_MIN_COUNT && s % 8 == 0 && s >= 16 && s <= 64 && nL >= 2;
+}
+
+template <bool TAB>
+using band_tile_fn = void (*)(const double *, const double *, double *, const double *,
+                              const double *, const double *, const double *, Geo, int,
+                              long long, long long);
+
+template <bool TAB>
+band_tile_fn<TAB> band_tile_kernel(long long s) {
+  switch (s / 8) {
+    case 2: return k_band_tile<2, 2, TAB>;
+    case 3: return k_band_tile<2, 3, TAB>;
+    case 4: return k_band_tile<2, 4, TAB>;
+    case 5: return k_band_tile<1, 5, TAB>;
+    case 6: return k_band_tile<1, 6, TAB>;
+    case 7: return k_band_tile<1, 7, TAB>;
+    default: return k_band_tile<1, 8, TAB>;
+  }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1917,6 +2155,10 @@ struct l2c_gpu_plan {
   cudaStream_t stream2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double *Wnear[2] = {nullptr, nullptr};  // precomputed band weights (optional)
+  // dense band weights of the full blocks for k_band_tile (built on first use)
+  double *Wtile[2] = {nullptr, nullptr};
+  int band_tile = -1;  // batches' band as dense register tiles: -1 when eligible, 0 never
+  int sms = 152;       // multiprocessors of the plan's device
   bool precompute = false;  // created with L2C_PLAN_PRECOMPUTE_NEAR
   bool use_w = false;       // this call's band reads Wnear (see TuneCfg::wtab)
   // nodal (Lagrange) form: T holds barycentric interpolation weights, A the
@@ -2267,7 +2509,7 @@ cudaError_t sweep_down(double *c, const Geo &g, const TreePlan &t, cudaStream_t 
 cudaError_t launch_near(const double *x, const double *out, double *y, const double *a,
                         const double *an, const double *dn, const double *W, Geo g, int c2l,
                         cudaStream_t st, bool pair, unsigned max_ctas, int max_vb,
-                        bool pdl = false, int threads = 256) {
+                        bool pdl = false, int threads = 256, long long jbeg = 0) {
   long long v = 0;
   while (v < g.count) {
     const long long left = g.count - v;
@@ -2280,10 +2522,10 @@ cudaError_t launch_near(const double *x, const double *out, double *y, const dou
     const double *os = out + v * g.dist;
     double *ys = y + v * g.N;
     if (!pair) {
-      unsigned grid = (unsigned)(((g.N + threads - 1) / threads) * groups);
+      unsigned grid = (unsigned)(((g.N - jbeg + threads - 1) / threads) * groups);
       if (max_ctas) grid = std::min(grid, max_ctas);
       auto *kern = vb == 8 ? k_near<8> : vb == 4 ? k_near<4> : vb == 2 ? k_near<2> : k_near<1>;
-      launch_k(pdl, kern, grid, threads, 0, st, xs, os, ys, a, an, dn, W, gg, c2l, 0LL);
+      launch_k(pdl, kern, grid, threads, 0, st, xs, os, ys, a, an, dn, W, gg, c2l, jbeg);
       const cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
       v += groups * vb;
@@ -2303,6 +2545,46 @@ cudaError_t launch_near(const double *x, const double *out, double *y, const dou
     v += groups * vb;
   }
   return cudaSuccess;
+}
+
+// Whether this call's band runs as k_band_tile (full blocks) + k_near (last block).
+bool use_band_tile(const l2c_gpu_plan *p, size_t count) {
+  return p->band_tile != 0 && p->L > 0 && band_tile_ok((long long)p->s, (long long)p->nL,
+                                                       (long long)count);
+}
+
+// Band of a batch through k_band_tile (the full blocks; Wt: its dense table or
+// nullptr for weights formed on the fly) and k_near (the last block, weights
+// formed on the fly: the same products, so the same bits).  Work units: the
+// run of blocks per unit (bseg) is the one whose rounds of units over the grid
+// finish first, counting half a block for the extra half window a unit loads.
+cudaError_t launch_band_tile(const l2c_gpu_plan *p, const double *x, const double *out,
+                             double *y, const double *Wt, Geo g, int c2l, cudaStream_t st,
+                             unsigned max_ctas, bool pdl) {
+  const long long VCH = 32LL * band_tile_c(g.s);
+  const long long nchunk = (g.count + VCH - 1) / VCH, nfull = g.nL - 1;
+  const long long grid_cap = max_ctas ? (long long)max_ctas : 2LL * p->sms;
+  long long best_seg = 1;
+  double best = 1e300;
+  for (long long bseg = 1; bseg <= std::min<long long>(nfull, 16); bseg++) {
+    const long long units = nchunk * ((nfull + bseg - 1) / bseg);
+    const long long grid = std::min(units, grid_cap);
+    const double t = (double)((units + grid - 1) / grid) * ((double)bseg + 0.5);
+    if (t < best) {
+      best = t;
+      best_seg = bseg;
+    }
+  }
+  const long long units = nchunk * ((nfull + best_seg - 1) / best_seg);
+  const unsigned grid = (unsigned)std::min(units, grid_cap);
+  auto *kern = Wt ? band_tile_kernel<true>(g.s) : band_tile_kernel<false>(g.s);
+  launch_k(pdl, kern, grid, BT_THREADS, band_tile_smem(g.s), st, x, out, y, Wt,
+           (const double *)p->a, (const double *)p->an, (const double *)p->dn, g, c2l, nchunk,
+           best_seg);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_near(x, out, y, p->a, p->an, p->dn, nullptr, g, c2l, st, false, 0, 8, pdl, 256,
+                     (g.nL - 1) * g.h);
 }
 
 // Pairs pay off when a warp's outputs have very unequal term counts (small
@@ -2531,7 +2813,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaGetLastError());
     x = p->x;
   }
-  const double *W = p->use_w ? p->Wnear[dir] : nullptr;
+  const double *W = p->use_w && !use_band_tile(p, count) ? p->Wnear[dir] : nullptr;
   if (near_only) {
     {
       PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, 8));
@@ -2559,7 +2841,12 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     if (ov && (cudaEventRecord(p->ev_fork, st) != cudaSuccess ||
                cudaStreamWaitEvent(st2, p->ev_fork, 0) != cudaSuccess))
       return false;
-    {
+    if (use_band_tile(p, count)) {
+      PhaseScope ps(p, L2C_PHASE_NEAR, 1 + near_launch_count(count, 8), stn);
+      if (launch_band_tile(p, x, out, p->y, p->use_w ? p->Wtile[dir] : nullptr, g, c2l, stn,
+                           ov ? p->near_ctas : 0, (sc.pdl & 2) && !ov) != cudaSuccess)
+        return false;
+    } else {
       PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, ov ? p->near_vb : 8), stn);
       if (launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, near_pair(p),
                       ov ? p->near_ctas : 0, ov ? p->near_vb : 8, (sc.pdl & 2) && !ov,
@@ -2666,6 +2953,24 @@ bool ensure_near_table(l2c_gpu_plan *p, size_t dir) {
   return cudaGetLastError() == cudaSuccess;
 }
 
+// The dense band weights of one direction for k_band_tile, built on first use
+// (outside any capture).  The same products as the compact table, so the band
+// gives the same bits with either table or none.
+bool ensure_band_tile_table(l2c_gpu_plan *p, size_t dir) {
+  if (p->Wtile[dir]) return true;
+  const size_t nw = band_tile_table_size(p->N, p->s);
+  if (cudaMalloc(&p->Wtile[dir], nw * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    p->Wtile[dir] = nullptr;
+    set_err("cudaMalloc of the tiled band weight table failed");
+    return false;
+  }
+  Geo g = make_geo(p, 1, p->N, 1);
+  k_band_tile_weights<<<blocks_for((long long)nw, 256), 256, 0, p->stream>>>(
+      p->Wtile[dir], p->a, p->an, p->dn, g, (int)dir);
+  return cudaGetLastError() == cudaSuccess;
+}
+
 size_t shape_dist(size_t count, size_t dist) { return count > 1 ? dist : 0; }
 
 const TunedShape *tuned_for(const l2c_gpu_plan *p, size_t dir, size_t count, size_t dist,
@@ -2689,7 +2994,11 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     const TuneCfg &c = p->forced ? *p->forced : ts ? ts->cfg : p->base;
     cfg_apply(p, c);
     p->use_w = wants_table(p, c, count);
-    if (p->use_w && !ensure_near_table(p, dir)) return 0;
+    if (p->use_w && use_band_tile(p, count)) {
+      if (!ensure_band_tile_table(p, dir)) return 0;
+    } else if (p->use_w && !ensure_near_table(p, dir)) {
+      return 0;
+    }
     if (p->use_w) p->cfg_sig |= 1ull << 63;
   }
   if (!ensure_scratch(p, count)) return 0;
@@ -3066,6 +3375,8 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_NEAR_THREADS"))
     p->near_threads = std::atoi(env) == 128 ? 128 : 256;
   if (const char *env = std::getenv("L2C_NEAR_PAIR")) p->near_pair = env[0] == '1' ? 1 : 0;
+  if (const char *env = std::getenv("L2C_BAND_TILE")) p->band_tile = env[0] == '0' ? 0 : -1;
+  PCK(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device));
   if (const char *env = std::getenv("L2C_PDL")) p->pdl = std::max(0, std::atoi(env));
   if (const char *env = std::getenv("L2C_CHAIN_PRIO")) p->chain_prio_mode = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_MZ_NBUF")) p->oz_nbuf = env[0] == '1' ? 1 : 2;
@@ -3305,6 +3616,13 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
       L2C_MZ_ATTR(5) L2C_MZ_ATTR(6) L2C_MZ_ATTR(7) L2C_MZ_ATTR(8)
 #undef L2C_MZ_ATTR
     }
+    if (band_tile_ok((long long)s, (long long)p->nL, BT_MIN_COUNT)) {
+      // the tiled band's three half-window slots can pass the 48 KB default
+      const cudaFuncAttribute smax = cudaFuncAttributeMaxDynamicSharedMemorySize;
+      const int bytes = (int)band_tile_smem((long long)s);
+      PCK(cudaFuncSetAttribute(band_tile_kernel<true>((long long)s), smax, bytes));
+      PCK(cudaFuncSetAttribute(band_tile_kernel<false>((long long)s), smax, bytes));
+    }
     if (flags & L2C_PLAN_PRECOMPUTE_NEAR) {
       const size_t nw = near_table_size(N, s);
       Geo g = make_geo(p, 1, N, 1);
@@ -3341,7 +3659,7 @@ void l2c_gpu_plan_destroy(l2c_gpu_plan *p) {
   if (p->ev_join) cudaEventDestroy(p->ev_join);
   if (p->stream2) cudaStreamDestroy(p->stream2);
   double *bufs[] = {p->a, p->an, p->dn, p->A[0], p->A[1], p->T, p->x, p->y, p->w, p->c,
-                    p->st_in, p->st_out, p->Wnear[0], p->Wnear[1]};
+                    p->st_in, p->st_out, p->Wnear[0], p->Wnear[1], p->Wtile[0], p->Wtile[1]};
   for (double *b : bufs)
     if (b) cudaFree(b);
   void *obufs[] = {p->oz_lu,     p->oz_tu,     p->oz_td,      p->oz_ld,      p->oz_lum,

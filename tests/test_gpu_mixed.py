@@ -96,13 +96,14 @@ def test_mixed_rejects_large_leaves(lib):
 
 
 @pytest.mark.parametrize("mixed", [False, True])
-@pytest.mark.parametrize("count", [1, 16])
+@pytest.mark.parametrize("count", [1, 16, 64])
 def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
     """Programmatic dependent launch, the band on the second stream, graph
     replay, the tile buffer depth, the chain's scheduling priority and the
     band's CTA size, vectors per thread, grid cap, weight table and fork point
     change only when work runs, never what it computes: every setting gives
-    the same bits as the default plan."""
+    the same bits as the default plan (count = 64: the band as dense register
+    tiles, with its table or weights formed on the fly)."""
     N = 16384
     x = np.ascontiguousarray(make_input(N * count, "gauss", 11).reshape(count, N))
 
@@ -178,3 +179,31 @@ def test_non_finite_inputs(lib, orc, bad):
         assert np.all(~np.isfinite(got[2]) >= want), d
         for v in (0, 1, 3, 4, 5):
             assert np.array_equal(got[v], clean[v]), (d, v)
+
+
+@pytest.mark.parametrize("N,maxs,count", [(16384, 16, 64), (16384, 16, 100), (4096, 32, 70),
+                                          (1024, 64, 96), (6000, 24, 65), (20000, 40, 64)])
+def test_band_tiles_vs_oracle(lib, orc, monkeypatch, N, maxs, count):
+    """Batches of 64 and more vectors take the band as dense register tiles
+    (full blocks) plus the per-output kernel (last block); chunks of 64 or 32
+    vectors, the last one partly filled.  Every vector against the oracle, and
+    the same batch with the tiles switched off (L2C_BAND_TILE=0) within the
+    same bar."""
+    x = np.ascontiguousarray(make_input(N * count, "gauss", count + N).reshape(count, N))
+    o = orc.Oracle(N, maxs, 2)
+    outs = {}
+    for env in ("1", "0"):
+        with monkeypatch.context() as m:
+            m.setenv("L2C_BAND_TILE", env)
+            p = lib.Plan(N, maxs)
+        for d in (0, 1):
+            out = np.zeros_like(x)
+            p.execute_batched(x, out, d, count, N, 1)
+            outs[env, d] = out
+        p.close()
+    for d in (0, 1):
+        want = np.zeros_like(x)
+        o.execute_batch(x, want, d, count, N)
+        for v in range(count):
+            assert relerr(outs["1", d][v], want[v]) <= TOL, (d, v)
+            assert relerr(outs["1", d][v], outs["0", d][v]) <= TOL, (d, v)
