@@ -1095,8 +1095,8 @@ inline unsigned blocks_for(long long n, int threads) {
 
 // ---------------------------------------------------------------------------
 // Band of a batch as dense register tiles (batches of at least BT_MIN_COUNT
-// vectors, leaf size s a multiple of 4; the band sums of directM / directL,
-// leg2cheb.c:236-302 and :392-459).
+// vectors, leaf size s a multiple of 8 in [16, 64]; the band sums of directM /
+// directL, leg2cheb.c:236-302 and :392-459).
 //
 // For a full block b < nL-1 and parity p the band is a small dense product
 //   Y[i'][v] = sum_{m' = i' .. 2s-1} W'[m'][i'] X[m'][v],
@@ -1106,40 +1106,45 @@ inline unsigned blocks_for(long long n, int threads) {
 // consecutive blocks: block b reads the two half windows x[v][(b + e) h + [0, h)]
 // (e = 0, 1), which pass through a ring of three shared-memory slots (rows of
 // 2s + 1 doubles, odd, so the lanes of a warp hit distinct banks), each filled
-// by cp.async one block ahead.  Every lane owns C vectors; every warp owns row
-// groups (4 consecutive rows i' of one parity) dealt in a snake order of their
-// trip counts 2s - i'0, so the warps run equal numbers of FMAs.  A thread
-// thus holds a 4 x C tile: per m' four weights (one address for the whole
-// warp: a table entry or, without the table, the same products formed on the
-// fly) and C shared-memory loads feed 4 C independent FMAs.  With this much
+// by cp.async one block ahead; at s = 16 the block's weights come the same way
+// (two buffers), at larger s from L2.  Every lane owns C vectors; every warp
+// owns row groups (4 consecutive rows i' of one parity) dealt in a snake order
+// of their trip counts 2s - i'0, so the warps run equal numbers of FMAs.  A
+// thread thus holds a 4 x C tile: per m' four weights (one address for the
+// whole warp: a table entry or, without the table, the same products formed on
+// the fly) and C shared-memory loads feed 4 C independent FMAs.  With this much
 // independent work a few warps keep the FP64 pipe busy, so the kernel runs on
-// one CTA per SM and leaves the SM's other pipes, most of its registers and
-// shared memory to the far-field chain beside it.  Each output sums its terms
-// in order of k in one FMA chain from zero, then y = out_in + sum, staged
-// through the slot the block no longer needs and written a row at a time.
-// The last (ragged) block is k_near's (jbeg = (nL - 1) h).
+// one or two CTAs per SM and leaves the SM's other pipes, most of its
+// registers and shared memory to the far-field chain beside it.  Each output
+// sums its terms in order of k in one FMA chain from zero, then
+// y = out_in + sum, staged through the slot the block no longer needs and
+// written a row at a time.  The last (ragged) block is k_near's
+// (jbeg = (nL - 1) h).  The leaf size is a template parameter, so every loop
+// bound and index below is a compile-time constant or a 32-bit offset.
 // ---------------------------------------------------------------------------
 constexpr int BT_WARPS = 4;
 constexpr int BT_THREADS = 32 * BT_WARPS;
 constexpr long long BT_MIN_COUNT = 64;
 
-// Vectors per lane: two while a chunk's three slots stay near 100 KB.
+template <int S>
+struct BandTile {
+  static constexpr int H = 2 * S;
+  static constexpr int C = S <= 32 ? 2 : 1;   // vectors per lane
+  static constexpr int VCH = 32 * C;          // vectors per chunk
+  static constexpr int LD = 2 * S + 1;        // slot row (odd)
+  static constexpr int SLOT = VCH * LD;       // doubles per slot
+  static constexpr int GROUPS = S / 2;        // row groups: 2 parities x s/4
+  static constexpr int GPW = (GROUPS + BT_WARPS - 1) / BT_WARPS;
+  static constexpr int WB = 4 * S * S;        // weights of one block, both parities
+  static constexpr bool WS = S == 16;         // weights staged in shared memory
+  static constexpr size_t SMEM = (3 * (size_t)SLOT + (WS ? 2 * (size_t)WB : 0)) * sizeof(double);
+};
+
 __host__ __device__ inline int band_tile_c(long long s) { return s <= 32 ? 2 : 1; }
-inline size_t band_tile_smem(long long s) {
-  return (size_t)3 * 32 * band_tile_c(s) * (2 * s + 1) * sizeof(double);
-}
 // Entries of the dense weight table: (nL - 1) blocks x 2 parities x 2s x s.
 inline size_t band_tile_table_size(size_t N, size_t s) {
   const size_t h = 2 * s, nL = N / h;
   return nL >= 2 ? (nL - 1) * 4 * s * s : 0;
-}
-
-// Weight of row r of the group at i'0 for m' (r <= m' - i'0 is the caller's).
-__device__ __forceinline__ double band_tile_weight(int c2l, long long mp, long long ip,
-                                                   long long j, const double *__restrict__ a,
-                                                   const double *__restrict__ an,
-                                                   const double *__restrict__ dn) {
-  return near_weight(c2l, mp - ip, j, a, an, dn);
 }
 
 // Plan time: the dense table W'[b][p][m'][i'] (zero where m' < i').
@@ -1152,21 +1157,23 @@ __global__ void k_band_tile_weights(double *__restrict__ Wt, const double *__res
   const long long ip = idx % g.s, mp = (idx / g.s) % (2 * g.s), bp = idx / (2 * g.s * g.s);
   const long long b = bp >> 1, p = bp & 1;
   const long long j = b * g.h + 2 * ip + p;
-  Wt[idx] = mp >= ip ? band_tile_weight(c2l, mp, ip, j, a, an, dn) : 0.0;
+  Wt[idx] = mp >= ip ? near_weight(c2l, mp - ip, j, a, an, dn) : 0.0;
 }
 
-template <int C, bool TAB>
+// One term step m' of a row group: rows r < ROWS of the 4 (the others have no
+// term at this m').  W (TAB): the four weights (16-byte aligned); without TAB
+// they are formed here (output j0 + 2 r, term k = m' - i'0 - r).
+template <int C, int ROWS, bool TAB>
 __device__ __forceinline__ void band_tile_step(const double *__restrict__ xs, int ld,
-                                               const double *__restrict__ Wr, long long mp,
-                                               long long ip0, long long j0, int c2l,
+                                               const double *W, int k0, long long j0, int c2l,
                                                const double *__restrict__ a,
                                                const double *__restrict__ an,
-                                               const double *__restrict__ dn, int rows,
+                                               const double *__restrict__ dn,
                                                double (&acc)[4][C]) {
   double w[4];
   if (TAB) {
-    const double2 q0 = __ldg(reinterpret_cast<const double2 *>(Wr));
-    const double2 q1 = __ldg(reinterpret_cast<const double2 *>(Wr) + 1);
+    const double2 q0 = reinterpret_cast<const double2 *>(W)[0];
+    const double2 q1 = reinterpret_cast<const double2 *>(W)[1];
     w[0] = q0.x;
     w[1] = q0.y;
     w[2] = q1.x;
@@ -1174,130 +1181,152 @@ __device__ __forceinline__ void band_tile_step(const double *__restrict__ xs, in
   } else {
 #pragma unroll
     for (int r = 0; r < 4; r++)
-      w[r] = r < rows ? band_tile_weight(c2l, mp, ip0 + r, j0 + 2 * r, a, an, dn) : 0.0;
+      w[r] = r < ROWS ? near_weight(c2l, k0 - r, j0 + 2 * r, a, an, dn) : 0.0;
   }
   double xv[C];
 #pragma unroll
   for (int c = 0; c < C; c++) xv[c] = xs[c * 32 * ld];
 #pragma unroll
-  for (int r = 0; r < 4; r++)
-    if (r < rows)
+  for (int r = 0; r < ROWS; r++)
 #pragma unroll
-      for (int c = 0; c < C; c++) acc[r][c] = fma(w[r], xv[c], acc[r][c]);
+    for (int c = 0; c < C; c++) acc[r][c] = fma(w[r], xv[c], acc[r][c]);
 }
 
-// One row group (parity p, rows i'0 .. i'0 + 3) of block b for the lane's C
-// vectors; sA / sB: the lane's rows in the two half-window slots.
-template <int C, bool TAB>
+// Row group (parity p, rows i'0 .. i'0 + 3) of one block for the lane's C
+// vectors.  sA / sB: the lane's rows in the two half-window slots; Wg: the
+// group's weights at m' = 0 (row stride S), or nullptr.
+template <int S, bool TAB>
 __device__ __forceinline__ void band_tile_group(const double *__restrict__ sA,
-                                                const double *__restrict__ sB, int ld,
-                                                const double *__restrict__ Wt, const Geo &g,
-                                                long long b, int p, long long ip0, int c2l,
-                                                const double *__restrict__ a,
+                                                const double *__restrict__ sB,
+                                                const double *Wg, int p, int ip0, long long j0,
+                                                int c2l, const double *__restrict__ a,
                                                 const double *__restrict__ an,
                                                 const double *__restrict__ dn,
-                                                double (&acc)[4][C]) {
-  const long long s = g.s, j0 = b * g.h + 2 * ip0 + p;
-  const double *Wb = TAB ? Wt + ((b * 2 + p) * 2 * s) * s + ip0 : nullptr;
+                                                double (&acc)[4][BandTile<S>::C]) {
+  using BT = BandTile<S>;
+  constexpr int C = BT::C, LD = BT::LD;
 #pragma unroll
   for (int r = 0; r < 4; r++)
 #pragma unroll
     for (int c = 0; c < C; c++) acc[r][c] = 0.0;
   // m' = i'0 .. i'0 + 2: only rows r <= m' - i'0 have a term (i'0 + 3 < s)
-#pragma unroll
-  for (int t = 0; t < 3; t++) {
-    const long long mp = ip0 + t;
-    band_tile_step<C, TAB>(sA + 2 * mp + p, ld, TAB ? Wb + mp * s : nullptr, mp, ip0, j0, c2l,
-                           a, an, dn, t + 1, acc);
-  }
+  band_tile_step<C, 1, TAB>(sA + 2 * ip0 + p, LD, TAB ? Wg + ip0 * S : nullptr, 0, j0, c2l, a,
+                            an, dn, acc);
+  band_tile_step<C, 2, TAB>(sA + 2 * ip0 + 2 + p, LD, TAB ? Wg + (ip0 + 1) * S : nullptr, 1, j0,
+                            c2l, a, an, dn, acc);
+  band_tile_step<C, 3, TAB>(sA + 2 * ip0 + 4 + p, LD, TAB ? Wg + (ip0 + 2) * S : nullptr, 2, j0,
+                            c2l, a, an, dn, acc);
 #pragma unroll 4
-  for (long long mp = ip0 + 3; mp < s; mp++)
-    band_tile_step<C, TAB>(sA + 2 * mp + p, ld, TAB ? Wb + mp * s : nullptr, mp, ip0, j0, c2l,
-                           a, an, dn, 4, acc);
-#pragma unroll 4
-  for (long long mp = s; mp < 2 * s; mp++)
-    band_tile_step<C, TAB>(sB + 2 * (mp - s) + p, ld, TAB ? Wb + mp * s : nullptr, mp, ip0, j0,
-                           c2l, a, an, dn, 4, acc);
+  for (int mp = ip0 + 3; mp < S; mp++)
+    band_tile_step<C, 4, TAB>(sA + 2 * mp + p, LD, TAB ? Wg + mp * S : nullptr, mp - ip0, j0,
+                              c2l, a, an, dn, acc);
+#pragma unroll(S <= 16 ? S : 8)
+  for (int mp = S; mp < 2 * S; mp++)
+    band_tile_step<C, 4, TAB>(sB + 2 * (mp - S) + p, LD, TAB ? Wg + mp * S : nullptr, mp - ip0,
+                              j0, c2l, a, an, dn, acc);
 }
 
 // Copies of half window hw of the chunk's vectors into slot dst (zeros for
 // vectors past the batch).
-__device__ __forceinline__ void band_tile_fill(double *dst, int ld, const double *__restrict__ x,
-                                               const Geo &g, long long v0, int vch,
-                                               long long hw) {
-  const int n = vch * (int)g.h;
-  for (int idx = threadIdx.x; idx < n; idx += BT_THREADS) {
-    const int vl = idx / (int)g.h, m = idx - vl * (int)g.h;
+template <int S>
+__device__ __forceinline__ void band_tile_fill(double *dst, const double *__restrict__ x,
+                                               const Geo &g, long long v0, long long hw) {
+  using BT = BandTile<S>;
+#pragma unroll 4
+  for (int idx = threadIdx.x; idx < BT::VCH * BT::H; idx += BT_THREADS) {
+    const int vl = idx / BT::H, m = idx % BT::H;
     const long long v = v0 + vl;
     const bool live = v < g.count;
-    l2c_oz::cp_async8(dst + vl * ld + m, live ? x + v * g.N + hw * g.h + m : x, live ? 8 : 0);
+    l2c_oz::cp_async8(dst + vl * BT::LD + m, live ? x + v * g.N + hw * BT::H + m : x,
+                      live ? 8 : 0);
   }
+}
+// Copies of the weights of block wb into wdst.
+template <int S>
+__device__ __forceinline__ void band_tile_fill_w(double *wdst, const double *__restrict__ Wt,
+                                                 long long wb) {
+  using BT = BandTile<S>;
+  const double *src = Wt + wb * BT::WB;
+#pragma unroll
+  for (int idx = threadIdx.x; idx < BT::WB / 2; idx += BT_THREADS)
+    l2c_oz::cp_async16(wdst + 2 * idx, src + 2 * idx, 16);
 }
 
 // Work unit u: vector chunk u % nchunk, blocks [seg bseg, (seg + 1) bseg) of
 // the nL - 1 full ones, seg = u / nchunk (a segment's chunks run side by side,
-// so its weights are read from L2 by all of them).  GPW row groups per warp:
-// warp w takes groups q = 8 t' + w and 8 t' + 7 - w (t' = 0, 1, ...), q < s/2.
-template <int C, int GPW, bool TAB>
-__global__ void __launch_bounds__(BT_THREADS)
+// so its weights are read from L2 by all of them).  Warp w takes the row
+// groups q = 8 t' + w and 8 t' + 7 - w (t' = 0, 1, ...), q < s/2.  At most
+// 128 registers per thread, so that one or two of these CTAs leave most of an
+// SM's register file to the kernels beside them.
+template <int S, bool TAB>
+__global__ void __launch_bounds__(BT_THREADS, 4)
     k_band_tile(const double *__restrict__ x, const double *out, double *__restrict__ y,
                 const double *__restrict__ Wt, const double *__restrict__ a,
                 const double *__restrict__ an, const double *__restrict__ dn, Geo g, int c2l,
                 long long nchunk, long long bseg) {
+  using BT = BandTile<S>;
+  constexpr int C = BT::C, VCH = BT::VCH, LD = BT::LD, H = BT::H;
+  constexpr bool WS = TAB && BT::WS;
   extern __shared__ __align__(16) double bt_smem[];
+  double *wsm = bt_smem + 3 * BT::SLOT;  // two weight buffers (WS)
   pdl_wait();
   pdl_trigger();
-  constexpr int VCH = 32 * C;
-  const int ld = 2 * (int)g.s + 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long nfull = g.nL - 1, nseg = (nfull + bseg - 1) / bseg;
-  const int groups = (int)g.s / 2;  // row groups: 2 parities x s/4
   for (long long u = blockIdx.x; u < nchunk * nseg; u += gridDim.x) {
     const long long v0 = (u % nchunk) * VCH, seg = u / nchunk;
     const long long b0 = seg * bseg, b1 = b0 + bseg < nfull ? b0 + bseg : nfull;
-    // half windows b0 and b0 + 1 (block b0 needs both)
-    band_tile_fill(bt_smem + (b0 % 3) * VCH * ld, ld, x, g, v0, VCH, b0);
+    // half windows b0 and b0 + 1 (block b0 needs both), block b0's weights
+    band_tile_fill<S>(bt_smem + (int)(b0 % 3) * BT::SLOT, x, g, v0, b0);
+    if (WS) band_tile_fill_w<S>(wsm + (int)(b0 & 1) * BT::WB, Wt, b0);
     l2c_oz::cp_commit();
-    band_tile_fill(bt_smem + ((b0 + 1) % 3) * VCH * ld, ld, x, g, v0, VCH, b0 + 1);
+    band_tile_fill<S>(bt_smem + (int)((b0 + 1) % 3) * BT::SLOT, x, g, v0, b0 + 1);
     l2c_oz::cp_commit();
     for (long long b = b0; b < b1; b++) {
-      // half window b + 2 for the next block, one block ahead
-      if (b + 2 <= b1)
-        band_tile_fill(bt_smem + ((b + 2) % 3) * VCH * ld, ld, x, g, v0, VCH, b + 2);
+      // half window b + 2 and block b + 1's weights, one block ahead
+      if (b + 2 <= b1) {
+        band_tile_fill<S>(bt_smem + (int)((b + 2) % 3) * BT::SLOT, x, g, v0, b + 2);
+        if (WS) band_tile_fill_w<S>(wsm + (int)((b + 1) & 1) * BT::WB, Wt, b + 1);
+      }
       l2c_oz::cp_commit();
-      l2c_oz::cp_wait1();  // halves b and b + 1 have landed
+      l2c_oz::cp_wait1();  // halves b, b + 1 and block b's weights have landed
       __syncthreads();
-      double *sA = bt_smem + (b % 3) * VCH * ld;
-      const double *sB = bt_smem + ((b + 1) % 3) * VCH * ld;
-      double res[GPW][4][C];
+      double *sA = bt_smem + (int)(b % 3) * BT::SLOT;
+      const double *sB = bt_smem + (int)((b + 1) % 3) * BT::SLOT;
+      const double *Wb = !TAB ? nullptr : WS ? wsm + (int)(b & 1) * BT::WB : Wt + b * BT::WB;
+      double res[BT::GPW][4][C];
 #pragma unroll
-      for (int t = 0; t < GPW; t++) {
+      for (int t = 0; t < BT::GPW; t++) {
         const int q = 8 * (t >> 1) + ((t & 1) ? 2 * BT_WARPS - 1 - warp : warp);
-        if (q < groups)
-          band_tile_group<C, TAB>(sA + lane * ld, sB + lane * ld, ld, Wt, g, b, q & 1,
-                                  4LL * (q >> 1), c2l, a, an, dn, res[t]);
+        if (q < BT::GROUPS) {
+          const int p = q & 1, ip0 = 4 * (q >> 1);
+          band_tile_group<S, TAB>(sA + lane * LD, sB + lane * LD,
+                                  TAB ? Wb + p * 2 * S * S + ip0 : nullptr, p, ip0,
+                                  b * H + 2 * ip0 + p, c2l, a, an, dn, res[t]);
+        }
       }
       __syncthreads();  // every warp is done reading slots A and B
       // the sums, staged in slot A (its inputs are no longer needed)
 #pragma unroll
-      for (int t = 0; t < GPW; t++) {
+      for (int t = 0; t < BT::GPW; t++) {
         const int q = 8 * (t >> 1) + ((t & 1) ? 2 * BT_WARPS - 1 - warp : warp);
-        if (q < groups)
+        if (q < BT::GROUPS)
 #pragma unroll
           for (int r = 0; r < 4; r++)
 #pragma unroll
             for (int c = 0; c < C; c++)
-              sA[(lane + 32 * c) * ld + 2 * (4 * (q >> 1) + r) + (q & 1)] = res[t][r][c];
+              sA[(lane + 32 * c) * LD + 2 * (4 * (q >> 1) + r) + (q & 1)] = res[t][r][c];
       }
       __syncthreads();
-      // y = out_in + band, a row of h outputs per vector
-      const int n = VCH * (int)g.h;
-      for (int idx = threadIdx.x; idx < n; idx += BT_THREADS) {
-        const int vl = idx / (int)g.h, i = idx - vl * (int)g.h;
+      // y = out_in + band, a row of h outputs per vector (eight loads of the
+      // thread in flight at a time)
+#pragma unroll 8
+      for (int idx = threadIdx.x; idx < VCH * H; idx += BT_THREADS) {
+        const int vl = idx / H, i = idx % H;
         const long long v = v0 + vl;
         if (v < g.count) {
-          const long long j = b * g.h + i;
-          y[v * g.N + j] = out[v * g.dist + j * g.stride] + sA[vl * ld + i];
+          const long long j = b * H + i;
+          y[v * g.N + j] = out[v * g.dist + j * g.stride] + sA[vl * LD + i];
         }
       }
       __syncthreads();  // slot A is refilled next
@@ -1308,7 +1337,7 @@ __global__ void __launch_bounds__(BT_THREADS)
 }
 
 // Whether a batch's band takes k_band_tile: count >= BT_MIN_COUNT, s a
-// multiple of 8 up to 64, at least one full block.
+// multiple of 8 in [16, 64], at least one full block.
 inline bool band_tile_ok(long long s, long long nL, long long count) {
   return count >= BT_MIN_COUNT && s % 8 == 0 && s >= 16 && s <= 64 && nL >= 2;
 }
@@ -1321,13 +1350,25 @@ using band_tile_fn = void (*)(const double *, const double *, double *, const do
 template <bool TAB>
 band_tile_fn<TAB> band_tile_kernel(long long s) {
   switch (s / 8) {
-    case 2: return k_band_tile<2, 2, TAB>;
-    case 3: return k_band_tile<2, 3, TAB>;
-    case 4: return k_band_tile<2, 4, TAB>;
-    case 5: return k_band_tile<1, 5, TAB>;
-    case 6: return k_band_tile<1, 6, TAB>;
-    case 7: return k_band_tile<1, 7, TAB>;
-    default: return k_band_tile<1, 8, TAB>;
+    case 2: return k_band_tile<16, TAB>;
+    case 3: return k_band_tile<24, TAB>;
+    case 4: return k_band_tile<32, TAB>;
+    case 5: return k_band_tile<40, TAB>;
+    case 6: return k_band_tile<48, TAB>;
+    case 7: return k_band_tile<56, TAB>;
+    default: return k_band_tile<64, TAB>;
+  }
+}
+
+inline size_t band_tile_smem(long long s) {
+  switch (s / 8) {
+    case 2: return BandTile<16>::SMEM;
+    case 3: return BandTile<24>::SMEM;
+    case 4: return BandTile<32>::SMEM;
+    case 5: return BandTile<40>::SMEM;
+    case 6: return BandTile<48>::SMEM;
+    case 7: return BandTile<56>::SMEM;
+    default: return BandTile<64>::SMEM;
   }
 }
 
@@ -3250,13 +3291,19 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
         int TuneCfg::*f;
         std::vector<int> vals;
       };
+      const bool tile = use_band_tile(p, count);
       std::vector<Knob> knobs = {{&TuneCfg::overlap, {0, 1}},
                                  {&TuneCfg::fork, {0, 1, 2, 3}},
                                  {&TuneCfg::pdl, {0, 1, 7}},
-                                 {&TuneCfg::prio, {0, 1}},
-                                 {&TuneCfg::nthreads, {128, 256}},
-                                 {&TuneCfg::nctas, {0, 3 * sms, 6 * sms}}};
-      if (count > 1) knobs.push_back({&TuneCfg::nvb, {1, 2, 4, 8}});
+                                 {&TuneCfg::prio, {0, 1}}};
+      if (tile) {
+        // k_band_tile's grid: 0 = two CTAs per SM, one, or three
+        knobs.push_back({&TuneCfg::nctas, {0, sms, 3 * sms}});
+      } else {
+        knobs.push_back({&TuneCfg::nthreads, {128, 256}});
+        knobs.push_back({&TuneCfg::nctas, {0, 3 * sms, 6 * sms}});
+        if (count > 1) knobs.push_back({&TuneCfg::nvb, {1, 2, 4, 8}});
+      }
       // the weight table: when the plan has one, or a batch's would be small
       if (p->precompute || (count > 1 && near_table_size(p->N, p->s) <= count * p->N))
         knobs.push_back({&TuneCfg::wtab, {0, 1}});
