@@ -1681,17 +1681,63 @@ size_t mz_leaf_up_smem(int KC, int nbuf) {
          (size_t)MXW * nbuf * 16 * (16 * KC + 1) * sizeof(double);
 }
 
-// Transfer trees, one level.  Columns col = (vector * 2 + parity) * np + j.
+// The levels a transfer kernel covers.  One launch per level (TOP = false):
+// one level, columns [0, count 2 np) of every tree, tiles over the grid.  The
+// top of the trees (TOP = true): levels lv[0], lv[1], ... in the order given
+// (up: coarser each step, down: finer), each CTA owning G whole trees, which
+// it carries through all those levels with a CTA barrier between levels (a
+// level's inputs are the CTA's own outputs of the level before, written to
+// global memory and read back by the same SM after the barrier).  The levels
+// at the top hold few slots per tree, so one launch replaces several whose
+// CTAs would each wait out a single tile's latency.
+constexpr int TREE_TOP_MAX = 8;
+struct TreeLevel {
+  long long pb, cb, np;  // parent / child slot base of the level, parents per tree
+};
+struct TreeLevels {
+  int n, G;  // levels, trees per CTA (TOP)
+  TreeLevel lv[TREE_TOP_MAX];
+};
+
+// The per-warp tile loop of a kernel: one level over the grid, or (TOP) the
+// CTA's trees through every level.  issue / work take the level and the
+// column range [c0, c1) the tile index counts from.
+template <bool TOP, int NBUF, class Issue, class Work>
+__device__ __forceinline__ void tree_levels_loop(const TreeLevels &T, long long count,
+                                                 Issue issue, Work work) {
+  const int wid = threadIdx.x >> 5;
+  if constexpr (!TOP) {
+    const TreeLevel Lv = T.lv[0];
+    const long long c1 = count * 2 * Lv.np;
+    oz_tile_loop<NBUF>(
+        (long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, (c1 + 15) / 16,
+        [&](long long t, int b) { issue(Lv, 0LL, c1, t, b); },
+        [&](long long t, int b) { work(Lv, 0LL, c1, t, b); });
+  } else {
+    const long long trees = count * 2, v0 = (long long)blockIdx.x * T.G;
+    const long long v1 = v0 + T.G < trees ? v0 + T.G : trees;
+    for (int k = 0; k < T.n; k++) {
+      const TreeLevel Lv = T.lv[k];
+      const long long c0 = v0 * Lv.np, c1 = v1 * Lv.np;
+      oz_tile_loop<NBUF>(
+          (long long)wid, (long long)MXW, (c1 - c0 + 15) / 16,
+          [&](long long t, int b) { issue(Lv, c0, c1, t, b); },
+          [&](long long t, int b) { work(Lv, c0, c1, t, b); });
+      __syncthreads();  // the level's outputs, in global memory, for the next
+    }
+  }
+}
+
+// Transfer trees.  Columns col = (vector * 2 + parity) * np + j.
 // Up: parent slot j of level l from child slots 2j+2, 2j+3 of level l+1
 // (36 contiguous coefficients, two stored columns), P = [B | B'] (18 x 36).
 // The transfer matrices' fragments hold only their first QMAX digit slices
 // (the slice-major layout makes that a prefix of each matrix's words).
 __host__ __device__ constexpr int oz_tree_words(int QMAX, int KC) { return QMAX * OZ_NT * KC * 32; }
-template <int QMAX, int NBUF>
+template <int QMAX, int NBUF, bool TOP = false>
 __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
     k_mz_tree_up(long long *w, int *wE, const unsigned *__restrict__ Pf,
-                 const int *__restrict__ Pm, Geo g, long long parent_base, long long child_base,
-                 long long np) {
+                 const int *__restrict__ Pm, Geo g, TreeLevels T) {
   extern __shared__ __align__(16) unsigned char mz_smem[];
   constexpr int NW = oz_tree_words(QMAX, 5);
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
@@ -1707,16 +1753,16 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
   __syncthreads();
   pdl_wait();
   pdl_trigger();
-  const long long ncol = g.count * 2 * np, ntile = (ncol + 15) / 16;
-  auto issue = [&](long long tile, int buf) {
+  auto issue = [&](const TreeLevel &Lv, long long c0, long long c1, long long tile, int buf) {
+    const long long np = Lv.np;
     long long *B = sB + buf * 16;
     int *Ex = sEx + buf * 32;
     if (lane < 16) {
-      const long long col = tile * 16 + lane;
+      const long long col = c0 + tile * 16 + lane;
       long long b = -1;
-      if (col < ncol) {
+      if (col < c1) {
         const long long vs = col / np, j = col - vs * np;
-        b = vs * g.slots + child_base + 2 * j + 2;  // first child slot
+        b = vs * g.slots + Lv.cb + 2 * j + 2;  // first child slot
       }
       B[lane] = b;
       cp_async4(Ex + lane, b >= 0 ? wE + b : wE, b >= 0 ? 4 : 0);
@@ -1730,18 +1776,19 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
       l2c_oz::cp_async16(X + r * OZ_TLD + 2 * k2, b >= 0 ? w + b * M + 2 * k2 : w, b >= 0 ? 16 : 0);
     }
   };
-  auto work = [&](long long tile, int buf) {
+  auto work = [&](const TreeLevel &Lv, long long cb0, long long c1, long long tile, int buf) {
+    const long long np = Lv.np;
     long long *X = Xw + buf * 16 * OZ_TLD;
     const int *Ex = sEx + buf * 32;
     l2c_oz::stage_cols<2 * M, M, 40>(X, OZ_TLD, Ex, Ex + 16, Es);
     long long T[OZ_NT][4];
     oz_tile_T<OZ_NT, 5, QMAX>(sP, X, OZ_TLD, 1, T);
-    const long long c0 = tile * 16;
+    const long long c0 = cb0 + tile * 16;
     auto dst = [&](int r) -> long long {  // parent slot index, -1: none
       const long long col = c0 + r;
-      if (col >= ncol) return -1;
+      if (col >= c1) return -1;
       const long long vs = col / np, j = col - vs * np;
-      return vs * g.slots + parent_base + j;
+      return vs * g.slots + Lv.pb + j;
     };
     const long long d0 = dst(gq), d1 = dst(gq + 8);
     oz_put18(
@@ -1759,8 +1806,7 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
       if (d1 >= 0) wE[d1] = Es[gq + 8] + sM[OZ_ROWS];
     }
   };
-  oz_tile_loop<NBUF>((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue,
-                     work);
+  tree_levels_loop<TOP, NBUF>(T, g.count, issue, work);
 }
 
 constexpr size_t oz_tree_up_smem(int QMAX, int NBUF) {
@@ -1772,11 +1818,10 @@ constexpr size_t oz_tree_up_smem(int QMAX, int NBUF) {
 // level l).  The child's own far field (prefetched with the parent) and the
 // product are added as integers on the coarser of their two scales, one bit
 // above the larger exponent.
-template <int QMAX, int NBUF>
+template <int QMAX, int NBUF, bool TOP = false>
 __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
     k_mz_tree_down(long long *c, int *cE, const unsigned *__restrict__ Pf,
-                   const int *__restrict__ Pm, Geo g, long long parent_base, long long child_base,
-                   long long np) {
+                   const int *__restrict__ Pm, Geo g, TreeLevels T) {
   extern __shared__ __align__(16) unsigned char mz_smem[];
   constexpr int NW = oz_tree_words(QMAX, 3);  // per matrix: B^T, then B^T'
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
@@ -1794,17 +1839,17 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
   __syncthreads();
   pdl_wait();
   pdl_trigger();
-  const long long ncol = g.count * 2 * np, ntile = (ncol + 15) / 16;
-  auto issue = [&](long long tile, int buf) {
+  auto issue = [&](const TreeLevel &Lv, long long c0, long long c1, long long tile, int buf) {
+    const long long np = Lv.np;
     long long *B = sB + buf * 32;
     int *Ex = sEx + buf * 48;
     if (lane < 16) {
-      const long long col = tile * 16 + lane;
+      const long long col = c0 + tile * 16 + lane;
       long long b = -1, cb = -1;
-      if (col < ncol) {
+      if (col < c1) {
         const long long vs = col / np, t = col - vs * np;
-        b = vs * g.slots + parent_base + t;
-        cb = vs * g.slots + child_base + 2 * t;
+        b = vs * g.slots + Lv.pb + t;
+        cb = vs * g.slots + Lv.cb + 2 * t;
       }
       B[lane] = b;
       B[16 + lane] = cb;
@@ -1825,7 +1870,7 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
       l2c_oz::cp_async16(C + r * 2 * M + 2 * k2, b >= 0 ? c + b * M + 2 * k2 : c, b >= 0 ? 16 : 0);
     }
   };
-  auto work = [&](long long tile, int buf) {
+  auto work = [&](const TreeLevel &, long long, long long, long long, int buf) {
     long long *X = Xw + buf * 16 * OZ_CLD;
     const long long *C = Cw + buf * 16 * 2 * M;
     const long long *B = sB + buf * 32;
@@ -1877,8 +1922,7 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
       }
     }
   };
-  oz_tile_loop<NBUF>((long long)blockIdx.x * MXW + wid, (long long)gridDim.x * MXW, ntile, issue,
-                     work);
+  tree_levels_loop<TOP, NBUF>(T, g.count, issue, work);
 }
 
 constexpr size_t oz_tree_down_smem(int QMAX, int NBUF) {
@@ -2229,6 +2273,8 @@ struct l2c_gpu_plan {
   int *wE = nullptr, *cE = nullptr;
   size_t cap_wE = 0, cap_cE = 0;
   int *bad = nullptr;  // per vector: an Inf or NaN input seen (mixed form)
+  bool mz_top = true;  // the coarsest transfer levels in one launch (mz_top_level)
+  int mz_top_g = 2;    // trees per CTA of that launch
   // captured launch sequences, keyed by the call's shape and pointers
   struct GraphEntry {
     size_t dir, count, dist, stride;
@@ -2693,6 +2739,31 @@ Sched sched_for(const l2c_gpu_plan *p, size_t count) {
 // band runs on the second stream.
 bool pdl_after_band(const Sched &sc) { return (sc.pdl & (sc.ov ? 1u : 4u)) != 0; }
 
+// Levels from .. to (either order), as a transfer kernel's list; G trees per CTA.
+TreeLevels tree_levels(long long from, long long to, int G) {
+  TreeLevels T{};
+  T.G = G;
+  const long long step = to >= from ? 1 : -1;
+  for (long long l = from;; l += step) {
+    T.lv[T.n++] = TreeLevel{2 * (long long)blocks_before((size_t)l),
+                            2 * (long long)blocks_before((size_t)l + 1),
+                            (long long)slots_at((size_t)l)};
+    if (l == to) break;
+  }
+  return T;
+}
+
+// The coarsest levels 0 .. lt of the mixed form's transfer trees go in one
+// launch, a CTA per tree (TOP kernels): those with at most 64 slots per tree,
+// i.e. at most one tile per warp (-1: none; L2C_MZ_TOP=0 turns this off).
+int mz_top_level(const l2c_gpu_plan *p) {
+  if (!p->mz_top || p->L < 2) return -1;
+  int lt = -1;
+  while (lt + 1 <= (int)p->L - 2 && lt + 1 < TREE_TOP_MAX && slots_at((size_t)lt + 1) <= 64)
+    lt++;
+  return lt;
+}
+
 template <int KC>
 void mz_leaf_up_launch(l2c_gpu_plan *p, const double *x, const Geo &g, cudaStream_t st,
                        LaunchOpt pdl) {
@@ -2728,20 +2799,24 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
     if (cudaGetLastError() != cudaSuccess) return false;
   }
   if (!band(1)) return false;
+  const int lt = mz_top_level(p);
   {
-    PhaseScope ps(p, L2C_PHASE_TREE_UP, (size_t)(g.L - 1));
+    PhaseScope ps(p, L2C_PHASE_TREE_UP, (size_t)(g.L - 2 - lt + (lt >= 0 ? 1 : 0)));
     const bool q2 = p->oz_tree_q == 2, nb1 = p->oz_nbuf == 1;
     auto *kup = q2 ? (nb1 ? k_mz_tree_up<2, 1> : k_mz_tree_up<2, 2>)
                    : (nb1 ? k_mz_tree_up<l2c_oz::SLICES, 1> : k_mz_tree_up<l2c_oz::SLICES, 2>);
-    for (long long l = g.L - 2; l >= 0; l--) {
-      const long long np = (long long)slots_at((size_t)l);
-      const long long tiles = (g.count * 2 * np + 15) / 16;
+    for (long long l = g.L - 2; l > lt; l--) {
+      const long long tiles = (g.count * 2 * (long long)slots_at((size_t)l) + 15) / 16;
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
-      const long long pb = 2 * (long long)blocks_before((size_t)l);
-      const long long cb = 2 * (long long)blocks_before((size_t)l + 1);
-      launch_k(chain, kup, grid, 32 * MXW, oz_tree_up_smem(p->oz_tree_q, p->oz_nbuf), st,
-               w, p->wE, (const unsigned *)p->oz_tu, (const int *)p->oz_tum, g, pb, cb, np);
+      launch_k(chain, kup, grid, 32 * MXW, oz_tree_up_smem(p->oz_tree_q, p->oz_nbuf), st, w,
+               p->wE, (const unsigned *)p->oz_tu, (const int *)p->oz_tum, g,
+               tree_levels(l, l, 1));
     }
+    if (lt >= 0)  // the top levels lt .. 0, each CTA mz_top_g trees
+      launch_k(chain, q2 ? k_mz_tree_up<2, 1, true> : k_mz_tree_up<l2c_oz::SLICES, 1, true>,
+               (unsigned)((g.count * 2 + p->mz_top_g - 1) / p->mz_top_g), 32 * MXW,
+               oz_tree_up_smem(p->oz_tree_q, 1), st, w, p->wE, (const unsigned *)p->oz_tu,
+               (const int *)p->oz_tum, g, tree_levels(lt, 0, p->mz_top_g));
     if (cudaGetLastError() != cudaSuccess) return false;
   }
   if (!band(2)) return false;
@@ -2765,20 +2840,23 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
   }
   if (!band(3)) return false;
   {
-    PhaseScope ps(p, L2C_PHASE_TREE_DOWN, (size_t)(g.L - 1));
+    PhaseScope ps(p, L2C_PHASE_TREE_DOWN, (size_t)(g.L - 2 - lt + (lt >= 0 ? 1 : 0)));
     const bool q2 = p->oz_tree_q == 2, nb1 = p->oz_nbuf == 1;
     auto *kdown = q2 ? (nb1 ? k_mz_tree_down<2, 1> : k_mz_tree_down<2, 2>)
                      : (nb1 ? k_mz_tree_down<l2c_oz::SLICES, 1>
                             : k_mz_tree_down<l2c_oz::SLICES, 2>);
-    for (long long l = 0; l + 1 < g.L; l++) {
-      const long long np = (long long)slots_at((size_t)l);
-      const long long tiles = (g.count * 2 * np + 15) / 16;
+    if (lt >= 0)  // the top levels 0 .. lt, each CTA mz_top_g trees
+      launch_k(chain,
+               q2 ? k_mz_tree_down<2, 1, true> : k_mz_tree_down<l2c_oz::SLICES, 1, true>,
+               (unsigned)((g.count * 2 + p->mz_top_g - 1) / p->mz_top_g), 32 * MXW,
+               oz_tree_down_smem(p->oz_tree_q, 1), st, c, p->cE, (const unsigned *)p->oz_td,
+               (const int *)p->oz_tdm, g, tree_levels(0, lt, p->mz_top_g));
+    for (long long l = lt + 1; l + 1 < g.L; l++) {
+      const long long tiles = (g.count * 2 * (long long)slots_at((size_t)l) + 15) / 16;
       const unsigned grid = (unsigned)std::min<long long>((tiles + MXW - 1) / MXW, 152 * 4);
-      const long long pb = 2 * (long long)blocks_before((size_t)l);
-      const long long cb = 2 * (long long)blocks_before((size_t)l + 1);
-      launch_k(chain, kdown, grid, 32 * MXW,
-               oz_tree_down_smem(p->oz_tree_q, p->oz_nbuf), st, c, p->cE,
-               (const unsigned *)p->oz_td, (const int *)p->oz_tdm, g, pb, cb, np);
+      launch_k(chain, kdown, grid, 32 * MXW, oz_tree_down_smem(p->oz_tree_q, p->oz_nbuf), st, c,
+               p->cE, (const unsigned *)p->oz_td, (const int *)p->oz_tdm, g,
+               tree_levels(l, l, 1));
     }
     if (cudaGetLastError() != cudaSuccess) return false;
   }
@@ -3423,6 +3501,8 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
     p->near_threads = std::atoi(env) == 128 ? 128 : 256;
   if (const char *env = std::getenv("L2C_NEAR_PAIR")) p->near_pair = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_BAND_TILE")) p->band_tile = env[0] == '0' ? 0 : -1;
+  if (const char *env = std::getenv("L2C_MZ_TOP")) p->mz_top = env[0] != '0';
+  if (const char *env = std::getenv("L2C_MZ_TOP_G")) p->mz_top_g = std::max(1, std::atoi(env));
   PCK(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device));
   if (const char *env = std::getenv("L2C_PDL")) p->pdl = std::max(0, std::atoi(env));
   if (const char *env = std::getenv("L2C_CHAIN_PRIO")) p->chain_prio_mode = env[0] == '1' ? 1 : 0;
@@ -3654,6 +3734,12 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
                                (int)oz_tree_down_smem(l2c_oz::SLICES, 1)));
       PCK(cudaFuncSetAttribute(k_mz_tree_down<l2c_oz::SLICES, 2>, smax,
                                (int)oz_tree_down_smem(l2c_oz::SLICES, 2)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_up<2, 1, true>, smax, (int)oz_tree_up_smem(2, 1)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_up<l2c_oz::SLICES, 1, true>, smax,
+                               (int)oz_tree_up_smem(l2c_oz::SLICES, 1)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_down<2, 1, true>, smax, (int)oz_tree_down_smem(2, 1)));
+      PCK(cudaFuncSetAttribute(k_mz_tree_down<l2c_oz::SLICES, 1, true>, smax,
+                               (int)oz_tree_down_smem(l2c_oz::SLICES, 1)));
       PCK(cudaFuncSetAttribute(k_mz_far<1>, smax, (int)oz_far_smem(1)));
       PCK(cudaFuncSetAttribute(k_mz_far<2>, smax, (int)oz_far_smem(2)));
 #define L2C_MZ_ATTR(kc)                                                                     \

@@ -100,10 +100,11 @@ def test_mixed_rejects_large_leaves(lib):
 def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
     """Programmatic dependent launch, the band on the second stream, graph
     replay, the tile buffer depth, the chain's scheduling priority and the
-    band's CTA size, vectors per thread, grid cap, weight table and fork point
-    change only when work runs, never what it computes: every setting gives
-    the same bits as the default plan (count = 64: the band as dense register
-    tiles, with its table or weights formed on the fly)."""
+    band's CTA size, vectors per thread, grid cap, weight table and fork point,
+    and (mixed form) the coarsest transfer levels in one launch or one launch
+    per level, change only when work runs, never what it computes: every
+    setting gives the same bits as the default plan (count = 64: the band as
+    dense register tiles, with its table or weights formed on the fly)."""
     N = 16384
     x = np.ascontiguousarray(make_input(N * count, "gauss", 11).reshape(count, N))
 
@@ -129,7 +130,9 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
                 {"L2C_NEAR_THREADS": "256", "L2C_NEAR_VB": "2", "L2C_NEAR_CTAS": "912"},
                 {"L2C_NEAR_TABLE": "0"}, {"L2C_NEAR_TABLE": "1"},
                 {"L2C_BAND_FORK": "1"}, {"L2C_BAND_FORK": "2"}, {"L2C_BAND_FORK": "3"},
-                {"L2C_BAND_FORK": "2", "L2C_PDL": "7"}):
+                {"L2C_BAND_FORK": "2", "L2C_PDL": "7"},
+                # the mixed form's coarsest transfer levels one launch each
+                {"L2C_MZ_TOP": "0"}, {"L2C_MZ_TOP": "0", "L2C_PDL": "0"}):
         with monkeypatch.context() as m:
             for k, v in env.items():
                 m.setenv(k, v)
