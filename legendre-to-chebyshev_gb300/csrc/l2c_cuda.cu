@@ -531,6 +531,103 @@ inline size_t near_table_size(size_t N, size_t s) {
   return n;
 }
 
+// Band of one vector with register windows (full blocks b < nL-1; s a
+// multiple of 8).  Output j = b h + 2 i' + p sums, over sources m' = i' ..
+// 2s-1 of block b and parity p, w(k, j) x[b h + 2 m' + p] with k = m' - i',
+// where w = lo[k] hi[j + k] (L2C: a[k] a[j+k]; C2L: -(dn[k] an[j+k]), with
+// -sqrt(pi) standing for dn[0], which gives the k = 0 term sqrt(pi) an[j]
+// exactly) and j + k = b h + p + i' + m'.  A thread owns 4 consecutive rows
+// i'0 .. i'0+3 of one parity: at source m' every row reads the same x, and as
+// m' advances by one the rows' lo values shift down one row and their hi
+// values up one row, so each step loads one x, one lo and one hi value for
+// 4 DMUL + 4 DFMA (the per-output kernel loads all three per term).  Each
+// thread takes row groups g and s/4-1-g, whose trip counts 2s - 4g add up to
+// the same total for every thread; the lanes of a warp take the same groups
+// of consecutive blocks.  Terms are summed in order of k into one
+// FMA chain from zero; y = out_in + sum.  TAB: weights from the plan's table
+// (k_near_weights' layout; the same products, the same bits).
+template <bool TAB>
+__device__ __forceinline__ void near_rows_group(const double *__restrict__ xb,
+                                                const double *__restrict__ lo,
+                                                const double *__restrict__ hi,
+                                                const double *__restrict__ Wb, long long hbase,
+                                                const Geo &g, int c2l, int p, int ip0,
+                                                double (&acc)[4]) {
+  const int s2 = 2 * (int)g.s;
+  auto lo_at = [&](int k) -> double { return c2l && k == 0 ? -SQRT_PI : lo[k]; };
+  auto tab = [&](int k, int ip) -> double {  // table entry of row i', term k
+    const long long off = k < g.s ? (long long)k * g.h
+                                  : 4 * g.s * k - (long long)k * k + k - g.s * g.s - g.s;
+    return Wb[off + 2 * ip + p];
+  };
+  double wl[4], wh[4];  // row r: lo[m' - i'0 - r], hi[hbase + i'0 + r + m']
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    acc[r] = 0.0;
+    wl[r] = 0.0;
+    wh[r] = TAB ? 0.0 : hi[hbase + ip0 + r + ip0];
+  }
+  for (int mp = ip0; mp < s2; mp++) {
+    const int t = mp - ip0;  // rows r <= t have a term at this m'
+    if (!TAB) {
+      // shift the windows to m' and bring in row 0's lo and row 3's hi
+#pragma unroll
+      for (int r = 3; r > 0; r--) wl[r] = wl[r - 1];
+      wl[0] = lo_at(t);
+      if (t > 0) {
+#pragma unroll
+        for (int r = 0; r < 3; r++) wh[r] = wh[r + 1];
+        wh[3] = hi[hbase + ip0 + 3 + mp];
+      }
+    }
+    const double xv = xb[2 * mp + p];
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+      if (r <= t) {
+        const double w = TAB ? tab(t - r, ip0 + r) : c2l ? -(wl[r] * wh[r]) : wl[r] * wh[r];
+        acc[r] = fma(w, xv, acc[r]);
+      }
+  }
+}
+
+template <bool TAB>
+__global__ void __launch_bounds__(256) k_near_rows(const double *__restrict__ x, const double *out,
+                                                   double *__restrict__ y,
+                                                   const double *__restrict__ a,
+                                                   const double *__restrict__ an,
+                                                   const double *__restrict__ dn,
+                                                   const double *__restrict__ W, Geo g, int c2l) {
+  pdl_wait();
+  pdl_trigger();
+  // items (parity, pair, block) with the block fastest: the lanes of a warp
+  // share their rows' trip counts (no divergence) and read at a stride of h
+  const long long G = g.s / 4, nb = g.nL - 1;
+  const long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (item >= nb * G) return;
+  const long long pq = item / nb, b = item - pq * nb;
+  const int p = (int)(pq / (G / 2)), q = (int)(pq % (G / 2));
+  const double *xb = x + b * g.h;
+  const double *lo = c2l ? dn : a, *hi = c2l ? an : a;
+  const double *Wb = TAB ? W + b * (3 * g.s * g.s + g.s) : nullptr;
+  const long long hbase = b * g.h + p;  // hi index = hbase + i' + m'
+#pragma unroll 1
+  for (int half = 0; half < 2; half++) {
+    const int gi = half == 0 ? q : (int)G - 1 - q, ip0 = 4 * gi;
+    double acc[4];
+    near_rows_group<TAB>(xb, lo, hi, Wb, hbase, g, c2l, p, ip0, acc);
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const long long j = b * g.h + 2 * (ip0 + r) + p;
+      y[j] = out[j * g.stride] + acc[r];
+    }
+  }
+}
+
+// Whether a single vector's band takes k_near_rows.
+inline bool near_rows_ok(long long s, long long nL, long long count) {
+  return count == 1 && s % 8 == 0 && nL >= 2;
+}
+
 // Step 1: leaf node t in [2, 2^(L+1)) of parity sg: w = sum_i x[t h + 2i + sg] T_sg[i][m].
 // xv: this vector's x; wv: this vector's w (2 parities x slots x M).
 __device__ __forceinline__ void leaf_up_item(const double *__restrict__ xv,
@@ -2243,6 +2340,7 @@ struct l2c_gpu_plan {
   // dense band weights of the full blocks for k_band_tile (built on first use)
   double *Wtile[2] = {nullptr, nullptr};
   int band_tile = -1;  // batches' band as dense register tiles: -1 when eligible, 0 never
+  bool near_rows = true;  // single vectors' band with register windows (k_near_rows)
   int sms = 152;       // multiprocessors of the plan's device
   bool precompute = false;  // created with L2C_PLAN_PRECOMPUTE_NEAR
   bool use_w = false;       // this call's band reads Wnear (see TuneCfg::wtab)
@@ -2640,6 +2738,14 @@ bool use_band_tile(const l2c_gpu_plan *p, size_t count) {
                                                        (long long)count);
 }
 
+// Whether this call's band runs as k_near_rows (full blocks) + k_near (last
+// block): single vectors, unless the paired kernel is forced (L2C_NEAR_PAIR)
+// or L2C_NEAR_ROWS=0.
+bool use_near_rows(const l2c_gpu_plan *p, size_t count) {
+  return p->near_rows && p->near_pair != 1 && p->L > 0 &&
+         near_rows_ok((long long)p->s, (long long)p->nL, (long long)count);
+}
+
 // Band of a batch through k_band_tile (the full blocks; Wt: its dense table or
 // nullptr for weights formed on the fly) and k_near (the last block, weights
 // formed on the fly: the same products, so the same bits).  Work units: the
@@ -2964,6 +3070,18 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
       PhaseScope ps(p, L2C_PHASE_NEAR, 1 + near_launch_count(count, 8), stn);
       if (launch_band_tile(p, x, out, p->y, p->use_w ? p->Wtile[dir] : nullptr, g, c2l, stn,
                            ov ? p->near_ctas : 0, (sc.pdl & 2) && !ov) != cudaSuccess)
+        return false;
+    } else if (use_near_rows(p, count)) {
+      // full blocks with register windows, the last block per output
+      PhaseScope ps(p, L2C_PHASE_NEAR, 2, stn);
+      const bool pdl = (sc.pdl & 2) && !ov;
+      launch_k(pdl, W ? k_near_rows<true> : k_near_rows<false>,
+               blocks_for((g.nL - 1) * (g.s / 4), 256), 256, 0, stn, x, (const double *)out,
+               p->y, (const double *)p->a, (const double *)p->an, (const double *)p->dn, W, g,
+               c2l);
+      if (cudaGetLastError() != cudaSuccess ||
+          launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, false, 0, 1, pdl, 256,
+                      (g.nL - 1) * g.h) != cudaSuccess)
         return false;
     } else {
       PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, ov ? p->near_vb : 8), stn);
@@ -3502,6 +3620,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_NEAR_PAIR")) p->near_pair = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_BAND_TILE")) p->band_tile = env[0] == '0' ? 0 : -1;
   if (const char *env = std::getenv("L2C_MZ_TOP")) p->mz_top = env[0] != '0';
+  if (const char *env = std::getenv("L2C_NEAR_ROWS")) p->near_rows = env[0] != '0';
   if (const char *env = std::getenv("L2C_MZ_TOP_G")) p->mz_top_g = std::max(1, std::atoi(env));
   PCK(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device));
   if (const char *env = std::getenv("L2C_PDL")) p->pdl = std::max(0, std::atoi(env));

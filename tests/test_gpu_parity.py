@@ -638,3 +638,27 @@ def test_random_2d_vs_lines(lib, orc, seed):
         if axis == 0 and o.L >= 1:  # FMM columns: the line-by-line transform
             lines = np.stack([o(np.ascontiguousarray(x[:, j]), d)[:N0] for j in range(N1)], axis=1)
             assert relerr(out, lines) <= TOL, why + (d,)
+
+
+@pytest.mark.parametrize("N,maxs,lagrange", [(1 << 20, 64, 0), (1 << 16, 32, 0), (40000, 64, 0),
+                                             (1 << 18, 16, 1), (20000, 24, 0)])
+def test_single_vector_band_rows_vs_oracle(lib, orc, monkeypatch, N, maxs, lagrange):
+    """Single vectors take the band's full blocks with register windows (rows
+    of a block share their sources); the same vector with the per-output
+    kernel (L2C_NEAR_ROWS=0) and the oracle agree within the bar."""
+    u = make_input(N, "sign", N + 3)
+    o = orc.Oracle(N, maxs, 2, lagrange)
+    outs = {}
+    for env in ("1", "0"):
+        with monkeypatch.context() as m:
+            m.setenv("L2C_NEAR_ROWS", env)
+            p = lib.Plan(N, maxs, lagrange=lagrange)
+        for d in (0, 1):
+            out = np.zeros(N)
+            p.execute(u, out, d)
+            outs[env, d] = out
+        p.close()
+    for d in (0, 1):
+        want = o(u, d)[:N]
+        assert relerr(outs["1", d], want) <= TOL, (N, d)
+        assert relerr(outs["1", d], outs["0", d]) <= TOL, (N, d)
