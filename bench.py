@@ -89,13 +89,14 @@ def hbm_peak_gbs():
 
 FP64_PEAK_SOURCE = ("FP64 DGEMM measured in this run (cuBLAS float64 matmul 4096^3); "
                     "MEASURED_PEAKS.json holds no FP64 figure")
-BAND_PROFILE = "profiles/k_near_single_N1048576.md"
+BAND_PROFILE = "profiles/band_single_N1048576.md"
 
 
-def profile_traffic(rel_path):
-    """DRAM bytes per launch from a committed ncu summary: the mean over its
-    launch columns of dram__bytes_read.sum + dram__bytes_write.sum, read from
-    the summary's table rows ("| dram__bytes_read.sum | 25.2 MB | 25.2 MB |")."""
+def profile_traffic(rel_path, calls=None):
+    """DRAM bytes from a committed ncu summary: dram__bytes_read.sum +
+    dram__bytes_write.sum over the summary's launch columns ("|
+    dram__bytes_read.sum | 25.2 MB | 25.2 MB |"), per launch (their mean) or,
+    with calls, per call (their sum over the calls the columns cover)."""
     units = {"B": 1.0, "KB": 1e3, "MB": 1e6, "GB": 1e9}
     try:
         with open(os.path.join(REPO, rel_path)) as f:
@@ -112,7 +113,9 @@ def profile_traffic(rel_path):
             parts = cell.split()
             vals.append(float(parts[0]) * units[parts[1] if len(parts) > 1 else "B"])
         cols = vals if cols is None else [a + b for a, b in zip(cols, vals)]
-    return sum(cols) / len(cols) if cols else None
+    if not cols:
+        return None
+    return sum(cols) / (calls if calls else len(cols))
 
 
 def phase_roofline(wl, L, s, Nb, phases, fp64_tf, hbm_gbs, lagrange):
@@ -940,31 +943,35 @@ def main():
         nf = sum(near_flops(N, s, d) for d, _, _ in wl.calls) * count / len(wl.calls)
 
         def band_rate(ph):
-            launches_near = ph["near"]["launches_per_step"] / len(wl.calls)
-            avg = ph["near"]["ms_per_step"] / ph["near"]["launches_per_step"]
-            return nf / launches_near, avg, nf / launches_near / (avg * 1e-3) / 1e12
+            # the band of one call (its launches: the full blocks, then the last block)
+            per_call = ph["near"]["ms_per_step"] / len(wl.calls)
+            return per_call, nf / (per_call * 1e-3) / 1e12, ph["near"]["launches_per_step"] / len(wl.calls)
 
-        flops_per_launch, avg_ms, achieved = band_rate(phases_iso)
-        _, avg_ms_step, achieved_step = band_rate(phases)
-        # DRAM bytes per band launch from the committed ncu summary of this same
-        # command (dram__bytes_read.sum + dram__bytes_write.sum, mean of the L2C
-        # and C2L launches); other workloads were not captured.
+        ms_call, achieved, launches_call = band_rate(phases_iso)
+        ms_call_step, achieved_step, _ = band_rate(phases)
+        # DRAM bytes of one call's band from the committed ncu summary of this
+        # same command (dram__bytes_read.sum + dram__bytes_write.sum of its
+        # launches, mean of the L2C and C2L calls); other workloads were not
+        # captured.
         captured = (wl.name == "single" and N == 1 << 20 and maxs == 64
                     and args.precompute == 0 and args.lagrange == 0)
-        traffic = profile_traffic(BAND_PROFILE) if captured else None
-        roof = {"bound": "fp64", "pipe": "fp64", "kernel": "k_near (near-field band)",
+        traffic = profile_traffic(BAND_PROFILE, calls=2) if captured else None
+        kernel = ("band: " + ("k_band_tile (full blocks) + k_near (last block)" if count >= 64 and s % 8 == 0
+                              else "k_near_rows (full blocks) + k_near (last block)" if count == 1 and s % 8 == 0
+                              else "k_near / k_near_pair"))
+        roof = {"bound": "fp64", "pipe": "fp64", "kernel": kernel,
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": traffic,
-                "traffic_unit": "DRAM bytes per launch",
+                "traffic_unit": "DRAM bytes per call (the call's band launches)",
                 "traffic_source": BAND_PROFILE if traffic is not None else None,
-                "algorithmic_bytes_per_launch": 24 * N * count,
+                "algorithmic_bytes_per_call": 24 * N * count,
                 "peak_source": FP64_PEAK_SOURCE,
-                "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_ms,
-                "timing": "band launches timed with CUDA events on their stream, in a pass "
-                          "of the same workload with the band on the plan's stream (the "
-                          "kernel alone on the GPU)",
+                "flops_per_call": nf, "ms_per_call": ms_call, "launches_per_call": launches_call,
+                "timing": "the band's launches of each call timed with CUDA events on their "
+                          "stream, in a pass of the same workload with the band on the plan's "
+                          "stream (the band alone on the GPU)",
                 "achieved_in_step": achieved_step, "frac_in_step": achieved_step / peak,
-                "avg_launch_ms_in_step": avg_ms_step,
+                "ms_per_call_in_step": ms_call_step,
                 "in_step_note": "in the timed step the band runs on a second stream beside "
                                 "the far-field chain, whose kernels have scheduling priority",
                 "note": "reference flop count of directM/directL (3 per band term); a term "

@@ -544,8 +544,9 @@ inline size_t near_table_size(size_t N, size_t s) {
 // thread takes row groups g and s/4-1-g, whose trip counts 2s - 4g add up to
 // the same total for every thread; the lanes of a warp take the same groups
 // of consecutive blocks.  Terms are summed in order of k into one
-// FMA chain from zero; y = out_in + sum.  TAB: weights from the plan's table
-// (k_near_weights' layout; the same products, the same bits).
+// FMA chain from zero; y = out_in + sum.  The last (ragged) block's outputs
+// take k_near's sums, one per thread, in the same launch.  TAB: weights from
+// the plan's table (k_near_weights' layout; the same products, the same bits).
 template <bool TAB>
 __device__ __forceinline__ void near_rows_group(const double *__restrict__ xb,
                                                 const double *__restrict__ lo,
@@ -599,10 +600,20 @@ __global__ void __launch_bounds__(256) k_near_rows(const double *__restrict__ x,
                                                    const double *__restrict__ W, Geo g, int c2l) {
   pdl_wait();
   pdl_trigger();
-  // items (parity, pair, block) with the block fastest: the lanes of a warp
-  // share their rows' trip counts (no divergence) and read at a stride of h
-  const long long G = g.s / 4, nb = g.nL - 1;
-  const long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  // the last (ragged) block first, one output per thread (k_near's sums), so
+  // its long chains start in the first wave; then items (parity, pair, block)
+  // with the block fastest: the lanes of a warp share their rows' trip counts
+  // (no divergence) and read at a stride of h
+  const long long G = g.s / 4, nb = g.nL - 1, jlast = nb * g.h, ntail = g.N - jlast;
+  long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (item < ntail) {
+    const long long j = jlast + item;
+    double res[1];
+    near_sums<1>(x + j, g.N, a, an, dn, W, g, c2l, j, res);
+    y[j] = out[j * g.stride] + res[0];
+    return;
+  }
+  item -= ntail;
   if (item >= nb * G) return;
   const long long pq = item / nb, b = item - pq * nb;
   const int p = (int)(pq / (G / 2)), q = (int)(pq % (G / 2));
@@ -1215,9 +1226,10 @@ inline unsigned blocks_for(long long n, int threads) {
 // registers and shared memory to the far-field chain beside it.  Each output
 // sums its terms in order of k in one FMA chain from zero, then
 // y = out_in + sum, staged through the slot the block no longer needs and
-// written a row at a time.  The last (ragged) block is k_near's
-// (jbeg = (nL - 1) h).  The leaf size is a template parameter, so every loop
-// bound and index below is a compile-time constant or a 32-bit offset.
+// written a row at a time.  The last (ragged) block takes k_near's sums, an
+// output of 8 vectors per thread, as the first work units of the same launch.  The leaf
+// size is a template parameter, so every loop bound and index below is a
+// compile-time constant or a 32-bit offset.
 // ---------------------------------------------------------------------------
 constexpr int BT_WARPS = 4;
 constexpr int BT_THREADS = 32 * BT_WARPS;
@@ -1349,7 +1361,8 @@ __device__ __forceinline__ void band_tile_fill_w(double *wdst, const double *__r
     l2c_oz::cp_async16(wdst + 2 * idx, src + 2 * idx, 16);
 }
 
-// Work unit u: vector chunk u % nchunk, blocks [seg bseg, (seg + 1) bseg) of
+// Work units: first, per vector chunk, its last (ragged) block; then unit
+// nchunk + u: vector chunk u % nchunk, blocks [seg bseg, (seg + 1) bseg) of
 // the nL - 1 full ones, seg = u / nchunk (a segment's chunks run side by side,
 // so its weights are read from L2 by all of them).  Warp w takes the row
 // groups q = 8 t' + w and 8 t' + 7 - w (t' = 0, 1, ...), q < s/2.  At most
@@ -1370,8 +1383,36 @@ __global__ void __launch_bounds__(BT_THREADS, 4)
   pdl_trigger();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long nfull = g.nL - 1, nseg = (nfull + bseg - 1) / bseg;
-  for (long long u = blockIdx.x; u < nchunk * nseg; u += gridDim.x) {
-    const long long v0 = (u % nchunk) * VCH, seg = u / nchunk;
+  const long long jlast = nfull * H, ntail = g.N - jlast;
+  for (long long u = blockIdx.x; u < nchunk * (nseg + 1); u += gridDim.x) {
+    if (u < nchunk) {
+      // the last (ragged) block of chunk u: k_near's sums (weights formed on
+      // the fly, each shared by 8 vectors; the same bits as k_near), an
+      // output of 8 vectors per thread, a vector at a time past the last
+      // full group of 8
+      const long long vb = u * VCH, nv = g.count - vb < VCH ? g.count - vb : VCH;
+      const long long n8 = nv / 8;
+      for (long long idx = threadIdx.x; idx < (n8 + (nv - 8 * n8)) * ntail;
+           idx += BT_THREADS) {
+        const long long grp = idx / ntail, j = jlast + idx % ntail;
+        if (grp < n8) {
+          const long long v0 = vb + 8 * grp;
+          double res[8];
+          near_sums<8>(x + v0 * g.N + j, g.N, a, an, dn, nullptr, g, c2l, j, res);
+#pragma unroll
+          for (int e = 0; e < 8; e++)
+            y[(v0 + e) * g.N + j] = out[(v0 + e) * g.dist + j * g.stride] + res[e];
+        } else {
+          const long long v = vb + 8 * n8 + (grp - n8);
+          double res[1];
+          near_sums<1>(x + v * g.N + j, g.N, a, an, dn, nullptr, g, c2l, j, res);
+          y[v * g.N + j] = out[v * g.dist + j * g.stride] + res[0];
+        }
+      }
+      continue;
+    }
+    const long long uu = u - nchunk;
+    const long long v0 = (uu % nchunk) * VCH, seg = uu / nchunk;
     const long long b0 = seg * bseg, b1 = b0 + bseg < nfull ? b0 + bseg : nfull;
     // half windows b0 and b0 + 1 (block b0 needs both), block b0's weights
     band_tile_fill<S>(bt_smem + (int)(b0 % 3) * BT::SLOT, x, g, v0, b0);
@@ -2738,17 +2779,17 @@ bool use_band_tile(const l2c_gpu_plan *p, size_t count) {
                                                        (long long)count);
 }
 
-// Whether this call's band runs as k_near_rows (full blocks) + k_near (last
-// block): single vectors, unless the paired kernel is forced (L2C_NEAR_PAIR)
-// or L2C_NEAR_ROWS=0.
+// Whether this call's band runs as k_near_rows (full blocks and, one output
+// per thread, the last block): single vectors, unless the paired kernel is
+// forced (L2C_NEAR_PAIR) or L2C_NEAR_ROWS=0.
 bool use_near_rows(const l2c_gpu_plan *p, size_t count) {
   return p->near_rows && p->near_pair != 1 && p->L > 0 &&
          near_rows_ok((long long)p->s, (long long)p->nL, (long long)count);
 }
 
-// Band of a batch through k_band_tile (the full blocks; Wt: its dense table or
-// nullptr for weights formed on the fly) and k_near (the last block, weights
-// formed on the fly: the same products, so the same bits).  Work units: the
+// Band of a batch through k_band_tile, one launch (the full blocks; Wt: its
+// dense table or nullptr for weights formed on the fly; the last block with
+// weights formed on the fly: the same products, so the same bits).  Work units: the
 // run of blocks per unit (bseg) is the one whose rounds of units over the grid
 // finish first, counting half a block for the extra half window a unit loads.
 cudaError_t launch_band_tile(const l2c_gpu_plan *p, const double *x, const double *out,
@@ -2768,16 +2809,14 @@ cudaError_t launch_band_tile(const l2c_gpu_plan *p, const double *x, const doubl
       best_seg = bseg;
     }
   }
-  const long long units = nchunk * ((nfull + best_seg - 1) / best_seg);
+  // the chunks' last-block units first, then the full blocks
+  const long long units = nchunk * (1 + (nfull + best_seg - 1) / best_seg);
   const unsigned grid = (unsigned)std::min(units, grid_cap);
   auto *kern = Wt ? band_tile_kernel<true>(g.s) : band_tile_kernel<false>(g.s);
   launch_k(pdl, kern, grid, BT_THREADS, band_tile_smem(g.s), st, x, out, y, Wt,
            (const double *)p->a, (const double *)p->an, (const double *)p->dn, g, c2l, nchunk,
            best_seg);
-  const cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  return launch_near(x, out, y, p->a, p->an, p->dn, nullptr, g, c2l, st, false, 0, 8, pdl, 256,
-                     (g.nL - 1) * g.h);
+  return cudaGetLastError();
 }
 
 // Pairs pay off when a warp's outputs have very unequal term counts (small
@@ -3067,22 +3106,18 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
                cudaStreamWaitEvent(st2, p->ev_fork, 0) != cudaSuccess))
       return false;
     if (use_band_tile(p, count)) {
-      PhaseScope ps(p, L2C_PHASE_NEAR, 1 + near_launch_count(count, 8), stn);
+      PhaseScope ps(p, L2C_PHASE_NEAR, 1, stn);
       if (launch_band_tile(p, x, out, p->y, p->use_w ? p->Wtile[dir] : nullptr, g, c2l, stn,
                            ov ? p->near_ctas : 0, (sc.pdl & 2) && !ov) != cudaSuccess)
         return false;
     } else if (use_near_rows(p, count)) {
-      // full blocks with register windows, the last block per output
-      PhaseScope ps(p, L2C_PHASE_NEAR, 2, stn);
-      const bool pdl = (sc.pdl & 2) && !ov;
-      launch_k(pdl, W ? k_near_rows<true> : k_near_rows<false>,
-               blocks_for((g.nL - 1) * (g.s / 4), 256), 256, 0, stn, x, (const double *)out,
-               p->y, (const double *)p->a, (const double *)p->an, (const double *)p->dn, W, g,
-               c2l);
-      if (cudaGetLastError() != cudaSuccess ||
-          launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, false, 0, 1, pdl, 256,
-                      (g.nL - 1) * g.h) != cudaSuccess)
-        return false;
+      // full blocks with register windows, the last block per output, one launch
+      PhaseScope ps(p, L2C_PHASE_NEAR, 1, stn);
+      launch_k((sc.pdl & 2) && !ov, W ? k_near_rows<true> : k_near_rows<false>,
+               blocks_for((g.nL - 1) * (g.s / 4) + g.N - (g.nL - 1) * g.h, 256), 256, 0, stn, x,
+               (const double *)out, p->y, (const double *)p->a, (const double *)p->an,
+               (const double *)p->dn, W, g, c2l);
+      if (cudaGetLastError() != cudaSuccess) return false;
     } else {
       PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, ov ? p->near_vb : 8), stn);
       if (launch_near(x, out, p->y, p->a, p->an, p->dn, W, g, c2l, stn, near_pair(p),
