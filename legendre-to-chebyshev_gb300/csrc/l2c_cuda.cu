@@ -2349,6 +2349,14 @@ struct PhaseScope;
 struct TuneCfg {
   int overlap = -1, pdl = -1, prio = -1, nthreads = 128, nvb = 8, npair = -1, nctas = 0,
       nbuf = 1, wtab = -1, fork = 0;
+  // the per-level structure of the far-field chain and the band's schedule:
+  //   mtop  mixed form: coarsest transfer level in the one top launch (-2: the
+  //         plan's rule, levels of at most 64 slots; -1: none)
+  //   mtopg mixed form: trees per CTA of that launch (0: the plan's)
+  //   tl0   plain form: level of the subtree roots of the transfer kernels
+  //         (-1: by the batch size)
+  //   bseg  tiled band: blocks per work unit (0: its cost model)
+  int mtop = -2, mtopg = 0, tl0 = -1, bseg = 0;
 };
 
 // A tuned call shape and its choices (dist is 0 for single vectors).
@@ -2413,7 +2421,11 @@ struct l2c_gpu_plan {
   size_t cap_wE = 0, cap_cE = 0;
   int *bad = nullptr;  // per vector: an Inf or NaN input seen (mixed form)
   bool mz_top = true;  // the coarsest transfer levels in one launch (mz_top_level)
+  int mz_top_lvl = -2;  // TuneCfg::mtop
+  int tree_l0 = -1;     // TuneCfg::tl0
+  int band_bseg = 0;    // TuneCfg::bseg
   int mz_top_g = 2;    // trees per CTA of that launch
+  int mz_top_g_base = 2;  // the plan's own (environment)
   // captured launch sequences, keyed by the call's shape and pointers
   struct GraphEntry {
     size_t dir, count, dist, stride;
@@ -2653,11 +2665,12 @@ struct TreePlan {
   bool staged;  // false: one tiled launch per level
 };
 
-TreePlan tree_plan(size_t L, size_t count) {
+TreePlan tree_plan(size_t L, size_t count, int l0_forced = -1) {
   TreePlan t{0, 0, 0, false};
   if (L < 4) return t;
   int l0 = 0;
   while (l0 + 1 < (int)L - 1 && (double)count * 2.0 * (double)(8LL << l0) <= 2.0 * 152) l0++;
+  if (l0_forced >= 0) l0 = std::min(l0_forced, (int)L - 2);
   if ((int)L - 1 - l0 > 7) l0 = (int)L - 8;
   t.l0 = l0;
   t.d = (int)L - 1 - l0;
@@ -2809,6 +2822,7 @@ cudaError_t launch_band_tile(const l2c_gpu_plan *p, const double *x, const doubl
       best_seg = bseg;
     }
   }
+  if (p->band_bseg > 0) best_seg = std::min<long long>(p->band_bseg, std::max(nfull, 1LL));
   // the chunks' last-block units first, then the full blocks
   const long long units = nchunk * (1 + (nfull + best_seg - 1) / best_seg);
   const unsigned grid = (unsigned)std::min(units, grid_cap);
@@ -2902,7 +2916,8 @@ TreeLevels tree_levels(long long from, long long to, int G) {
 // launch, a CTA per tree (TOP kernels): those with at most 64 slots per tree,
 // i.e. at most one tile per warp (-1: none; L2C_MZ_TOP=0 turns this off).
 int mz_top_level(const l2c_gpu_plan *p) {
-  if (!p->mz_top || p->L < 2) return -1;
+  if (!p->mz_top || p->L < 2 || p->mz_top_lvl == -1) return -1;
+  if (p->mz_top_lvl >= 0) return std::min({p->mz_top_lvl, (int)p->L - 2, TREE_TOP_MAX - 1});
   int lt = -1;
   while (lt + 1 <= (int)p->L - 2 && lt + 1 < TREE_TOP_MAX && slots_at((size_t)lt + 1) <= 64)
     lt++;
@@ -3138,7 +3153,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaGetLastError());
   }
   if (!band(1)) return 0;
-  const TreePlan tp = tree_plan(p->L, count);
+  const TreePlan tp = tree_plan(p->L, count, p->tree_l0);
   {
     PhaseScope ps(p, L2C_PHASE_TREE_UP, tree_launches(tp, p->L));
     CK(sweep_up(p->w, g, tp, st, LaunchOpt(sc.pdl & 1, sc.prio), p->nodal));
@@ -3184,6 +3199,10 @@ unsigned long long cfg_signature(const TuneCfg &c) {
   put(c.nctas, 24);
   put(c.wtab, 2);
   put(c.fork, 3);
+  put(c.mtop + 1, 3);  // -2 .. 5
+  put(c.mtopg, 3);
+  put(c.tl0, 4);
+  put(c.bseg, 5);
   return v;
 }
 
@@ -3197,6 +3216,10 @@ void cfg_apply(l2c_gpu_plan *p, const TuneCfg &c) {
   p->near_ctas = (unsigned)c.nctas;
   p->oz_nbuf = c.nbuf;
   p->band_fork = c.fork;
+  p->mz_top_lvl = c.mtop;
+  p->mz_top_g = c.mtopg > 0 ? c.mtopg : p->mz_top_g_base;
+  p->tree_l0 = c.tl0;
+  p->band_bseg = c.bseg;
   p->oz_ld_ctas = p->oz_ld_ctas_nb[c.nbuf == 2 ? 2 : 1];
   p->cfg_sig = cfg_signature(c);
 }
@@ -3385,15 +3408,17 @@ TuneCfg resolved_cfg(l2c_gpu_plan *p, size_t count) {
 
 void cfg_text(const TuneCfg &c, char *buf, size_t len) {
   snprintf(buf, len, "overlap=%d band_fork=%d pdl=%d prio=%d near_threads=%d near_vb=%d "
-           "near_pair=%d near_ctas=%d nbuf=%d near_table=%d", c.overlap, c.fork, c.pdl, c.prio,
-           c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, c.wtab);
+           "near_pair=%d near_ctas=%d nbuf=%d near_table=%d mz_top=%d mz_top_g=%d tree_l0=%d "
+           "band_bseg=%d", c.overlap, c.fork, c.pdl, c.prio, c.nthreads, c.nvb, c.npair,
+           c.nctas, c.nbuf, c.wtab, c.mtop, c.mtopg, c.tl0, c.bseg);
 }
 
 // Cache file: one line per tuned shape, fields separated by '|':
-// l2c-tune-3|device|SMs|N|maxs|form|precompute|dir|count|dist|stride|
-//   overlap|pdl|prio|nthreads|nvb|npair|nctas|nbuf|wtab|fork|ms|ms_default
+// l2c-tune-4|device|SMs|N|maxs|form|precompute|dir|count|dist|stride|
+//   overlap|pdl|prio|nthreads|nvb|npair|nctas|nbuf|wtab|fork|mtop|mtopg|tl0|bseg|
+//   ms|ms_default
 // (form 0 modal, 1 nodal, 2 mixed).  Later lines win.
-constexpr int TUNE_FIELDS = 23;
+constexpr int TUNE_FIELDS = 27;
 
 struct TuneKey {
   char dev[256];
@@ -3425,11 +3450,11 @@ void cache_append(const l2c_gpu_plan *p, const TunedShape &t) {
   if (!f) return;  // an unwritable cache leaves the tuning in the plan only
   const TuneCfg &c = t.cfg;
   std::fprintf(f,
-               "l2c-tune-3|%s|%d|%zu|%zu|%d|%d|%zu|%zu|%zu|%zu|%d|%d|%d|%d|%d|%d|%d|%d|%d|%d|"
-               "%.6f|%.6f\n",
+               "l2c-tune-4|%s|%d|%zu|%zu|%d|%d|%zu|%zu|%zu|%zu|%d|%d|%d|%d|%d|%d|%d|%d|%d|%d|"
+               "%d|%d|%d|%d|%.6f|%.6f\n",
                k.dev, k.sms, p->N, p->maxs, k.form, k.pre, t.dir, t.count, t.dist, t.stride,
                c.overlap, c.pdl, c.prio, c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, c.wtab,
-               c.fork, t.ms, t.ms_default);
+               c.fork, c.mtop, c.mtopg, c.tl0, c.bseg, t.ms, t.ms_default);
   std::fclose(f);
 }
 
@@ -3451,7 +3476,7 @@ void cache_load(l2c_gpu_plan *p) {
         *q = 0;
         fld[n++] = q + 1;
       }
-    if (n != TUNE_FIELDS || std::strcmp(fld[0], "l2c-tune-3") != 0) continue;
+    if (n != TUNE_FIELDS || std::strcmp(fld[0], "l2c-tune-4") != 0) continue;
     if (std::strcmp(fld[1], k.dev) != 0 || std::atoi(fld[2]) != k.sms) continue;
     auto u = [&](int i) { return (size_t)std::strtoull(fld[i], nullptr, 10); };
     auto iv = [&](int i) { return (int)std::strtol(fld[i], nullptr, 10); };
@@ -3471,8 +3496,12 @@ void cache_load(l2c_gpu_plan *p) {
     t.cfg.nbuf = iv(18);
     t.cfg.wtab = iv(19);
     t.cfg.fork = iv(20);
-    t.ms = std::strtod(fld[21], nullptr);
-    t.ms_default = std::strtod(fld[22], nullptr);
+    t.cfg.mtop = iv(21);
+    t.cfg.mtopg = iv(22);
+    t.cfg.tl0 = iv(23);
+    t.cfg.bseg = iv(24);
+    t.ms = std::strtod(fld[25], nullptr);
+    t.ms_default = std::strtod(fld[26], nullptr);
     t.from_cache = true;
     // only values the launches accept
     const TuneCfg &c = t.cfg;
@@ -3480,7 +3509,8 @@ void cache_load(l2c_gpu_plan *p) {
         c.pdl < 0 || c.pdl > 7 || c.prio < 0 || c.prio > 1 ||
         (c.nthreads != 128 && c.nthreads != 256) || c.nvb < 1 || c.nvb > 8 || c.npair < -1 ||
         c.npair > 1 || c.nctas < 0 || c.nbuf < 1 || c.nbuf > 2 || c.wtab < -1 || c.wtab > 1 ||
-        c.fork < 0 || c.fork > 3)
+        c.fork < 0 || c.fork > 3 || c.mtop < -2 || c.mtop > 5 || c.mtopg < 0 || c.mtopg > 7 ||
+        c.tl0 < -1 || c.tl0 > 14 || c.bseg < 0 || c.bseg > 31)
       continue;
     p->tuned.push_back(t);
   }
@@ -3539,6 +3569,21 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
       if (p->precompute || (count > 1 && near_table_size(p->N, p->s) <= count * p->N))
         knobs.push_back({&TuneCfg::wtab, {0, 1}});
       if (p->mixed) knobs.push_back({&TuneCfg::nbuf, {1, 2}});
+      // the per-level structure: the mixed form's top launch (its coarsest
+      // level and trees per CTA), the plain form's subtree roots, the tiled
+      // band's blocks per work unit
+      if (p->mixed && p->L >= 4) {
+        knobs.push_back({&TuneCfg::mtop, {-2, -1, 3, 5}});
+        knobs.push_back({&TuneCfg::mtopg, {0, 1, 4}});
+      }
+      if (!p->mixed && p->L >= 4) {
+        const int l0 = tree_plan(p->L, count).l0;
+        std::vector<int> v = {-1};
+        for (int d = -2; d <= 2; d++)
+          if (d != 0 && l0 + d >= 0 && l0 + d <= (int)p->L - 2) v.push_back(l0 + d);
+        knobs.push_back({&TuneCfg::tl0, v});
+      }
+      if (tile) knobs.push_back({&TuneCfg::bseg, {0, 1, 2, 4}});
       for (int pass = 0; pass < 2 && best > 0.0; pass++) {
         bool kept = false;
         for (const Knob &kb : knobs)
@@ -3657,6 +3702,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_MZ_TOP")) p->mz_top = env[0] != '0';
   if (const char *env = std::getenv("L2C_NEAR_ROWS")) p->near_rows = env[0] != '0';
   if (const char *env = std::getenv("L2C_MZ_TOP_G")) p->mz_top_g = std::max(1, std::atoi(env));
+  p->mz_top_g_base = p->mz_top_g;
   PCK(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device));
   if (const char *env = std::getenv("L2C_PDL")) p->pdl = std::max(0, std::atoi(env));
   if (const char *env = std::getenv("L2C_CHAIN_PRIO")) p->chain_prio_mode = env[0] == '1' ? 1 : 0;
@@ -3670,6 +3716,13 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_NEAR_TABLE")) p->base.wtab = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_BAND_FORK"))
     p->base.fork = std::min(3, std::max(0, std::atoi(env)));
+  // the per-level structure (TuneCfg::mtop, mtopg, tl0, bseg)
+  if (const char *env = std::getenv("L2C_MZ_TOP_LVL"))
+    p->base.mtop = std::min(5, std::max(-2, std::atoi(env)));
+  if (const char *env = std::getenv("L2C_TREE_L0"))
+    p->base.tl0 = std::min(14, std::max(-1, std::atoi(env)));
+  if (const char *env = std::getenv("L2C_BAND_BSEG"))
+    p->base.bseg = std::min(31, std::max(0, std::atoi(env)));
   p->precompute = (flags & L2C_PLAN_PRECOMPUTE_NEAR) != 0;
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;

@@ -132,7 +132,11 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
                 {"L2C_BAND_FORK": "1"}, {"L2C_BAND_FORK": "2"}, {"L2C_BAND_FORK": "3"},
                 {"L2C_BAND_FORK": "2", "L2C_PDL": "7"},
                 # the mixed form's coarsest transfer levels one launch each
-                {"L2C_MZ_TOP": "0"}, {"L2C_MZ_TOP": "0", "L2C_PDL": "0"}):
+                {"L2C_MZ_TOP": "0"}, {"L2C_MZ_TOP": "0", "L2C_PDL": "0"},
+                # the per-level structure the autotuner searches
+                {"L2C_MZ_TOP_LVL": "5"}, {"L2C_MZ_TOP_LVL": "3", "L2C_MZ_TOP_G": "1"},
+                {"L2C_MZ_TOP_G": "4"}, {"L2C_TREE_L0": "1"}, {"L2C_TREE_L0": "3"},
+                {"L2C_BAND_BSEG": "1"}, {"L2C_BAND_BSEG": "4"}):
         with monkeypatch.context() as m:
             for k, v in env.items():
                 m.setenv(k, v)
