@@ -531,64 +531,117 @@ inline size_t near_table_size(size_t N, size_t s) {
   return n;
 }
 
-// Band of one vector with register windows (full blocks b < nL-1; s a
-// multiple of 8).  Output j = b h + 2 i' + p sums, over sources m' = i' ..
-// 2s-1 of block b and parity p, w(k, j) x[b h + 2 m' + p] with k = m' - i',
-// where w = lo[k] hi[j + k] (L2C: a[k] a[j+k]; C2L: -(dn[k] an[j+k]), with
-// -sqrt(pi) standing for dn[0], which gives the k = 0 term sqrt(pi) an[j]
-// exactly) and j + k = b h + p + i' + m'.  A thread owns 4 consecutive rows
-// i'0 .. i'0+3 of one parity: at source m' every row reads the same x, and as
-// m' advances by one the rows' lo values shift down one row and their hi
-// values up one row, so each step loads one x, one lo and one hi value for
-// 4 DMUL + 4 DFMA (the per-output kernel loads all three per term).  Each
-// thread takes row groups g and s/4-1-g, whose trip counts 2s - 4g add up to
-// the same total for every thread; the lanes of a warp take the same groups
-// of consecutive blocks.  Terms are summed in order of k into one
-// FMA chain from zero; y = out_in + sum.  The last (ragged) block's outputs
-// take k_near's sums, one per thread, in the same launch.  TAB: weights from
-// the plan's table (k_near_weights' layout; the same products, the same bits).
+// Band of one vector with register windows (full blocks b < nL-1).  Output
+// j = b h + 2 i' + p sums, over sources m' = i' .. 2s-1 of block b and parity
+// p, w(k, j) x[b h + 2 m' + p] with k = m' - i', where w = lo[k] hi[j + k]
+// (L2C: a[k] a[j+k]; C2L: -(dn[k] an[j+k]), with -sqrt(pi) standing for dn[0],
+// which gives the k = 0 term sqrt(pi) an[j] exactly) and j + k = b h + p + i'
+// + m'.  A thread owns a row group, up to 4 consecutive rows i'0 .. i'0+3 of
+// one parity: at source m' every row reads the same x, and as m' advances by
+// one the rows' lo values shift down one row and their hi values up one row,
+// so each step loads one x, one lo and one hi value for 4 DMUL + 4 DFMA (the
+// per-output kernel loads all three per term).  The lanes of a warp take the
+// same row group of consecutive blocks, so they run the same trip count.
+// Terms are summed in order of k into one FMA chain from zero; y = out_in +
+// sum.  TAB: weights from the dense per-block table of k_band_tile_weights
+// (W'[b][p][m'][i'], the row group's four at one m' contiguous; the same
+// products, the same bits; that loop is unrolled so that the table loads of
+// several steps are in flight together).
 template <bool TAB>
 __device__ __forceinline__ void near_rows_group(const double *__restrict__ xb,
                                                 const double *__restrict__ lo,
                                                 const double *__restrict__ hi,
-                                                const double *__restrict__ Wb, long long hbase,
-                                                const Geo &g, int c2l, int p, int ip0,
+                                                const double *__restrict__ Wg, long long hbase,
+                                                const Geo &g, int c2l, int p, int ip0, int R,
                                                 double (&acc)[4]) {
   const int s2 = 2 * (int)g.s;
   auto lo_at = [&](int k) -> double { return c2l && k == 0 ? -SQRT_PI : lo[k]; };
-  auto tab = [&](int k, int ip) -> double {  // table entry of row i', term k
-    const long long off = k < g.s ? (long long)k * g.h
-                                  : 4 * g.s * k - (long long)k * k + k - g.s * g.s - g.s;
-    return Wb[off + 2 * ip + p];
-  };
   double wl[4], wh[4];  // row r: lo[m' - i'0 - r], hi[hbase + i'0 + r + m']
 #pragma unroll
   for (int r = 0; r < 4; r++) {
     acc[r] = 0.0;
     wl[r] = 0.0;
-    wh[r] = TAB ? 0.0 : hi[hbase + ip0 + r + ip0];
+    wh[r] = TAB || r >= R ? 0.0 : hi[hbase + ip0 + r + ip0];
   }
+#pragma unroll(TAB ? 8 : 1)
   for (int mp = ip0; mp < s2; mp++) {
     const int t = mp - ip0;  // rows r <= t have a term at this m'
-    if (!TAB) {
-      // shift the windows to m' and bring in row 0's lo and row 3's hi
+    double wt[4];
+    if (TAB) {
+      const double2 q0 = __ldg(reinterpret_cast<const double2 *>(Wg + (long long)mp * g.s));
+      const double2 q1 = __ldg(reinterpret_cast<const double2 *>(Wg + (long long)mp * g.s) + 1);
+      wt[0] = q0.x;
+      wt[1] = q0.y;
+      wt[2] = q1.x;
+      wt[3] = q1.y;
+    } else {
+      // shift the windows to m' and bring in row 0's lo and row R-1's hi
 #pragma unroll
       for (int r = 3; r > 0; r--) wl[r] = wl[r - 1];
       wl[0] = lo_at(t);
       if (t > 0) {
 #pragma unroll
         for (int r = 0; r < 3; r++) wh[r] = wh[r + 1];
-        wh[3] = hi[hbase + ip0 + 3 + mp];
+        if (R == 4) {
+          wh[3] = hi[hbase + ip0 + 3 + mp];
+        } else {
+#pragma unroll
+          for (int r = 0; r < 3; r++)
+            if (r == R - 1) wh[r] = hi[hbase + ip0 + r + mp];
+        }
       }
     }
     const double xv = xb[2 * mp + p];
 #pragma unroll
     for (int r = 0; r < 4; r++)
-      if (r <= t) {
-        const double w = TAB ? tab(t - r, ip0 + r) : c2l ? -(wl[r] * wh[r]) : wl[r] * wh[r];
+      if (r <= t && r < R) {
+        const double w = TAB ? wt[r] : c2l ? -(wl[r] * wh[r]) : wl[r] * wh[r];
         acc[r] = fma(w, xv, acc[r]);
       }
   }
+}
+
+// Item it of a vector's band with register windows: the last (ragged) block
+// first, one output per thread (k_near's sums, weights formed on the fly),
+// then (parity, row group, block) with the block fastest.  x, out, y: the
+// vector's arrays (out with g.stride); a, an, dn: its Lambda tables; W: its
+// dense weight table (k_band_tile_weights) or nullptr.
+template <bool TAB>
+__device__ __forceinline__ void near_rows_item(const double *__restrict__ x, const double *out,
+                                               double *__restrict__ y,
+                                               const double *__restrict__ a,
+                                               const double *__restrict__ an,
+                                               const double *__restrict__ dn,
+                                               const double *__restrict__ W, const Geo &g,
+                                               int c2l, long long it) {
+  const long long nb = g.nL - 1, jlast = nb * g.h, ntail = g.N - jlast;
+  if (it < ntail) {
+    const long long j = jlast + it;
+    double res[1];
+    near_sums<1>(x + j, g.N, a, an, dn, nullptr, g, c2l, j, res);
+    y[j] = out[j * g.stride] + res[0];
+    return;
+  }
+  it -= ntail;
+  const long long G = (g.s + 3) / 4;  // row groups per parity
+  const long long pg = it / nb, b = it - pg * nb;
+  const int p = (int)(pg / G), gi = (int)(pg % G), ip0 = 4 * gi;
+  const int R = (int)g.s - ip0 < 4 ? (int)g.s - ip0 : 4;
+  double acc[4];
+  near_rows_group<TAB>(x + b * g.h, c2l ? dn : a, c2l ? an : a,
+                       TAB ? W + ((b * 2 + p) * 2 * g.s) * g.s + ip0 : nullptr, b * g.h + p, g,
+                       c2l, p, ip0, R, acc);
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+    if (r < R) {
+      const long long j = b * g.h + 2 * (ip0 + r) + p;
+      y[j] = out[j * g.stride] + acc[r];
+    }
+}
+
+// Items of a vector's band (near_rows_item).
+__host__ __device__ inline long long near_rows_items(const Geo &g) {
+  return (g.N - (g.nL - 1) * g.h) + (g.nL - 1) * 2 * ((g.s + 3) / 4);
 }
 
 template <bool TAB>
@@ -600,43 +653,18 @@ __global__ void __launch_bounds__(256) k_near_rows(const double *__restrict__ x,
                                                    const double *__restrict__ W, Geo g, int c2l) {
   pdl_wait();
   pdl_trigger();
-  // the last (ragged) block first, one output per thread (k_near's sums), so
-  // its long chains start in the first wave; then items (parity, pair, block)
-  // with the block fastest: the lanes of a warp share their rows' trip counts
-  // (no divergence) and read at a stride of h
-  const long long G = g.s / 4, nb = g.nL - 1, jlast = nb * g.h, ntail = g.N - jlast;
-  long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (item < ntail) {
-    const long long j = jlast + item;
-    double res[1];
-    near_sums<1>(x + j, g.N, a, an, dn, W, g, c2l, j, res);
-    y[j] = out[j * g.stride] + res[0];
-    return;
-  }
-  item -= ntail;
-  if (item >= nb * G) return;
-  const long long pq = item / nb, b = item - pq * nb;
-  const int p = (int)(pq / (G / 2)), q = (int)(pq % (G / 2));
-  const double *xb = x + b * g.h;
-  const double *lo = c2l ? dn : a, *hi = c2l ? an : a;
-  const double *Wb = TAB ? W + b * (3 * g.s * g.s + g.s) : nullptr;
-  const long long hbase = b * g.h + p;  // hi index = hbase + i' + m'
-#pragma unroll 1
-  for (int half = 0; half < 2; half++) {
-    const int gi = half == 0 ? q : (int)G - 1 - q, ip0 = 4 * gi;
-    double acc[4];
-    near_rows_group<TAB>(xb, lo, hi, Wb, hbase, g, c2l, p, ip0, acc);
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-      const long long j = b * g.h + 2 * (ip0 + r) + p;
-      y[j] = out[j * g.stride] + acc[r];
-    }
-  }
+  const long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (it < near_rows_items(g)) near_rows_item<TAB>(x, out, y, a, an, dn, W, g, c2l, it);
 }
 
-// Whether a single vector's band takes k_near_rows.
-inline bool near_rows_ok(long long s, long long nL, long long count) {
-  return count == 1 && s % 8 == 0 && nL >= 2;
+// Whether a single vector's band takes k_near_rows: at least 64 CTAs of row
+// items (any = true: any size).  Its sums are chains of up to 2s dependent
+// FMAs, so a vector with fewer blocks is bound by their latency and takes the
+// per-output kernel, whose two chains per output are half as long and whose
+// threads are four times as many.
+inline bool near_rows_ok(long long s, long long nL, long long count, bool any = false) {
+  return count == 1 && s >= 1 && nL >= 2 &&
+         (any || (nL - 1) * 2 * ((s + 3) / 4) >= 64 * 256);
 }
 
 // Step 1: leaf node t in [2, 2^(L+1)) of parity sg: w = sum_i x[t h + 2i + sg] T_sg[i][m].
@@ -2389,7 +2417,7 @@ struct l2c_gpu_plan {
   // dense band weights of the full blocks for k_band_tile (built on first use)
   double *Wtile[2] = {nullptr, nullptr};
   int band_tile = -1;  // batches' band as dense register tiles: -1 when eligible, 0 never
-  bool near_rows = true;  // single vectors' band with register windows (k_near_rows)
+  int near_rows = -1;  // single vectors' band with register windows: -1 by size, 0 never, 1 always
   int sms = 152;       // multiprocessors of the plan's device
   bool precompute = false;  // created with L2C_PLAN_PRECOMPUTE_NEAR
   bool use_w = false;       // this call's band reads Wnear (see TuneCfg::wtab)
@@ -2793,11 +2821,12 @@ bool use_band_tile(const l2c_gpu_plan *p, size_t count) {
 }
 
 // Whether this call's band runs as k_near_rows (full blocks and, one output
-// per thread, the last block): single vectors, unless the paired kernel is
-// forced (L2C_NEAR_PAIR) or L2C_NEAR_ROWS=0.
+// per thread, the last block): single vectors with enough blocks (any with
+// L2C_NEAR_ROWS=1, none with 0), unless the paired kernel is forced
+// (L2C_NEAR_PAIR).
 bool use_near_rows(const l2c_gpu_plan *p, size_t count) {
-  return p->near_rows && p->near_pair != 1 && p->L > 0 &&
-         near_rows_ok((long long)p->s, (long long)p->nL, (long long)count);
+  return p->near_rows != 0 && p->near_pair != 1 && p->L > 0 &&
+         near_rows_ok((long long)p->s, (long long)p->nL, (long long)count, p->near_rows == 1);
 }
 
 // Band of a batch through k_band_tile, one launch (the full blocks; Wt: its
@@ -3092,7 +3121,9 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     CK(cudaGetLastError());
     x = p->x;
   }
-  const double *W = p->use_w && !use_band_tile(p, count) ? p->Wnear[dir] : nullptr;
+  const bool dense_w = use_band_tile(p, count) || use_near_rows(p, count);
+  const double *W = p->use_w && !dense_w ? p->Wnear[dir] : nullptr;
+  const double *Wt = p->use_w && dense_w ? p->Wtile[dir] : nullptr;
   if (near_only) {
     {
       PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, 8));
@@ -3128,10 +3159,10 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     } else if (use_near_rows(p, count)) {
       // full blocks with register windows, the last block per output, one launch
       PhaseScope ps(p, L2C_PHASE_NEAR, 1, stn);
-      launch_k((sc.pdl & 2) && !ov, W ? k_near_rows<true> : k_near_rows<false>,
-               blocks_for((g.nL - 1) * (g.s / 4) + g.N - (g.nL - 1) * g.h, 256), 256, 0, stn, x,
+      launch_k((sc.pdl & 2) && !ov, Wt ? k_near_rows<true> : k_near_rows<false>,
+               blocks_for(near_rows_items(g), 256), 256, 0, stn, x,
                (const double *)out, p->y, (const double *)p->a, (const double *)p->an,
-               (const double *)p->dn, W, g, c2l);
+               (const double *)p->dn, Wt, g, c2l);
       if (cudaGetLastError() != cudaSuccess) return false;
     } else {
       PhaseScope ps(p, L2C_PHASE_NEAR, near_launch_count(count, ov ? p->near_vb : 8), stn);
@@ -3289,7 +3320,7 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     const TuneCfg &c = p->forced ? *p->forced : ts ? ts->cfg : p->base;
     cfg_apply(p, c);
     p->use_w = wants_table(p, c, count);
-    if (p->use_w && use_band_tile(p, count)) {
+    if (p->use_w && (use_band_tile(p, count) || use_near_rows(p, count))) {
       if (!ensure_band_tile_table(p, dir)) return 0;
     } else if (p->use_w && !ensure_near_table(p, dir)) {
       return 0;
@@ -3700,7 +3731,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_NEAR_PAIR")) p->near_pair = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_BAND_TILE")) p->band_tile = env[0] == '0' ? 0 : -1;
   if (const char *env = std::getenv("L2C_MZ_TOP")) p->mz_top = env[0] != '0';
-  if (const char *env = std::getenv("L2C_NEAR_ROWS")) p->near_rows = env[0] != '0';
+  if (const char *env = std::getenv("L2C_NEAR_ROWS")) p->near_rows = env[0] == '0' ? 0 : 1;
   if (const char *env = std::getenv("L2C_MZ_TOP_G")) p->mz_top_g = std::max(1, std::atoi(env));
   p->mz_top_g_base = p->mz_top_g;
   PCK(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device));
@@ -3964,13 +3995,16 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
       PCK(cudaFuncSetAttribute(band_tile_kernel<false>((long long)s), smax, bytes));
     }
     if (flags & L2C_PLAN_PRECOMPUTE_NEAR) {
-      const size_t nw = near_table_size(N, s);
+      // the band weights now, in the dense layout single vectors and large
+      // batches read (the per-output layout of other batches is built on its
+      // first use); the same products either way
+      const size_t nw = band_tile_table_size(N, s);
       Geo g = make_geo(p, 1, N, 1);
-      for (int d = 0; d < 2; d++) {
+      for (int d = 0; d < 2 && nw > 0; d++) {
         if (!(directions == (size_t)d || directions == 2)) continue;
-        PCK(cudaMalloc(&p->Wnear[d], nw * sizeof(double)));
-        k_near_weights<<<blocks_for((long long)N, 256), 256, 0, st>>>(p->Wnear[d], p->a, p->an,
-                                                                       p->dn, g, d);
+        PCK(cudaMalloc(&p->Wtile[d], nw * sizeof(double)));
+        k_band_tile_weights<<<blocks_for((long long)nw, 256), 256, 0, st>>>(p->Wtile[d], p->a,
+                                                                            p->an, p->dn, g, d);
         PCK(cudaGetLastError());
       }
     }
@@ -4422,6 +4456,24 @@ __global__ void k_r_gather(const double *__restrict__ in, double *__restrict__ x
   gather_item(in + r.io, x + r.io, 1, c2l, idx - pre[v]);
 }
 
+// The band of every FMM vector with register windows (near_rows_item): items
+// counted by pre (near_rows_items per vector, 0 for direct-method vectors).
+__global__ void __launch_bounds__(256) k_r_near_rows(const double *__restrict__ x,
+                                                     const double *out, double *__restrict__ y,
+                                                     const RVec *__restrict__ V,
+                                                     const RDonor *__restrict__ D,
+                                                     const long long *__restrict__ pre, int nvec,
+                                                     int c2l) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= pre[nvec]) return;
+  const int v = find_vec(pre, nvec, idx);
+  const RVec &r = V[v];
+  if (r.direct) return;
+  const RDonor &d = D[r.donor];
+  near_rows_item<false>(x + r.io, out + r.io, y + r.io, d.a, d.an, d.dn, nullptr, r.g, c2l,
+                        idx - pre[v]);
+}
+
 __global__ void __launch_bounds__(256) k_r_near(const double *__restrict__ x, const double *out,
                                                 double *__restrict__ y,
                                                 const RVec *__restrict__ V,
@@ -4576,6 +4628,7 @@ struct l2c_gpu_ragged {
   RDonor *D = nullptr;
   long long *pre_all = nullptr;  // every prefix array, back to back
   long long *pre_coef = nullptr, *pre_leaf = nullptr, *pre_far = nullptr;
+  long long *pre_rows = nullptr, tot_rows = 0;  // k_r_near_rows items
   std::vector<long long *> pre_up, pre_down;  // index d (1..Lmax-1), l (0..Lmax-2)
   long long tot_coef = 0, tot_leaf = 0, tot_far = 0;
   std::vector<long long> tot_up, tot_down;
@@ -4619,8 +4672,8 @@ size_t ragged_launch(l2c_gpu_ragged *r, const double *in, double *out, size_t di
       CK(cudaEventRecord(r->ev_fork, st));
       CK(cudaStreamWaitEvent(r->stream2, r->ev_fork, 0));
     }
-    k_r_near<<<blocks_for(r->tot_coef, 256), 256, 0, sb>>>(x, out, r->y, r->V, r->D, r->pre_coef,
-                                                           n, c2l);
+    k_r_near_rows<<<blocks_for(r->tot_rows, 256), 256, 0, sb>>>(x, out, r->y, r->V, r->D,
+                                                                r->pre_rows, n, c2l);
     r->launches++;
     if (ov && r->any_direct) {  // other vectors' outputs: no order with the chain
       k_r_direct<<<blocks_for(r->tot_coef, 256), 256, 0, sb>>>(in, out, r->V, r->D, r->pre_coef,
@@ -4771,7 +4824,7 @@ l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *Ns, size_t max
   // descriptors and the prefix sums of each phase's work items
   std::vector<RVec> hV(count);
   const int Lmax = r->Lmax;
-  std::vector<long long> pc(count + 1), pl(count + 1), pf(count + 1);
+  std::vector<long long> pc(count + 1), pl(count + 1), pf(count + 1), pr(count + 1);
   std::vector<std::vector<long long>> pu(std::max(Lmax, 1), std::vector<long long>(count + 1)),
       pd(std::max(Lmax, 1), std::vector<long long>(count + 1));
   long long io = 0, wc = 0;
@@ -4809,6 +4862,7 @@ l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *Ns, size_t max
       r->any_direct = true;
     }
     pc[v + 1] = pc[v] + g.N;
+    pr[v + 1] = pr[v] + (e.direct ? 0 : near_rows_items(g));
     pl[v + 1] = pl[v] + n_leaf;
     pf[v + 1] = pf[v] + n_far;
     for (int d = 1; d < Lmax; d++) {
@@ -4829,7 +4883,7 @@ l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *Ns, size_t max
   r->tot_up.assign(std::max(Lmax, 1), 0);
   r->tot_down.assign(std::max(Lmax, 1), 0);
   const size_t nlev = (size_t)std::max(Lmax, 1);
-  const size_t npre = (3 + 2 * nlev) * (count + 1);
+  const size_t npre = (4 + 2 * nlev) * (count + 1);
   RCK(cudaMalloc(&r->pre_all, npre * sizeof(long long)));
   std::vector<long long> all;
   all.reserve(npre);
@@ -4839,7 +4893,10 @@ l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *Ns, size_t max
   push(pf);
   for (size_t d = 0; d < nlev; d++) push(pu[d]);
   for (size_t l = 0; l < nlev; l++) push(pd[l]);
+  push(pr);
   RCK(cudaMemcpy(r->pre_all, all.data(), npre * sizeof(long long), cudaMemcpyHostToDevice));
+  r->pre_rows = r->pre_all + (3 + 2 * nlev) * (count + 1);
+  r->tot_rows = pr[count];
   r->pre_coef = r->pre_all;
   r->pre_leaf = r->pre_all + (count + 1);
   r->pre_far = r->pre_all + 2 * (count + 1);

@@ -641,10 +641,13 @@ def test_random_2d_vs_lines(lib, orc, seed):
 
 
 @pytest.mark.parametrize("N,maxs,lagrange", [(1 << 20, 64, 0), (1 << 16, 32, 0), (40000, 64, 0),
-                                             (1 << 18, 16, 1), (20000, 24, 0)])
+                                             (1 << 18, 16, 1), (20000, 24, 0), (30001, 64, 0),
+                                             (9000, 21, 0), (3000, 10, 1)])
 def test_single_vector_band_rows_vs_oracle(lib, orc, monkeypatch, N, maxs, lagrange):
-    """Single vectors take the band's full blocks with register windows (rows
-    of a block share their sources); the same vector with the per-output
+    """The band's full blocks with register windows (rows of a block share
+    their sources; leaf sizes not a multiple of 4 leave a partial row group:
+    s = 59, 18, 6), forced on for every size (L2C_NEAR_ROWS=1; by default only
+    vectors with many blocks take it); the same vector with the per-output
     kernel (L2C_NEAR_ROWS=0) and the oracle agree within the bar."""
     u = make_input(N, "sign", N + 3)
     o = orc.Oracle(N, maxs, 2, lagrange)
