@@ -1272,6 +1272,12 @@ struct BandTile {
   static constexpr int SLOT = VCH * LD;       // doubles per slot
   static constexpr int GROUPS = S / 2;        // row groups: 2 parities x s/4
   static constexpr int GPW = (GROUPS + BT_WARPS - 1) / BT_WARPS;
+  // s = 16: each warp runs a pair of same-parity row groups (g, s/4 - 1 - g)
+  // in one pass (band_tile_pair); larger leaves, whose groups have longer
+  // loops, one group at a time (their registers would not hold a pair's sums)
+  static constexpr bool PAIRED = S == 16;
+  static constexpr int PAIRS = S / 4;
+  static constexpr int PPW = (PAIRS + BT_WARPS - 1) / BT_WARPS;
   static constexpr int WB = 4 * S * S;        // weights of one block, both parities
   static constexpr bool WS = S == 16;         // weights staged in shared memory
   static constexpr size_t SMEM = (3 * (size_t)SLOT + (WS ? 2 * (size_t)WB : 0)) * sizeof(double);
@@ -1361,6 +1367,105 @@ __device__ __forceinline__ void band_tile_group(const double *__restrict__ sA,
   for (int mp = S; mp < 2 * S; mp++)
     band_tile_step<C, 4, TAB>(sB + 2 * (mp - S) + p, LD, TAB ? Wg + mp * S : nullptr, mp - ip0,
                               j0, c2l, a, an, dn, acc);
+}
+
+// One term step m' of two row groups of one parity: group a (all 4 rows) and
+// group b (rows r < ROWS_B): they read the same source x, so a step issues
+// 4 C + ROWS_B C independent FMAs from two weight quads and C shared loads.
+template <int C, int ROWS_B, bool TAB>
+__device__ __forceinline__ void band_tile_step2(const double *__restrict__ xs, int ld,
+                                                const double *Wa, const double *Wb, int ka0,
+                                                int kb0, long long ja0, long long jb0, int c2l,
+                                                const double *__restrict__ a,
+                                                const double *__restrict__ an,
+                                                const double *__restrict__ dn,
+                                                double (&acca)[4][C], double (&accb)[4][C]) {
+  double wa[4], wb[4];
+  if (TAB) {
+    const double2 a0 = reinterpret_cast<const double2 *>(Wa)[0];
+    const double2 a1 = reinterpret_cast<const double2 *>(Wa)[1];
+    const double2 b0 = reinterpret_cast<const double2 *>(Wb)[0];
+    const double2 b1 = reinterpret_cast<const double2 *>(Wb)[1];
+    wa[0] = a0.x;
+    wa[1] = a0.y;
+    wa[2] = a1.x;
+    wa[3] = a1.y;
+    wb[0] = b0.x;
+    wb[1] = b0.y;
+    wb[2] = b1.x;
+    wb[3] = b1.y;
+  } else {
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      wa[r] = near_weight(c2l, ka0 - r, ja0 + 2 * r, a, an, dn);
+      wb[r] = r < ROWS_B ? near_weight(c2l, kb0 - r, jb0 + 2 * r, a, an, dn) : 0.0;
+    }
+  }
+  double xv[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) xv[c] = xs[c * 32 * ld];
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+#pragma unroll
+    for (int c = 0; c < C; c++) acca[r][c] = fma(wa[r], xv[c], acca[r][c]);
+#pragma unroll
+  for (int r = 0; r < ROWS_B; r++)
+#pragma unroll
+    for (int c = 0; c < C; c++) accb[r][c] = fma(wb[r], xv[c], accb[r][c]);
+}
+
+// Two row groups of one parity in one pass: a from row ia, b from row ib
+// (ia + 4 <= ib <= s - 4).  Group a runs alone over m' = ia .. ib-1; from
+// m' = ib both share each source, which doubles the independent FMAs per step
+// (more work per warp between loads, so fewer warps keep the FP64 pipe busy).
+// Each row's terms are still summed in order of k in one chain.
+template <int S, bool TAB>
+__device__ __forceinline__ void band_tile_pair(const double *__restrict__ sA,
+                                               const double *__restrict__ sB, const double *Wga,
+                                               const double *Wgb, int p, int ia, int ib,
+                                               long long ja0, long long jb0, int c2l,
+                                               const double *__restrict__ a,
+                                               const double *__restrict__ an,
+                                               const double *__restrict__ dn,
+                                               double (&acca)[4][BandTile<S>::C],
+                                               double (&accb)[4][BandTile<S>::C]) {
+  using BT = BandTile<S>;
+  constexpr int C = BT::C, LD = BT::LD;
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+#pragma unroll
+    for (int c = 0; c < C; c++) acca[r][c] = accb[r][c] = 0.0;
+  // group a alone: its first three steps have rows r <= m' - ia only
+  band_tile_step<C, 1, TAB>(sA + 2 * ia + p, LD, TAB ? Wga + ia * S : nullptr, 0, ja0, c2l, a,
+                            an, dn, acca);
+  band_tile_step<C, 2, TAB>(sA + 2 * ia + 2 + p, LD, TAB ? Wga + (ia + 1) * S : nullptr, 1, ja0,
+                            c2l, a, an, dn, acca);
+  band_tile_step<C, 3, TAB>(sA + 2 * ia + 4 + p, LD, TAB ? Wga + (ia + 2) * S : nullptr, 2, ja0,
+                            c2l, a, an, dn, acca);
+#pragma unroll 4
+  for (int mp = ia + 3; mp < ib; mp++)
+    band_tile_step<C, 4, TAB>(sA + 2 * mp + p, LD, TAB ? Wga + mp * S : nullptr, mp - ia, ja0,
+                              c2l, a, an, dn, acca);
+  // both groups (b's first three steps with rows r <= m' - ib); ib + 2 < s
+  band_tile_step2<C, 1, TAB>(sA + 2 * ib + p, LD, TAB ? Wga + ib * S : nullptr,
+                             TAB ? Wgb + ib * S : nullptr, ib - ia, 0, ja0, jb0, c2l, a, an, dn,
+                             acca, accb);
+  band_tile_step2<C, 2, TAB>(sA + 2 * ib + 2 + p, LD, TAB ? Wga + (ib + 1) * S : nullptr,
+                             TAB ? Wgb + (ib + 1) * S : nullptr, ib + 1 - ia, 1, ja0, jb0, c2l, a,
+                             an, dn, acca, accb);
+  band_tile_step2<C, 3, TAB>(sA + 2 * ib + 4 + p, LD, TAB ? Wga + (ib + 2) * S : nullptr,
+                             TAB ? Wgb + (ib + 2) * S : nullptr, ib + 2 - ia, 2, ja0, jb0, c2l, a,
+                             an, dn, acca, accb);
+#pragma unroll 4
+  for (int mp = ib + 3; mp < S; mp++)
+    band_tile_step2<C, 4, TAB>(sA + 2 * mp + p, LD, TAB ? Wga + mp * S : nullptr,
+                               TAB ? Wgb + mp * S : nullptr, mp - ia, mp - ib, ja0, jb0, c2l, a,
+                               an, dn, acca, accb);
+#pragma unroll(S <= 16 ? S : 8)
+  for (int mp = S; mp < 2 * S; mp++)
+    band_tile_step2<C, 4, TAB>(sB + 2 * (mp - S) + p, LD, TAB ? Wga + mp * S : nullptr,
+                               TAB ? Wgb + mp * S : nullptr, mp - ia, mp - ib, ja0, jb0, c2l, a,
+                               an, dn, acca, accb);
 }
 
 // Copies of half window hw of the chunk's vectors into slot dst (zeros for
@@ -1460,28 +1565,60 @@ __global__ void __launch_bounds__(BT_THREADS, 4)
       double *sA = bt_smem + (int)(b % 3) * BT::SLOT;
       const double *sB = bt_smem + (int)((b + 1) % 3) * BT::SLOT;
       const double *Wb = !TAB ? nullptr : WS ? wsm + (int)(b & 1) * BT::WB : Wt + b * BT::WB;
-      double res[BT::GPW][4][C];
-#pragma unroll
-      for (int t = 0; t < BT::GPW; t++) {
-        const int q = 8 * (t >> 1) + ((t & 1) ? 2 * BT_WARPS - 1 - warp : warp);
-        if (q < BT::GROUPS) {
-          const int p = q & 1, ip0 = 4 * (q >> 1);
-          band_tile_group<S, TAB>(sA + lane * LD, sB + lane * LD,
-                                  TAB ? Wb + p * 2 * S * S + ip0 : nullptr, p, ip0,
-                                  b * H + 2 * ip0 + p, c2l, a, an, dn, res[t]);
+      if constexpr (BT::PAIRED) {
+        // warp w: pairs q = w, w + 4, ... of same-parity row groups (g, s/4-1-g)
+        double res[BT::PPW][2][4][C];
+  #pragma unroll
+        for (int t = 0; t < BT::PPW; t++) {
+          const int q = warp + BT_WARPS * t;
+          if (q < BT::PAIRS) {
+            const int p = q / (S / 8), ga = q % (S / 8), ia = 4 * ga, ib = S - 4 - ia;
+            const double *Wp = TAB ? Wb + p * 2 * S * S : nullptr;
+            band_tile_pair<S, TAB>(sA + lane * LD, sB + lane * LD, TAB ? Wp + ia : nullptr,
+                                   TAB ? Wp + ib : nullptr, p, ia, ib, b * H + 2 * ia + p,
+                                   b * H + 2 * ib + p, c2l, a, an, dn, res[t][0], res[t][1]);
+          }
         }
-      }
-      __syncthreads();  // every warp is done reading slots A and B
-      // the sums, staged in slot A (its inputs are no longer needed)
-#pragma unroll
-      for (int t = 0; t < BT::GPW; t++) {
-        const int q = 8 * (t >> 1) + ((t & 1) ? 2 * BT_WARPS - 1 - warp : warp);
-        if (q < BT::GROUPS)
-#pragma unroll
-          for (int r = 0; r < 4; r++)
-#pragma unroll
-            for (int c = 0; c < C; c++)
-              sA[(lane + 32 * c) * LD + 2 * (4 * (q >> 1) + r) + (q & 1)] = res[t][r][c];
+        __syncthreads();  // every warp is done reading slots A and B
+        // the sums, staged in slot A (its inputs are no longer needed)
+  #pragma unroll
+        for (int t = 0; t < BT::PPW; t++) {
+          const int q = warp + BT_WARPS * t;
+          if (q < BT::PAIRS) {
+            const int p = q / (S / 8), ia = 4 * (q % (S / 8)), ib = S - 4 - ia;
+  #pragma unroll
+            for (int r = 0; r < 4; r++)
+  #pragma unroll
+              for (int c = 0; c < C; c++) {
+                sA[(lane + 32 * c) * LD + 2 * (ia + r) + p] = res[t][0][r][c];
+                sA[(lane + 32 * c) * LD + 2 * (ib + r) + p] = res[t][1][r][c];
+              }
+          }
+        }
+      } else {
+        double res[BT::GPW][4][C];
+  #pragma unroll
+        for (int t = 0; t < BT::GPW; t++) {
+          const int q = 8 * (t >> 1) + ((t & 1) ? 2 * BT_WARPS - 1 - warp : warp);
+          if (q < BT::GROUPS) {
+            const int p = q & 1, ip0 = 4 * (q >> 1);
+            band_tile_group<S, TAB>(sA + lane * LD, sB + lane * LD,
+                                    TAB ? Wb + p * 2 * S * S + ip0 : nullptr, p, ip0,
+                                    b * H + 2 * ip0 + p, c2l, a, an, dn, res[t]);
+          }
+        }
+        __syncthreads();  // every warp is done reading slots A and B
+        // the sums, staged in slot A (its inputs are no longer needed)
+  #pragma unroll
+        for (int t = 0; t < BT::GPW; t++) {
+          const int q = 8 * (t >> 1) + ((t & 1) ? 2 * BT_WARPS - 1 - warp : warp);
+          if (q < BT::GROUPS)
+  #pragma unroll
+            for (int r = 0; r < 4; r++)
+  #pragma unroll
+              for (int c = 0; c < C; c++)
+                sA[(lane + 32 * c) * LD + 2 * (4 * (q >> 1) + r) + (q & 1)] = res[t][r][c];
+        }
       }
       __syncthreads();
       // y = out_in + band, a row of h outputs per vector (eight loads of the
