@@ -725,7 +725,7 @@ def run_mixed(args):
     clk = clocks.stop()
     if "speedup_vs_best_plain" not in rec:  # a subset of the plans (profiling runs)
         print(json.dumps({"plans": rec["plans"], "errors": rec["max_rel_err_vs_oracle"],
-                          "clocks": clk}))
+                          "e2e_mixed": rec["e2e_mixed"], "clocks": clk}))
         return 0
     mixed = rec["plans"]["mixed"]
     line = {

@@ -102,7 +102,8 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
     replay, the tile buffer depth, the chain's scheduling priority and the
     band's CTA size, vectors per thread, grid cap, weight table and fork point,
     and (mixed form) the coarsest transfer levels in one launch or one launch
-    per level, change only when work runs, never what it computes: every
+    per level and the finest levels' far field on a third stream, change only
+    when work runs, never what it computes: every
     setting gives the same bits as the default plan (count = 64: the band as
     dense register tiles, with its table or weights formed on the fly)."""
     N = 16384
@@ -136,7 +137,13 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
                 # the per-level structure the autotuner searches
                 {"L2C_MZ_TOP_LVL": "5"}, {"L2C_MZ_TOP_LVL": "3", "L2C_MZ_TOP_G": "1"},
                 {"L2C_MZ_TOP_G": "4"}, {"L2C_TREE_L0": "1"}, {"L2C_TREE_L0": "3"},
-                {"L2C_BAND_BSEG": "1"}, {"L2C_BAND_BSEG": "4"}):
+                {"L2C_BAND_BSEG": "1"}, {"L2C_BAND_BSEG": "4"},
+                # the finest levels' far field on a third stream (none, 1 .. 4
+                # levels), also without graphs and with the top launch off
+                {"L2C_FAR_SPLIT": "0"}, {"L2C_FAR_SPLIT": "1"}, {"L2C_FAR_SPLIT": "3"},
+                {"L2C_FAR_SPLIT": "4"}, {"L2C_FAR_SPLIT": "3", "L2C_NO_GRAPHS": "1"},
+                {"L2C_FAR_SPLIT": "3", "L2C_MZ_TOP": "0"},
+                {"L2C_FAR_SPLIT": "2", "L2C_MZ_TOP_LVL": "5", "L2C_BAND_FORK": "3"}):
         with monkeypatch.context() as m:
             for k, v in env.items():
                 m.setenv(k, v)
