@@ -1263,10 +1263,12 @@ constexpr int BT_WARPS = 4;
 constexpr int BT_THREADS = 32 * BT_WARPS;
 constexpr long long BT_MIN_COUNT = 64;
 
-template <int S>
+// CC: vectors per lane (the default, or 1 for the thin variant at s = 16,
+// band_tile_thin).
+template <int S, int CC = (S <= 32 ? 2 : 1)>
 struct BandTile {
   static constexpr int H = 2 * S;
-  static constexpr int C = S <= 32 ? 2 : 1;   // vectors per lane
+  static constexpr int C = CC;                // vectors per lane
   static constexpr int VCH = 32 * C;          // vectors per chunk
   static constexpr int LD = 2 * S + 1;        // slot row (odd)
   static constexpr int SLOT = VCH * LD;       // doubles per slot
@@ -1283,7 +1285,10 @@ struct BandTile {
   static constexpr size_t SMEM = (3 * (size_t)SLOT + (WS ? 2 * (size_t)WB : 0)) * sizeof(double);
 };
 
-__host__ __device__ inline int band_tile_c(long long s) { return s <= 32 ? 2 : 1; }
+// Vectors per lane of the tiled band (thin: the thin variant, s = 16 only).
+__host__ __device__ inline int band_tile_c(long long s, bool thin = false) {
+  return thin && s == 16 ? 1 : s <= 32 ? 2 : 1;
+}
 // Entries of the dense weight table: (nL - 1) blocks x 2 parities x 2s x s.
 inline size_t band_tile_table_size(size_t N, size_t s) {
   const size_t h = 2 * s, nL = N / h;
@@ -1338,15 +1343,15 @@ __device__ __forceinline__ void band_tile_step(const double *__restrict__ xs, in
 // Row group (parity p, rows i'0 .. i'0 + 3) of one block for the lane's C
 // vectors.  sA / sB: the lane's rows in the two half-window slots; Wg: the
 // group's weights at m' = 0 (row stride S), or nullptr.
-template <int S, bool TAB>
+template <int S, int CC, bool TAB>
 __device__ __forceinline__ void band_tile_group(const double *__restrict__ sA,
                                                 const double *__restrict__ sB,
                                                 const double *Wg, int p, int ip0, long long j0,
                                                 int c2l, const double *__restrict__ a,
                                                 const double *__restrict__ an,
                                                 const double *__restrict__ dn,
-                                                double (&acc)[4][BandTile<S>::C]) {
-  using BT = BandTile<S>;
+                                                double (&acc)[4][CC]) {
+  using BT = BandTile<S, CC>;
   constexpr int C = BT::C, LD = BT::LD;
 #pragma unroll
   for (int r = 0; r < 4; r++)
@@ -1419,7 +1424,7 @@ __device__ __forceinline__ void band_tile_step2(const double *__restrict__ xs, i
 // m' = ib both share each source, which doubles the independent FMAs per step
 // (more work per warp between loads, so fewer warps keep the FP64 pipe busy).
 // Each row's terms are still summed in order of k in one chain.
-template <int S, bool TAB>
+template <int S, int CC, bool TAB>
 __device__ __forceinline__ void band_tile_pair(const double *__restrict__ sA,
                                                const double *__restrict__ sB, const double *Wga,
                                                const double *Wgb, int p, int ia, int ib,
@@ -1427,9 +1432,8 @@ __device__ __forceinline__ void band_tile_pair(const double *__restrict__ sA,
                                                const double *__restrict__ a,
                                                const double *__restrict__ an,
                                                const double *__restrict__ dn,
-                                               double (&acca)[4][BandTile<S>::C],
-                                               double (&accb)[4][BandTile<S>::C]) {
-  using BT = BandTile<S>;
+                                               double (&acca)[4][CC], double (&accb)[4][CC]) {
+  using BT = BandTile<S, CC>;
   constexpr int C = BT::C, LD = BT::LD;
 #pragma unroll
   for (int r = 0; r < 4; r++)
@@ -1470,10 +1474,10 @@ __device__ __forceinline__ void band_tile_pair(const double *__restrict__ sA,
 
 // Copies of half window hw of the chunk's vectors into slot dst (zeros for
 // vectors past the batch).
-template <int S>
+template <int S, int CC>
 __device__ __forceinline__ void band_tile_fill(double *dst, const double *__restrict__ x,
                                                const Geo &g, long long v0, long long hw) {
-  using BT = BandTile<S>;
+  using BT = BandTile<S, CC>;
 #pragma unroll 4
   for (int idx = threadIdx.x; idx < BT::VCH * BT::H; idx += BT_THREADS) {
     const int vl = idx / BT::H, m = idx % BT::H;
@@ -1500,14 +1504,15 @@ __device__ __forceinline__ void band_tile_fill_w(double *wdst, const double *__r
 // so its weights are read from L2 by all of them).  Warp w takes the row
 // groups q = 8 t' + w and 8 t' + 7 - w (t' = 0, 1, ...), q < s/2.  At most
 // 128 registers per thread, so that one or two of these CTAs leave most of an
-// SM's register file to the kernels beside them.
-template <int S, bool TAB>
-__global__ void __launch_bounds__(BT_THREADS, 4)
+// SM's register file to the kernels beside them (the thin variant, one vector
+// per lane: at most 64, and half the shared memory).
+template <int S, bool TAB, int CC = BandTile<S>::C>
+__global__ void __launch_bounds__(BT_THREADS, CC < BandTile<S>::C ? 8 : 4)
     k_band_tile(const double *__restrict__ x, const double *out, double *__restrict__ y,
                 const double *__restrict__ Wt, const double *__restrict__ a,
                 const double *__restrict__ an, const double *__restrict__ dn, Geo g, int c2l,
                 long long nchunk, long long bseg) {
-  using BT = BandTile<S>;
+  using BT = BandTile<S, CC>;
   constexpr int C = BT::C, VCH = BT::VCH, LD = BT::LD, H = BT::H;
   constexpr bool WS = TAB && BT::WS;
   extern __shared__ __align__(16) double bt_smem[];
@@ -1520,23 +1525,24 @@ __global__ void __launch_bounds__(BT_THREADS, 4)
   for (long long u = blockIdx.x; u < nchunk * (nseg + 1); u += gridDim.x) {
     if (u < nchunk) {
       // the last (ragged) block of chunk u: k_near's sums (weights formed on
-      // the fly, each shared by 8 vectors; the same bits as k_near), an
-      // output of 8 vectors per thread, a vector at a time past the last
-      // full group of 8
+      // the fly, each shared by TV vectors; the same bits as k_near), an
+      // output of TV vectors per thread (4 in the thin variant, within its
+      // registers), a vector at a time past the last full group
+      constexpr int TV = CC < BandTile<S>::C ? 4 : 8;  // vectors per thread
       const long long vb = u * VCH, nv = g.count - vb < VCH ? g.count - vb : VCH;
-      const long long n8 = nv / 8;
-      for (long long idx = threadIdx.x; idx < (n8 + (nv - 8 * n8)) * ntail;
+      const long long ngrp = nv / TV;
+      for (long long idx = threadIdx.x; idx < (ngrp + (nv - TV * ngrp)) * ntail;
            idx += BT_THREADS) {
         const long long grp = idx / ntail, j = jlast + idx % ntail;
-        if (grp < n8) {
-          const long long v0 = vb + 8 * grp;
-          double res[8];
-          near_sums<8>(x + v0 * g.N + j, g.N, a, an, dn, nullptr, g, c2l, j, res);
+        if (grp < ngrp) {
+          const long long v0 = vb + TV * grp;
+          double res[TV];
+          near_sums<TV>(x + v0 * g.N + j, g.N, a, an, dn, nullptr, g, c2l, j, res);
 #pragma unroll
-          for (int e = 0; e < 8; e++)
+          for (int e = 0; e < TV; e++)
             y[(v0 + e) * g.N + j] = out[(v0 + e) * g.dist + j * g.stride] + res[e];
         } else {
-          const long long v = vb + 8 * n8 + (grp - n8);
+          const long long v = vb + TV * ngrp + (grp - ngrp);
           double res[1];
           near_sums<1>(x + v * g.N + j, g.N, a, an, dn, nullptr, g, c2l, j, res);
           y[v * g.N + j] = out[v * g.dist + j * g.stride] + res[0];
@@ -1548,15 +1554,15 @@ __global__ void __launch_bounds__(BT_THREADS, 4)
     const long long v0 = (uu % nchunk) * VCH, seg = uu / nchunk;
     const long long b0 = seg * bseg, b1 = b0 + bseg < nfull ? b0 + bseg : nfull;
     // half windows b0 and b0 + 1 (block b0 needs both), block b0's weights
-    band_tile_fill<S>(bt_smem + (int)(b0 % 3) * BT::SLOT, x, g, v0, b0);
+    band_tile_fill<S, CC>(bt_smem + (int)(b0 % 3) * BT::SLOT, x, g, v0, b0);
     if (WS) band_tile_fill_w<S>(wsm + (int)(b0 & 1) * BT::WB, Wt, b0);
     l2c_oz::cp_commit();
-    band_tile_fill<S>(bt_smem + (int)((b0 + 1) % 3) * BT::SLOT, x, g, v0, b0 + 1);
+    band_tile_fill<S, CC>(bt_smem + (int)((b0 + 1) % 3) * BT::SLOT, x, g, v0, b0 + 1);
     l2c_oz::cp_commit();
     for (long long b = b0; b < b1; b++) {
       // half window b + 2 and block b + 1's weights, one block ahead
       if (b + 2 <= b1) {
-        band_tile_fill<S>(bt_smem + (int)((b + 2) % 3) * BT::SLOT, x, g, v0, b + 2);
+        band_tile_fill<S, CC>(bt_smem + (int)((b + 2) % 3) * BT::SLOT, x, g, v0, b + 2);
         if (WS) band_tile_fill_w<S>(wsm + (int)((b + 1) & 1) * BT::WB, Wt, b + 1);
       }
       l2c_oz::cp_commit();
@@ -1574,7 +1580,7 @@ __global__ void __launch_bounds__(BT_THREADS, 4)
           if (q < BT::PAIRS) {
             const int p = q / (S / 8), ga = q % (S / 8), ia = 4 * ga, ib = S - 4 - ia;
             const double *Wp = TAB ? Wb + p * 2 * S * S : nullptr;
-            band_tile_pair<S, TAB>(sA + lane * LD, sB + lane * LD, TAB ? Wp + ia : nullptr,
+            band_tile_pair<S, CC, TAB>(sA + lane * LD, sB + lane * LD, TAB ? Wp + ia : nullptr,
                                    TAB ? Wp + ib : nullptr, p, ia, ib, b * H + 2 * ia + p,
                                    b * H + 2 * ib + p, c2l, a, an, dn, res[t][0], res[t][1]);
           }
@@ -1602,7 +1608,7 @@ __global__ void __launch_bounds__(BT_THREADS, 4)
           const int q = 8 * (t >> 1) + ((t & 1) ? 2 * BT_WARPS - 1 - warp : warp);
           if (q < BT::GROUPS) {
             const int p = q & 1, ip0 = 4 * (q >> 1);
-            band_tile_group<S, TAB>(sA + lane * LD, sB + lane * LD,
+            band_tile_group<S, CC, TAB>(sA + lane * LD, sB + lane * LD,
                                     TAB ? Wb + p * 2 * S * S + ip0 : nullptr, p, ip0,
                                     b * H + 2 * ip0 + p, c2l, a, an, dn, res[t]);
           }
@@ -1651,9 +1657,9 @@ using band_tile_fn = void (*)(const double *, const double *, double *, const do
                               long long, long long);
 
 template <bool TAB>
-band_tile_fn<TAB> band_tile_kernel(long long s) {
+band_tile_fn<TAB> band_tile_kernel(long long s, bool thin = false) {
   switch (s / 8) {
-    case 2: return k_band_tile<16, TAB>;
+    case 2: return thin ? k_band_tile<16, TAB, 1> : k_band_tile<16, TAB>;
     case 3: return k_band_tile<24, TAB>;
     case 4: return k_band_tile<32, TAB>;
     case 5: return k_band_tile<40, TAB>;
@@ -1663,9 +1669,9 @@ band_tile_fn<TAB> band_tile_kernel(long long s) {
   }
 }
 
-inline size_t band_tile_smem(long long s) {
+inline size_t band_tile_smem(long long s, bool thin = false) {
   switch (s / 8) {
-    case 2: return BandTile<16>::SMEM;
+    case 2: return thin ? BandTile<16, 1>::SMEM : BandTile<16>::SMEM;
     case 3: return BandTile<24>::SMEM;
     case 4: return BandTile<32>::SMEM;
     case 5: return BandTile<40>::SMEM;
@@ -1738,27 +1744,36 @@ __host__ __device__ inline void oz_meta(const int *E, int *meta) {
   meta[OZ_ROWS] = emax + 7;
 }
 
-// Far-field block fragments: block gb, part 0 = [A0 A1] (18 x 36), part 1 = A2
-// (18 x 18); words at F + gb * OZ_FAR_WORDS, metadata at Pm + gb * 2 * OZ_META.
-// One thread per (block, part).
-constexpr int OZ_FAR_W0 = oz_words(OZ_NT, 5), OZ_FAR_WORDS = OZ_FAR_W0 + oz_words(OZ_NT, 3);
+// Far-field block fragments: block gb as one 40 x 40 matrix
+//   [[A0 A1]   rows 0 .. 17: the block's first slot (slot 2 gb)
+//    [ 0 A2]]  rows 18 .. 35: its second slot (2 gb + 1); rows 36 .. 39 zero
+// over the two slots' 36 moments (columns 36 .. 39 zero), NT = 5 n-tiles and
+// KC = 5 chunks: one product per data tile serves both output slots from one
+// digit extraction.  Words at F + gb * OZ_FAR_WORDS, metadata at
+// Pm + gb * 2 * OZ_META (part 0: rows 0 .. 17, part 1: rows 18 .. 35).  One
+// thread per (block, part).
+constexpr int OZ_FAR_NT = 5, OZ_FAR_KC = 5;
+constexpr int OZ_FAR_WORDS = oz_words(OZ_FAR_NT, OZ_FAR_KC);
 __global__ void k_oz_pack_far(const double *__restrict__ A, long long nblocks, unsigned *F,
                               int *Pm) {
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= nblocks * 2) return;
   const long long gb = idx >> 1;
   const int part = (int)(idx & 1);
-  unsigned *Fb = F + gb * OZ_FAR_WORDS + (part ? OZ_FAR_W0 : 0);
-  int E[OZ_ROWS];
-  for (int n = 0; n < OZ_ROWS; n++) {
-    const double *A0 = A + 3 * gb * MM + (n < M ? n : 0) * M;
+  unsigned *Fb = F + gb * OZ_FAR_WORDS;
+  int E[8 * OZ_FAR_NT];
+  const int n0 = part ? M : 0, n1 = part ? 8 * OZ_FAR_NT : M;
+  for (int n = n0; n < n1; n++) {
+    const int r = n - n0;  // row of the part's blocks
+    const double *Ar = A + 3 * gb * MM + (r < M ? r : 0) * M;
     if (part == 0)
-      oz_pack_row([&](int k) { return k < M ? A0[k] : A0[MM + k - M]; }, n < M, n, 2 * M, OZ_NT,
-                  5, Fb, E);
+      oz_pack_row([&](int k) { return k < M ? Ar[k] : Ar[MM + k - M]; }, true, n, 2 * M,
+                  OZ_FAR_NT, OZ_FAR_KC, Fb, E);
     else
-      oz_pack_row([&](int k) { return A0[2 * MM + k]; }, n < M, n, M, OZ_NT, 3, Fb, E);
+      oz_pack_row([&](int k) { return k < M ? 0.0 : Ar[2 * MM + k - M]; }, r < M, n, 2 * M,
+                  OZ_FAR_NT, OZ_FAR_KC, Fb, E);
   }
-  oz_meta(E, Pm + (gb * 2 + part) * OZ_META);
+  oz_meta(E + n0, Pm + (gb * 2 + part) * OZ_META);
 }
 
 // Copy nwords fragment words (and nint metadata ints) into shared memory.
@@ -2236,8 +2251,10 @@ constexpr size_t oz_tree_down_smem(int QMAX, int NBUF) {
 }
 
 // Far field (step 3): CTA = (block gb, chunk of columns vs = vector * 2 +
-// parity).  c0 = [A0 A1] [w0; w1] (K = 36), c1 = A2 w1 (K = 18); both parts
-// use the scale of the whole column [w0; w1].
+// parity).  c0 = [A0 A1] [w0; w1] and c1 = A2 w1 as one product of the 40-row
+// matrix of k_oz_pack_far with the column [w0; w1] (K = 36), on the scale of
+// the whole column: the same integers as two products over the same staged
+// words, with the digits extracted once.
 constexpr int OZ_FAR_COLS = 16 * MXW * 2;  // columns per CTA
 // Far-field blocks gb0 + blockIdx.x (a launch may cover one level's blocks).
 template <int NBUF>
@@ -2282,31 +2299,42 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
     const int *Ex = sEx + buf * 32;
     l2c_oz::stage_cols<2 * M, M, OZ_TLD>(X, OZ_TLD, Ex, Ex + 16, Es);
     const long long cA = c0 + tile * 16 + gq, cB = cA + 8;
-#pragma unroll 1
-    for (int part = 0; part < 2; part++) {
-      long long T[OZ_NT][4];
-      if (part == 0)
-        oz_tile_T<OZ_NT, 5>(sP, X, OZ_TLD, 1, T);
+    // the tile's digits once, then the 40-row product one n-tile at a time;
+    // n-tiles 3 and 4 (rows 24 .. 39, the second slot's) have zero weights on
+    // the first slot's moments (chunk pair 0)
+    l2c_oz::Digits<OZ_FAR_KC> D;
+    l2c_oz::load_digits<OZ_FAR_KC>(X, OZ_TLD, 1, D);
+#pragma unroll
+    for (int nt = 0; nt < OZ_FAR_NT; nt++) {
+      float acc[l2c_oz::NDIAG][4];
+      if (nt < 3)
+        l2c_oz::mma_nt<OZ_FAR_NT, OZ_FAR_KC>(sP, D, nt, acc);
       else
-        oz_tile_T<OZ_NT, 3>(sP + OZ_FAR_W0, X + M, OZ_TLD, 1, T);
-      const int *meta = sM + part * OZ_META;
-      oz_put18(
-          T, meta,
-          [&](int r, int n, long long a, long long b) {
-            const long long col = r < 8 ? cA : cB;
-            if (col < ncol)
-              *reinterpret_cast<longlong2 *>(c + (col * g.slots + 2 * gb + part) * M + n) =
-                  make_longlong2(a, b);
-          },
-          [&](int r, int n, long long a) {
-            const long long col = r < 8 ? cA : cB;
-            if (col < ncol) c[(col * g.slots + 2 * gb + part) * M + n] = a;
-          });
-      if (t4 == 0) {
-        if (cA < ncol) cE[cA * g.slots + 2 * gb + part] = Es[gq] + meta[OZ_ROWS];
-        if (cB < ncol) cE[cB * g.slots + 2 * gb + part] = Es[gq + 8] + meta[OZ_ROWS];
+        l2c_oz::mma_nt<OZ_FAR_NT, OZ_FAR_KC, l2c_oz::SLICES, 1>(sP, D, nt, acc);
+      // the lane's outputs: rows n, n + 1 of data columns cA (e = 0, 1) and
+      // cB (e = 2, 3); rows 0 .. 17 go to slot 2 gb, 18 .. 35 to 2 gb + 1
+      const int n = 8 * nt + 2 * t4;
+      if (n < 2 * M) {
+        const int part = n >= M ? 1 : 0, r = n - part * M;
+        const int *meta = sM + part * OZ_META;
+#pragma unroll
+        for (int hr = 0; hr < 2; hr++) {
+          const long long col = hr ? cB : cA;
+          const long long V0 = l2c_oz::shift_s64(l2c_oz::combine1(acc, 2 * hr), meta[r]);
+          const long long V1 = l2c_oz::shift_s64(l2c_oz::combine1(acc, 2 * hr + 1), meta[r + 1]);
+          if (col < ncol)
+            *reinterpret_cast<longlong2 *>(c + (col * g.slots + 2 * gb + part) * M + r) =
+                make_longlong2(V0, V1);
+        }
       }
     }
+    if (t4 == 0)
+#pragma unroll
+      for (int part = 0; part < 2; part++) {
+        const int eo = sM[part * OZ_META + OZ_ROWS];
+        if (cA < ncol) cE[cA * g.slots + 2 * gb + part] = Es[gq] + eo;
+        if (cB < ncol) cE[cB * g.slots + 2 * gb + part] = Es[gq + 8] + eo;
+      }
   };
   oz_tile_loop<NBUF>(wid, MXW, ntile, issue, work);
 }
@@ -2527,7 +2555,10 @@ struct TuneCfg {
   //         run on a third stream, each level as soon as the upward sweep has
   //         its moments, beside the coarser levels' latency-bound launches
   //         (-1: the plan's rule)
-  int mtop = -2, mtopg = 0, tl0 = -1, bseg = 0, fsplit = -1;
+  //   bthin tiled band at s = 16: the thin variant (one vector per lane, at
+  //         most 64 registers, half the shared memory), which leaves room for
+  //         more CTAs of the kernels beside it (-1: the plan's rule)
+  int mtop = -2, mtopg = 0, tl0 = -1, bseg = 0, fsplit = -1, bthin = -1;
 };
 
 // A tuned call shape and its choices (dist is 0 for single vectors).
@@ -2561,6 +2592,7 @@ struct l2c_gpu_plan {
   cudaStream_t stream3 = nullptr;
   cudaEvent_t ev_ff[FAR_SPLIT_MAX] = {}, ev_fj[FAR_SPLIT_MAX] = {};
   int far_split = -1;  // TuneCfg::fsplit
+  int band_thin = -1;  // TuneCfg::bthin
   double *Wnear[2] = {nullptr, nullptr};  // precomputed band weights (optional)
   // dense band weights of the full blocks for k_band_tile (built on first use)
   double *Wtile[2] = {nullptr, nullptr};
@@ -2978,6 +3010,16 @@ bool use_near_rows(const l2c_gpu_plan *p, size_t count) {
          near_rows_ok((long long)p->s, (long long)p->nL, (long long)count, p->near_rows == 1);
 }
 
+// Whether the tiled band takes its thin variant (TuneCfg::bthin; s = 16 only).
+// By default in the mixed form, where the chain beside the band is bound by
+// integer latency and gains from the registers and shared memory the thin
+// band leaves it (256 x 16384, untuned: 0.824 -> 0.768 ms per L2C + C2L); the
+// FP64 chain of plain batches needs no more room.  The same sums per output,
+// so the same bits.
+bool band_tile_thin(const l2c_gpu_plan *p) {
+  return p->s == 16 && (p->band_thin >= 0 ? p->band_thin == 1 : p->mixed);
+}
+
 // Band of a batch through k_band_tile, one launch (the full blocks; Wt: its
 // dense table or nullptr for weights formed on the fly; the last block with
 // weights formed on the fly: the same products, so the same bits).  Work units: the
@@ -2986,7 +3028,8 @@ bool use_near_rows(const l2c_gpu_plan *p, size_t count) {
 cudaError_t launch_band_tile(const l2c_gpu_plan *p, const double *x, const double *out,
                              double *y, const double *Wt, Geo g, int c2l, cudaStream_t st,
                              unsigned max_ctas, bool pdl) {
-  const long long VCH = 32LL * band_tile_c(g.s);
+  const bool thin = band_tile_thin(p);
+  const long long VCH = 32LL * band_tile_c(g.s, thin);
   const long long nchunk = (g.count + VCH - 1) / VCH, nfull = g.nL - 1;
   const long long grid_cap = max_ctas ? (long long)max_ctas : 2LL * p->sms;
   long long best_seg = 1;
@@ -3004,8 +3047,8 @@ cudaError_t launch_band_tile(const l2c_gpu_plan *p, const double *x, const doubl
   // the chunks' last-block units first, then the full blocks
   const long long units = nchunk * (1 + (nfull + best_seg - 1) / best_seg);
   const unsigned grid = (unsigned)std::min(units, grid_cap);
-  auto *kern = Wt ? band_tile_kernel<true>(g.s) : band_tile_kernel<false>(g.s);
-  launch_k(pdl, kern, grid, BT_THREADS, band_tile_smem(g.s), st, x, out, y, Wt,
+  auto *kern = Wt ? band_tile_kernel<true>(g.s, thin) : band_tile_kernel<false>(g.s, thin);
+  launch_k(pdl, kern, grid, BT_THREADS, band_tile_smem(g.s, thin), st, x, out, y, Wt,
            (const double *)p->a, (const double *)p->an, (const double *)p->dn, g, c2l, nchunk,
            best_seg);
   return cudaGetLastError();
@@ -3439,6 +3482,7 @@ unsigned long long cfg_signature(const TuneCfg &c) {
   put(c.tl0, 4);
   put(c.bseg, 5);
   put(c.fsplit, 3);  // -1 .. 4
+  put(c.bthin, 2);   // -1 .. 1
   return v;
 }
 
@@ -3457,6 +3501,7 @@ void cfg_apply(l2c_gpu_plan *p, const TuneCfg &c) {
   p->tree_l0 = c.tl0;
   p->band_bseg = c.bseg;
   p->far_split = c.fsplit;
+  p->band_thin = c.bthin;
   p->oz_ld_ctas = p->oz_ld_ctas_nb[c.nbuf == 2 ? 2 : 1];
   p->cfg_sig = cfg_signature(c);
 }
@@ -3646,16 +3691,17 @@ TuneCfg resolved_cfg(l2c_gpu_plan *p, size_t count) {
 void cfg_text(const TuneCfg &c, char *buf, size_t len) {
   snprintf(buf, len, "overlap=%d band_fork=%d pdl=%d prio=%d near_threads=%d near_vb=%d "
            "near_pair=%d near_ctas=%d nbuf=%d near_table=%d mz_top=%d mz_top_g=%d tree_l0=%d "
-           "band_bseg=%d far_split=%d", c.overlap, c.fork, c.pdl, c.prio, c.nthreads, c.nvb,
-           c.npair, c.nctas, c.nbuf, c.wtab, c.mtop, c.mtopg, c.tl0, c.bseg, c.fsplit);
+           "band_bseg=%d far_split=%d band_thin=%d", c.overlap, c.fork, c.pdl, c.prio,
+           c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, c.wtab, c.mtop, c.mtopg, c.tl0, c.bseg,
+           c.fsplit, c.bthin);
 }
 
 // Cache file: one line per tuned shape, fields separated by '|':
 // l2c-tune-5|device|SMs|N|maxs|form|precompute|dir|count|dist|stride|
 //   overlap|pdl|prio|nthreads|nvb|npair|nctas|nbuf|wtab|fork|mtop|mtopg|tl0|bseg|
-//   fsplit|ms|ms_default
+//   fsplit|bthin|ms|ms_default
 // (form 0 modal, 1 nodal, 2 mixed).  Later lines win.
-constexpr int TUNE_FIELDS = 28;
+constexpr int TUNE_FIELDS = 29;
 
 struct TuneKey {
   char dev[256];
@@ -3688,10 +3734,10 @@ void cache_append(const l2c_gpu_plan *p, const TunedShape &t) {
   const TuneCfg &c = t.cfg;
   std::fprintf(f,
                "l2c-tune-5|%s|%d|%zu|%zu|%d|%d|%zu|%zu|%zu|%zu|%d|%d|%d|%d|%d|%d|%d|%d|%d|%d|"
-               "%d|%d|%d|%d|%d|%.6f|%.6f\n",
+               "%d|%d|%d|%d|%d|%d|%.6f|%.6f\n",
                k.dev, k.sms, p->N, p->maxs, k.form, k.pre, t.dir, t.count, t.dist, t.stride,
                c.overlap, c.pdl, c.prio, c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, c.wtab,
-               c.fork, c.mtop, c.mtopg, c.tl0, c.bseg, c.fsplit, t.ms, t.ms_default);
+               c.fork, c.mtop, c.mtopg, c.tl0, c.bseg, c.fsplit, c.bthin, t.ms, t.ms_default);
   std::fclose(f);
 }
 
@@ -3738,8 +3784,9 @@ void cache_load(l2c_gpu_plan *p) {
     t.cfg.tl0 = iv(23);
     t.cfg.bseg = iv(24);
     t.cfg.fsplit = iv(25);
-    t.ms = std::strtod(fld[26], nullptr);
-    t.ms_default = std::strtod(fld[27], nullptr);
+    t.cfg.bthin = iv(26);
+    t.ms = std::strtod(fld[27], nullptr);
+    t.ms_default = std::strtod(fld[28], nullptr);
     t.from_cache = true;
     // only values the launches accept
     const TuneCfg &c = t.cfg;
@@ -3749,7 +3796,7 @@ void cache_load(l2c_gpu_plan *p) {
         c.npair > 1 || c.nctas < 0 || c.nbuf < 1 || c.nbuf > 2 || c.wtab < -1 || c.wtab > 1 ||
         c.fork < 0 || c.fork > 3 || c.mtop < -2 || c.mtop > 5 || c.mtopg < 0 || c.mtopg > 7 ||
         c.tl0 < -1 || c.tl0 > 14 || c.bseg < 0 || c.bseg > 31 || c.fsplit < -1 ||
-        c.fsplit > FAR_SPLIT_MAX)
+        c.fsplit > FAR_SPLIT_MAX || c.bthin < -1 || c.bthin > 1)
       continue;
     p->tuned.push_back(t);
   }
@@ -3827,6 +3874,7 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
         knobs.push_back({&TuneCfg::tl0, v});
       }
       if (tile) knobs.push_back({&TuneCfg::bseg, {0, 1, 2, 4}});
+      if (tile && p->s == 16) knobs.push_back({&TuneCfg::bthin, {0, 1}});
       if (p->mixed && count >= 4 && p->L >= 3) knobs.push_back({&TuneCfg::fsplit, {0, 1, 2, 3}});
       for (int pass = 0; pass < 2 && best > 0.0; pass++) {
         bool kept = false;
@@ -3999,6 +4047,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
     p->base.bseg = std::min(31, std::max(0, std::atoi(env)));
   if (const char *env = std::getenv("L2C_FAR_SPLIT"))
     p->base.fsplit = std::min(FAR_SPLIT_MAX, std::max(-1, std::atoi(env)));
+  if (const char *env = std::getenv("L2C_BAND_THIN")) p->base.bthin = env[0] == '1' ? 1 : 0;
   p->precompute = (flags & L2C_PLAN_PRECOMPUTE_NEAR) != 0;
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
@@ -4235,9 +4284,11 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
     if (band_tile_ok((long long)s, (long long)p->nL, BT_MIN_COUNT)) {
       // the tiled band's three half-window slots can pass the 48 KB default
       const cudaFuncAttribute smax = cudaFuncAttributeMaxDynamicSharedMemorySize;
-      const int bytes = (int)band_tile_smem((long long)s);
-      PCK(cudaFuncSetAttribute(band_tile_kernel<true>((long long)s), smax, bytes));
-      PCK(cudaFuncSetAttribute(band_tile_kernel<false>((long long)s), smax, bytes));
+      for (bool thin : {false, true}) {
+        const int bytes = (int)band_tile_smem((long long)s, thin);
+        PCK(cudaFuncSetAttribute(band_tile_kernel<true>((long long)s, thin), smax, bytes));
+        PCK(cudaFuncSetAttribute(band_tile_kernel<false>((long long)s, thin), smax, bytes));
+      }
     }
     if (flags & L2C_PLAN_PRECOMPUTE_NEAR) {
       // the band weights now, in the dense layout single vectors and large

@@ -328,9 +328,10 @@ __device__ __forceinline__ void load_digits(const long long *Ys, int yld, int ks
 }
 
 // One n-tile nt of a tile from cached digits: acc[d][.] = the diagonal-d sums
-// over all KC chunks (KC <= KMAX / 8 keeps them exact), as mma_tile does for
-// that n-tile.
-template <int NT, int KC, int QMAX = SLICES>
+// over the KC chunks from chunk pair CP0 on (KC <= KMAX / 8 keeps them exact;
+// CP0 > 0 skips pairs whose fragment words are zero for this n-tile), as
+// mma_tile does for that n-tile.
+template <int NT, int KC, int QMAX = SLICES, int CP0 = 0>
 __device__ __forceinline__ void mma_nt(const unsigned *__restrict__ Pf, const Digits<KC> &D,
                                        int nt, float (&acc)[NDIAG][4]) {
   static_assert(KC <= KMAX / 8, "accumulation would not be exact");
@@ -340,7 +341,7 @@ __device__ __forceinline__ void mma_nt(const unsigned *__restrict__ Pf, const Di
 #pragma unroll
     for (int e = 0; e < 4; e++) acc[d][e] = 0.f;
 #pragma unroll
-  for (int cp = 0; cp < KC / 2; cp++) {
+  for (int cp = CP0; cp < KC / 2; cp++) {
 #pragma unroll
     for (int q = 1; q <= QMAX; q++) {
       const uint2 b = *reinterpret_cast<const uint2 *>(Pf + frag_index(q, nt, 2 * cp, lane, NT, KC));

@@ -143,7 +143,10 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
                 {"L2C_FAR_SPLIT": "0"}, {"L2C_FAR_SPLIT": "1"}, {"L2C_FAR_SPLIT": "3"},
                 {"L2C_FAR_SPLIT": "4"}, {"L2C_FAR_SPLIT": "3", "L2C_NO_GRAPHS": "1"},
                 {"L2C_FAR_SPLIT": "3", "L2C_MZ_TOP": "0"},
-                {"L2C_FAR_SPLIT": "2", "L2C_MZ_TOP_LVL": "5", "L2C_BAND_FORK": "3"}):
+                {"L2C_FAR_SPLIT": "2", "L2C_MZ_TOP_LVL": "5", "L2C_BAND_FORK": "3"},
+                # the tiled band's thin variant (one vector per lane)
+                {"L2C_BAND_THIN": "1"}, {"L2C_BAND_THIN": "1", "L2C_NEAR_TABLE": "0"},
+                {"L2C_BAND_THIN": "1", "L2C_NEAR_CTAS": "608"}):
         with monkeypatch.context() as m:
             for k, v in env.items():
                 m.setenv(k, v)
