@@ -2560,6 +2560,11 @@ struct TuneCfg {
   //         more CTAs of the kernels beside it (-1: the plan's rule)
   int mtop = -2, mtopg = 0, tl0 = -1, bseg = 0, fsplit = -1, bthin = -1;
 };
+// Two configurations are the same when every choice is (TuneCfg holds only
+// ints, so its bytes are its fields).
+inline bool same_cfg(const TuneCfg &a, const TuneCfg &b) {
+  return std::memcmp(&a, &b, sizeof(TuneCfg)) == 0;
+}
 
 // A tuned call shape and its choices (dist is 0 for single vectors).
 struct TunedShape {
@@ -2640,7 +2645,8 @@ struct l2c_gpu_plan {
     const void *in;
     void *out;
     unsigned mode;
-    unsigned long long sig;  // launch choices the graph was captured with
+    TuneCfg cfg;  // launch choices the graph was captured with
+    bool use_w;   // and whether its band read the weight table
     cudaGraphExec_t exec;
     size_t launches;
     size_t last_use;
@@ -2665,12 +2671,12 @@ struct l2c_gpu_plan {
   int band_fork = 0;  // TuneCfg::fork
   int prio_greatest = 0;  // cudaDeviceGetStreamPriorityRange's greatest priority
   // autotuner: the plan's own choices (defaults and environment), the tuned
-  // shapes, a configuration forced while one is timed, and the signature of
-  // the configuration the fields hold (part of every captured graph's key)
+  // shapes, a configuration forced while one is timed, and the configuration
+  // the fields hold (part of every captured graph's key, with use_w)
   TuneCfg base;
   std::vector<TunedShape> tuned;
   const TuneCfg *forced = nullptr;
-  unsigned long long cfg_sig = 0;
+  TuneCfg cfg_cur;
   bool autotune = false;          // L2C_AUTOTUNE=1: tune each new shape on its first call
   char tune_cache[1024] = {0};    // L2C_AUTOTUNE_CACHE: file of tuned shapes
   bool tune_cache_loaded = false;
@@ -3461,31 +3467,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   return 1;
 }
 
-// Launch choices -> the plan's fields (and a signature of them).
-unsigned long long cfg_signature(const TuneCfg &c) {
-  unsigned long long v = 0;
-  auto put = [&](long long x, int bits) {
-    v = (v << bits) | ((unsigned long long)(x + 1) & ((1ull << bits) - 1));
-  };
-  put(c.overlap, 2);
-  put(c.pdl, 4);
-  put(c.prio, 2);
-  put(c.nthreads / 128, 2);
-  put(c.nvb, 4);
-  put(c.npair, 2);
-  put(c.nbuf, 2);
-  put(c.nctas, 24);
-  put(c.wtab, 2);
-  put(c.fork, 3);
-  put(c.mtop + 1, 3);  // -2 .. 5
-  put(c.mtopg, 3);
-  put(c.tl0, 4);
-  put(c.bseg, 5);
-  put(c.fsplit, 3);  // -1 .. 4
-  put(c.bthin, 2);   // -1 .. 1
-  return v;
-}
-
+// Launch choices -> the plan's fields.
 void cfg_apply(l2c_gpu_plan *p, const TuneCfg &c) {
   p->overlap = c.overlap;
   p->pdl = c.pdl;
@@ -3503,7 +3485,7 @@ void cfg_apply(l2c_gpu_plan *p, const TuneCfg &c) {
   p->far_split = c.fsplit;
   p->band_thin = c.bthin;
   p->oz_ld_ctas = p->oz_ld_ctas_nb[c.nbuf == 2 ? 2 : 1];
-  p->cfg_sig = cfg_signature(c);
+  p->cfg_cur = c;
 }
 
 // Whether a call's band reads the weight table (TuneCfg::wtab).
@@ -3576,7 +3558,6 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     } else if (p->use_w && !ensure_near_table(p, dir)) {
       return 0;
     }
-    if (p->use_w) p->cfg_sig |= 1ull << 63;
   }
   if (!ensure_scratch(p, count)) return 0;
   if (p->mixed && p->L > 0 && count >= 4 && !ensure_mixed_far(p, dir)) return 0;
@@ -3587,7 +3568,7 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   p->use_clock++;
   for (auto &e : p->graphs) {
     if (e.dir == dir && e.count == count && e.dist == dist && e.stride == stride && e.in == in &&
-        e.out == out && e.mode == mode && e.sig == p->cfg_sig) {
+        e.out == out && e.mode == mode && e.use_w == p->use_w && same_cfg(e.cfg, p->cfg_cur)) {
       e.last_use = p->use_clock;
       CK(cudaGraphLaunch(e.exec, p->stream));
       p->launches += e.launches;
@@ -3615,7 +3596,8 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     set_err("cudaGraphInstantiate failed: %s", cudaGetErrorString(ei));
     return 0;
   }
-  l2c_gpu_plan::GraphEntry e{dir,  count, dist, stride, in, out, mode, p->cfg_sig, exec,
+  l2c_gpu_plan::GraphEntry e{dir,        count,    dist, stride, in,
+                             out,        mode,     p->cfg_cur, p->use_w, exec,
                              p->launches - before, p->use_clock};
   if (p->graphs.size() >= 8) {
     auto oldest = std::min_element(p->graphs.begin(), p->graphs.end(),
@@ -3898,7 +3880,7 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
       }
       // confirmation: the plan's choices and the search's, timed again in
       // turn; the search's stay only if they still save 1 %
-      if (best > 0.0 && cfg_signature(cur) != cfg_signature(dflt)) {
+      if (best > 0.0 && !same_cfg(cur, dflt)) {
         double td = -1.0, tc = -1.0;
         for (int r = 0; r < 2 && best > 0.0; r++) {
           const double a = tune_time(p, din, dout, dir, count, dist, stride, dflt, e0, e1);
