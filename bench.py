@@ -811,7 +811,7 @@ def main():
     N, maxs, count = wl.N, wl.maxs, wl.count
     ragged = wl.name == "ragged"
     if ragged:
-        plan = l2c.RaggedPlan(wl.Ns, maxs)
+        plan = l2c.RaggedPlan(wl.Ns, maxs, precompute=args.precompute)
     else:
         plan = l2c.Plan(N, maxs, precompute=args.precompute, lagrange=args.lagrange)
     stream = torch.cuda.ExternalStream(plan.stream, device=dev)

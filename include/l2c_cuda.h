@@ -158,8 +158,11 @@ size_t l2c_gpu_execute_noalloc(l2c_gpu_plan *plan, const double *in, double *out
  * the caller's arrays: vector v starts at N[0] + ... + N[v-1]), each transformed
  * exactly as execute() with create_fmm(N[v], maxs, 18, directions, 0, 0, 0)
  * would (vectors with L < 1 take the direct method), in one set of launches whose
- * count does not depend on the number of vectors.  No counterpart in the
- * reference (its callers loop execute over plans, src/bin/l2c.c harnesses). */
+ * count does not depend on the number of vectors.  flags: L2C_PLAN_PRECOMPUTE_NEAR
+ * keeps the band weights of each leaf size in the list in device memory (one
+ * table per leaf size, serving every vector with it; the same bits, one FP64
+ * instruction per band term instead of two).  No counterpart in the reference
+ * (its callers loop execute over plans, src/bin/l2c.c harnesses). */
 typedef struct l2c_gpu_ragged l2c_gpu_ragged;
 l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *N, size_t maxs,
                                       size_t directions, unsigned flags);

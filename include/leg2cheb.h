@@ -199,7 +199,9 @@ fmm_plan *create_fmm_ex(const size_t N, const size_t maxs, const size_t M, const
 /* Ragged batch: count vectors of lengths N[0..count), packed back to back
  * (vector v starts at N[0] + ... + N[v-1]); each is transformed exactly as
  * execute() with create_fmm(N[v], maxs, M, direction, ...) would, all in one set
- * of GPU launches.  Returns the summed flop count, 0 on failure. */
+ * of GPU launches; precompute = 1 keeps the band weights in device memory, as
+ * create_fmm's does (one table per leaf size in the list).  Returns the summed
+ * flop count, 0 on failure. */
 typedef struct {
   size_t count;
   size_t total; /* sum of N */

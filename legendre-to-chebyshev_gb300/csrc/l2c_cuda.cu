@@ -568,12 +568,20 @@ __device__ __forceinline__ void near_rows_group(const double *__restrict__ xb,
     const int t = mp - ip0;  // rows r <= t have a term at this m'
     double wt[4];
     if (TAB) {
-      const double2 q0 = __ldg(reinterpret_cast<const double2 *>(Wg + (long long)mp * g.s));
-      const double2 q1 = __ldg(reinterpret_cast<const double2 *>(Wg + (long long)mp * g.s) + 1);
-      wt[0] = q0.x;
-      wt[1] = q0.y;
-      wt[2] = q1.x;
-      wt[3] = q1.y;
+      // the group's four weights at m' (16-byte aligned when s is even: the
+      // table's rows are s doubles long)
+      const double *wq = Wg + (long long)mp * g.s;
+      if ((g.s & 1) == 0) {
+        const double2 q0 = __ldg(reinterpret_cast<const double2 *>(wq));
+        const double2 q1 = __ldg(reinterpret_cast<const double2 *>(wq) + 1);
+        wt[0] = q0.x;
+        wt[1] = q0.y;
+        wt[2] = q1.x;
+        wt[3] = q1.y;
+      } else {
+#pragma unroll
+        for (int r = 0; r < 4; r++) wt[r] = __ldg(wq + r);
+      }
     } else {
       // shift the windows to m' and bring in row 0's lo and row R-1's hi
 #pragma unroll
@@ -4717,6 +4725,9 @@ struct RVec {
 
 struct RDonor {
   const double *a, *an, *dn, *T, *A[2];
+  // dense band weights per direction (lists made with L2C_PLAN_PRECOMPUTE_NEAR):
+  // block b of any vector with this leaf size is block b of the donor
+  const double *Wt[2];
 };
 
 __device__ __forceinline__ int find_vec(const long long *__restrict__ pre, int nvec, long long idx) {
@@ -4742,6 +4753,9 @@ __global__ void k_r_gather(const double *__restrict__ in, double *__restrict__ x
 
 // The band of every FMM vector with register windows (near_rows_item): items
 // counted by pre (near_rows_items per vector, 0 for direct-method vectors).
+// TAB: the band weights from the donors' dense tables (the same products, so
+// the same bits as forming them here).
+template <bool TAB>
 __global__ void __launch_bounds__(256) k_r_near_rows(const double *__restrict__ x,
                                                      const double *out, double *__restrict__ y,
                                                      const RVec *__restrict__ V,
@@ -4754,8 +4768,8 @@ __global__ void __launch_bounds__(256) k_r_near_rows(const double *__restrict__ 
   const RVec &r = V[v];
   if (r.direct) return;
   const RDonor &d = D[r.donor];
-  near_rows_item<false>(x + r.io, out + r.io, y + r.io, d.a, d.an, d.dn, nullptr, r.g, c2l,
-                        idx - pre[v]);
+  near_rows_item<TAB>(x + r.io, out + r.io, y + r.io, d.a, d.an, d.dn, TAB ? d.Wt[c2l] : nullptr,
+                      r.g, c2l, idx - pre[v]);
 }
 
 __global__ void __launch_bounds__(256) k_r_near(const double *__restrict__ x, const double *out,
@@ -4934,6 +4948,9 @@ struct l2c_gpu_ragged {
   int tuned_ov[2] = {-1, -1}, tuned_prio[2] = {-1, -1};
   double tuned_ms[2] = {0, 0}, tuned_ms_default[2] = {0, 0};
   bool autotune = false;
+  // L2C_PLAN_PRECOMPUTE_NEAR: each donor keeps its dense band weights, which
+  // the band of every vector with that leaf size reads (one DFMA per term)
+  bool precompute = false;
 };
 
 namespace {
@@ -4956,8 +4973,9 @@ size_t ragged_launch(l2c_gpu_ragged *r, const double *in, double *out, size_t di
       CK(cudaEventRecord(r->ev_fork, st));
       CK(cudaStreamWaitEvent(r->stream2, r->ev_fork, 0));
     }
-    k_r_near_rows<<<blocks_for(r->tot_rows, 256), 256, 0, sb>>>(x, out, r->y, r->V, r->D,
-                                                                r->pre_rows, n, c2l);
+    (r->precompute ? k_r_near_rows<true> : k_r_near_rows<false>)<<<blocks_for(r->tot_rows, 256),
+                                                                    256, 0, sb>>>(
+        x, out, r->y, r->V, r->D, r->pre_rows, n, c2l);
     r->launches++;
     if (ov && r->any_direct) {  // other vectors' outputs: no order with the chain
       k_r_direct<<<blocks_for(r->tot_coef, 256), 256, 0, sb>>>(in, out, r->V, r->D, r->pre_coef,
@@ -5020,7 +5038,6 @@ void l2c_gpu_ragged_destroy(l2c_gpu_ragged *r) {
 
 l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *Ns, size_t maxs,
                                       size_t directions, unsigned flags) {
-  (void)flags;
   g_err[0] = 0;
   if (count == 0 || !Ns || directions > 2) {
     set_err("ragged plan needs count > 0, lengths, and direction 0, 1 or 2");
@@ -5056,6 +5073,7 @@ l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *Ns, size_t max
   if (const char *env = std::getenv("L2C_OVERLAP")) r->overlap = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_CHAIN_PRIO")) r->chain_prio = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_AUTOTUNE")) r->autotune = env[0] == '1';
+  r->precompute = (flags & L2C_PLAN_PRECOMPUTE_NEAR) != 0;
   // geometry of every vector; largest level count per leaf size s
   std::vector<size_t> L(count), S(count);
   std::vector<std::pair<size_t, size_t>> smax;  // (s, Lmax)
@@ -5086,7 +5104,8 @@ l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *Ns, size_t max
   std::vector<int> donor_of_s(smax.size());
   for (size_t k = 0; k < smax.size(); k++) {
     const size_t sv = smax[k].first, Lm = smax[k].second;
-    l2c_gpu_plan *d = l2c_gpu_plan_create(sv << (Lm + 2), sv, directions, 0);
+    l2c_gpu_plan *d = l2c_gpu_plan_create(sv << (Lm + 2), sv, directions,
+                                          flags & L2C_PLAN_PRECOMPUTE_NEAR);
     if (!d) return fail();
     if (d->L != Lm || d->s != sv) {
       set_err("internal: donor geometry mismatch");
@@ -5094,7 +5113,8 @@ l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *Ns, size_t max
       return fail();
     }
     r->donors.push_back(d);
-    hD.push_back(RDonor{d->a, d->an, d->dn, d->T, {d->A[0], d->A[1]}});
+    hD.push_back(RDonor{d->a, d->an, d->dn, d->T, {d->A[0], d->A[1]},
+                        {d->Wtile[0], d->Wtile[1]}});
     r->Lmax = std::max(r->Lmax, (int)Lm);
   }
   int direct_donor = -1;
@@ -5102,7 +5122,7 @@ l2c_gpu_ragged *l2c_gpu_ragged_create(size_t count, const size_t *Ns, size_t max
     l2c_gpu_plan *d = l2c_gpu_plan_create(max_direct_N, 1, directions, L2C_PLAN_DIRECT_ONLY);
     if (!d) return fail();
     r->donors.push_back(d);
-    hD.push_back(RDonor{d->a, d->an, d->dn, nullptr, {nullptr, nullptr}});
+    hD.push_back(RDonor{d->a, d->an, d->dn, nullptr, {nullptr, nullptr}, {nullptr, nullptr}});
     direct_donor = (int)hD.size() - 1;
   }
   // descriptors and the prefix sums of each phase's work items

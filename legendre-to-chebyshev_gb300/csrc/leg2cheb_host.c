@@ -522,7 +522,6 @@ size_t execute2D(const double *input_array, double *output_array, fmm_plan_2d *p
 fmm_plan_ragged *create_fmm_ragged(size_t count, const size_t *N, size_t maxs, size_t M,
                                    size_t direction, size_t lagrange, size_t precompute,
                                    size_t v) {
-  (void)precompute;
   host_err[0] = 0;
   if (M != L2C_M || lagrange != 0) {
     herr("only the modal form with M = 18 is implemented");
@@ -533,7 +532,8 @@ fmm_plan_ragged *create_fmm_ragged(size_t count, const size_t *N, size_t maxs, s
     herr("out of host memory");
     return NULL;
   }
-  l2c_gpu_ragged *g = l2c_gpu_ragged_create(count, N, maxs, direction, 0);
+  l2c_gpu_ragged *g =
+      l2c_gpu_ragged_create(count, N, maxs, direction, precompute ? L2C_PLAN_PRECOMPUTE_NEAR : 0);
   if (!g) {
     free(p);
     return NULL;

@@ -305,14 +305,14 @@ class RaggedPlan:
     vectors of lengths Ns packed back to back, all transformed in one set of
     GPU launches."""
 
-    def __init__(self, Ns, maxs=64, direction=BOTH, verbose=0):
+    def __init__(self, Ns, maxs=64, direction=BOTH, verbose=0, precompute=0):
         lib = load()
         self.Ns = np.asarray(Ns, dtype=np.uint64)
         self.offsets = np.concatenate([[0], np.cumsum(self.Ns)]).astype(np.int64)
         self.total = int(self.offsets[-1])
         arr = np.ascontiguousarray(self.Ns, dtype=np.uint64)
-        self._p = lib.create_fmm_ragged(len(arr), arr.ctypes.data, maxs, 18, direction, 0, 0,
-                                        verbose)
+        self._p = lib.create_fmm_ragged(len(arr), arr.ctypes.data, maxs, 18, direction, 0,
+                                        precompute, verbose)
         if not self._p:
             raise L2CError("create_fmm_ragged failed: " + last_error())
         self._gpu = ctypes.c_void_p(ctypes.cast(self._p, ctypes.POINTER(ctypes.c_void_p * 5))

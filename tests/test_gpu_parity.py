@@ -276,10 +276,13 @@ def test_full_size_properties(lib, N):
     assert relerr(back, u) < 1e-12
 
 
-@pytest.mark.parametrize("N,maxs", [(4096, 64), (5001, 64), (1 << 20, 32), (300, 64)])
+@pytest.mark.parametrize("N,maxs", [(4096, 64), (5001, 64), (1 << 20, 32), (300, 64),
+                                    ((1 << 20) + 1, 64), (200000, 50)])
 def test_precomputed_band_weights_bitwise(lib, N, maxs):
     # create_fmm's precompute = 1 keeps the band weights in device memory; the
-    # weights are the same products, so results are bit-identical
+    # weights are the same products, so results are bit-identical (odd leaf
+    # sizes too: s = 33 and 49 with the register-window band, whose table rows
+    # are then not 16-byte aligned)
     u = make_input(N, "uniform", N + 1)
     p0 = lib.Plan(N, maxs)
     p1 = lib.Plan(N, maxs, precompute=1)
@@ -553,6 +556,34 @@ def test_random_ragged_vs_oracle(lib, orc, seed):
             w = pre[a:b].copy()
             orc.Oracle(N, maxs, 2).execute(np.ascontiguousarray(u[a:b]), w, d)
             assert relerr(out[a:b], w) <= TOL, (seed, v, N, maxs, d)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_ragged_precompute_bitwise(lib, orc, seed):
+    """Ragged lists made with precompute = 1 read the band weights from one
+    table per leaf size (each table serving every vector with that leaf size,
+    whatever its length): the bits of precompute = 0, and the oracle's results
+    within the bar.  Lists mix lengths of one leaf size and direct vectors."""
+    rng = np.random.default_rng(5000 + seed)
+    count = int(rng.integers(20, 80))
+    Ns = [int(n) for n in np.exp(rng.uniform(np.log(20), np.log(70000), count))]
+    maxs = (64, 32, 50, 17)[seed]
+    u = make_input(sum(Ns), "sign", seed + 9)
+    outs = {}
+    for pre in (0, 1):
+        p = lib.RaggedPlan(Ns, maxs, precompute=pre)
+        for d in (0, 1):
+            out = np.zeros(p.total)
+            p(u, out, d)
+            outs[pre, d] = out
+        p.close()
+    offs = np.concatenate([[0], np.cumsum(Ns)])
+    for d in (0, 1):
+        assert np.array_equal(outs[1, d], outs[0, d]), (seed, d)
+        for v in (0, count // 2, count - 1):
+            a, b = offs[v], offs[v + 1]
+            want = orc.Oracle(Ns[v], maxs, 2)(np.ascontiguousarray(u[a:b]), d)[:Ns[v]]
+            assert relerr(outs[1, d][a:b], want) <= TOL, (seed, v, Ns[v], d)
 
 
 def random_layout(seed):
