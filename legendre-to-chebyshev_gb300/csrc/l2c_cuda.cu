@@ -2548,10 +2548,11 @@ struct PhaseScope;
 //              plans created with precompute
 //   fork     : where the band joins the chain's stream order when it overlaps:
 //              0 from the start, 1 after leaf-up, 2 after the upward sweep,
-//              3 after the far field (it always finishes before leaf-down)
+//              3 after the far field (it always finishes before leaf-down);
+//              -1 by shape (band_fork_for)
 struct TuneCfg {
   int overlap = -1, pdl = -1, prio = -1, nthreads = 128, nvb = 8, npair = -1, nctas = 0,
-      nbuf = 1, wtab = -1, fork = 0;
+      nbuf = 1, wtab = -1, fork = -1;
   // the per-level structure of the far-field chain and the band's schedule:
   //   mtop  mixed form: coarsest transfer level in the one top launch (-2: the
   //         plan's rule, levels of at most 64 slots; -1: none)
@@ -2676,7 +2677,7 @@ struct l2c_gpu_plan {
   //  chain_prio_mode: the chain's kernels at the device's greatest priority.
   int pdl = -1;
   int chain_prio_mode = -1;
-  int band_fork = 0;  // TuneCfg::fork
+  int band_fork = -1;  // TuneCfg::fork
   int prio_greatest = 0;  // cudaDeviceGetStreamPriorityRange's greatest priority
   // autotuner: the plan's own choices (defaults and environment), the tuned
   // shapes, a configuration forced while one is timed, and the configuration
@@ -3119,12 +3120,26 @@ struct Sched {
   int prio;      // priority of the chain's kernels (0: the stream's)
 };
 
+// The band's fork point when the plan leaves it to the shape (TuneCfg::fork
+// = -1): single plain vectors whose band takes k_near_rows (large N, the band
+// the longer stream) start it after leaf-up, so that leaf-up has the GPU to
+// itself and the band then runs at the chain's priority (N = 2^20, L2C + C2L:
+// 1.110 -> 1.081 ms per step; with the chain at the greatest priority 1.086);
+// everything else from the start.
+int band_fork_for(const l2c_gpu_plan *p, size_t count) {
+  if (p->band_fork >= 0) return std::min(p->band_fork, 3);
+  return !p->mixed && use_near_rows(p, count) ? 1 : 0;
+}
+
 Sched sched_for(const l2c_gpu_plan *p, size_t count) {
   Sched sc;
   sc.ov = p->overlap >= 0 ? p->overlap == 1 : true;
   const bool latency = p->mixed || count == 1;
   sc.pdl = p->pdl >= 0 ? (unsigned)p->pdl : latency ? 1u : 0u;
-  const bool prio = p->chain_prio_mode >= 0 ? p->chain_prio_mode == 1 : latency;
+  // a band that enters after leaf-up (band_fork_for) is the longer stream
+  // from then on: the chain beside it takes the SMs it leaves, at its own priority
+  const bool prio = p->chain_prio_mode >= 0 ? p->chain_prio_mode == 1
+                                            : latency && band_fork_for(p, count) == 0;
   sc.prio = prio && sc.ov ? p->prio_greatest : 0;
   return sc;
 }
@@ -3404,7 +3419,7 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   const Sched sc = sched_for(p, count);
   const bool ov = sc.ov;
   cudaStream_t stn = ov ? st2 : st;
-  const int fork = ov ? std::min(std::max(p->band_fork, 0), 3) : 0;
+  const int fork = ov ? band_fork_for(p, count) : 0;
   bool band_done = false;
   auto band = [&](int pos) -> bool {
     if (band_done || pos < fork) return true;
@@ -3674,7 +3689,10 @@ TuneCfg resolved_cfg(l2c_gpu_plan *p, size_t count) {
   TuneCfg c = p->base;
   c.overlap = sc.ov ? 1 : 0;
   c.pdl = (int)sc.pdl;
-  c.prio = p->chain_prio_mode >= 0 ? p->chain_prio_mode : ((p->mixed || count == 1) ? 1 : 0);
+  c.prio = p->chain_prio_mode >= 0
+               ? p->chain_prio_mode
+               : ((p->mixed || count == 1) && band_fork_for(p, count) == 0 ? 1 : 0);
+  c.fork = band_fork_for(p, count);
   return c;
 }
 
