@@ -3120,15 +3120,14 @@ struct Sched {
   int prio;      // priority of the chain's kernels (0: the stream's)
 };
 
-// The band's fork point when the plan leaves it to the shape (TuneCfg::fork
-// = -1): single plain vectors whose band takes k_near_rows (large N, the band
-// the longer stream) start it after leaf-up, so that leaf-up has the GPU to
-// itself and the band then runs at the chain's priority (N = 2^20, L2C + C2L:
-// 1.110 -> 1.081 ms per step; with the chain at the greatest priority 1.086);
-// everything else from the start.
+// The band's fork point when the plan leaves it open (TuneCfg::fork = -1):
+// from the start.  Where entering after leaf-up pays depends on the size
+// (single vectors, L2C + C2L, ms per step, from the start with chain priority
+// / after leaf-up without: N = 2^18 0.374 / 0.450, 2^20 1.110 / 1.081, 2^22
+// 4.008 / 4.045), so it is left to the autotuner.
 int band_fork_for(const l2c_gpu_plan *p, size_t count) {
-  if (p->band_fork >= 0) return std::min(p->band_fork, 3);
-  return !p->mixed && use_near_rows(p, count) ? 1 : 0;
+  (void)count;
+  return p->band_fork >= 0 ? std::min(p->band_fork, 3) : 0;
 }
 
 Sched sched_for(const l2c_gpu_plan *p, size_t count) {
@@ -3661,21 +3660,34 @@ __global__ void k_tune_fill(double *v, long long n) {
 }
 
 // ms per call under c (< 0 on error).
+// One configuration's time per call: after capture and two warm-up replays,
+// the best of three runs of three calls.  Each timed call starts from an L2
+// that another buffer has just filled (flush, flush_bytes; none if null), as a
+// call does whose inputs and tables were not the last thing the GPU touched:
+// with the tables warm in L2 the chain looked shorter than it is and the
+// search favoured the wrong fork point for large single vectors.
 double tune_time(l2c_gpu_plan *p, const double *in, double *out, size_t dir, size_t count,
-                 size_t dist, size_t stride, const TuneCfg &c, cudaEvent_t e0, cudaEvent_t e1) {
+                 size_t dist, size_t stride, const TuneCfg &c, cudaEvent_t e0, cudaEvent_t e1,
+                 void *flush, size_t flush_bytes) {
   p->forced = &c;
   double best = -1.0;
   bool ok = true;
   for (int i = 0; i < 2 && ok; i++)
     ok = run_device(p, in, out, dir, count, dist, stride, false, false) != 0;
   for (int rep = 0; rep < 3 && ok; rep++) {
-    ok = cudaEventRecord(e0, p->stream) == cudaSuccess;
-    for (int i = 0; i < 3 && ok; i++)
-      ok = run_device(p, in, out, dir, count, dist, stride, false, false) != 0;
-    float ms = 0.f;
-    ok = ok && cudaEventRecord(e1, p->stream) == cudaSuccess &&
-         cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
-    if (ok && (best < 0.0 || ms / 3.0 < best)) best = ms / 3.0;
+    double sum = 0.0;
+    for (int i = 0; i < 3 && ok; i++) {
+      if (flush)
+        ok = cudaMemsetAsync(flush, (rep * 3 + i) & 0xff, flush_bytes, p->stream) == cudaSuccess;
+      ok = ok && cudaEventRecord(e0, p->stream) == cudaSuccess;
+      ok = ok && run_device(p, in, out, dir, count, dist, stride, false, false) != 0;
+      float ms = 0.f;
+      ok = ok && cudaEventRecord(e1, p->stream) == cudaSuccess &&
+           cudaEventSynchronize(e1) == cudaSuccess &&
+           cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+      sum += ms;
+    }
+    if (ok && (best < 0.0 || sum / 3.0 < best)) best = sum / 3.0;
   }
   p->forced = nullptr;
   return ok ? best : -1.0;
@@ -3828,8 +3840,17 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
   double *din = nullptr, *dout = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   double result = 0.0;
-  int sms = 152;
+  int sms = 152, l2 = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
+  cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, p->device);
+  // a buffer twice the L2 to write before each timed call (none if it cannot
+  // be had: the timings are then taken with warm caches)
+  void *flush = nullptr;
+  const size_t flush_bytes = std::max<size_t>(2 * (size_t)l2, (size_t)64 << 20);
+  if (cudaMalloc(&flush, flush_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    flush = nullptr;
+  }
   if (cudaMalloc(&din, span * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&dout, span * sizeof(double)) != cudaSuccess ||
       cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
@@ -3842,8 +3863,10 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
     const TuneCfg dflt = cur;
     // a first timing brings the GPU's clocks up (the first shape tuned after
     // an idle spell read ~15 % slow) and is dropped
-    tune_time(p, din, dout, dir, count, dist, stride, cur, e0, e1);
-    double t_default = tune_time(p, din, dout, dir, count, dist, stride, cur, e0, e1);
+    tune_time(p, din, dout, dir, count, dist, stride, cur, e0, e1, flush,
+              flush_bytes);
+    double t_default = tune_time(p, din, dout, dir, count, dist, stride, cur, e0, e1, flush,
+                                 flush_bytes);
     double best = t_default;
     if (best > 0.0 && p->L > 0) {
       struct Knob {
@@ -3891,7 +3914,8 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
             if (cur.*(kb.f) == v) continue;
             TuneCfg c = cur;
             c.*(kb.f) = v;
-            const double t = tune_time(p, din, dout, dir, count, dist, stride, c, e0, e1);
+            const double t = tune_time(p, din, dout, dir, count, dist, stride, c, e0, e1, flush,
+                                       flush_bytes);
             if (t < 0.0) {
               best = -1.0;
               break;
@@ -3909,8 +3933,10 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
       if (best > 0.0 && !same_cfg(cur, dflt)) {
         double td = -1.0, tc = -1.0;
         for (int r = 0; r < 2 && best > 0.0; r++) {
-          const double a = tune_time(p, din, dout, dir, count, dist, stride, dflt, e0, e1);
-          const double b = tune_time(p, din, dout, dir, count, dist, stride, cur, e0, e1);
+          const double a = tune_time(p, din, dout, dir, count, dist, stride, dflt, e0, e1, flush,
+                                     flush_bytes);
+          const double b = tune_time(p, din, dout, dir, count, dist, stride, cur, e0, e1, flush,
+                                     flush_bytes);
           if (a < 0.0 || b < 0.0) {
             best = -1.0;
           } else {
@@ -3960,6 +3986,7 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
   if (e1) cudaEventDestroy(e1);
   if (din) cudaFree(din);
   if (dout) cudaFree(dout);
+  if (flush) cudaFree(flush);
   return result;
 }
 
