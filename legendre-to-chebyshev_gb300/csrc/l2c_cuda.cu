@@ -1589,8 +1589,9 @@ __global__ void __launch_bounds__(BT_THREADS, CC < BandTile<S>::C ? 8 : 4)
             const int p = q / (S / 8), ga = q % (S / 8), ia = 4 * ga, ib = S - 4 - ia;
             const double *Wp = TAB ? Wb + p * 2 * S * S : nullptr;
             band_tile_pair<S, CC, TAB>(sA + lane * LD, sB + lane * LD, TAB ? Wp + ia : nullptr,
-                                   TAB ? Wp + ib : nullptr, p, ia, ib, b * H + 2 * ia + p,
-                                   b * H + 2 * ib + p, c2l, a, an, dn, res[t][0], res[t][1]);
+                                       TAB ? Wp + ib : nullptr, p, ia, ib, b * H + 2 * ia + p,
+                                       b * H + 2 * ib + p, c2l, a, an, dn, res[t][0],
+                                       res[t][1]);
           }
         }
         __syncthreads();  // every warp is done reading slots A and B
@@ -1617,8 +1618,8 @@ __global__ void __launch_bounds__(BT_THREADS, CC < BandTile<S>::C ? 8 : 4)
           if (q < BT::GROUPS) {
             const int p = q & 1, ip0 = 4 * (q >> 1);
             band_tile_group<S, CC, TAB>(sA + lane * LD, sB + lane * LD,
-                                    TAB ? Wb + p * 2 * S * S + ip0 : nullptr, p, ip0,
-                                    b * H + 2 * ip0 + p, c2l, a, an, dn, res[t]);
+                                        TAB ? Wb + p * 2 * S * S + ip0 : nullptr, p, ip0,
+                                        b * H + 2 * ip0 + p, c2l, a, an, dn, res[t]);
           }
         }
         __syncthreads();  // every warp is done reading slots A and B
@@ -2549,7 +2550,7 @@ struct PhaseScope;
 //   fork     : where the band joins the chain's stream order when it overlaps:
 //              0 from the start, 1 after leaf-up, 2 after the upward sweep,
 //              3 after the far field (it always finishes before leaf-down);
-//              -1 by shape (band_fork_for)
+//              -1 the plan's rule (band_fork_for: from the start)
 struct TuneCfg {
   int overlap = -1, pdl = -1, prio = -1, nthreads = 128, nvb = 8, npair = -1, nctas = 0,
       nbuf = 1, wtab = -1, fork = -1;
