@@ -4990,7 +4990,9 @@ struct l2c_gpu_ragged {
   // L2C_CHAIN_PRIO); tuned_*: the autotuner's, per direction (-1: none).
   cudaStream_t stream2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  int overlap = 1, chain_prio = 1, prio_greatest = 0;
+  // (the chain at its stream's priority by default: the band carries a ragged
+  // list's step, 2000-vector list 17.18 -> 16.78 ms per L2C + C2L untuned)
+  int overlap = 1, chain_prio = 0, prio_greatest = 0;
   int tuned_ov[2] = {-1, -1}, tuned_prio[2] = {-1, -1};
   double tuned_ms[2] = {0, 0}, tuned_ms_default[2] = {0, 0};
   bool autotune = false;
