@@ -20,7 +20,7 @@ INCLUDE = os.path.join(REPO, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CUDA_SOURCES = [os.path.join(CSRC, "l2c_cuda.cu")]
-CUDA_DEPS = CUDA_SOURCES + [os.path.join(CSRC, f) for f in ("l2c_lambda.h", "l2c_tables.h", "l2c_ozaki.cuh")] + [
+CUDA_DEPS = CUDA_SOURCES + [os.path.join(CSRC, f) for f in ("l2c_lambda.h", "l2c_tables.h", "l2c_ozaki.cuh", "l2c_tc.cuh")] + [
     os.path.join(INCLUDE, "l2c_cuda.h")
 ]
 HOST_SOURCES = [os.path.join(CSRC, "leg2cheb_host.c")]

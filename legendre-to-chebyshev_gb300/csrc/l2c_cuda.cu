@@ -34,6 +34,7 @@
 #include "../../include/l2c_cuda.h"
 #include "l2c_lambda.h"
 #include "l2c_ozaki.cuh"
+#include "l2c_tc.cuh"
 
 namespace {
 
@@ -2353,6 +2354,319 @@ constexpr size_t oz_far_smem(int NBUF) {
          (size_t)MXW * NBUF * 16 * OZ_TLD * sizeof(long long);
 }
 
+// Far field on the fifth-generation tensor cores (TuneCfg::fartc): the product
+// of k_mz_far -- the 40-row block matrix of k_oz_pack_far times the columns
+// [w0; w1] -- with the diagonal sums accumulated in tensor memory instead of
+// registers.  CTA = (block gb, 128 columns vs = vector * 2 + parity): column m
+// of the CTA is row m of an M = 128, N = 48 MMA (output rows 0 .. 47).  Its two
+// slots' moments (18 + 18) sit at K positions 0 .. 17 and 24 .. 41 of three
+// 16-wide k-steps; the other K positions are zero, as are the packed matrix's
+// there (k_oz_pack_far_tc).  One MMA per digit pair and k-step: each reads its
+// 128-row operand tile from shared memory once, so few wide products cost
+// less than many narrow ones.  The six diagonals are formed in three passes of
+// two (d = 2 pass, 2 pass + 1: 3, 7 and 11 digit pairs) into two tensor-memory
+// buffers of 128 columns (diagonal 2 pass + e at 128 (pass % 2) + 64 e), so a
+// pass is read out while the next one multiplies; each lane adds its outputs'
+// share of the combination (l2c_oz::combine6, split by diagonal pairs) in
+// 64-bit registers.  Every diagonal sum is the same integer as k_mz_far's (the
+// accumulation is exact), so are the outputs.  The digits of the columns are
+// written to shared memory in the K-major no-swizzle layout of l2c_tc.cuh, the
+// block matrix's arrive by one bulk copy.
+constexpr int FTC_COLS = 128, FTC_THREADS = 256;
+constexpr uint32_t FTC_A_BYTES = l2c_oz::SLICES * 3 * 4096;  // digits of 128 columns
+constexpr uint32_t FTC_B_BYTES = l2c_oz::SLICES * 3 * 1536;  // digits of the 48-row matrix
+constexpr int FTC_B_WORDS = (int)(FTC_B_BYTES / 4);
+constexpr uint32_t FTC_TMEM_COLS = 256;  // two buffers of two diagonals
+constexpr size_t ftc_smem() {
+  return FTC_A_BYTES + FTC_B_BYTES + 2 * OZ_META * 4 + 4 * 8 + 16;
+}
+// Tensor memory holds 512 columns per SM: with more than a third of the SM's
+// 228 KB of shared memory per CTA, at most two of these CTAs are resident on
+// an SM, and their allocations always fit (an allocation never waits).
+static_assert(3 * (ftc_smem() + 1024) > 228 * 1024, "a third CTA could wait for tensor memory");
+static_assert(2 * (ftc_smem() + 1024) <= 228 * 1024, "two CTAs per SM");
+
+// Far-field block fragments in k_mz_far_tc's operand layout, from the words of
+// k_oz_pack_far (the same digits): per block FTC_B_WORDS words; the FP16 pair
+// at K positions (kp, kp + 1) of row n, digit slice q, lies in k-step
+// ks = kp / 16 at byte ((q - 1) 3 + ks) 1536 + l2c_tc::tile_offset(n, kp % 16).
+// K position kp holds moment kp (kp < 18) or kp - 6 (24 <= kp < 42), zero
+// elsewhere; rows 40 .. 47 are zero.  One thread per word.
+__global__ void k_oz_pack_far_tc(const unsigned *__restrict__ F, long long nblocks,
+                                 unsigned *__restrict__ Ft) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= nblocks * FTC_B_WORDS) return;
+  const long long gb = idx / FTC_B_WORDS;
+  const int off = 4 * (int)(idx - gb * FTC_B_WORDS);
+  const int reg = off / 1536, in = off - reg * 1536;
+  const int q = reg / 3 + 1, ks = reg % 3;
+  const int n = (in / 256) * 8 + (in % 128) / 16;
+  const int kp = ks * 16 + ((in % 256) / 128) * 8 + (in % 16) / 2;
+  const int k = kp < M ? kp : (kp >= 24 && kp < 24 + M ? kp - 6 : -1);
+  unsigned v = 0u;
+  if (n < 8 * OZ_FAR_NT && k >= 0)
+    v = F[gb * OZ_FAR_WORDS + l2c_oz::frag_index(q, n / 8, k / 8, 4 * (n % 8) + (k % 8) / 2,
+                                                 OZ_FAR_NT, OZ_FAR_KC)];
+  Ft[idx] = v;
+}
+
+// Read-out of pass P for the lane's column: the FP32 sums of diagonals 2P and
+// 2P + 1 of outputs N0 .. N0 + 2 NW - 1 at tensor-memory columns ta + [0, 2 NW)
+// and ta + 64 + [0, 2 NW); those in [NB, NB + 18) add their share of
+// l2c_oz::combine6 to T[n - NB] (modulo 2^64, as combine6 forms it).
+template <int P, int NW, int N0, int NB>
+__device__ __forceinline__ void ftc_pass_chunk(uint32_t ta, long long (&T)[M]) {
+  uint32_t r[2][2 * NW];
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    if constexpr (NW == 4) {
+      l2c_tc::tmem_ld8(ta + 64 * e, *reinterpret_cast<uint32_t(*)[8]>(r[e]));
+    } else if constexpr (NW == 2) {
+      l2c_tc::tmem_ld4(ta + 64 * e, *reinterpret_cast<uint32_t(*)[4]>(r[e]));
+    } else {
+      l2c_tc::tmem_ld2(ta + 64 * e, *reinterpret_cast<uint32_t(*)[2]>(r[e]));
+    }
+  }
+  l2c_tc::tmem_ld_wait();
+#pragma unroll
+  for (int j = 0; j < 2 * NW; j++) {
+    const int n = N0 + j;
+    if (n >= NB && n < NB + M) {
+      const int a = __float2int_rn(__uint_as_float(r[0][j]));
+      const int b = __float2int_rn(__uint_as_float(r[1][j]));
+      long long &t = T[(n - NB) % M];
+      if constexpr (P == 0) {
+        t = (long long)((unsigned long long)((long long)b * (1 << 27)) +
+                        ((unsigned long long)((unsigned)a << 4) << 32));
+      } else if constexpr (P == 1) {
+        t += (long long)a * (1 << 18) + (long long)b * (1 << 9);
+      } else {
+        t += (long long)(a + (b >> 9));
+      }
+    }
+  }
+}
+
+// Pass P's read-out for the lane (half 0: outputs 0 .. 17, half 1: 18 .. 35)
+// from the buffer at tensor-memory address ta.
+template <int P>
+__device__ __forceinline__ void ftc_pass(uint32_t ta, int half, long long (&T)[M]) {
+  if (half == 0) {
+    ftc_pass_chunk<P, 4, 0, 0>(ta + 0, T);
+    ftc_pass_chunk<P, 4, 8, 0>(ta + 8, T);
+    ftc_pass_chunk<P, 1, 16, 0>(ta + 16, T);
+  } else {
+    ftc_pass_chunk<P, 4, 16, M>(ta + 16, T);
+    ftc_pass_chunk<P, 4, 24, M>(ta + 24, T);
+    ftc_pass_chunk<P, 2, 32, M>(ta + 32, T);
+  }
+}
+
+// The MMAs of pass P (diagonals 2P and 2P + 1, all 48 output rows) into the
+// buffer at tensor-memory column tbuf: diagonal 2P + e at tbuf + 64 e.
+template <int P>
+__device__ __forceinline__ void ftc_issue(uint32_t tbuf, const unsigned char *sA,
+                                          const unsigned char *sB) {
+  const uint32_t id = l2c_tc::idesc_f16_f32(128, 48);
+#pragma unroll 1
+  for (int ks = 0; ks < 3; ks++)
+#pragma unroll
+    for (int q = 1; q <= l2c_oz::SLICES; q++) {
+      const uint64_t bd = l2c_tc::smem_desc(l2c_tc::smem_u32(sB + ((q - 1) * 3 + ks) * 1536),
+                                            l2c_tc::CORE_LBO, l2c_tc::CORE_SBO);
+#pragma unroll
+      for (int p = 1; p + q <= l2c_oz::DMAX; p++) {
+        const int e = p + q - 2 - 2 * P;
+        if (e == 0 || e == 1)
+          l2c_tc::mma_f16(tbuf + 64 * e,
+                          l2c_tc::smem_desc(l2c_tc::smem_u32(sA + ((p - 1) * 3 + ks) * 4096),
+                                            l2c_tc::CORE_LBO, l2c_tc::CORE_SBO),
+                          bd, id, (ks > 0 || q > 1) ? 1u : 0u);
+      }
+    }
+}
+
+// Far-field blocks gb0 + blockIdx.x, columns 128 blockIdx.y ...  The tensor
+// memory is allocated once the CTA's operands are staged, after the grid
+// dependency wait (a CTA never holds it while waiting on another grid), and
+// two CTAs' allocations fit an SM's tensor memory.  Every mbarrier wait is bounded (about a second); when one runs out the CTA
+// waits (bounded) for its copy and products in flight, marks its vectors in
+// bad (their outputs become NaN) and frees its tensor memory.
+__global__ void __launch_bounds__(FTC_THREADS, 2)
+    k_mz_far_tc(const long long *__restrict__ w, const int *__restrict__ wE,
+                long long *__restrict__ c, int *__restrict__ cE, const unsigned *__restrict__ Pt,
+                const int *__restrict__ Pm, Geo g, long long gb0, int *__restrict__ bad) {
+  extern __shared__ __align__(16) unsigned char mz_smem[];
+  unsigned char *sA = mz_smem, *sB = sA + FTC_A_BYTES;
+  int *sM = reinterpret_cast<int *>(sB + FTC_B_BYTES);
+  // bars: [0] the matrix copy, [1] [2] the products of the two buffers,
+  // [3] everything issued (error path)
+  uint64_t *bars = reinterpret_cast<uint64_t *>(sM + 2 * OZ_META);
+  uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 4);
+  volatile int *s_err = reinterpret_cast<volatile int *>(slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long gb = gb0 + blockIdx.x;
+  const long long ncol = 2 * g.count, c0 = (long long)blockIdx.y * FTC_COLS;
+  if (tid == 0) {
+    for (int i = 0; i < 4; i++) l2c_tc::bar_init(&bars[i], 1);
+    *s_err = 0;
+    l2c_tc::bar_init_fence();
+  }
+  __syncthreads();
+  if (tid == 0) l2c_tc::bulk_load(sB, Pt + gb * FTC_B_WORDS, FTC_B_BYTES, &bars[0]);
+  for (int i = tid; i < 2 * OZ_META; i += FTC_THREADS) sM[i] = Pm[gb * 2 * OZ_META + i];
+  __syncthreads();
+  pdl_wait();
+  pdl_trigger();
+  {
+    // Staging as l2c_oz::stage_cols does it: two threads per column (lanes
+    // r and r + 16), thread h holding slot 2 gb + h's 18 moments in registers;
+    // then the six digit slices into the operand tile.
+    const int m = warp * 16 + (lane & 15), h = lane >> 4;
+    const long long col = c0 + m;
+    const bool ok = col < ncol;
+    long long v[M];
+    int e = 0;
+    if (ok) {
+      const longlong2 *src =
+          reinterpret_cast<const longlong2 *>(w + (col * g.slots + 2 * gb + h) * M);
+#pragma unroll
+      for (int i = 0; i < M / 2; i++) {
+        const longlong2 t = src[i];
+        v[2 * i] = t.x;
+        v[2 * i + 1] = t.y;
+      }
+      e = wE[col * g.slots + 2 * gb + h];
+    } else {
+#pragma unroll
+      for (int i = 0; i < M; i++) v[i] = 0;
+    }
+    const int ec = max(e, __shfl_xor_sync(0xffffffffu, e, 16));
+    unsigned long long mx = 0;
+#pragma unroll
+    for (int i = 0; i < M; i++) {
+      v[i] = l2c_oz::shift_s64(v[i], e - ec);
+      const unsigned long long a =
+          v[i] < 0 ? 0ull - (unsigned long long)v[i] : (unsigned long long)v[i];
+      mx = a > mx ? a : mx;
+    }
+    const unsigned long long mo = __shfl_xor_sync(0xffffffffu, mx, 16);
+    mx = mo > mx ? mo : mx;
+    const int B = 64 - __clzll((long long)mx);
+    const int sh = l2c_oz::FRAC - B;
+    l2c_oz::Ysplit ys[M];
+#pragma unroll
+    for (int i = 0; i < M; i++)
+      ys[i] = l2c_oz::ysplit((sh >= 0 ? v[i] << sh : v[i] >> -sh) + l2c_oz::RBAL);
+    if (ok) cE[col * g.slots + 2 * gb + h] = ec - l2c_oz::VBITS + B + sM[h * OZ_META + OZ_ROWS];
+    // K group 3 h + j (8 positions) of row m: k-step (3 h + j) / 2, half (3 h + j) % 2
+    unsigned char *row = sA + (m >> 3) * l2c_tc::CORE_SBO + (m & 7) * 16;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int grp = 3 * h + j;
+      unsigned char *dst = row + (grp >> 1) * 4096 + (grp & 1) * l2c_tc::CORE_LBO;
+#define L2C_FTC_SLICE(P)                                                         \
+  {                                                                              \
+    uint4 u;                                                                     \
+    if (j < 2) {                                                                 \
+      u.x = l2c_oz::dig2<P>(ys[8 * j], ys[8 * j + 1]);                           \
+      u.y = l2c_oz::dig2<P>(ys[8 * j + 2], ys[8 * j + 3]);                       \
+      u.z = l2c_oz::dig2<P>(ys[8 * j + 4], ys[8 * j + 5]);                       \
+      u.w = l2c_oz::dig2<P>(ys[8 * j + 6], ys[8 * j + 7]);                       \
+    } else {                                                                     \
+      u.x = l2c_oz::dig2<P>(ys[M - 2], ys[M - 1]);                               \
+      u.y = u.z = u.w = 0u;                                                      \
+    }                                                                            \
+    *reinterpret_cast<uint4 *>(dst + (P - 1) * 3 * 4096) = u;                    \
+  }
+      L2C_FTC_SLICE(1) L2C_FTC_SLICE(2) L2C_FTC_SLICE(3)
+      L2C_FTC_SLICE(4) L2C_FTC_SLICE(5) L2C_FTC_SLICE(6)
+#undef L2C_FTC_SLICE
+    }
+  }
+  l2c_tc::fence_async_smem();
+  __syncthreads();
+  if (warp == 0) l2c_tc::tmem_alloc(slot, FTC_TMEM_COLS);
+  l2c_tc::fence_before_sync();
+  __syncthreads();
+  l2c_tc::fence_after_sync();
+  const uint32_t tb = *slot;
+  // bars[1] / bars[2]: the products of buffer 0 (passes 0 and 2) / buffer 1 (pass 1)
+  bool issued = false;
+  if (tid == 0) {
+    if (!l2c_tc::bar_wait(&bars[0], 0)) {
+      *s_err = 1;
+    } else {
+      ftc_issue<0>(tb, sA, sB);
+      l2c_tc::mma_commit(&bars[1]);
+      ftc_issue<1>(tb + 128, sA, sB);
+      l2c_tc::mma_commit(&bars[2]);
+      issued = true;
+    }
+  }
+  __syncthreads();
+  // Reading out: warp w reads tensor-memory lanes 32 (w % 4) .. + 31 (columns
+  // m of the CTA); warps 0 .. 3 the first slot's rows 0 .. 17, warps 4 .. 7
+  // the second slot's, 18 .. 35.
+  const int q4 = warp & 3, half = warp >> 2;
+  const long long col = c0 + 32 * q4 + lane;
+  const uint32_t ta = tb + ((uint32_t)(32 * q4) << 16);
+  long long T[M];
+  bool ok = *s_err == 0;
+  ok = __all_sync(0xffffffffu, ok && l2c_tc::bar_wait(&bars[1], 0));
+  if (ok) {
+    l2c_tc::fence_after_sync();
+    ftc_pass<0>(ta, half, T);
+  } else {
+    *s_err = 1;
+  }
+  l2c_tc::fence_before_sync();
+  __syncthreads();
+  ok = ok && *s_err == 0;
+  if (tid == 0 && ok) {
+    l2c_tc::fence_after_sync();
+    ftc_issue<2>(tb, sA, sB);
+    l2c_tc::mma_commit(&bars[1]);
+  }
+  ok = __all_sync(0xffffffffu, ok && l2c_tc::bar_wait(&bars[2], 0));
+  if (ok) {
+    l2c_tc::fence_after_sync();
+    ftc_pass<1>(ta + 128, half, T);
+  }
+  ok = __all_sync(0xffffffffu, ok && l2c_tc::bar_wait(&bars[1], 1));
+  if (ok) {
+    l2c_tc::fence_after_sync();
+    ftc_pass<2>(ta, half, T);
+    if (col < ncol) {
+      const int *meta = sM + half * OZ_META;
+      long long *out = c + (col * g.slots + 2 * gb + half) * M;
+#pragma unroll
+      for (int i = 0; i < M; i += 2)
+        *reinterpret_cast<longlong2 *>(out + i) = make_longlong2(
+            l2c_oz::shift_s64(T[i], meta[i]), l2c_oz::shift_s64(T[i + 1], meta[i + 1]));
+    }
+  } else {
+    *s_err = 1;
+  }
+  l2c_tc::fence_before_sync();
+  __syncthreads();
+  if (*s_err != 0) {
+    if (tid == 0) {
+      l2c_tc::bar_wait(&bars[0], 0);
+      if (issued) {
+        l2c_tc::mma_commit(&bars[3]);
+        l2c_tc::bar_wait(&bars[3], 0);
+      }
+    }
+    if (tid < FTC_COLS && c0 + tid < ncol) bad[(c0 + tid) >> 1] = 1;
+  }
+  if (warp == 0) {
+    __syncwarp();
+    l2c_tc::fence_after_sync();
+    l2c_tc::tmem_dealloc(tb, FTC_TMEM_COLS);
+  }
+}
+
 // Leaf down (step 5) + final scaling: tile = 16 consecutive leaf targets of one
 // vector, both parities; P_sg = T_sg (s x 18) in passes of 16 output rows
 // (two n-tiles, KC = 3).  For tile row r, pass ps and parity sg a lane quad
@@ -2568,7 +2882,10 @@ struct TuneCfg {
   //   bthin tiled band at s = 16: the thin variant (one vector per lane, at
   //         most 64 registers, half the shared memory), which leaves room for
   //         more CTAs of the kernels beside it (-1: the plan's rule)
-  int mtop = -2, mtopg = 0, tl0 = -1, bseg = 0, fsplit = -1, bthin = -1;
+  //   fartc mixed batches: the far-field products on the fifth-generation
+  //         tensor cores (k_mz_far_tc, accumulators in tensor memory) instead
+  //         of mma.sync (k_mz_far); the same bits (-1: the plan's rule)
+  int mtop = -2, mtopg = 0, tl0 = -1, bseg = 0, fsplit = -1, bthin = -1, fartc = -1;
 };
 // Two configurations are the same when every choice is (TuneCfg holds only
 // ints, so its bytes are its fields).
@@ -2608,6 +2925,7 @@ struct l2c_gpu_plan {
   cudaEvent_t ev_ff[FAR_SPLIT_MAX] = {}, ev_fj[FAR_SPLIT_MAX] = {};
   int far_split = -1;  // TuneCfg::fsplit
   int band_thin = -1;  // TuneCfg::bthin
+  int far_tc = -1;     // TuneCfg::fartc
   double *Wnear[2] = {nullptr, nullptr};  // precomputed band weights (optional)
   // dense band weights of the full blocks for k_band_tile (built on first use)
   double *Wtile[2] = {nullptr, nullptr};
@@ -2638,6 +2956,7 @@ struct l2c_gpu_plan {
   int oz_nbuf = 1;
   bool zero_copy = true;  // page-locked host buffers used in place (L2C_ZERO_COPY=0: staged)
   unsigned *oz_far[2] = {nullptr, nullptr};
+  unsigned *oz_far_tc[2] = {nullptr, nullptr};  // the same words in k_mz_far_tc's layout
   int *oz_farm[2] = {nullptr, nullptr};
   // column exponents of w and c (mixed form: w, c hold column-format integers)
   int *wE = nullptr, *cE = nullptr;
@@ -3174,6 +3493,10 @@ int mz_top_level(const l2c_gpu_plan *p) {
   return lt;
 }
 
+// Whether a mixed batch's far field runs on the fifth-generation tensor cores
+// (TuneCfg::fartc; the plan's rule: mma.sync).
+bool far_tc_on(const l2c_gpu_plan *p) { return p->far_tc == 1; }
+
 // The mixed form's far-field split (TuneCfg::fsplit): the far-field blocks
 // of levels L - n .. L - 1 run on the plan's third stream, level by level as
 // the upward sweep writes their moments, beside the coarser levels' transfer
@@ -3228,6 +3551,14 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
   const bool tc = g.count >= 4 && p->oz_far[dir] != nullptr;
   // far-field blocks gb0 .. gb1 - 1 (tensor-core form)
   auto far_launch = [&](long long gb0, long long gb1, cudaStream_t s, LaunchOpt o) {
+    if (gb1 <= gb0) return;
+    if (far_tc_on(p)) {
+      const dim3 grid((unsigned)(gb1 - gb0), (unsigned)((2 * g.count + FTC_COLS - 1) / FTC_COLS));
+      launch_k(o, k_mz_far_tc, grid, FTC_THREADS, ftc_smem(), s, (const long long *)w,
+               (const int *)p->wE, c, p->cE, (const unsigned *)p->oz_far_tc[dir],
+               (const int *)p->oz_farm[dir], g, gb0, p->bad);
+      return;
+    }
     const dim3 grid((unsigned)(gb1 - gb0),
                     (unsigned)((2 * g.count + OZ_FAR_COLS - 1) / OZ_FAR_COLS));
     launch_k(o, p->oz_nbuf == 1 ? k_mz_far<1> : k_mz_far<2>, grid, 32 * MXW,
@@ -3353,6 +3684,23 @@ bool ensure_mixed_far(l2c_gpu_plan *p, size_t dir) {
   }
   k_oz_pack_far<<<blocks_for((long long)(nb * 2), 128), 128, 0, p->stream>>>(
       p->A[dir], (long long)nb, p->oz_far[dir], p->oz_farm[dir]);
+  return cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(p->stream) == cudaSuccess;
+}
+
+// The far-field fragments in k_mz_far_tc's layout, built on the first call
+// that uses that kernel (after ensure_mixed_far).
+bool ensure_mixed_far_tc(l2c_gpu_plan *p, size_t dir) {
+  if (p->oz_far_tc[dir]) return true;
+  const long long nb = (long long)p->Nb;
+  if (cudaMalloc(&p->oz_far_tc[dir], (size_t)nb * FTC_B_WORDS * sizeof(unsigned)) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    p->oz_far_tc[dir] = nullptr;
+    set_err("cudaMalloc of the tensor-memory far-field fragments failed");
+    return false;
+  }
+  k_oz_pack_far_tc<<<blocks_for(nb * FTC_B_WORDS, 256), 256, 0, p->stream>>>(
+      p->oz_far[dir], nb, p->oz_far_tc[dir]);
   return cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(p->stream) == cudaSuccess;
 }
 
@@ -3507,6 +3855,7 @@ void cfg_apply(l2c_gpu_plan *p, const TuneCfg &c) {
   p->band_bseg = c.bseg;
   p->far_split = c.fsplit;
   p->band_thin = c.bthin;
+  p->far_tc = c.fartc;
   p->oz_ld_ctas = p->oz_ld_ctas_nb[c.nbuf == 2 ? 2 : 1];
   p->cfg_cur = c;
 }
@@ -3584,6 +3933,8 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   }
   if (!ensure_scratch(p, count)) return 0;
   if (p->mixed && p->L > 0 && count >= 4 && !ensure_mixed_far(p, dir)) return 0;
+  if (p->mixed && p->L > 0 && count >= 4 && far_tc_on(p) && !ensure_mixed_far_tc(p, dir))
+    return 0;
   const unsigned mode = (near_only ? 1u : 0u) | (input_ready ? 2u : 0u) | (in_host ? 4u : 0u);
   if (p->profiling || !p->use_graphs) {
     return launch_all(p, in, out, dir, count, dist, stride, near_only, input_ready, in_host);
@@ -3712,17 +4063,17 @@ TuneCfg resolved_cfg(l2c_gpu_plan *p, size_t count) {
 void cfg_text(const TuneCfg &c, char *buf, size_t len) {
   snprintf(buf, len, "overlap=%d band_fork=%d pdl=%d prio=%d near_threads=%d near_vb=%d "
            "near_pair=%d near_ctas=%d nbuf=%d near_table=%d mz_top=%d mz_top_g=%d tree_l0=%d "
-           "band_bseg=%d far_split=%d band_thin=%d", c.overlap, c.fork, c.pdl, c.prio,
+           "band_bseg=%d far_split=%d band_thin=%d far_tc=%d", c.overlap, c.fork, c.pdl, c.prio,
            c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, c.wtab, c.mtop, c.mtopg, c.tl0, c.bseg,
-           c.fsplit, c.bthin);
+           c.fsplit, c.bthin, c.fartc);
 }
 
 // Cache file: one line per tuned shape, fields separated by '|':
-// l2c-tune-5|device|SMs|N|maxs|form|precompute|dir|count|dist|stride|
+// l2c-tune-6|device|SMs|N|maxs|form|precompute|dir|count|dist|stride|
 //   overlap|pdl|prio|nthreads|nvb|npair|nctas|nbuf|wtab|fork|mtop|mtopg|tl0|bseg|
-//   fsplit|bthin|ms|ms_default
+//   fsplit|bthin|fartc|ms|ms_default
 // (form 0 modal, 1 nodal, 2 mixed).  Later lines win.
-constexpr int TUNE_FIELDS = 29;
+constexpr int TUNE_FIELDS = 30;
 
 struct TuneKey {
   char dev[256];
@@ -3754,11 +4105,12 @@ void cache_append(const l2c_gpu_plan *p, const TunedShape &t) {
   if (!f) return;  // an unwritable cache leaves the tuning in the plan only
   const TuneCfg &c = t.cfg;
   std::fprintf(f,
-               "l2c-tune-5|%s|%d|%zu|%zu|%d|%d|%zu|%zu|%zu|%zu|%d|%d|%d|%d|%d|%d|%d|%d|%d|%d|"
-               "%d|%d|%d|%d|%d|%d|%.6f|%.6f\n",
+               "l2c-tune-6|%s|%d|%zu|%zu|%d|%d|%zu|%zu|%zu|%zu|%d|%d|%d|%d|%d|%d|%d|%d|%d|%d|"
+               "%d|%d|%d|%d|%d|%d|%d|%.6f|%.6f\n",
                k.dev, k.sms, p->N, p->maxs, k.form, k.pre, t.dir, t.count, t.dist, t.stride,
                c.overlap, c.pdl, c.prio, c.nthreads, c.nvb, c.npair, c.nctas, c.nbuf, c.wtab,
-               c.fork, c.mtop, c.mtopg, c.tl0, c.bseg, c.fsplit, c.bthin, t.ms, t.ms_default);
+               c.fork, c.mtop, c.mtopg, c.tl0, c.bseg, c.fsplit, c.bthin, c.fartc, t.ms,
+               t.ms_default);
   std::fclose(f);
 }
 
@@ -3780,7 +4132,7 @@ void cache_load(l2c_gpu_plan *p) {
         *q = 0;
         fld[n++] = q + 1;
       }
-    if (n != TUNE_FIELDS || std::strcmp(fld[0], "l2c-tune-5") != 0) continue;
+    if (n != TUNE_FIELDS || std::strcmp(fld[0], "l2c-tune-6") != 0) continue;
     if (std::strcmp(fld[1], k.dev) != 0 || std::atoi(fld[2]) != k.sms) continue;
     auto u = [&](int i) { return (size_t)std::strtoull(fld[i], nullptr, 10); };
     auto iv = [&](int i) { return (int)std::strtol(fld[i], nullptr, 10); };
@@ -3806,8 +4158,9 @@ void cache_load(l2c_gpu_plan *p) {
     t.cfg.bseg = iv(24);
     t.cfg.fsplit = iv(25);
     t.cfg.bthin = iv(26);
-    t.ms = std::strtod(fld[27], nullptr);
-    t.ms_default = std::strtod(fld[28], nullptr);
+    t.cfg.fartc = iv(27);
+    t.ms = std::strtod(fld[28], nullptr);
+    t.ms_default = std::strtod(fld[29], nullptr);
     t.from_cache = true;
     // only values the launches accept
     const TuneCfg &c = t.cfg;
@@ -3817,7 +4170,7 @@ void cache_load(l2c_gpu_plan *p) {
         c.npair > 1 || c.nctas < 0 || c.nbuf < 1 || c.nbuf > 2 || c.wtab < -1 || c.wtab > 1 ||
         c.fork < 0 || c.fork > 3 || c.mtop < -2 || c.mtop > 5 || c.mtopg < 0 || c.mtopg > 7 ||
         c.tl0 < -1 || c.tl0 > 14 || c.bseg < 0 || c.bseg > 31 || c.fsplit < -1 ||
-        c.fsplit > FAR_SPLIT_MAX || c.bthin < -1 || c.bthin > 1)
+        c.fsplit > FAR_SPLIT_MAX || c.bthin < -1 || c.bthin > 1 || c.fartc < -1 || c.fartc > 1)
       continue;
     p->tuned.push_back(t);
   }
@@ -3908,6 +4261,11 @@ double tune_shape(l2c_gpu_plan *p, size_t dir, size_t count, size_t dist, size_t
       if (tile) knobs.push_back({&TuneCfg::bseg, {0, 1, 2, 4}});
       if (tile && p->s == 16) knobs.push_back({&TuneCfg::bthin, {0, 1}});
       if (p->mixed && count >= 4 && p->L >= 3) knobs.push_back({&TuneCfg::fsplit, {0, 1, 2, 3}});
+      // the tensor-memory far field, where its fragment copy (27 KB per block
+      // and direction) stays under 1 GB
+      if (p->mixed && count >= 4 && p->L >= 2 &&
+          p->Nb * (size_t)FTC_B_WORDS * sizeof(unsigned) <= ((size_t)1 << 30))
+        knobs.push_back({&TuneCfg::fartc, {0, 1}});
       for (int pass = 0; pass < 2 && best > 0.0; pass++) {
         bool kept = false;
         for (const Knob &kb : knobs)
@@ -4084,6 +4442,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_FAR_SPLIT"))
     p->base.fsplit = std::min(FAR_SPLIT_MAX, std::max(-1, std::atoi(env)));
   if (const char *env = std::getenv("L2C_BAND_THIN")) p->base.bthin = env[0] == '1' ? 1 : 0;
+  if (const char *env = std::getenv("L2C_FAR_TC")) p->base.fartc = env[0] == '1' ? 1 : 0;
   p->precompute = (flags & L2C_PLAN_PRECOMPUTE_NEAR) != 0;
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
@@ -4310,6 +4669,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
                                (int)oz_tree_down_smem(l2c_oz::SLICES, 1)));
       PCK(cudaFuncSetAttribute(k_mz_far<1>, smax, (int)oz_far_smem(1)));
       PCK(cudaFuncSetAttribute(k_mz_far<2>, smax, (int)oz_far_smem(2)));
+      PCK(cudaFuncSetAttribute(k_mz_far_tc, smax, (int)ftc_smem()));
 #define L2C_MZ_ATTR(kc)                                                                     \
   PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc, 1>, smax, (int)mz_leaf_up_smem(kc, 1)));        \
   PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc, 2>, smax, (int)mz_leaf_up_smem(kc, 2)));
@@ -4376,7 +4736,8 @@ void l2c_gpu_plan_destroy(l2c_gpu_plan *p) {
     if (b) cudaFree(b);
   void *obufs[] = {p->oz_lu,     p->oz_tu,     p->oz_td,      p->oz_ld,      p->oz_lum,
                    p->oz_tum,    p->oz_tdm,    p->oz_lde,     p->oz_far[0],  p->oz_far[1],
-                   p->oz_farm[0], p->oz_farm[1], p->wE,        p->cE,         p->bad};
+                   p->oz_farm[0], p->oz_farm[1], p->wE,        p->cE,         p->bad,
+                   p->oz_far_tc[0], p->oz_far_tc[1]};
   for (void *b : obufs)
     if (b) cudaFree(b);
   if (p->stream) cudaStreamDestroy(p->stream);

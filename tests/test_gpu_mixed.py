@@ -146,13 +146,48 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
                 {"L2C_FAR_SPLIT": "2", "L2C_MZ_TOP_LVL": "5", "L2C_BAND_FORK": "3"},
                 # the tiled band's thin variant (one vector per lane)
                 {"L2C_BAND_THIN": "1"}, {"L2C_BAND_THIN": "1", "L2C_NEAR_TABLE": "0"},
-                {"L2C_BAND_THIN": "1", "L2C_NEAR_CTAS": "608"}):
+                {"L2C_BAND_THIN": "1", "L2C_NEAR_CTAS": "608"},
+                # the far field on the fifth-generation tensor cores
+                {"L2C_FAR_TC": "1"}, {"L2C_FAR_TC": "1", "L2C_FAR_SPLIT": "0"},
+                {"L2C_FAR_TC": "1", "L2C_PDL": "7"}, {"L2C_FAR_TC": "1", "L2C_NO_GRAPHS": "1"}):
         with monkeypatch.context() as m:
             for k, v in env.items():
                 m.setenv(k, v)
             got = run()
         for d in (0, 1):
             assert np.array_equal(got[d], want[d]), (env, d)
+
+
+@pytest.mark.parametrize("N,maxs,count", [(2000, 16, 65), (4096, 32, 100), (1024, 64, 96),
+                                          (5000, 50, 8), (16384, 16, 256)])
+def test_far_tc_bitwise(lib, orc, monkeypatch, N, maxs, count):
+    """The far field on the fifth-generation tensor cores (L2C_FAR_TC=1:
+    tcgen05 products with the diagonal sums in tensor memory, k_mz_far_tc)
+    forms the same integers as the mma.sync far field, so every output has the
+    same bits; column chunks past 128 columns and a partly filled last chunk
+    (count 65, 100), leaf sizes 16 .. 64, and the 256 x 16384 batch.  Some
+    vectors are also checked against the oracle."""
+    x = np.ascontiguousarray(make_input(N * count, "gauss", 3 + count).reshape(count, N))
+
+    def run():
+        p = lib.Plan(N, maxs, mixed=True)
+        outs = []
+        for d in (0, 1):
+            out = np.zeros_like(x)
+            p.execute_batched(x, out, d, count, N, 1)
+            outs.append(out)
+        p.close()
+        return outs
+
+    want = run()
+    with monkeypatch.context() as m:
+        m.setenv("L2C_FAR_TC", "1")
+        got = run()
+    o = orc.Oracle(N, maxs, 2)
+    for d in (0, 1):
+        assert np.array_equal(got[d], want[d]), d
+        for v in (0, count // 2, count - 1):
+            assert relerr(got[d][v], o(x[v], d)[:N]) <= TOL, (d, v)
 
 
 @pytest.mark.parametrize("count", [65, 100])
