@@ -2264,14 +2264,15 @@ constexpr size_t oz_tree_down_smem(int QMAX, int NBUF) {
 // parity).  c0 = [A0 A1] [w0; w1] and c1 = A2 w1 as one product of the 40-row
 // matrix of k_oz_pack_far with the column [w0; w1] (K = 36), on the scale of
 // the whole column: the same integers as two products over the same staged
-// words, with the digits extracted once.
-constexpr int OZ_FAR_COLS = 16 * MXW * 2;  // columns per CTA
+// words, with the digits extracted once.  A CTA takes cols columns (a
+// multiple of 16 MXW: one or two 16-column tiles per warp, in turn).
+constexpr int OZ_FAR_COLS = 16 * MXW * 2;  // columns per CTA (at most)
 // Far-field blocks gb0 + blockIdx.x (a launch may cover one level's blocks).
 template <int NBUF>
 __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
     k_mz_far(const long long *__restrict__ w, const int *__restrict__ wE, long long *__restrict__ c,
              int *__restrict__ cE, const unsigned *__restrict__ Pf, const int *__restrict__ Pm,
-             Geo g, long long gb0) {
+             Geo g, long long gb0, int cols) {
   extern __shared__ __align__(16) unsigned char mz_smem[];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
   unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);
@@ -2285,8 +2286,8 @@ __global__ void __launch_bounds__(32 * MXW, oz_min_ctas(NBUF))
   __syncthreads();
   pdl_wait();
   pdl_trigger();
-  const long long ncol = 2 * g.count, c0 = (long long)blockIdx.y * OZ_FAR_COLS;
-  const long long ntile = (min(ncol - c0, (long long)OZ_FAR_COLS) + 15) / 16;
+  const long long ncol = 2 * g.count, c0 = (long long)blockIdx.y * cols;
+  const long long ntile = (min(ncol - c0, (long long)cols) + 15) / 16;
   auto issue = [&](long long tile, int buf) {
     long long *X = Xw + buf * 16 * OZ_TLD;
     int *Ex = sEx + buf * 32;
@@ -2926,6 +2927,7 @@ struct l2c_gpu_plan {
   int far_split = -1;  // TuneCfg::fsplit
   int band_thin = -1;  // TuneCfg::bthin
   int far_tc = -1;     // TuneCfg::fartc
+  int far_cols = 0;    // k_mz_far's columns per CTA (L2C_FAR_COLS=64|128; 0: by the launch's size)
   double *Wnear[2] = {nullptr, nullptr};  // precomputed band weights (optional)
   // dense band weights of the full blocks for k_band_tile (built on first use)
   double *Wtile[2] = {nullptr, nullptr};
@@ -3559,11 +3561,15 @@ bool launch_mixed_far(l2c_gpu_plan *p, const double *x, double *out, size_t dir,
                (const int *)p->oz_farm[dir], g, gb0, p->bad);
       return;
     }
-    const dim3 grid((unsigned)(gb1 - gb0),
-                    (unsigned)((2 * g.count + OZ_FAR_COLS - 1) / OZ_FAR_COLS));
+    // columns per CTA: one tile per warp when the launch would not fill
+    // the GPU once with two (its latency is then one tile's), else two
+    const long long nc2 = (2 * g.count + OZ_FAR_COLS - 1) / OZ_FAR_COLS;
+    const int cols = p->far_cols > 0 ? p->far_cols
+                     : (gb1 - gb0) * nc2 <= 4LL * p->sms ? OZ_FAR_COLS / 2 : OZ_FAR_COLS;
+    const dim3 grid((unsigned)(gb1 - gb0), (unsigned)((2 * g.count + cols - 1) / cols));
     launch_k(o, p->oz_nbuf == 1 ? k_mz_far<1> : k_mz_far<2>, grid, 32 * MXW,
              oz_far_smem(p->oz_nbuf), s, (const long long *)w, (const int *)p->wE, c, p->cE,
-             (const unsigned *)p->oz_far[dir], (const int *)p->oz_farm[dir], g, gb0);
+             (const unsigned *)p->oz_far[dir], (const int *)p->oz_farm[dir], g, gb0, cols);
   };
   // The finest nsplit levels' far field on stream3 (mz_far_split): level l
   // (split index L - 1 - l) forks once the chain has its moments and joins
@@ -4443,6 +4449,10 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
     p->base.fsplit = std::min(FAR_SPLIT_MAX, std::max(-1, std::atoi(env)));
   if (const char *env = std::getenv("L2C_BAND_THIN")) p->base.bthin = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_FAR_TC")) p->base.fartc = env[0] == '1' ? 1 : 0;
+  if (const char *env = std::getenv("L2C_FAR_COLS")) {
+    const int v = std::atoi(env);
+    p->far_cols = v == OZ_FAR_COLS / 2 || v == OZ_FAR_COLS ? v : 0;
+  }
   p->precompute = (flags & L2C_PLAN_PRECOMPUTE_NEAR) != 0;
   if (flags & L2C_PLAN_DIRECT_ONLY) {
     p->L = 0;
