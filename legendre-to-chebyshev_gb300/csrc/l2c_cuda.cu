@@ -2795,6 +2795,125 @@ size_t mz_leaf_down_smem(int npass, int nbuf, long long h) {
          (size_t)MXW * nbuf * 2 * 16 * OZ_CLD * 8 + (size_t)MXW * 16 * (h + 1) * 8;
 }
 
+// ---------------------------------------------------------------------------
+// Mixed form, batches at s = 16: the near-field band of the full blocks on the
+// tensor cores.  Block b and parity p: outputs j = b h + 2 i' + p (i' < s) from
+// the window x[v][b h + 2 m' + p] (m' < 2s) through W'[m'][i'] =
+// near_weight(m' - i', j) (zero where m' < i'; k_band_tile's table), i.e. the
+// product of P = W'^T (s x 2s) with a column per vector, exact in integers
+// (l2c_ozaki.cuh: K = 32 terms) and rounded once: y = out_in + P x.  A warp
+// takes 16 vectors of one block: their windows (2h = 64 doubles each, both
+// parities) are staged once, normalised per vector and parity (stage_fix), and
+// give both parities' products; the sums are staged back over the consumed
+// words and written a row of h outputs at a time.  The last (ragged) block
+// keeps the FP64 sums of k_near (k_mz_band_last).  Error: a few units of 2^-53
+// |W'|_row |x|_window per output, the order of the FP64 band's own rounding.
+// ---------------------------------------------------------------------------
+constexpr int MB_S = 16;                         // the leaf size of this form
+constexpr int MB_NT = 2, MB_KC = 4;              // s = 16 outputs, 2s = 32 terms
+constexpr int MB_WORDS = oz_words(MB_NT, MB_KC);  // one (block, parity) matrix
+constexpr int MB_XLD = 4 * MB_S + 1;             // a staged window of 2h = 64, padded
+
+// Plan time: the fragments F[(b 2 + p) MB_WORDS ..] and row exponents
+// Fe[(b 2 + p) 16 + i'] of P for the full blocks b < nL - 1.  One thread per
+// (block, parity, row).
+__global__ void k_oz_pack_band(const double *__restrict__ a, const double *__restrict__ an,
+                               const double *__restrict__ dn, Geo g, int c2l,
+                               unsigned *__restrict__ F, int *__restrict__ Fe) {
+  const long long n = (g.nL - 1) * 2 * MB_S;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const long long bp = idx / MB_S;
+  const int ip = (int)(idx - bp * MB_S);
+  const long long b = bp >> 1, p = bp & 1, j = b * g.h + 2 * ip + p;
+  oz_pack_row([&](int mp) { return mp >= ip ? near_weight(c2l, mp - ip, j, a, an, dn) : 0.0; },
+              true, ip, 2 * MB_S, MB_NT, MB_KC, F + bp * MB_WORDS, Fe + bp * MB_S);
+}
+
+constexpr size_t mz_band_smem() {
+  return (size_t)(2 * MB_WORDS + 2 * MB_S + MXW * 2 * 16) * 4 +
+         (size_t)MXW * 16 * MB_XLD * sizeof(double);
+}
+
+// CTA = (full block blockIdx.x, 64 vectors), a warp per 16 vectors.
+__global__ void __launch_bounds__(32 * MXW, 4)
+    k_mz_band(const double *__restrict__ x, const double *out, double *__restrict__ y,
+              const unsigned *__restrict__ F, const int *__restrict__ Fe, Geo g) {
+  extern __shared__ __align__(16) unsigned char mz_smem[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
+  unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);  // both parities' fragments
+  int *sE = reinterpret_cast<int *>(sP + 2 * MB_WORDS);   // their row exponents
+  int *Es = sE + 2 * MB_S + wid * 2 * 16;                 // [parity][16] column exponents
+  double *X = reinterpret_cast<double *>(sE + 2 * MB_S + MXW * 2 * 16) + wid * 16 * MB_XLD;
+  const long long b = blockIdx.x;
+  oz_load_frag(sP, F + b * 2 * MB_WORDS, 2 * MB_WORDS, sE, Fe + b * 2 * MB_S, 2 * MB_S);
+  __syncthreads();
+  pdl_wait();
+  pdl_trigger();
+  const long long v0 = ((long long)blockIdx.y * MXW + wid) * 16;
+  if (v0 >= g.count) return;
+  const int nv = (int)min(16LL, g.count - v0);
+  for (int e = lane; e < 16 * 4 * MB_S; e += 32) {
+    const int r = e / (4 * MB_S), m = e - r * (4 * MB_S);
+    const bool ok = r < nv;
+    l2c_oz::cp_async8(X + r * MB_XLD + m, ok ? x + (v0 + r) * g.N + b * g.h + m : x, ok ? 8 : 0);
+  }
+  l2c_oz::cp_commit();
+  l2c_oz::cp_wait0();
+  __syncwarp();
+  l2c_oz::stage_fix<2 * MB_S>(X, MB_XLD, 2, 2 * MB_S, Es);
+  l2c_oz::stage_fix<2 * MB_S>(X + 1, MB_XLD, 2, 2 * MB_S, Es + 16);
+  const long long *Ys = reinterpret_cast<const long long *>(X);
+#pragma unroll 1
+  for (int p = 0; p < 2; p++) {
+    float acc[l2c_oz::NDIAG][MB_NT][4];
+    l2c_oz::mma_tile<MB_NT, MB_KC>(sP + p * MB_WORDS, Ys + p, MB_XLD, 2, acc);
+    double val[MB_NT][4];
+#pragma unroll
+    for (int nt = 0; nt < MB_NT; nt++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const int ip = 8 * nt + 2 * t4 + (e & 1), r = gq + 8 * (e >> 1);
+        val[nt][e] = l2c_oz::to_double(l2c_oz::combine<MB_NT>(acc, nt, e),
+                                       sE[p * MB_S + ip] + Es[p * 16 + r] - 52);
+      }
+    // the sums over this parity's consumed words (the other parity's are the
+    // odd / even places, not written here)
+    __syncwarp();
+#pragma unroll
+    for (int nt = 0; nt < MB_NT; nt++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const int ip = 8 * nt + 2 * t4 + (e & 1), r = gq + 8 * (e >> 1);
+        X[r * MB_XLD + 2 * ip + p] = val[nt][e];
+      }
+  }
+  __syncwarp();
+  // y = out_in + band, a row of h outputs per vector
+  for (int e = lane; e < 16 * 2 * MB_S; e += 32) {
+    const int r = e / (2 * MB_S), i = e - r * (2 * MB_S);
+    if (r < nv) {
+      const long long v = v0 + r, j = b * g.h + i;
+      y[v * g.N + j] = out[v * g.dist + j * g.stride] + X[r * MB_XLD + i];
+    }
+  }
+}
+
+// The outputs of the last (ragged) block, j >= (nL - 1) h: k_near's FP64 sums.
+__global__ void k_mz_band_last(const double *__restrict__ x, const double *out,
+                               double *__restrict__ y, const double *__restrict__ a,
+                               const double *__restrict__ an, const double *__restrict__ dn,
+                               Geo g, int c2l) {
+  const long long jlast = (g.nL - 1) * g.h, ntail = g.N - jlast;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (ntail <= 0 || idx >= g.count * ntail) return;
+  const long long v = idx / ntail, j = jlast + (idx - v * ntail);
+  double res[1];
+  near_sums<1>(x + v * g.N + j, g.N, a, an, dn, nullptr, g, c2l, j, res);
+  y[v * g.N + j] = out[v * g.dist + j * g.stride] + res[0];
+}
+
+
 // Column format <-> doubles, in place, one thread per 18-coefficient column
 // (for the FP64 far-field kernel of single vectors).
 __global__ void k_oz_cols_to_double(long long *V, const int *__restrict__ E, long long ncol) {
@@ -2959,6 +3078,11 @@ struct l2c_gpu_plan {
   bool zero_copy = true;  // page-locked host buffers used in place (L2C_ZERO_COPY=0: staged)
   unsigned *oz_far[2] = {nullptr, nullptr};
   unsigned *oz_far_tc[2] = {nullptr, nullptr};  // the same words in k_mz_far_tc's layout
+  // the band of the full blocks on the tensor cores (k_mz_band): fragments and
+  // row exponents per direction, built on the first call that uses them
+  unsigned *mz_band[2] = {nullptr, nullptr};
+  int *mz_bande[2] = {nullptr, nullptr};
+  bool mz_band_on = true;  // L2C_MZ_BAND=0: the FP64 tiled band
   int *oz_farm[2] = {nullptr, nullptr};
   // column exponents of w and c (mixed form: w, c hold column-format integers)
   int *wE = nullptr, *cE = nullptr;
@@ -3338,6 +3462,13 @@ bool use_band_tile(const l2c_gpu_plan *p, size_t count) {
                                                        (long long)count);
 }
 
+// Whether a mixed batch's band runs on the tensor cores (k_mz_band): the
+// batches whose FP64 band would be dense tiles, at s = 16.
+bool use_mz_band(const l2c_gpu_plan *p, size_t count) {
+  return p->mixed && p->mz_band_on && p->s == (size_t)MB_S && p->nL >= 2 &&
+         use_band_tile(p, count);
+}
+
 // Whether this call's band runs as k_near_rows (full blocks and, one output
 // per thread, the last block): single vectors with enough blocks (any with
 // L2C_NEAR_ROWS=1, none with 0), unless the paired kernel is forced
@@ -3693,6 +3824,23 @@ bool ensure_mixed_far(l2c_gpu_plan *p, size_t dir) {
   return cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(p->stream) == cudaSuccess;
 }
 
+// The band fragments of one direction for k_mz_band, built on the first call
+// that uses them (outside any capture).
+bool ensure_mz_band(l2c_gpu_plan *p, size_t dir) {
+  if (p->mz_band[dir]) return true;
+  const long long nbp = ((long long)p->nL - 1) * 2;
+  if (cudaMalloc(&p->mz_band[dir], (size_t)nbp * MB_WORDS * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&p->mz_bande[dir], (size_t)nbp * MB_S * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    set_err("cudaMalloc of the tensor-core band fragments failed");
+    return false;
+  }
+  Geo g = make_geo(p, 1, p->N, 1);
+  k_oz_pack_band<<<blocks_for(nbp * MB_S, 128), 128, 0, p->stream>>>(
+      p->a, p->an, p->dn, g, (int)dir, p->mz_band[dir], p->mz_bande[dir]);
+  return cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(p->stream) == cudaSuccess;
+}
+
 // The far-field fragments in k_mz_far_tc's layout, built on the first call
 // that uses that kernel (after ensure_mixed_far).
 bool ensure_mixed_far_tc(l2c_gpu_plan *p, size_t dir) {
@@ -3781,7 +3929,18 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     if (ov && (cudaEventRecord(p->ev_fork, st) != cudaSuccess ||
                cudaStreamWaitEvent(st2, p->ev_fork, 0) != cudaSuccess))
       return false;
-    if (use_band_tile(p, count)) {
+    if (use_mz_band(p, count)) {
+      // the full blocks on the tensor cores, the last block in FP64
+      PhaseScope ps(p, L2C_PHASE_NEAR, 2, stn);
+      launch_k((sc.pdl & 2) && !ov, k_mz_band,
+               dim3((unsigned)(g.nL - 1), (unsigned)((g.count + 16 * MXW - 1) / (16 * MXW))),
+               32 * MXW, mz_band_smem(), stn, x, (const double *)out, p->y,
+               (const unsigned *)p->mz_band[dir], (const int *)p->mz_bande[dir], g);
+      const long long ntail = g.N - (g.nL - 1) * g.h;
+      k_mz_band_last<<<blocks_for(g.count * ntail, 256), 256, 0, stn>>>(
+          x, out, p->y, p->a, p->an, p->dn, g, c2l);
+      if (cudaGetLastError() != cudaSuccess) return false;
+    } else if (use_band_tile(p, count)) {
       PhaseScope ps(p, L2C_PHASE_NEAR, 1, stn);
       if (launch_band_tile(p, x, out, p->y, p->use_w ? p->Wtile[dir] : nullptr, g, c2l, stn,
                            ov ? p->near_ctas : 0, (sc.pdl & 2) && !ov) != cudaSuccess)
@@ -3941,6 +4100,7 @@ size_t run_device(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
   if (p->mixed && p->L > 0 && count >= 4 && !ensure_mixed_far(p, dir)) return 0;
   if (p->mixed && p->L > 0 && count >= 4 && far_tc_on(p) && !ensure_mixed_far_tc(p, dir))
     return 0;
+  if (use_mz_band(p, count) && !ensure_mz_band(p, dir)) return 0;
   const unsigned mode = (near_only ? 1u : 0u) | (input_ready ? 2u : 0u) | (in_host ? 4u : 0u);
   if (p->profiling || !p->use_graphs) {
     return launch_all(p, in, out, dir, count, dist, stride, near_only, input_ready, in_host);
@@ -4449,6 +4609,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
     p->base.fsplit = std::min(FAR_SPLIT_MAX, std::max(-1, std::atoi(env)));
   if (const char *env = std::getenv("L2C_BAND_THIN")) p->base.bthin = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_FAR_TC")) p->base.fartc = env[0] == '1' ? 1 : 0;
+  if (const char *env = std::getenv("L2C_MZ_BAND")) p->mz_band_on = env[0] != '0';
   if (const char *env = std::getenv("L2C_FAR_COLS")) {
     const int v = std::atoi(env);
     p->far_cols = v == OZ_FAR_COLS / 2 || v == OZ_FAR_COLS ? v : 0;
@@ -4680,6 +4841,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
       PCK(cudaFuncSetAttribute(k_mz_far<1>, smax, (int)oz_far_smem(1)));
       PCK(cudaFuncSetAttribute(k_mz_far<2>, smax, (int)oz_far_smem(2)));
       PCK(cudaFuncSetAttribute(k_mz_far_tc, smax, (int)ftc_smem()));
+      PCK(cudaFuncSetAttribute(k_mz_band, smax, (int)mz_band_smem()));
 #define L2C_MZ_ATTR(kc)                                                                     \
   PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc, 1>, smax, (int)mz_leaf_up_smem(kc, 1)));        \
   PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc, 2>, smax, (int)mz_leaf_up_smem(kc, 2)));
@@ -4747,7 +4909,8 @@ void l2c_gpu_plan_destroy(l2c_gpu_plan *p) {
   void *obufs[] = {p->oz_lu,     p->oz_tu,     p->oz_td,      p->oz_ld,      p->oz_lum,
                    p->oz_tum,    p->oz_tdm,    p->oz_lde,     p->oz_far[0],  p->oz_far[1],
                    p->oz_farm[0], p->oz_farm[1], p->wE,        p->cE,         p->bad,
-                   p->oz_far_tc[0], p->oz_far_tc[1]};
+                   p->oz_far_tc[0], p->oz_far_tc[1], p->mz_band[0], p->mz_band[1],
+                   p->mz_bande[0], p->mz_bande[1]};
   for (void *b : obufs)
     if (b) cudaFree(b);
   if (p->stream) cudaStreamDestroy(p->stream);
