@@ -30,8 +30,10 @@ typedef struct l2c_gpu_plan l2c_gpu_plan;
 #define L2C_PLAN_MIXED 4u /* mixed form: leaf, transfer and far-field products on
                                 FP16 tensor cores, FP64-accurate (operands split into
                                 exact 9-bit digit slices, products recombined exactly
-                                in integers; no FP64 instructions); near-field band,
-                                accumulation and scaling in FP64.  Leaf sizes s <= 64. */
+                                in integers; no FP64 instructions); for batches at
+                                s = 16 also the full blocks of the near-field band;
+                                the rest of the band, accumulation and scaling in FP64.
+                                Leaf sizes s <= 64. */
 
 #define L2C_PLAN_NODAL 8u /* nodal (Lagrange) form, create_fmm's lagrange = 1
                                 (leg2cheb.c:997-1031, 1076-1100): leaf matrices of
