@@ -2850,52 +2850,56 @@ __global__ void __launch_bounds__(32 * MXW, 4)
   __syncthreads();
   pdl_wait();
   pdl_trigger();
-  const long long v0 = ((long long)blockIdx.y * MXW + wid) * 16;
-  if (v0 >= g.count) return;
-  const int nv = (int)min(16LL, g.count - v0);
-  for (int e = lane; e < 16 * 4 * MB_S; e += 32) {
-    const int r = e / (4 * MB_S), m = e - r * (4 * MB_S);
-    const bool ok = r < nv;
-    l2c_oz::cp_async8(X + r * MB_XLD + m, ok ? x + (v0 + r) * g.N + b * g.h + m : x, ok ? 8 : 0);
-  }
-  l2c_oz::cp_commit();
-  l2c_oz::cp_wait0();
-  __syncwarp();
-  l2c_oz::stage_fix<2 * MB_S>(X, MB_XLD, 2, 2 * MB_S, Es);
-  l2c_oz::stage_fix<2 * MB_S>(X + 1, MB_XLD, 2, 2 * MB_S, Es + 16);
-  const long long *Ys = reinterpret_cast<const long long *>(X);
-#pragma unroll 1
-  for (int p = 0; p < 2; p++) {
-    float acc[l2c_oz::NDIAG][MB_NT][4];
-    l2c_oz::mma_tile<MB_NT, MB_KC>(sP + p * MB_WORDS, Ys + p, MB_XLD, 2, acc);
-    double val[MB_NT][4];
-#pragma unroll
-    for (int nt = 0; nt < MB_NT; nt++)
-#pragma unroll
-      for (int e = 0; e < 4; e++) {
-        const int ip = 8 * nt + 2 * t4 + (e & 1), r = gq + 8 * (e >> 1);
-        val[nt][e] = l2c_oz::to_double(l2c_oz::combine<MB_NT>(acc, nt, e),
-                                       sE[p * MB_S + ip] + Es[p * 16 + r] - 52);
-      }
-    // the sums over this parity's consumed words (the other parity's are the
-    // odd / even places, not written here)
-    __syncwarp();
-#pragma unroll
-    for (int nt = 0; nt < MB_NT; nt++)
-#pragma unroll
-      for (int e = 0; e < 4; e++) {
-        const int ip = 8 * nt + 2 * t4 + (e & 1), r = gq + 8 * (e >> 1);
-        X[r * MB_XLD + 2 * ip + p] = val[nt][e];
-      }
-  }
-  __syncwarp();
-  // y = out_in + band, a row of h outputs per vector
-  for (int e = lane; e < 16 * 2 * MB_S; e += 32) {
-    const int r = e / (2 * MB_S), i = e - r * (2 * MB_S);
-    if (r < nv) {
-      const long long v = v0 + r, j = b * g.h + i;
-      y[v * g.N + j] = out[v * g.dist + j * g.stride] + X[r * MB_XLD + i];
+  // tiles of 16 vectors blockIdx.y MXW + wid, + gridDim.y MXW, ...
+  for (long long tile = (long long)blockIdx.y * MXW + wid; tile * 16 < g.count;
+       tile += (long long)gridDim.y * MXW) {
+    const long long v0 = tile * 16;
+    const int nv = (int)min(16LL, g.count - v0);
+    for (int e = lane; e < 16 * 4 * MB_S; e += 32) {
+      const int r = e / (4 * MB_S), m = e - r * (4 * MB_S);
+      const bool ok = r < nv;
+      l2c_oz::cp_async8(X + r * MB_XLD + m, ok ? x + (v0 + r) * g.N + b * g.h + m : x, ok ? 8 : 0);
     }
+    l2c_oz::cp_commit();
+    l2c_oz::cp_wait0();
+    __syncwarp();
+    l2c_oz::stage_fix<2 * MB_S>(X, MB_XLD, 2, 2 * MB_S, Es);
+    l2c_oz::stage_fix<2 * MB_S>(X + 1, MB_XLD, 2, 2 * MB_S, Es + 16);
+    const long long *Ys = reinterpret_cast<const long long *>(X);
+#pragma unroll 1
+    for (int p = 0; p < 2; p++) {
+      float acc[l2c_oz::NDIAG][MB_NT][4];
+      l2c_oz::mma_tile<MB_NT, MB_KC>(sP + p * MB_WORDS, Ys + p, MB_XLD, 2, acc);
+      double val[MB_NT][4];
+#pragma unroll
+      for (int nt = 0; nt < MB_NT; nt++)
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const int ip = 8 * nt + 2 * t4 + (e & 1), r = gq + 8 * (e >> 1);
+          val[nt][e] = l2c_oz::to_double(l2c_oz::combine<MB_NT>(acc, nt, e),
+                                         sE[p * MB_S + ip] + Es[p * 16 + r] - 52);
+        }
+      // the sums over this parity's consumed words (the other parity's are the
+      // odd / even places, not written here)
+      __syncwarp();
+#pragma unroll
+      for (int nt = 0; nt < MB_NT; nt++)
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const int ip = 8 * nt + 2 * t4 + (e & 1), r = gq + 8 * (e >> 1);
+          X[r * MB_XLD + 2 * ip + p] = val[nt][e];
+        }
+    }
+    __syncwarp();
+    // y = out_in + band, a row of h outputs per vector
+    for (int e = lane; e < 16 * 2 * MB_S; e += 32) {
+      const int r = e / (2 * MB_S), i = e - r * (2 * MB_S);
+      if (r < nv) {
+        const long long v = v0 + r, j = b * g.h + i;
+        y[v * g.N + j] = out[v * g.dist + j * g.stride] + X[r * MB_XLD + i];
+      }
+    }
+    __syncwarp();  // the next tile's copies reuse X
   }
 }
 
@@ -3083,6 +3087,7 @@ struct l2c_gpu_plan {
   unsigned *mz_band[2] = {nullptr, nullptr};
   int *mz_bande[2] = {nullptr, nullptr};
   bool mz_band_on = true;  // L2C_MZ_BAND=0: the FP64 tiled band
+  int mz_band_tpw = 1;     // k_mz_band's 16-vector tiles per warp (L2C_MZ_BAND_TPW)
   int *oz_farm[2] = {nullptr, nullptr};
   // column exponents of w and c (mixed form: w, c hold column-format integers)
   int *wE = nullptr, *cE = nullptr;
@@ -3933,7 +3938,8 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
       // the full blocks on the tensor cores, the last block in FP64
       PhaseScope ps(p, L2C_PHASE_NEAR, 2, stn);
       launch_k((sc.pdl & 2) && !ov, k_mz_band,
-               dim3((unsigned)(g.nL - 1), (unsigned)((g.count + 16 * MXW - 1) / (16 * MXW))),
+               dim3((unsigned)(g.nL - 1),
+                    (unsigned)((g.count + 16 * MXW * p->mz_band_tpw - 1) / (16 * MXW * p->mz_band_tpw))),
                32 * MXW, mz_band_smem(), stn, x, (const double *)out, p->y,
                (const unsigned *)p->mz_band[dir], (const int *)p->mz_bande[dir], g);
       const long long ntail = g.N - (g.nL - 1) * g.h;
@@ -4610,6 +4616,8 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
   if (const char *env = std::getenv("L2C_BAND_THIN")) p->base.bthin = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_FAR_TC")) p->base.fartc = env[0] == '1' ? 1 : 0;
   if (const char *env = std::getenv("L2C_MZ_BAND")) p->mz_band_on = env[0] != '0';
+  if (const char *env = std::getenv("L2C_MZ_BAND_TPW"))
+    p->mz_band_tpw = std::min(16, std::max(1, std::atoi(env)));
   if (const char *env = std::getenv("L2C_FAR_COLS")) {
     const int v = std::atoi(env);
     p->far_cols = v == OZ_FAR_COLS / 2 || v == OZ_FAR_COLS ? v : 0;

@@ -152,7 +152,9 @@ def test_launch_options_bitwise(lib, monkeypatch, mixed, count):
                 {"L2C_FAR_TC": "1", "L2C_PDL": "7"}, {"L2C_FAR_TC": "1", "L2C_NO_GRAPHS": "1"},
                 # the far field's columns per CTA (one or two tiles per warp)
                 {"L2C_FAR_COLS": "64"}, {"L2C_FAR_COLS": "128"},
-                {"L2C_FAR_COLS": "64", "L2C_FAR_SPLIT": "0"}):
+                {"L2C_FAR_COLS": "64", "L2C_FAR_SPLIT": "0"},
+                # the tensor-core band's 16-vector tiles per warp
+                {"L2C_MZ_BAND_TPW": "2"}, {"L2C_MZ_BAND_TPW": "4"}):
         with monkeypatch.context() as m:
             for k, v in env.items():
                 m.setenv(k, v)
