@@ -570,18 +570,22 @@ def load_library():
 
 
 MIXED_FORM = ("f64 (mixed: far-field, leaf and transfer products on FP16 tensor cores from "
-              "exact 9-bit digit slices with exact integer recombination; band, Lambda and "
-              "output accumulation in FP64)")
+              "exact 9-bit digit slices with exact integer recombination; Lambda and output "
+              "accumulation in FP64; near-field band in FP64 (plan 'mixed') or, for the full "
+              "blocks of a batch, on the same exact tensor-core scheme (plan 'mixed_tc_band'))")
 
 
 def compare_mixed(l2c, workload, N, maxs_mixed, steps, warmup, autotune, dev, torch,
-                  only=None):
+                  only=None, maxs_tc=32):
     """Mixed form against plain FP64 on the same inputs (single vector N = 2^22
     or 256 vectors of N = 16384, iid N(0,1), seed 1; L2C and C2L of the same
-    input per step).  Plain plans at maxs 16, 32 and 64 (and the mixed plan's
-    own leaf bound) are each autotuned and timed; every output is compared with
-    the oracle port.  Returns the record: per plan ms, coef/s, launches and
-    phases; errors per direction; the speed-up against the fastest plain plan."""
+    input per step).  Plain plans at maxs 16, 32 and 64 (and the mixed plans'
+    leaf bounds) are each autotuned and timed; every output is compared with
+    the oracle port.  Two mixed plans: 'mixed' (maxs_mixed) keeps the near-field
+    band in FP64 (L2C_MZ_BAND=0), 'mixed_tc_band' (maxs_tc) runs a batch's full
+    band blocks on the tensor cores too.  Returns the record: per plan ms,
+    coef/s, launches and phases; errors per direction; the speed-ups of the
+    fastest mixed plan and of the FP64-band one against the fastest plain plan."""
     import ctypes
 
     wl = Workload(workload, N, maxs_mixed, 1)
@@ -649,14 +653,23 @@ def compare_mixed(l2c, workload, N, maxs_mixed, steps, warmup, autotune, dev, to
                 "d2h_bytes_per_step": 2 * nbytes, "ms_per_step": st * 1e3}
 
     results = {}
-    e2e_mixed = None
-    plain_bounds = sorted({16, 32, 64, maxs_mixed})
-    for name, maxs, mixed in ([(f"plain_maxs{m}", m, False) for m in plain_bounds]
-                              + [("mixed", maxs_mixed, True)]):
+    plain_bounds = sorted({16, 32, 64, maxs_mixed, maxs_tc})
+    for name, maxs, mixed, band in ([(f"plain_maxs{m}", m, False, None) for m in plain_bounds]
+                                    + [("mixed", maxs_mixed, True, "0"),
+                                       ("mixed_tc_band", maxs_tc, True, "1")]):
         if only and name not in only:
             continue
         t_plan0 = time.perf_counter()
-        plan = l2c.Plan(N, maxs, mixed=mixed)
+        saved = os.environ.get("L2C_MZ_BAND")
+        if band is not None:
+            os.environ["L2C_MZ_BAND"] = band  # read when the plan is created
+        try:
+            plan = l2c.Plan(N, maxs, mixed=mixed)
+        finally:
+            if saved is None:
+                os.environ.pop("L2C_MZ_BAND", None)
+            else:
+                os.environ["L2C_MZ_BAND"] = saved
         plan_ms = (time.perf_counter() - t_plan0) * 1e3
         tuned = autotune_plan(plan, ((0,), (1,)), count, N) if autotune else None
         ms, outs, launches, phases = time_plan(plan)
@@ -666,7 +679,7 @@ def compare_mixed(l2c, workload, N, maxs_mixed, steps, warmup, autotune, dev, to
                          "create_fmm_ms": round(plan_ms, 3),
                          "flops": plan.flops(0) + plan.flops(1), "outs": outs}
         if mixed:
-            e2e_mixed = time_e2e(plan)
+            results[name]["e2e"] = time_e2e(plan)
         plan.close()
     # accuracy against the oracle port (FP64) on the same inputs, every vector
     sys.path.insert(0, REPO)
@@ -688,17 +701,25 @@ def compare_mixed(l2c, workload, N, maxs_mixed, steps, warmup, autotune, dev, to
         o.close()
         errs[name] = {"l2c": e[0], "c2l": e[1]}
         del r["outs"]
-    if "mixed" not in results or not any(k.startswith("plain") for k in results):
-        return {"plans": results, "max_rel_err_vs_oracle": errs, "e2e_mixed": e2e_mixed}
-    mixed = results["mixed"]
+    mixed_names = [k for k in results if k.startswith("mixed")]
+    if not mixed_names or not any(k.startswith("plain") for k in results):
+        return {"plans": results, "max_rel_err_vs_oracle": errs,
+                "e2e_mixed": {k: results[k]["e2e"] for k in mixed_names}}
+    best_mixed = min((results[k]["ms_per_step"], k) for k in mixed_names)[1]
+    mixed = results[best_mixed]
+    e2e_mixed = mixed["e2e"]
     best_plain = min((results[k]["ms_per_step"], k) for k in results if k.startswith("plain"))
     return {
         "workload": (f"mixed vs plain FP64, {'single vector' if count == 1 else str(count) + ' vectors'} "
                      f"of N={N}, iid N(0,1), L2C and C2L of the same input per step"),
         "N": N, "vectors": count, "maxs_mixed": maxs_mixed, "steps": steps, "warmup": warmup,
+        "best_mixed": best_mixed,
         "ms_per_step_mixed": mixed["ms_per_step"], "value_mixed": mixed["value"],
         "ms_per_step_best_plain": best_plain[0], "best_plain": best_plain[1],
         "speedup_vs_best_plain": best_plain[0] / mixed["ms_per_step"],
+        # the mixed form as the benchmark's configuration describes it (band in FP64)
+        "speedup_vs_best_plain_fp64_band": (best_plain[0] / results["mixed"]["ms_per_step"]
+                                            if "mixed" in results else None),
         "speedup_vs_plain_maxs64": results["plain_maxs64"]["ms_per_step"] / mixed["ms_per_step"],
         "max_rel_err_vs_oracle": errs,
         "error_note": "relative max-norm per vector (max over the batch), per direction, "
@@ -721,24 +742,26 @@ def run_mixed(args):
     clocks.start()
     only = set(args.mixed_plans.split(",")) if args.mixed_plans else None
     rec = compare_mixed(l2c, args.workload, args.N, args.maxs_mixed, args.steps, args.warmup,
-                        args.autotune, dev, torch, only)
+                        args.autotune, dev, torch, only, args.maxs_mixed_tc)
     clk = clocks.stop()
     if "speedup_vs_best_plain" not in rec:  # a subset of the plans (profiling runs)
         print(json.dumps({"plans": rec["plans"], "errors": rec["max_rel_err_vs_oracle"],
                           "e2e_mixed": rec["e2e_mixed"], "clocks": clk}))
         return 0
-    mixed = rec["plans"]["mixed"]
+    mixed = rec["plans"][rec["best_mixed"]]
     line = {
         "metric": METRIC, "value": mixed["value"], "unit": "coef/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": MIXED_FORM, "data": "synthetic (seeded iid N(0,1))",
         "config": {"workload": rec["workload"], "N": rec["N"], "vectors": rec["vectors"],
-                   "maxs_mixed": args.maxs_mixed, "l2_flush": "256 MiB write between steps"},
+                   "maxs_mixed": args.maxs_mixed, "maxs_mixed_tc": args.maxs_mixed_tc,
+                   "best_mixed": rec["best_mixed"], "l2_flush": "256 MiB write between steps"},
         "plans": rec["plans"],
         "max_rel_err_vs_oracle": rec["max_rel_err_vs_oracle"],
         "speedup_mixed_vs_plain_maxs64": rec["speedup_vs_plain_maxs64"],
         "speedup_mixed_vs_best_plain": rec["speedup_vs_best_plain"],
+        "speedup_mixed_fp64_band_vs_best_plain": rec["speedup_vs_best_plain_fp64_band"],
         "best_plain": rec["best_plain"],
         "clocks": clk,
         "fp64_peak_tflops_measured": peak,
@@ -759,9 +782,12 @@ def main():
                     choices=["single", "batch", "ragged", "mixed_single", "mixed_batch"])
     ap.add_argument("--mixed-plans", default=None,
                     help="mixed_* workloads: comma-separated subset of the plans to time "
-                         "(plain_maxs16, plain_maxs32, plain_maxs64, mixed), for profiling")
+                         "(plain_maxs16, plain_maxs32, plain_maxs64, mixed, mixed_tc_band), "
+                         "for profiling")
     ap.add_argument("--maxs-mixed", type=int, default=16,
-                    help="leaf size bound of the mixed-form plan (mixed_* workloads)")
+                    help="leaf size bound of the mixed-form plan with the FP64 band")
+    ap.add_argument("--maxs-mixed-tc", type=int, default=32,
+                    help="leaf size bound of the mixed-form plan with the tensor-core band")
     ap.add_argument("--N", type=int, default=None)
     ap.add_argument("--maxs", type=int, default=64)
     ap.add_argument("--precompute", type=int, default=0,
@@ -1033,7 +1059,7 @@ def main():
             clk_m = ClockSampler(local)
             clk_m.start()
             rec = compare_mixed(l2c, wname, n_mixed, args.maxs_mixed, min(args.steps, 20),
-                                args.warmup, args.autotune, dev, torch)
+                                args.warmup, args.autotune, dev, torch, None, args.maxs_mixed_tc)
             rec["clocks"] = clk_m.stop()
             line["mixed"][key] = rec
     if rank == 0:

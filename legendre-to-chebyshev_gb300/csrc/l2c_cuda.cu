@@ -2903,6 +2903,122 @@ __global__ void __launch_bounds__(32 * MXW, 4)
   }
 }
 
+// The same band at s = 32: per (block, parity) 32 output rows x 64 terms as
+// four 16 x 32 pieces (output half hf, term half kh), each with its own row
+// scales, and each vector's window normalised per term half: the weights of a
+// row fall off along it, so scaling the far half apart keeps its precision
+// (one 64-term scale per row gave 1.1e-14).  The two halves' products are
+// rounded once each and added in FP64.  A CTA per (block, parity, 64 vectors),
+// so that one parity's fragments (24 KB) and its warps' windows fit three CTAs
+// per SM; a warp stages its 16 vectors' 64 same-parity values contiguously.
+constexpr int MB2_S = 32;
+constexpr int MB2_KC = MB2_S / 8;              // 32 terms per piece
+constexpr int MB2_WORDS = oz_words(2, MB2_KC);  // one 16 x 32 piece
+constexpr int MB2_XLD = 2 * MB2_S + 1;
+
+// Plan time: piece (hf, kh) of (block b, parity p) at F[((bp 2 + hf) 2 + kh)
+// MB2_WORDS ..], its row exponents at Fe[((bp 2 + hf) 2 + kh) 16 ..], bp = 2 b
+// + p.  One thread per (block, parity, row, term half).
+__global__ void k_oz_pack_band2(const double *__restrict__ a, const double *__restrict__ an,
+                                const double *__restrict__ dn, Geo g, int c2l,
+                                unsigned *__restrict__ F, int *__restrict__ Fe) {
+  const long long n = (g.nL - 1) * 2 * MB2_S * 2;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const int kh = (int)(idx & 1);
+  const long long r2 = idx >> 1, bp = r2 / MB2_S;
+  const int ip = (int)(r2 - bp * MB2_S), hf = ip >> 4;
+  const long long b = bp >> 1, p = bp & 1, j = b * g.h + 2 * ip + p;
+  const long long piece = (bp * 2 + hf) * 2 + kh;
+  oz_pack_row(
+      [&](int k) {
+        const int mp = 32 * kh + k;
+        return mp >= ip ? near_weight(c2l, mp - ip, j, a, an, dn) : 0.0;
+      },
+      true, ip & 15, 32, 2, MB2_KC, F + piece * MB2_WORDS, Fe + piece * 16);
+}
+
+constexpr size_t mz_band2_smem() {
+  return (size_t)(4 * MB2_WORDS + 4 * 16 + MXW * 2 * 16) * 4 +
+         (size_t)MXW * 16 * MB2_XLD * sizeof(double);
+}
+
+// CTA = (full block blockIdx.x, parity blockIdx.y & 1, 64 vectors from
+// 64 (blockIdx.y >> 1)), a warp per 16 vectors.
+__global__ void __launch_bounds__(32 * MXW, 3)
+    k_mz_band2(const double *__restrict__ x, const double *out, double *__restrict__ y,
+               const unsigned *__restrict__ F, const int *__restrict__ Fe, Geo g) {
+  extern __shared__ __align__(16) unsigned char mz_smem[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
+  unsigned *sP = reinterpret_cast<unsigned *>(mz_smem);  // the parity's four pieces
+  int *sE = reinterpret_cast<int *>(sP + 4 * MB2_WORDS);  // their row exponents
+  int *Es = sE + 4 * 16 + wid * 2 * 16;                   // [term half][16] column exponents
+  double *X = reinterpret_cast<double *>(sE + 4 * 16 + MXW * 2 * 16) + wid * 16 * MB2_XLD;
+  const long long b = blockIdx.x;
+  const int p = (int)(blockIdx.y & 1);
+  const long long bp = b * 2 + p;
+  oz_load_frag(sP, F + bp * 4 * MB2_WORDS, 4 * MB2_WORDS, sE, Fe + bp * 4 * 16, 4 * 16);
+  __syncthreads();
+  pdl_wait();
+  pdl_trigger();
+  const long long v0 = ((long long)(blockIdx.y >> 1) * MXW + wid) * 16;
+  if (v0 >= g.count) return;
+  const int nv = (int)min(16LL, g.count - v0);
+  for (int e = lane; e < 16 * 2 * MB2_S; e += 32) {  // x[v][b h + 2 m' + p], m' < 2s
+    const int r = e / (2 * MB2_S), m = e - r * (2 * MB2_S);
+    const bool ok = r < nv;
+    l2c_oz::cp_async8(X + r * MB2_XLD + m, ok ? x + (v0 + r) * g.N + b * g.h + 2 * m + p : x,
+                      ok ? 8 : 0);
+  }
+  l2c_oz::cp_commit();
+  l2c_oz::cp_wait0();
+  __syncwarp();
+  l2c_oz::stage_fix<32>(X, MB2_XLD, 1, 32, Es);            // terms 0 .. 31
+  l2c_oz::stage_fix<32>(X + 32, MB2_XLD, 1, 32, Es + 16);  // terms 32 .. 63
+  const long long *Ys = reinterpret_cast<const long long *>(X);
+  double val[2][2][4];
+#pragma unroll 1
+  for (int hf = 0; hf < 2; hf++) {
+#pragma unroll
+    for (int nt = 0; nt < 2; nt++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) val[hf][nt][e] = 0.0;
+#pragma unroll 1
+    for (int kh = 0; kh < 2; kh++) {
+      const int pc = hf * 2 + kh;
+      long long T[2][4];
+      oz_tile_T<2, MB2_KC>(sP + pc * MB2_WORDS, Ys + 32 * kh, MB2_XLD, 1, T);
+#pragma unroll
+      for (int nt = 0; nt < 2; nt++)
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const int ipl = 8 * nt + 2 * t4 + (e & 1), r = gq + 8 * (e >> 1);
+          val[hf][nt][e] +=
+              l2c_oz::to_double(T[nt][e], sE[pc * 16 + ipl] + Es[16 * kh + r] - 52);
+        }
+    }
+  }
+  __syncwarp();  // every lane is done with the staged words
+#pragma unroll
+  for (int hf = 0; hf < 2; hf++)
+#pragma unroll
+    for (int nt = 0; nt < 2; nt++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const int ip = 16 * hf + 8 * nt + 2 * t4 + (e & 1), r = gq + 8 * (e >> 1);
+        X[r * MB2_XLD + ip] = val[hf][nt][e];
+      }
+  __syncwarp();
+  // y = out_in + band at this parity's outputs j = b h + 2 i' + p
+  for (int e = lane; e < 16 * MB2_S; e += 32) {
+    const int r = e / MB2_S, i = e - r * MB2_S;
+    if (r < nv) {
+      const long long v = v0 + r, j = b * g.h + 2 * i + p;
+      y[v * g.N + j] = out[v * g.dist + j * g.stride] + X[r * MB2_XLD + i];
+    }
+  }
+}
+
 // The outputs of the last (ragged) block, j >= (nL - 1) h: k_near's FP64 sums.
 __global__ void k_mz_band_last(const double *__restrict__ x, const double *out,
                                double *__restrict__ y, const double *__restrict__ a,
@@ -3470,8 +3586,8 @@ bool use_band_tile(const l2c_gpu_plan *p, size_t count) {
 // Whether a mixed batch's band runs on the tensor cores (k_mz_band): the
 // batches whose FP64 band would be dense tiles, at s = 16.
 bool use_mz_band(const l2c_gpu_plan *p, size_t count) {
-  return p->mixed && p->mz_band_on && p->s == (size_t)MB_S && p->nL >= 2 &&
-         use_band_tile(p, count);
+  return p->mixed && p->mz_band_on && (p->s == (size_t)MB_S || p->s == (size_t)MB2_S) &&
+         p->nL >= 2 && use_band_tile(p, count);
 }
 
 // Whether this call's band runs as k_near_rows (full blocks and, one output
@@ -3834,15 +3950,22 @@ bool ensure_mixed_far(l2c_gpu_plan *p, size_t dir) {
 bool ensure_mz_band(l2c_gpu_plan *p, size_t dir) {
   if (p->mz_band[dir]) return true;
   const long long nbp = ((long long)p->nL - 1) * 2;
-  if (cudaMalloc(&p->mz_band[dir], (size_t)nbp * MB_WORDS * sizeof(unsigned)) != cudaSuccess ||
-      cudaMalloc(&p->mz_bande[dir], (size_t)nbp * MB_S * sizeof(int)) != cudaSuccess) {
+  const bool s32 = p->s == (size_t)MB2_S;
+  const size_t words = s32 ? 4 * (size_t)MB2_WORDS : (size_t)MB_WORDS;
+  const size_t rows = s32 ? 4 * 16 : (size_t)MB_S;  // row exponents per (block, parity)
+  if (cudaMalloc(&p->mz_band[dir], (size_t)nbp * words * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&p->mz_bande[dir], (size_t)nbp * rows * sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     set_err("cudaMalloc of the tensor-core band fragments failed");
     return false;
   }
   Geo g = make_geo(p, 1, p->N, 1);
-  k_oz_pack_band<<<blocks_for(nbp * MB_S, 128), 128, 0, p->stream>>>(
-      p->a, p->an, p->dn, g, (int)dir, p->mz_band[dir], p->mz_bande[dir]);
+  if (s32)
+    k_oz_pack_band2<<<blocks_for(nbp * MB2_S * 2, 128), 128, 0, p->stream>>>(
+        p->a, p->an, p->dn, g, (int)dir, p->mz_band[dir], p->mz_bande[dir]);
+  else
+    k_oz_pack_band<<<blocks_for(nbp * MB_S, 128), 128, 0, p->stream>>>(
+        p->a, p->an, p->dn, g, (int)dir, p->mz_band[dir], p->mz_bande[dir]);
   return cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(p->stream) == cudaSuccess;
 }
 
@@ -3937,11 +4060,17 @@ size_t launch_all(l2c_gpu_plan *p, const double *in, double *out, size_t dir, si
     if (use_mz_band(p, count)) {
       // the full blocks on the tensor cores, the last block in FP64
       PhaseScope ps(p, L2C_PHASE_NEAR, 2, stn);
-      launch_k((sc.pdl & 2) && !ov, k_mz_band,
-               dim3((unsigned)(g.nL - 1),
-                    (unsigned)((g.count + 16 * MXW * p->mz_band_tpw - 1) / (16 * MXW * p->mz_band_tpw))),
-               32 * MXW, mz_band_smem(), stn, x, (const double *)out, p->y,
-               (const unsigned *)p->mz_band[dir], (const int *)p->mz_bande[dir], g);
+      if (g.s == MB2_S)
+        launch_k((sc.pdl & 2) && !ov, k_mz_band2,
+                 dim3((unsigned)(g.nL - 1), 2 * (unsigned)((g.count + 16 * MXW - 1) / (16 * MXW))),
+                 32 * MXW, mz_band2_smem(), stn, x, (const double *)out, p->y,
+                 (const unsigned *)p->mz_band[dir], (const int *)p->mz_bande[dir], g);
+      else
+        launch_k((sc.pdl & 2) && !ov, k_mz_band,
+                 dim3((unsigned)(g.nL - 1), (unsigned)((g.count + 16 * MXW * p->mz_band_tpw - 1) /
+                                                       (16 * MXW * p->mz_band_tpw))),
+                 32 * MXW, mz_band_smem(), stn, x, (const double *)out, p->y,
+                 (const unsigned *)p->mz_band[dir], (const int *)p->mz_bande[dir], g);
       const long long ntail = g.N - (g.nL - 1) * g.h;
       k_mz_band_last<<<blocks_for(g.count * ntail, 256), 256, 0, stn>>>(
           x, out, p->y, p->a, p->an, p->dn, g, c2l);
@@ -4850,6 +4979,7 @@ l2c_gpu_plan *l2c_gpu_plan_create(size_t N, size_t maxs, size_t directions, unsi
       PCK(cudaFuncSetAttribute(k_mz_far<2>, smax, (int)oz_far_smem(2)));
       PCK(cudaFuncSetAttribute(k_mz_far_tc, smax, (int)ftc_smem()));
       PCK(cudaFuncSetAttribute(k_mz_band, smax, (int)mz_band_smem()));
+      PCK(cudaFuncSetAttribute(k_mz_band2, smax, (int)mz_band2_smem()));
 #define L2C_MZ_ATTR(kc)                                                                     \
   PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc, 1>, smax, (int)mz_leaf_up_smem(kc, 1)));        \
   PCK(cudaFuncSetAttribute(k_mz_leaf_up<kc, 2>, smax, (int)mz_leaf_up_smem(kc, 2)));

@@ -195,20 +195,23 @@ def test_far_tc_bitwise(lib, orc, monkeypatch, N, maxs, count):
             assert relerr(got[d][v], o(x[v], d)[:N]) <= TOL, (d, v)
 
 
-@pytest.mark.parametrize("N,count,dist", [(16384, 256, "gauss"), (4096, 70, "uniform"),
-                                          (1000, 64, "gauss"), (20000, 100, "sign")])
-def test_mixed_band_forms(lib, orc, monkeypatch, N, count, dist):
-    """Batches at s = 16 run the near-field band of the full blocks on the
-    tensor cores (k_mz_band: exact integer products of the split weights and
-    windows, one rounding) and the last block in FP64; L2C_MZ_BAND=0 keeps the
-    FP64 tiled band.  Both agree with the oracle to 1e-14 on every vector."""
+@pytest.mark.parametrize("N,maxs,count,dist", [(16384, 16, 256, "gauss"), (4096, 16, 70, "uniform"),
+                                               (1000, 16, 64, "gauss"), (20000, 16, 100, "sign"),
+                                               (16384, 32, 256, "gauss"), (8192, 32, 65, "uniform"),
+                                               (3000, 32, 64, "sign")])
+def test_mixed_band_forms(lib, orc, monkeypatch, N, maxs, count, dist):
+    """Batches at s = 16 and s = 32 run the near-field band of the full blocks
+    on the tensor cores (k_mz_band, k_mz_band2: exact integer products of the
+    split weights and windows, one rounding) and the last block in FP64;
+    L2C_MZ_BAND=0 keeps the FP64 tiled band.  Both agree with the oracle to
+    1e-14 on every vector."""
     x = np.ascontiguousarray(make_input(N * count, dist, 9 + count).reshape(count, N))
-    o = orc.Oracle(N, 16, 2)
+    o = orc.Oracle(N, maxs, 2)
     want = [np.stack([o(x[v], d)[:N] for v in range(count)]) for d in (0, 1)]
     for env in ("1", "0"):
         with monkeypatch.context() as m:
             m.setenv("L2C_MZ_BAND", env)
-            p = lib.Plan(N, 16, mixed=True)
+            p = lib.Plan(N, maxs, mixed=True)
             for d in (0, 1):
                 out = np.zeros_like(x)
                 p.execute_batched(x, out, d, count, N, 1)
