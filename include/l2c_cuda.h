@@ -31,7 +31,7 @@ typedef struct l2c_gpu_plan l2c_gpu_plan;
                                 FP16 tensor cores, FP64-accurate (operands split into
                                 exact 9-bit digit slices, products recombined exactly
                                 in integers; no FP64 instructions); for batches at
-                                s = 16 also the full blocks of the near-field band;
+                                s = 16 or 32 also the full blocks of the near-field band;
                                 the rest of the band, accumulation and scaling in FP64.
                                 Leaf sizes s <= 64. */
 

@@ -188,7 +188,7 @@ size_t execute_batched(const double *input_array, double *output_array, fmm_plan
 /* create_fmm with extra plan options (bit flags):
  *   L2C_FMM_MIXED   the mixed form: leaf, transfer and far-field products on FP16
  *                   tensor cores, FP64-accurate (exact 9-bit digit slices, exact
- *                   integer recombination), for batches at leaf size 16 also
+ *                   integer recombination), for batches at leaf size 16 or 32 also
  *                   the full blocks of the near-field band; the rest of the band,
  *                   accumulation and scaling in FP64 (maxs <= 64)
  * Same semantics as create_fmm otherwise. */
